@@ -1,0 +1,813 @@
+/*
+ * oracle.c -- CPU restatement of the IDRS package's solve path.
+ *
+ * TEST INFRASTRUCTURE ONLY (parity checker and CPU baseline); see oracle.h
+ * for the rules on who may load it and for the parity status.
+ */
+#include "oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define OR_NCHUNK 64
+#define OR_MAXS 64
+
+/* ------------------------------------------------------------------------ */
+/* shadow-space generator: splitmix64 of the element index, shared bit for  */
+/* bit with the CUDA library (csrc/common.cuh idrs_uniform).                */
+/* ------------------------------------------------------------------------ */
+static inline uint64_t or_splitmix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+double or_uniform(uint64_t seed, uint64_t index) {
+  uint64_t z = or_splitmix64(index ^ or_splitmix64(seed));
+  return (double)(z >> 11) * 0x1.0p-53;
+}
+
+void or_set_threads(int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+}
+int or_get_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* GROT: M/IDRS/dense_la_module.f90:683-742 (BLAS rotg style)              */
+/* ------------------------------------------------------------------------ */
+void or_rgrot(double a, double b, double *c, double *s, double *r) {
+  if (fabs(a) < DBL_EPSILON) {
+    *c = 0.; *s = 1.; *r = b;
+  } else {
+    double rho = hypot(fabs(a), fabs(b));
+    double alpha = a / fabs(a);
+    *c = fabs(a) / rho;
+    *s = alpha * b / rho;
+    *r = alpha * rho;
+  }
+}
+void or_cgrot(or_cplx a, or_cplx b, or_cplx *c, or_cplx *s, or_cplx *r) {
+  if (cabs(a) < DBL_EPSILON) {
+    *c = 0.; *s = 1.; *r = b;
+  } else {
+    double rho = hypot(cabs(a), cabs(b));
+    or_cplx alpha = a / cabs(a);
+    *c = cabs(a) / rho;
+    *s = alpha * conj(b) / rho;
+    *r = alpha * rho;
+  }
+}
+static void or_grot__r(double a, double b, double *c, double *s, double *r) { or_rgrot(a, b, c, s, r); }
+static void or_grot__c(or_cplx a, or_cplx b, or_cplx *c, or_cplx *s, or_cplx *r) { or_cgrot(a, b, c, s, r); }
+
+/* ------------------------------------------------------------------------ */
+/* element-type-generic part                                                */
+/* ------------------------------------------------------------------------ */
+#define T double
+#define SFX(name) name##_r
+#define CONJ(x) (x)
+#define ABSV(x) fabs(x)
+#define IS_CPLX 0
+#include "oracle_core.inc"
+#undef T
+#undef SFX
+#undef CONJ
+#undef ABSV
+#undef IS_CPLX
+
+#define T or_cplx
+#define SFX(name) name##_c
+#define CONJ(x) conj(x)
+#define ABSV(x) cabs(x)
+#define IS_CPLX 1
+#include "oracle_core.inc"
+#undef T
+#undef SFX
+#undef CONJ
+#undef ABSV
+#undef IS_CPLX
+
+void or_rsolve(int n, const double *A, const double *b, double *x) { or_solve__r(n, A, b, x); }
+void or_csolve(int n, const or_cplx *A, const or_cplx *b, or_cplx *x) { or_solve__c(n, A, b, x); }
+
+/* ------------------------------------------------------------------------ */
+/* user_module constructors: M/PP_MATRIX/user_module.f90:829-958            */
+/* ------------------------------------------------------------------------ */
+static or_umat *umat_new(int format, int nrows, int ncols) {
+  or_umat *A = calloc(1, sizeof(or_umat));
+  if (!A) return NULL;
+  A->format = format; A->nrows = nrows; A->ncols = ncols;
+  return A;
+}
+
+/* crs_format: user_module.f90:829-863.  Indices arrive 1-based.  The
+ * reference's quirk of storing ival into rval (:860) is immaterial here:
+ * integer matrices arrive as real values. */
+int or_crs_format(int nrows, int ncols, const int *row_ptr1, const int *col_ind1,
+                  const double *rval, const double *cval, or_umat **out) {
+  if (nrows < 0 || ncols < 0 || !row_ptr1 || !out) return OR_EARG;
+  int nnz = row_ptr1[nrows] - row_ptr1[0];
+  if (nnz < 0) return OR_EARG;
+  or_umat *A = umat_new(OR_CRS, nrows, ncols);
+  A->nnz = nnz;
+  A->row_ptr = malloc(sizeof(int) * (nrows + 1));
+  A->col_ind = malloc(sizeof(int) * (nnz > 0 ? nnz : 1));
+  for (int i = 0; i <= nrows; ++i) A->row_ptr[i] = row_ptr1[i] - row_ptr1[0];
+  for (int k = 0; k < nnz; ++k) {
+    int c = col_ind1[k] - 1;
+    if (c < 0 || c >= ncols) { or_umat_free(A); return OR_EARG; }
+    A->col_ind[k] = c;
+  }
+  if (cval) {
+    A->vals = 2; A->cval = malloc(sizeof(or_cplx) * (nnz > 0 ? nnz : 1));
+    memcpy(A->cval, cval, sizeof(or_cplx) * nnz);
+  } else if (rval) {
+    A->vals = 1; A->rval = malloc(sizeof(double) * (nnz > 0 ? nnz : 1));
+    memcpy(A->rval, rval, sizeof(double) * nnz);
+  }
+  *out = A;
+  return OR_OK;
+}
+
+/* coo_format: user_module.f90:865-898 */
+int or_coo_format(int nrows, int ncols, int nnz, const int *indx1, const int *jndx1,
+                  const double *rval, const double *cval, or_umat **out) {
+  if (nrows < 0 || ncols < 0 || nnz < 0 || !out) return OR_EARG;
+  or_umat *A = umat_new(OR_COO, nrows, ncols);
+  A->nnz = nnz;
+  A->indx = malloc(sizeof(int) * (nnz > 0 ? nnz : 1));
+  A->jndx = malloc(sizeof(int) * (nnz > 0 ? nnz : 1));
+  for (int k = 0; k < nnz; ++k) {
+    A->indx[k] = indx1[k] - 1; A->jndx[k] = jndx1[k] - 1;
+    if (A->indx[k] < 0 || A->indx[k] >= nrows || A->jndx[k] < 0 || A->jndx[k] >= ncols) {
+      or_umat_free(A); return OR_EARG;
+    }
+  }
+  if (cval) {
+    A->vals = 2; A->cval = malloc(sizeof(or_cplx) * (nnz > 0 ? nnz : 1));
+    memcpy(A->cval, cval, sizeof(or_cplx) * nnz);
+  } else if (rval) {
+    A->vals = 1; A->rval = malloc(sizeof(double) * (nnz > 0 ? nnz : 1));
+    memcpy(A->rval, rval, sizeof(double) * nnz);
+  }
+  *out = A;
+  return OR_OK;
+}
+
+/* cds_format: user_module.f90:932-958 (band(nrows,-hb:hb), column-major) */
+int or_cds_format(int nrows, int ncols, int half_band, const double *rband,
+                  const double *cband, or_umat **out) {
+  if (nrows < 0 || half_band < 0 || !out) return OR_EARG;
+  or_umat *A = umat_new(OR_CDS, nrows, ncols);
+  A->half_band = half_band;
+  size_t cnt = (size_t)nrows * (2 * half_band + 1);
+  if (cband) {
+    A->vals = 2; A->cband = malloc(sizeof(or_cplx) * (cnt ? cnt : 1));
+    memcpy(A->cband, cband, sizeof(or_cplx) * cnt);
+  } else if (rband) {
+    A->vals = 1; A->rband = malloc(sizeof(double) * (cnt ? cnt : 1));
+    memcpy(A->rband, rband, sizeof(double) * cnt);
+  }
+  *out = A;
+  return OR_OK;
+}
+
+/* dense_format: user_module.f90:900-930 */
+int or_dense_format(int nrows, int ncols, const double *rmat, const double *cmat,
+                    or_umat **out) {
+  if (nrows < 0 || ncols < 0 || !out) return OR_EARG;
+  or_umat *A = umat_new(OR_DENSE, nrows, ncols);
+  size_t cnt = (size_t)nrows * ncols;
+  if (cmat) {
+    A->vals = 2; A->cmat = malloc(sizeof(or_cplx) * (cnt ? cnt : 1));
+    memcpy(A->cmat, cmat, sizeof(or_cplx) * cnt);
+  } else {
+    A->vals = 1; A->rmat = malloc(sizeof(double) * (cnt ? cnt : 1));
+    if (rmat) memcpy(A->rmat, rmat, sizeof(double) * cnt); else memset(A->rmat, 0, sizeof(double) * cnt);
+  }
+  *out = A;
+  return OR_OK;
+}
+
+/* matrix-free stencil: E/STENCIL/user_module.f90:39-63 (coefficients c,w,e,s,n,f,b) */
+int or_stencil7_format(int nx, int ny, int nz, const double coef[7], or_umat **out) {
+  if (nx < 1 || ny < 1 || nz < 1 || !coef || !out) return OR_EARG;
+  or_umat *A = umat_new(OR_STENCIL7, nx * ny * nz, nx * ny * nz);
+  A->nx = nx; A->ny = ny; A->nz = nz; A->vals = 1;
+  memcpy(A->st, coef, sizeof(double) * 7);
+  *out = A;
+  return OR_OK;
+}
+
+void or_umat_free(or_umat *A) {
+  if (!A) return;
+  free(A->rmat); free(A->cmat); free(A->row_ptr); free(A->col_ind); free(A->indx);
+  free(A->jndx); free(A->rval); free(A->cval); free(A->rband); free(A->cband);
+  free(A);
+}
+
+/* real_diagonal: user_module.f90:960-1047 (single image: phi == me always).
+ * The stencil format (an extension) has the constant diagonal c. */
+int or_real_diagonal(const or_umat *A, double *D) {
+  int n = A->nrows;
+  for (int i = 0; i < n; ++i) D[i] = 0.;
+  switch (A->format) {
+  case OR_DENSE:
+    if (A->rmat) for (int i = 0; i < n; ++i) D[i] = A->rmat[i + (size_t)n * i];
+    break;
+  case OR_CRS:
+    for (int i = 0; i < n; ++i)
+      for (int j = A->row_ptr[i]; j < A->row_ptr[i + 1]; ++j)
+        if (A->col_ind[j] == i) D[i] += (A->vals == 1) ? A->rval[j] : (A->vals == 0 ? 1. : creal(A->cval[j]));
+    break;
+  case OR_COO:
+    for (int k = 0; k < A->nnz; ++k)
+      if (A->indx[k] == A->jndx[k]) D[A->indx[k]] += (A->vals == 1) ? A->rval[k] : (A->vals == 0 ? 1. : creal(A->cval[k]));
+    break;
+  case OR_CDS:
+    if (A->rband) for (int i = 0; i < n; ++i) D[i] = A->rband[i + (size_t)n * A->half_band];
+    else for (int i = 0; i < n; ++i) D[i] = 1.;
+    break;
+  case OR_STENCIL7:
+    for (int i = 0; i < n; ++i) D[i] = A->st[0];
+    break;
+  }
+  for (int i = 0; i < n; ++i) if (D[i] == 0) D[i] = 1.;
+  return OR_OK;
+}
+int or_complex_diagonal(const or_umat *A, or_cplx *D) {
+  int n = A->nrows;
+  for (int i = 0; i < n; ++i) D[i] = 0.;
+  switch (A->format) {
+  case OR_DENSE:
+    for (int i = 0; i < n; ++i) D[i] = A->cmat ? A->cmat[i + (size_t)n * i] : A->rmat[i + (size_t)n * i];
+    break;
+  case OR_CRS:
+    for (int i = 0; i < n; ++i)
+      for (int j = A->row_ptr[i]; j < A->row_ptr[i + 1]; ++j)
+        if (A->col_ind[j] == i) D[i] += (A->vals == 2) ? A->cval[j] : (A->vals == 1 ? A->rval[j] : 1.);
+    break;
+  case OR_COO:
+    for (int k = 0; k < A->nnz; ++k)
+      if (A->indx[k] == A->jndx[k]) D[A->indx[k]] += (A->vals == 2) ? A->cval[k] : (A->vals == 1 ? A->rval[k] : 1.);
+    break;
+  case OR_CDS:
+    for (int i = 0; i < n; ++i)
+      D[i] = A->cband ? A->cband[i + (size_t)n * A->half_band] : (A->rband ? A->rband[i + (size_t)n * A->half_band] : 1.);
+    break;
+  case OR_STENCIL7:
+    for (int i = 0; i < n; ++i) D[i] = A->st[0];
+    break;
+  }
+  for (int i = 0; i < n; ++i) if (D[i] == 0) D[i] = 1.;
+  return OR_OK;
+}
+
+/* REAL_PRECON: user_module.f90:1327-1381, which_precon = 1 (diagonal
+ * scaling, optionally shifted: D(K) - shift).  Dense/band LU are out of scope. */
+int or_real_precon(int which_precon, const or_umat *K, const double *shift, or_umat **out) {
+  if (!K || !out) return OR_EARG;
+  or_umat *P = umat_new(0, K->nrows, K->ncols);
+  P->which_precon = which_precon;
+  if (which_precon == 1) {
+    P->format = OR_CDS; P->half_band = 0; P->vals = 1;
+    P->rband = malloc(sizeof(double) * (K->nrows > 0 ? K->nrows : 1));
+    or_real_diagonal(K, P->rband);
+    if (shift) for (int i = 0; i < K->nrows; ++i) P->rband[i] -= *shift;
+  } else if (which_precon != 0) {
+    or_umat_free(P); return OR_EUNSUP;
+  }
+  *out = P;
+  return OR_OK;
+}
+int or_complex_precon(int which_precon, const or_umat *K, const double *shift, or_umat **out) {
+  if (!K || !out) return OR_EARG;
+  or_umat *P = umat_new(0, K->nrows, K->ncols);
+  P->which_precon = which_precon;
+  if (which_precon == 1) {
+    P->format = OR_CDS; P->half_band = 0; P->vals = 2;
+    P->cband = malloc(sizeof(or_cplx) * (K->nrows > 0 ? K->nrows : 1));
+    or_complex_diagonal(K, P->cband);
+    if (shift) for (int i = 0; i < K->nrows; ++i) P->cband[i] -= shift[0] + I * shift[1];
+  } else if (which_precon != 0) {
+    or_umat_free(P); return OR_EUNSUP;
+  }
+  *out = P;
+  return OR_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* type(matrix): M/PP_MATRIX/matrix_module.f90:38-81                        */
+/* ------------------------------------------------------------------------ */
+int or_matrix_create(const or_umat *K, const or_umat *P, const double *seed, int cplx, or_mat **out) {
+  if (!K || !out) return OR_EARG;
+  or_mat *A = calloc(1, sizeof(or_mat));
+  A->K = K; A->P = P;
+  if (seed) {
+    if (cplx) A->cseed = seed[0] + I * seed[1];
+    else A->rseed = seed[0];
+  }
+  *out = A;
+  return OR_OK;
+}
+void or_matrix_free(or_mat *A) {
+  if (!A) return;
+  free(A->ralpha_p); free(A->calpha_p); free(A->ralpha_s); free(A->calpha_s);
+  free(A);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Polynomial preconditioners: matrix_module.f90:851-1019                   */
+/* ------------------------------------------------------------------------ */
+#define DEF_COMPUTE_ALPHA(NAME, TT)                                                     \
+  int NAME(int degree, const TT *H, int ldh, int nh, TT *alpha) {                      \
+    if (degree == 0) { alpha[0] = 1.; return OR_OK; }                                  \
+    if (ldh < degree + 2 || nh < degree + 1) return OR_EARG;                            \
+    int d2 = degree + 2;                                                                \
+    TT *r = calloc((size_t)d2 * d2, sizeof(TT));                                        \
+    r[0] = 1.;                                                                           \
+    for (int i = 1; i <= degree + 1; ++i) {                                             \
+      for (int c = 1; c <= degree + 1; ++c) r[i + d2 * c] = r[(i - 1) + d2 * (c - 1)];  \
+      for (int j = 0; j <= i - 1; ++j) {                                                \
+        TT hji = H[j + (size_t)ldh * (i - 1)];                                          \
+        for (int c = 0; c <= degree + 1; ++c) r[i + d2 * c] = r[i + d2 * c] - hji * r[j + d2 * c]; \
+      }                                                                                 \
+      TT hd = H[i + (size_t)ldh * (i - 1)];                                             \
+      for (int c = 0; c <= degree + 1; ++c) r[i + d2 * c] = r[i + d2 * c] / hd;          \
+    }                                                                                   \
+    for (int c = 1; c <= degree + 1; ++c) alpha[c - 1] = -r[(degree + 1) + d2 * c];     \
+    free(r);                                                                            \
+    return OR_OK;                                                                       \
+  }
+/* rcompute_alpha: matrix_module.f90:983-1019 */
+DEF_COMPUTE_ALPHA(or_rcompute_alpha, double)
+/* ccompute_alpha: matrix_module.f90:1021-1057 */
+DEF_COMPUTE_ALPHA(or_ccompute_alpha, or_cplx)
+
+#define DEF_NEUMANN(NAME, TT, CA)                                                       \
+  int NAME(int degree, TT center, TT *alpha) {                                          \
+    int ld = degree + 2;                                                                \
+    TT *J = calloc((size_t)ld * (degree + 1), sizeof(TT));                              \
+    for (int i = 1; i <= degree + 1; ++i) {                                             \
+      J[(i - 1) + ld * (i - 1)] = center;                                               \
+      J[i + ld * (i - 1)] = -center;                                                    \
+    }                                                                                   \
+    int st = CA(degree, J, ld, degree + 1, alpha);                                      \
+    free(J);                                                                            \
+    return st;                                                                          \
+  }
+/* rneumann: matrix_module.f90:851-875; cneumann :877-901 */
+DEF_NEUMANN(or_rneumann, double, or_rcompute_alpha)
+DEF_NEUMANN(or_cneumann, or_cplx, or_ccompute_alpha)
+
+#define DEF_CHEBYSHEV(NAME, TT, CA)                                                     \
+  int NAME(int degree, const TT foci[2], TT *alpha) {                                   \
+    TT theta = (foci[0] + foci[1]) / 2.;                                                \
+    TT delta = (foci[0] - foci[1]) / 2.;                                                \
+    TT sigma = theta / delta;                                                           \
+    int ld = degree + 2;                                                                \
+    TT *J = calloc((size_t)ld * (degree + 1), sizeof(TT));                              \
+    J[0] = theta;                                                                       \
+    J[1] = -theta;                                                                      \
+    TT rho = 1. / sigma;                                                                \
+    for (int i = 2; i <= degree + 1; ++i) {                                             \
+      J[(i - 2) + ld * (i - 1)] = -delta * rho / 2.;                                    \
+      J[(i - 1) + ld * (i - 1)] = delta * sigma;                                        \
+      J[i + ld * (i - 1)] = -delta * sigma + delta * rho / 2.;                          \
+      rho = 1. / (2. * sigma - rho);                                                    \
+    }                                                                                   \
+    int st = CA(degree, J, ld, degree + 1, alpha);                                      \
+    free(J);                                                                            \
+    return st;                                                                          \
+  }
+/* rchebyshev: matrix_module.f90:903-941; cchebyshev :943-981 */
+DEF_CHEBYSHEV(or_rchebyshev, double, or_rcompute_alpha)
+DEF_CHEBYSHEV(or_cchebyshev, or_cplx, or_ccompute_alpha)
+
+/* ------------------------------------------------------------------------ */
+/* QR eigenvalues: dense_la_module.f90:42-83 (CQR_factorization, refine=2), */
+/* :192-293 (CQR_eig) and :295-403 (RQR_eig)                               */
+/* ------------------------------------------------------------------------ */
+static int cqr_factorization(int m, or_cplx *V, int ldv, or_cplx *Q, or_cplx *R) {
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i < m; ++i) { Q[i + m * j] = V[i + ldv * j]; R[i + m * j] = 0; }
+  for (int j = 0; j < m; ++j) {
+    for (int k = 0; k < 2; ++k)
+      for (int i = 0; i < j; ++i) {
+        or_cplx t = 0;
+        for (int q = 0; q < m; ++q) t += conj(Q[q + m * i]) * Q[q + m * j];
+        for (int q = 0; q < m; ++q) Q[q + m * j] = Q[q + m * j] - t * Q[q + m * i];
+        R[i + m * j] = R[i + m * j] + t;
+      }
+    double nr = 0;
+    for (int q = 0; q < m; ++q) { double a = cabs(Q[q + m * j]); nr += a * a; }
+    R[j + m * j] = R[j + m * j] + sqrt(nr);
+    if (cabs(R[j + m * j]) > DBL_MIN) {
+      for (int q = 0; q < m; ++q) Q[q + m * j] = Q[q + m * j] / R[j + m * j];
+    } else {
+      return j + 1;
+    }
+  }
+  return 0;
+}
+
+static int qr_eig_core(int n, or_cplx *V, int real_version, or_cplx *eig, int *converged) {
+  int iter = 0, m = n, maxit = real_version ? 100 * n : 10 * n;
+  const double tol = DBL_EPSILON;
+  or_cplx shift = 0;
+  or_cplx *Q = malloc(sizeof(or_cplx) * n * n), *R = malloc(sizeof(or_cplx) * n * n),
+          *RQ = malloc(sizeof(or_cplx) * n * n);
+#define VV(i, j) V[(i) + n * (j)]
+  if (real_version) {
+    for (int i = 0; i < m; ++i) if (cabs(VV(i, i)) > cabs(shift)) shift = VV(i, i);
+    shift = shift * (1. + 1. * I);
+  } else {
+    shift = VV(n - 1, n - 1);
+  }
+  while (m > 1 && iter < maxit) {
+    for (int i = 0; i < m; ++i) VV(i, i) = VV(i, i) - shift;
+    int info = cqr_factorization(m, V, n, Q, R);
+    if (info > 0) break;
+    for (int j = 0; j < m; ++j)
+      for (int i = 0; i < m; ++i) {
+        or_cplx acc = 0;
+        for (int q = 0; q < m; ++q) acc += R[i + m * q] * Q[q + m * j];
+        RQ[i + m * j] = acc;
+      }
+    for (int j = 0; j < m; ++j)
+      for (int i = 0; i < m; ++i) VV(i, j) = RQ[i + m * j];
+    for (int i = 0; i < m; ++i) VV(i, i) = VV(i, i) + shift;
+    if (cabs(VV(m - 1, m - 2)) < tol * cabs(VV(m - 1, m - 1))) m = m - 1;
+    if (real_version) {
+      shift = 0;
+      for (int i = 0; i < m; ++i) if (cabs(VV(i, i)) > cabs(shift)) shift = VV(i, i);
+    } else {
+      shift = VV(m - 1, m - 1);
+    }
+    iter = iter + 1;
+  }
+  for (int i = 0; i < n; ++i) eig[i] = VV(i, i);
+  if (converged) *converged = n - m + 1;
+#undef VV
+  free(Q); free(R); free(RQ);
+  return OR_OK;
+}
+int or_rqr_eig(const double *H, int ldh, int n, or_cplx *eig, int *converged) {
+  or_cplx *V = malloc(sizeof(or_cplx) * n * n);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) V[i + n * j] = H[i + (size_t)ldh * j];
+  int st = qr_eig_core(n, V, 1, eig, converged);
+  free(V);
+  return st;
+}
+int or_cqr_eig(const or_cplx *H, int ldh, int n, or_cplx *eig, int *converged) {
+  or_cplx *V = malloc(sizeof(or_cplx) * n * n);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) V[i + n * j] = H[i + (size_t)ldh * j];
+  int st = qr_eig_core(n, V, 0, eig, converged);
+  free(V);
+  return st;
+}
+
+/* filter_ritzval: matrix_module.f90:1059-1077 */
+static void filter_ritzval(int n, const or_cplx *rv, int *outlier) {
+  or_cplx center = 0;
+  for (int i = 0; i < n; ++i) center += rv[i];
+  center = center / n;
+  double sg = 0;
+  for (int i = 0; i < n; ++i) { double a = cabs(rv[i] - center); sg += a * a; }
+  sg = sqrt(sg / n);
+  for (int i = 0; i < n; ++i) outlier[i] = cabs(rv[i] - center) > 1.5 * sg;
+}
+
+/* ranalyse_spectrum: matrix_module.f90:1079-1181 */
+int or_ranalyse_spectrum(const double *H, int ldh, int n, double *foci, double *center,
+                         double *shift) {
+  or_cplx *rv = malloc(sizeof(or_cplx) * n);
+  int *out = malloc(sizeof(int) * n);
+  or_rqr_eig(H, ldh, n, rv, NULL);
+  filter_ritzval(n, rv, out);
+  double left = INFINITY, right = -INFINITY, bottom = INFINITY, top = -INFINITY;
+  for (int i = 0; i < n; ++i) {
+    if (out[i]) continue;
+    double re = creal(rv[i]), im = cimag(rv[i]);
+    if (re < left) left = re;
+    if (re > right) right = re;
+    if (im < bottom) bottom = im;
+    if (im > top) top = im;
+  }
+  double center_box = (right + left) / 2.;
+  double radius = -INFINITY;
+  for (int i = 0; i < n; ++i) if (!out[i]) { double a = cabs(rv[i] - center_box); if (a > radius) radius = a; }
+  double center_circle = center_box;
+  if (fabs(center_box) / radius < 1) {
+    double correction = fabs(center_box) / radius;
+    center_circle = center_box / correction;
+  }
+  double shift_circle = center_box - center_circle;
+  double x0 = (right - left) / 2., y0 = (top - bottom) / 2.;
+  double a = sqrt(x0 * (x0 + y0)), b = sqrt(y0 * (x0 + y0));
+  double center_ellipse = center_box;
+  if (fabs(center_box) / a < 1.) {
+    double correction = fabs(center_box) / a;
+    center_ellipse = center_box / correction;
+  }
+  double f1, f2;
+  if (a > b) {
+    double c = sqrt(a * a - b * b);
+    f1 = center_ellipse - c; f2 = center_ellipse + c;
+  } else {
+    double c = 0.15 * center_ellipse;
+    f1 = center_ellipse - c; f2 = center_ellipse + c;
+  }
+  if (foci) { foci[0] = f1; foci[1] = f2; }
+  if (center) *center = center_circle;
+  if (shift) *shift = shift_circle;
+  free(rv); free(out);
+  return OR_OK;
+}
+
+/* canalyse_spectrum: matrix_module.f90:1183-1282 */
+int or_canalyse_spectrum(const or_cplx *H, int ldh, int n, or_cplx *foci, or_cplx *center,
+                         or_cplx *shift) {
+  or_cplx *rv = malloc(sizeof(or_cplx) * n);
+  int *out = malloc(sizeof(int) * n);
+  or_cqr_eig(H, ldh, n, rv, NULL);
+  filter_ritzval(n, rv, out);
+  double left = INFINITY, right = -INFINITY, bottom = INFINITY, top = -INFINITY;
+  for (int i = 0; i < n; ++i) {
+    if (out[i]) continue;
+    double re = creal(rv[i]), im = cimag(rv[i]);
+    if (re < left) left = re;
+    if (re > right) right = re;
+    if (im < bottom) bottom = im;
+    if (im > top) top = im;
+  }
+  or_cplx center_box = ((right + left) + I * (top + bottom)) / 2.;
+  double radius = -INFINITY;
+  for (int i = 0; i < n; ++i) if (!out[i]) { double a = cabs(rv[i] - center_box); if (a > radius) radius = a; }
+  or_cplx center_circle = center_box;
+  if (cabs(center_box) / radius < 1) {
+    double correction = cabs(center_box) / radius;
+    center_circle = center_box / correction;
+  }
+  or_cplx shift_circle = center_box - center_circle;
+  double x0 = (right - left) / 2., y0 = (top - bottom) / 2.;
+  double a = sqrt(x0 * (x0 + y0)), b = sqrt(y0 * (x0 + y0));
+  or_cplx center_ellipse = center_box;
+  double q = pow(creal(center_box) / a, 2) + pow(cimag(center_box) / b, 2);
+  if (q < 1.) center_ellipse = center_box / sqrt(q);
+  or_cplx f1, f2;
+  if (a > b) {
+    double c = sqrt(a * a - b * b);
+    f1 = center_ellipse - c; f2 = center_ellipse + c;
+  } else {
+    double c = sqrt(b * b - a * a);
+    f1 = center_ellipse - I * c; f2 = center_ellipse + I * c;
+  }
+  if (foci) { foci[0] = f1; foci[1] = f2; }
+  if (center) *center = center_circle;
+  if (shift) *shift = shift_circle;
+  free(rv); free(out);
+  return OR_OK;
+}
+
+/* real_preconditioner: matrix_module.f90:551-635 */
+int or_real_preconditioner(or_mat *A, int preconditioner, int degree, const double *foci,
+                           const double *center, const double *H, int ldh, int nh) {
+  A->preconditioner = preconditioner;
+  A->degree = (preconditioner == 0) ? 0 : degree;
+  free(A->ralpha_p); A->ralpha_p = NULL;
+  if (preconditioner == 0) return OR_OK;
+  A->ralpha_p = calloc(degree + 1, sizeof(double));
+  if (preconditioner == 1) {
+    double c;
+    if (center) c = *center - A->rseed;
+    else if (H) or_ranalyse_spectrum(H, ldh, nh, NULL, &c, NULL);
+    else c = 1.;
+    return or_rneumann(degree, c, A->ralpha_p);
+  } else if (preconditioner == 2) {
+    double f[2];
+    if (foci) { f[0] = foci[0] - A->rseed; f[1] = foci[1] - A->rseed; }
+    else if (H) or_ranalyse_spectrum(H, ldh, nh, f, NULL, NULL);
+    else { f[0] = 0.25; f[1] = 1.75; }
+    return or_rchebyshev(degree, f, A->ralpha_p);
+  } else if (preconditioner == 3) {
+    if (!H) return OR_EARG;
+    return or_rcompute_alpha(degree, H, ldh, nh, A->ralpha_p);
+  }
+  return OR_EARG;
+}
+/* complex_preconditioner: matrix_module.f90:637-722 */
+int or_complex_preconditioner(or_mat *A, int preconditioner, int degree, const or_cplx *foci,
+                              const or_cplx *center, const or_cplx *H, int ldh, int nh) {
+  A->preconditioner = preconditioner;
+  A->degree = (preconditioner == 0) ? 0 : degree;
+  free(A->calpha_p); A->calpha_p = NULL;
+  if (preconditioner == 0) return OR_OK;
+  A->calpha_p = calloc(degree + 1, sizeof(or_cplx));
+  if (preconditioner == 1) {
+    or_cplx c;
+    if (center) c = *center - A->cseed;
+    else if (H) or_canalyse_spectrum(H, ldh, nh, NULL, &c, NULL);
+    else c = 1.;
+    return or_cneumann(degree, c, A->calpha_p);
+  } else if (preconditioner == 2) {
+    or_cplx f[2];
+    if (foci) { f[0] = foci[0] - A->cseed; f[1] = foci[1] - A->cseed; }
+    else if (H) or_canalyse_spectrum(H, ldh, nh, f, NULL, NULL);
+    else { f[0] = 0.25; f[1] = 1.75; }
+    return or_cchebyshev(degree, f, A->calpha_p);
+  } else if (preconditioner == 3) {
+    if (!H) return OR_EARG;
+    return or_ccompute_alpha(degree, H, ldh, nh, A->calpha_p);
+  }
+  return OR_EARG;
+}
+
+/* real_ms_parameters: matrix_module.f90:485-549 (no shift-and-invert) */
+int or_real_ms_parameters(or_mat *A, int n_sigma, const double *sigma, double *sigma_p) {
+  int d = A->degree;
+  free(A->ralpha_s); A->ralpha_s = NULL; A->n_sigma = n_sigma;
+  for (int i = 0; i < n_sigma; ++i) {
+    double ss = sigma[i] - A->rseed;
+    if (d > 0) {
+      if (!A->ralpha_s) A->ralpha_s = calloc((size_t)(d + 1) * n_sigma, sizeof(double));
+      double *as = A->ralpha_s + (size_t)(d + 1) * i;
+      as[d] = A->ralpha_p[d];
+      for (int k = d - 1; k >= 0; --k) as[k] = A->ralpha_p[k] + ss * as[k + 1];
+      sigma_p[i] = ss * as[0];
+    } else sigma_p[i] = ss;
+  }
+  return OR_OK;
+}
+/* complex_ms_parameters: matrix_module.f90:402-483 */
+int or_complex_ms_parameters(or_mat *A, int n_sigma, const or_cplx *sigma, or_cplx *sigma_p) {
+  int d = A->degree;
+  free(A->calpha_s); A->calpha_s = NULL; A->n_sigma = n_sigma;
+  for (int i = 0; i < n_sigma; ++i) {
+    or_cplx ss = sigma[i] - A->cseed;
+    if (d > 0) {
+      if (!A->calpha_s) A->calpha_s = calloc((size_t)(d + 1) * n_sigma, sizeof(or_cplx));
+      or_cplx *as = A->calpha_s + (size_t)(d + 1) * i;
+      as[d] = A->calpha_p[d];
+      for (int k = d - 1; k >= 0; --k) as[k] = A->calpha_p[k] + ss * as[k + 1];
+      sigma_p[i] = ss * as[0];
+    } else sigma_p[i] = ss;
+  }
+  return OR_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* IDRS_RITZ: M/IDRS/ritz_module.f90:389-556 (H output; recycling omitted)  */
+/* ------------------------------------------------------------------------ */
+int or_idrs_ritz_r(const or_mat *A, int n, const double *b, int s, const or_opts *o, double *x,
+                   int *nritz) {
+  double tol = (o && o->tolerance) ? *o->tolerance : (double)1e-6f;
+  if (tol < 0) return OR_EARG;
+  int maxit = (2 * n < 1000) ? 2 * n : 1000;
+  if (o && o->maximum_iterations) maxit = *o->maximum_iterations;
+  int method = (o && o->variant) ? *o->variant : 1;
+  double *Hf = calloc((size_t)(maxit + 1) * maxit, sizeof(double));
+  double *resnrm = calloc(maxit + 1, sizeof(double));
+  double *xs = calloc(n, sizeof(double));
+  if (o && o->x0) memcpy(xs, o->x0, sizeof(double) * n);
+  int conv = -1, iter = 0; double relnrm = 1;
+  or_opts io; memset(&io, 0, sizeof io);
+  io.M1 = o ? o->M1 : NULL;
+  io.tolerance = &tol; io.maximum_iterations = &maxit; io.variant = &method;
+  io.flag = &conv; io.relres = &relnrm; io.iterations = &iter; io.x0 = xs;
+  io.resvec = resnrm; io.resvec_len = maxit + 1;
+  io.H = Hf; io.H_rows = maxit + 1; io.H_cols = maxit;
+  io.PT = o ? o->PT : NULL; io.p_seed = o ? o->p_seed : 0;
+  int st = or_idrs_r(A, n, b, s, &io, x);
+  if (st != OR_OK) { free(Hf); free(resnrm); free(xs); return st; }
+  if (nritz) *nritz = (iter / (s + 1)) * s + iter % (s + 1);
+  if (o && o->flag) *o->flag = conv;
+  if (o && o->relres) *o->relres = relnrm;
+  if (o && o->iterations) *o->iterations = iter;
+  if (o && o->resvec) memcpy(o->resvec, resnrm, sizeof(double) * (maxit + 1));
+  if (o && o->H) {
+    if ((long)o->H_rows * o->H_cols > (long)(maxit + 1) * maxit) { free(Hf); free(resnrm); free(xs); return OR_EARG; }
+    double *H = o->H;
+    for (int j = 0; j < o->H_cols; ++j)
+      for (int i = 0; i < o->H_rows; ++i) H[i + (size_t)o->H_rows * j] = Hf[i + (size_t)(maxit + 1) * j];
+  }
+  free(Hf); free(resnrm); free(xs);
+  return OR_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* PP_IDRS (real, single rhs): M/PP_IDRS/pp_idrs_module.f90:118-162 with    */
+/* real_matrix.inc, real_preconditioner.inc:10-34 and run_idrs.inc:9-60.    */
+/* ------------------------------------------------------------------------ */
+int or_pp_idrs_r(const or_umat *K, const or_umat *P, int n, const double *b, or_pp_args *a,
+                 double *x) {
+  or_mat *A;
+  or_matrix_create(K, P, NULL, 0, &A);
+  double *x0 = calloc(n, sizeof(double)), *y = malloc(sizeof(double) * n),
+         *t = malloc(sizeof(double) * n);
+  int preconditioner = a->degree == 0 ? 0 : a->preconditioner;
+  int estimate = 1;
+  if (preconditioner == 0) estimate = 0;
+  if (preconditioner == 1 && a->center) estimate = 0;
+  if (preconditioner == 2 && a->foci) estimate = 0;
+  a->ritz_iterations = 0; a->nritz_used = 0;
+  int st = OR_OK;
+  if (estimate) {
+    int ini_iter = a->n_ritz + a->n_ritz / a->s;
+    int ldh = ini_iter + 1;
+    double *H = calloc((size_t)ldh * ini_iter, sizeof(double));
+    int flag = -1, iter = 0, one = 1, nritz = 0; double relres = 1;
+    or_opts o; memset(&o, 0, sizeof o);
+    o.tolerance = &a->tol; o.maximum_iterations = &ini_iter; o.variant = &one;
+    o.flag = &flag; o.relres = &relres; o.iterations = &iter;
+    o.H = H; o.H_rows = ldh; o.H_cols = ini_iter; o.p_seed = a->p_seed;
+    st = or_idrs_ritz_r(A, n, b, a->s, &o, x0, &nritz);
+    a->ritz_iterations = iter;
+    a->nritz_used = (iter / (a->s + 1)) * a->s + iter % (a->s + 1);
+    if (st == OR_OK) {
+      or_ranalyse_spectrum(H, ldh, a->nritz_used, a->foci_used, &a->center_used, NULL);
+      st = or_real_preconditioner(A, preconditioner, a->degree, NULL, NULL, H, ldh, a->nritz_used);
+    }
+    free(H);
+  } else {
+    double f[2] = {0.15, 1.85}, c = 1.;
+    if (a->foci) { f[0] = a->foci[0]; f[1] = a->foci[1]; }
+    if (a->center) c = *a->center;
+    a->foci_used[0] = f[0]; a->foci_used[1] = f[1]; a->center_used = c;
+    st = or_real_preconditioner(A, preconditioner, a->degree, f, &c, NULL, 0, 0);
+  }
+  if (st == OR_OK) {
+    for (int i = 0; i <= A->degree && i < 64; ++i) a->alpha_p[i] = A->ralpha_p ? A->ralpha_p[i] : 1.;
+    or_opts o; memset(&o, 0, sizeof o);
+    o.tolerance = &a->tol; o.maximum_iterations = &a->maxit; o.x0 = x0; o.p_seed = a->p_seed;
+    o.flag = &a->flag; o.relres = &a->relres_solver; o.iterations = &a->iterations;
+    int variant = a->method == 2 ? 2 : 1;
+    if (a->method == 0) {
+      o.inner_s = &a->in_s; o.inner_tolerance = &a->in_tol; o.inner_iterations = &a->in_it;
+      st = or_qmridr_r(A, n, b, a->s, &o, y);
+    } else {
+      o.variant = &variant;
+      st = or_idrs_r(A, n, b, a->s, &o, y);
+    }
+  }
+  if (st == OR_OK) {
+    or_scaleback_r(A, n, b, y, x);
+    or_user_mv_r(K, x, t);
+    for (int i = 0; i < n; ++i) t[i] = b[i] - t[i];
+    a->relres_original = or_norm_r(n, t) / or_norm_r(n, b);
+  }
+  free(x0); free(y); free(t);
+  or_matrix_free(A);
+  return st;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Adjoint helpers (new; no counterpart in the reference)                   */
+/* ------------------------------------------------------------------------ */
+void or_sparse_outer_grad(const or_umat *K, const double *lambda, const double *x, double *g) {
+  long n = K->nrows;
+  _Pragma("omp parallel for schedule(static) if(n > 32768)")
+  for (long i = 0; i < n; ++i)
+    for (int j = K->row_ptr[i]; j < K->row_ptr[i + 1]; ++j) g[j] = -lambda[i] * x[K->col_ind[j]];
+}
+int or_crs_transpose(const or_umat *K, or_umat **out) {
+  if (!K || K->format != OR_CRS || !out) return OR_EARG;
+  int n = K->nrows, m = K->ncols, nnz = K->row_ptr[n];
+  or_umat *A = umat_new(OR_CRS, m, n);
+  A->nnz = nnz; A->vals = K->vals;
+  A->row_ptr = calloc(m + 1, sizeof(int));
+  A->col_ind = malloc(sizeof(int) * (nnz > 0 ? nnz : 1));
+  if (K->vals == 1) A->rval = malloc(sizeof(double) * (nnz > 0 ? nnz : 1));
+  if (K->vals == 2) A->cval = malloc(sizeof(or_cplx) * (nnz > 0 ? nnz : 1));
+  for (int k = 0; k < nnz; ++k) A->row_ptr[K->col_ind[k] + 1]++;
+  for (int j = 0; j < m; ++j) A->row_ptr[j + 1] += A->row_ptr[j];
+  int *pos = malloc(sizeof(int) * (m > 0 ? m : 1));
+  memcpy(pos, A->row_ptr, sizeof(int) * m);
+  for (int i = 0; i < n; ++i)
+    for (int k = K->row_ptr[i]; k < K->row_ptr[i + 1]; ++k) {
+      int j = K->col_ind[k], p = pos[j]++;
+      A->col_ind[p] = i;
+      if (K->vals == 1) A->rval[p] = K->rval[k];
+      if (K->vals == 2) A->cval[p] = K->cval[k];
+    }
+  free(pos);
+  *out = A;
+  return OR_OK;
+}
