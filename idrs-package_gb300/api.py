@@ -1,0 +1,516 @@
+"""Python host mirror of the IDRS package's Fortran API over the C ABI.
+
+The names, argument meanings and error behaviour follow the Fortran modules
+(M/ = IDRS/MODULES of the IDRS package):
+
+  user_module   : crs_format, coo_format, cds_format, dense_format,
+                  stencil7_format (matrix-free stencil of E/STENCIL),
+                  real_precon / complex_precon, real_diagonal, UserMatrix * v
+  matrix_module : Matrix (type(matrix)), real_preconditioner /
+                  complex_preconditioner, ms_parameters, A * v, v / A,
+                  scaleback
+  idrs_module   : IDRS, QMRIDR, NORM, INPROD (and IDRS_RITZ, PP_IDRS)
+
+Every call goes through libidrs_gb300.so (CUDA, sm_103a).  There is no CPU
+fallback: importing this module raises if the library is missing, and a
+failing C call raises IDRSError with the library's message, the equivalent
+of the reference's `error stop`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libidrs_gb300.so")
+
+IDRS_OK, IDRS_ERR_ARG, IDRS_ERR_CUDA, IDRS_ERR_ALLOC, IDRS_ERR_STATE, IDRS_ERR_UNSUPPORTED = range(6)
+POINTER_HOST, POINTER_DEVICE = 0, 1
+
+
+class IDRSError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"[status {status}] {msg}")
+        self.status = status
+
+
+_lib = None
+_i = C.c_int
+_d = C.c_double
+_vp = C.c_void_p
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+
+# C prototypes (include/idrs_gb300.h)
+_PROTOS = {
+    "idrs_last_error": (C.c_char_p, []),
+    "idrs_version": (_i, []),
+    "idrs_crs_format": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp]),
+    "idrs_coo_format": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
+    "idrs_cds_format": (_i, [_i, _i, _i, _vp, _vp, _vp]),
+    "idrs_dense_format": (_i, [_i, _i, _vp, _vp, _vp]),
+    "idrs_stencil7_format": (_i, [_i, _i, _i, _vp, _vp]),
+    "idrs_real_precon": (_i, [_i, _vp, _vp, _vp]),
+    "idrs_complex_precon": (_i, [_i, _vp, _vp, _vp]),
+    "idrs_real_diagonal": (_i, [_vp, _vp]),
+    "idrs_complex_diagonal": (_i, [_vp, _vp]),
+    "idrs_ruser_mv": (_i, [_vp, _vp, _vp]),
+    "idrs_cuser_mv": (_i, [_vp, _vp, _vp]),
+    "idrs_user_matrix_free": (_i, [_vp]),
+    "idrs_matrix_create": (_i, [_vp, _vp, _i, _vp, _vp]),
+    "idrs_matrix_free": (_i, [_vp]),
+    "idrs_matrix_set_stream": (_i, [_vp, _vp]),
+    "idrs_matrix_set_pointer_mode": (_i, [_vp, _i]),
+    "idrs_matrix_set_shadow": (_i, [_vp, _i, _vp]),
+    "idrs_real_preconditioner": (_i, [_vp, _i, _i, _vp, _vp, _vp, _i, _i]),
+    "idrs_complex_preconditioner": (_i, [_vp, _i, _i, _vp, _vp, _vp, _i, _i]),
+    "idrs_matrix_get_alpha": (_i, [_vp, _vp, _vp]),
+    "idrs_real_ms_parameters": (_i, [_vp, _i, _vp, _vp]),
+    "idrs_complex_ms_parameters": (_i, [_vp, _i, _vp, _vp]),
+    "idrs_rmatvec": (_i, [_vp, _vp, _vp]),
+    "idrs_cmatvec": (_i, [_vp, _vp, _vp]),
+    "idrs_rprecon": (_i, [_vp, _vp, _vp]),
+    "idrs_cprecon": (_i, [_vp, _vp, _vp]),
+    "idrs_rscaleback": (_i, [_vp, _vp, _vp, _vp]),
+    "idrs_cscaleback": (_i, [_vp, _vp, _vp, _vp]),
+    "idrs_ms_rscaleback": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
+    "idrs_ms_cscaleback": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
+    "idrs_time_matvec": (_i, [_vp, _i, _i, _i, _vp, _vp]),
+    "idrs_ridrs": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp,
+                        _i, _vp, _i, _i, _vp]),
+    "idrs_cidrs": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp,
+                        _i, _vp, _i, _i, _vp]),
+    "idrs_rqmridr": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                          _i, _vp, _i, _vp, _vp]),
+    "idrs_cqmridr": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                          _i, _vp, _i, _vp, _vp]),
+    "idrs_rnorm": (_i, [_vp, _vp, _vp]),
+    "idrs_cnorm": (_i, [_vp, _vp, _vp]),
+    "idrs_rinprod": (_i, [_vp, _vp, _vp, _vp]),
+    "idrs_cinprod": (_i, [_vp, _vp, _vp, _vp]),
+    "idrs_ridrs_ritz": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp]),
+    "idrs_rpp_idrs": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+}
+
+
+class PPOptions(C.Structure):
+    _fields_ = [("method", C.c_int), ("s", C.c_int), ("tol", C.c_double), ("maxit", C.c_int),
+                ("in_s", C.c_int), ("in_it", C.c_int), ("in_tol", C.c_double),
+                ("preconditioner", C.c_int), ("degree", C.c_int), ("n_ritz", C.c_int),
+                ("inner_precision", C.c_int)]
+
+
+class PPReport(C.Structure):
+    _fields_ = [("flag", C.c_int), ("iterations", C.c_int), ("ritz_iterations", C.c_int),
+                ("nritz", C.c_int), ("relres_solver", C.c_double),
+                ("relres_original", C.c_double), ("foci", C.c_double * 2), ("center", C.c_double),
+                ("seconds_setup", C.c_double), ("seconds_solve", C.c_double),
+                ("seconds_total", C.c_double)]
+
+
+def load(path: str | None = None):
+    """Load libidrs_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise ImportError(f"libidrs_gb300.so not found at {path}: run "
+                          "`python idrs-package_gb300/build.py` (or __graft_entry__.build())")
+    lib = C.CDLL(path)
+    for name, (res, args) in _PROTOS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def lib():
+    return _lib if _lib is not None else load()
+
+
+def _check(status):
+    if status != IDRS_OK:
+        msg = lib().idrs_last_error()
+        raise IDRSError(status, msg.decode() if msg else "")
+
+
+def _p(a):
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    return a.ctypes.data
+
+
+def _ref_int(v):
+    return None if v is None else C.byref(C.c_int(int(v)))
+
+
+def _ref_dbl(v):
+    return None if v is None else C.byref(C.c_double(float(v)))
+
+
+def _arr(a, cplx):
+    if a is None:
+        return None
+    return np.ascontiguousarray(a, dtype=np.complex128 if cplx else np.float64)
+
+
+class Result(dict):
+    """x plus the optional outputs of the Fortran call (flag, relres, ...)."""
+    __getattr__ = dict.__getitem__
+
+
+# ---------------------------------------------------------------------------
+# user_module
+# ---------------------------------------------------------------------------
+class UserMatrix:
+    """type(user_matrix) (M/PP_MATRIX/user_module.f90:134-167), device resident."""
+
+    def __init__(self, handle, nrows, ncols, cplx):
+        self.handle, self.nrows, self.ncols, self.cplx = handle, nrows, ncols, cplx
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h and _lib is not None:
+            _lib.idrs_user_matrix_free(h)
+            self.handle = None
+
+    def __mul__(self, v):
+        """K*v: ruser_mv / cuser_mv (user_module.f90:182-241)."""
+        cplx = self.cplx or np.iscomplexobj(v)
+        v = _arr(v, cplx)
+        w = np.empty(self.nrows, dtype=v.dtype)
+        fn = lib().idrs_cuser_mv if cplx else lib().idrs_ruser_mv
+        _check(fn(self.handle, _p(v), _p(w)))
+        return w
+
+
+def _values(rval, cval):
+    if cval is not None:
+        return None, np.ascontiguousarray(cval, dtype=np.complex128)
+    if rval is not None:
+        rv = np.asarray(rval)
+        if np.iscomplexobj(rv):
+            return None, np.ascontiguousarray(rv, dtype=np.complex128)
+        return np.ascontiguousarray(rv, dtype=np.float64), None
+    return None, None
+
+
+def crs_format(nrows, ncols, row_ptr, col_ind, rval=None, ival=None, cval=None) -> UserMatrix:
+    """crs_format (user_module.f90:829-863); indices 1-based."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+    ci = np.ascontiguousarray(col_ind, dtype=np.int32)
+    if ival is not None and rval is None:
+        rval = np.asarray(ival, dtype=np.float64)
+    rv, cv = _values(rval, cval)
+    h = C.c_void_p()
+    _check(lib().idrs_crs_format(int(nrows), int(ncols), _p(rp), _p(ci), _p(rv), _p(cv), C.byref(h)))
+    return UserMatrix(h.value, nrows, ncols, cv is not None)
+
+
+def coo_format(nrows, ncols, nnz, indx, jndx, rval=None, ival=None, cval=None) -> UserMatrix:
+    """coo_format (user_module.f90:865-898); indices 1-based."""
+    ii = np.ascontiguousarray(indx[:nnz], dtype=np.int32)
+    jj = np.ascontiguousarray(jndx[:nnz], dtype=np.int32)
+    if ival is not None and rval is None:
+        rval = np.asarray(ival, dtype=np.float64)
+    rv, cv = _values(None if rval is None else np.asarray(rval)[:nnz],
+                     None if cval is None else np.asarray(cval)[:nnz])
+    h = C.c_void_p()
+    _check(lib().idrs_coo_format(int(nrows), int(ncols), int(nnz), _p(ii), _p(jj), _p(rv), _p(cv),
+                                 C.byref(h)))
+    return UserMatrix(h.value, nrows, ncols, cv is not None)
+
+
+def cds_format(nrows, ncols, half_band, rband=None, iband=None, cband=None) -> UserMatrix:
+    """cds_format (user_module.f90:932-958); band shape (nrows, 2*half_band+1)."""
+    if iband is not None and rband is None:
+        rband = np.asarray(iband, dtype=np.float64)
+    band = cband if cband is not None else rband
+    rv = cv = None
+    if band is not None:
+        flat = np.asarray(band).reshape(nrows, 2 * half_band + 1).ravel(order="F")
+        rv, cv = _values(None if np.iscomplexobj(flat) else flat, flat if np.iscomplexobj(flat) else None)
+    h = C.c_void_p()
+    _check(lib().idrs_cds_format(int(nrows), int(ncols), int(half_band), _p(rv), _p(cv), C.byref(h)))
+    return UserMatrix(h.value, nrows, ncols, cv is not None)
+
+
+def dense_format(rmat=None, imat=None, cmat=None) -> UserMatrix:
+    """dense_format (user_module.f90:900-930)."""
+    mat = cmat if cmat is not None else (rmat if rmat is not None else imat)
+    mat = np.asarray(mat)
+    flat = mat.ravel(order="F")
+    rv, cv = _values(None if np.iscomplexobj(flat) else flat.astype(np.float64),
+                     flat if np.iscomplexobj(flat) else None)
+    h = C.c_void_p()
+    _check(lib().idrs_dense_format(mat.shape[0], mat.shape[1], _p(rv), _p(cv), C.byref(h)))
+    return UserMatrix(h.value, mat.shape[0], mat.shape[1], cv is not None)
+
+
+def stencil7_format(nx, ny, nz, coef) -> UserMatrix:
+    """Matrix-free 7-point stencil of E/STENCIL/user_module.f90 (coef c,w,e,s,n,f,b)."""
+    c = np.ascontiguousarray(coef, dtype=np.float64)
+    h = C.c_void_p()
+    _check(lib().idrs_stencil7_format(int(nx), int(ny), int(nz), _p(c), C.byref(h)))
+    n = nx * ny * nz
+    return UserMatrix(h.value, n, n, False)
+
+
+def real_precon(which_precon, K: UserMatrix, shift=None) -> UserMatrix:
+    """REAL_PRECON (user_module.f90:1327-1463): 0 none, 1 diagonal scaling."""
+    h = C.c_void_p()
+    _check(lib().idrs_real_precon(int(which_precon), K.handle, _ref_dbl(shift), C.byref(h)))
+    return UserMatrix(h.value, K.nrows, K.ncols, False)
+
+
+def complex_precon(which_precon, K: UserMatrix, shift=None) -> UserMatrix:
+    h = C.c_void_p()
+    sh = None if shift is None else np.array([np.real(shift), np.imag(shift)])
+    _check(lib().idrs_complex_precon(int(which_precon), K.handle, _p(sh), C.byref(h)))
+    return UserMatrix(h.value, K.nrows, K.ncols, True)
+
+
+def real_diagonal(K: UserMatrix):
+    d = np.empty(K.nrows)
+    _check(lib().idrs_real_diagonal(K.handle, _p(d)))
+    return d
+
+
+def complex_diagonal(K: UserMatrix):
+    d = np.empty(K.nrows, dtype=np.complex128)
+    _check(lib().idrs_complex_diagonal(K.handle, _p(d)))
+    return d
+
+
+# ---------------------------------------------------------------------------
+# matrix_module
+# ---------------------------------------------------------------------------
+class Matrix:
+    """type(matrix) (M/PP_MATRIX/matrix_module.f90:38-81): K, the diagonal
+    preconditioner P, the seed shift and the polynomial preconditioner."""
+
+    def __init__(self, K: UserMatrix, P: UserMatrix | None = None, seed=None, complex=False):
+        self.K, self.P, self.cplx, self.n = K, P, bool(complex), K.nrows
+        sd = None if seed is None else np.array([np.real(seed), np.imag(seed)], dtype=np.float64)
+        h = C.c_void_p()
+        _check(lib().idrs_matrix_create(K.handle, P.handle if P else None, int(self.cplx), _p(sd),
+                                        C.byref(h)))
+        self.handle = h.value
+        self.device_pointers = False
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h and _lib is not None:
+            _lib.idrs_matrix_free(h)
+            self.handle = None
+
+    @property
+    def dtype(self):
+        return np.complex128 if self.cplx else np.float64
+
+    def set_stream(self, stream_handle: int):
+        _check(lib().idrs_matrix_set_stream(self.handle, C.c_void_p(stream_handle)))
+
+    def set_pointer_mode(self, mode: int):
+        _check(lib().idrs_matrix_set_pointer_mode(self.handle, int(mode)))
+        self.device_pointers = mode == POINTER_DEVICE
+
+    def set_shadow(self, s, PT):
+        """Inject the shadow space P (s x n, rows contiguous) for solves with this s."""
+        pt = None if PT is None else np.ascontiguousarray(PT, dtype=self.dtype)
+        _check(lib().idrs_matrix_set_shadow(self.handle, int(s), _p(pt)))
+
+    def preconditioner(self, preconditioner=0, degree=0, foci=None, center=None, H=None):
+        """real_preconditioner / complex_preconditioner (matrix_module.f90:551-722)."""
+        dt = self.dtype
+        f = None if foci is None else np.ascontiguousarray(foci, dtype=dt)
+        c = None if center is None else np.array([center], dtype=dt)
+        Hf = None if H is None else np.asfortranarray(H, dtype=dt)
+        ldh, nh = (0, 0) if Hf is None else Hf.shape
+        fn = lib().idrs_complex_preconditioner if self.cplx else lib().idrs_real_preconditioner
+        _check(fn(self.handle, int(preconditioner), int(degree), _p(f), _p(c), _p(Hf), ldh, nh))
+
+    real_preconditioner = preconditioner
+    complex_preconditioner = preconditioner
+
+    @property
+    def alpha_p(self):
+        deg = C.c_int()
+        _check(lib().idrs_matrix_get_alpha(self.handle, None, C.byref(deg)))
+        a = np.empty(deg.value + 1, dtype=self.dtype)
+        _check(lib().idrs_matrix_get_alpha(self.handle, _p(a), None))
+        return a
+
+    def time_matvec(self, prec=64, warmup=3, reps=20):
+        """CUDA-event time of one product A*v (ms) and of one SpMV launch (ms)."""
+        a, b = C.c_double(), C.c_double()
+        _check(lib().idrs_time_matvec(self.handle, int(prec), int(warmup), int(reps), C.byref(a),
+                                      C.byref(b)))
+        return a.value, b.value
+
+    def ms_parameters(self, sigma):
+        sigma = np.ascontiguousarray(sigma, dtype=self.dtype)
+        sp = np.empty_like(sigma)
+        fn = lib().idrs_complex_ms_parameters if self.cplx else lib().idrs_real_ms_parameters
+        _check(fn(self.handle, len(sigma), _p(sigma), _p(sp)))
+        return sp
+
+    def __mul__(self, v):
+        """A*v: rmatvec / cmatvec (matrix_module.f90:135-167)."""
+        v = _arr(v, self.cplx)
+        w = np.empty_like(v)
+        fn = lib().idrs_cmatvec if self.cplx else lib().idrs_rmatvec
+        _check(fn(self.handle, _p(v), _p(w)))
+        return w
+
+    def __rtruediv__(self, v):
+        """v/A: rprecon / cprecon (matrix_module.f90:306-400)."""
+        v = _arr(v, self.cplx)
+        w = np.empty_like(v)
+        fn = lib().idrs_cprecon if self.cplx else lib().idrs_rprecon
+        _check(fn(self.handle, _p(v), _p(w)))
+        return w
+
+    def scaleback(self, b, y):
+        """scaleback(A, b, y) (matrix_module.f90:811-849)."""
+        y = _arr(y, self.cplx)
+        b = _arr(b, self.cplx)
+        x = np.empty_like(y)
+        fn = lib().idrs_cscaleback if self.cplx else lib().idrs_rscaleback
+        _check(fn(self.handle, _p(b), _p(y), _p(x)))
+        return x
+
+    def ms_scaleback(self, sigma, b, Y):
+        """scaleback(A, sigma, b, y) (matrix_module.f90:724-809); Y is n x n_sigma."""
+        Y = np.asfortranarray(Y, dtype=self.dtype)
+        X = np.empty_like(Y, order="F")
+        sg = np.ascontiguousarray(sigma, dtype=self.dtype)
+        b = _arr(b, self.cplx)
+        fn = lib().idrs_ms_cscaleback if self.cplx else lib().idrs_ms_rscaleback
+        _check(fn(self.handle, Y.shape[1], _p(sg), _p(b), _p(Y), _p(X)))
+        return X
+
+
+# ---------------------------------------------------------------------------
+# idrs_module
+# ---------------------------------------------------------------------------
+def _solver_common(A: Matrix, b):
+    if A.device_pointers:
+        raise ValueError("the numpy mirror works in host-pointer mode")
+    return _arr(b, A.cplx)
+
+
+def IDRS(A: Matrix, b, s, M1: Matrix | None = None, tolerance=None, maximum_iterations=None,
+         variant=None, x0=None, U0=None, omega=None, resvec=False, H=None) -> Result:
+    """x = IDRS(A, b, s, ...) (RIDRS/CIDRS, idrs_module.f90:107-251).
+
+    resvec=True returns the residual history (maxit+1 entries); H=nritz
+    returns the (nritz+1) x nritz Hessenberg matrix."""
+    b = _solver_common(A, b)
+    n = len(b)
+    maxit = maximum_iterations if maximum_iterations is not None else min(2 * n, 1000)
+    x = np.empty_like(b)
+    flag, relres, iters = C.c_int(), C.c_double(), C.c_int()
+    x0a = _arr(x0, A.cplx)
+    U0a = None if U0 is None else np.asfortranarray(U0, dtype=A.dtype)
+    om = _arr(omega, A.cplx)
+    rv = np.zeros(maxit + 1) if resvec else None
+    Hm = np.zeros((H + 1, H), dtype=A.dtype, order="F") if H else None
+    fn = lib().idrs_cidrs if A.cplx else lib().idrs_ridrs
+    _check(fn(A.handle, _p(b), int(s), M1.handle if M1 else None, _ref_dbl(tolerance),
+              _ref_int(maximum_iterations), _ref_int(variant), C.byref(flag), C.byref(relres),
+              C.byref(iters), _p(x0a), _p(U0a), _p(om), 0 if om is None else len(om), _p(rv),
+              0 if rv is None else len(rv), _p(Hm), 0 if Hm is None else H + 1, H or 0, _p(x)))
+    r = Result(x=x, flag=flag.value, relres=relres.value, iterations=iters.value)
+    if rv is not None:
+        r["resvec"] = rv
+    if Hm is not None:
+        r["H"] = Hm
+    return r
+
+
+def QMRIDR(A: Matrix, b, s, M1: Matrix | None = None, tolerance=None, maximum_iterations=None,
+           inner_s=None, inner_tolerance=None, inner_iterations=None, x0=None, omega=None,
+           resvec=False, inner_precision=None) -> Result:
+    """x = QMRIDR(A, b, s, ...) (RQMRIDR/CQMRIDR, idrs_module.f90:253-408).
+    inner_precision=32 runs the inner IDR(inner_s) in fp32 / complex64."""
+    b = _solver_common(A, b)
+    n = len(b)
+    maxit = maximum_iterations if maximum_iterations is not None else min(2 * n, 1000)
+    x = np.empty_like(b)
+    flag, relres, iters = C.c_int(), C.c_double(), C.c_int()
+    x0a = _arr(x0, A.cplx)
+    om = _arr(omega, A.cplx)
+    rv = np.zeros(maxit + 1) if resvec else None
+    fn = lib().idrs_cqmridr if A.cplx else lib().idrs_rqmridr
+    _check(fn(A.handle, _p(b), int(s), M1.handle if M1 else None, _ref_dbl(tolerance),
+              _ref_int(maximum_iterations), C.byref(flag), C.byref(relres), C.byref(iters),
+              _ref_int(inner_s), _ref_dbl(inner_tolerance), _ref_int(inner_iterations), _p(x0a),
+              _p(om), 0 if om is None else len(om), _p(rv), 0 if rv is None else len(rv),
+              _ref_int(inner_precision), _p(x)))
+    r = Result(x=x, flag=flag.value, relres=relres.value, iterations=iters.value)
+    if rv is not None:
+        r["resvec"] = rv
+    return r
+
+
+def NORM(A: Matrix, w) -> float:
+    w = _arr(w, A.cplx)
+    out = np.zeros(1)
+    fn = lib().idrs_cnorm if A.cplx else lib().idrs_rnorm
+    _check(fn(A.handle, _p(w), _p(out)))
+    return float(out[0])
+
+
+def INPROD(A: Matrix, u, v):
+    u = _arr(u, A.cplx)
+    v = _arr(v, A.cplx)
+    out = np.zeros(2)
+    fn = lib().idrs_cinprod if A.cplx else lib().idrs_rinprod
+    _check(fn(A.handle, _p(u), _p(v), _p(out)))
+    return complex(out[0], out[1]) if A.cplx else float(out[0])
+
+
+def IDRS_RITZ(A: Matrix, b, s, tolerance=None, maximum_iterations=None, x0=None, H_shape=None):
+    """IDRS_RITZ (ritz_module.f90:389-556): Hessenberg output and nritz."""
+    b = _solver_common(A, b)
+    x = np.empty_like(b)
+    flag, relres, iters, nritz = C.c_int(), C.c_double(), C.c_int(), C.c_int()
+    Hm = None
+    if H_shape:
+        Hm = np.zeros(H_shape, order="F")
+    _check(lib().idrs_ridrs_ritz(A.handle, _p(b), int(s), _ref_dbl(tolerance),
+                                 _ref_int(maximum_iterations), C.byref(flag), C.byref(relres),
+                                 C.byref(iters), _p(_arr(x0, False)), _p(Hm),
+                                 0 if Hm is None else H_shape[0], 0 if Hm is None else H_shape[1],
+                                 C.byref(nritz), _p(x)))
+    r = Result(x=x, flag=flag.value, relres=relres.value, iterations=iters.value, nritz=nritz.value)
+    if Hm is not None:
+        r["H"] = Hm
+    return r
+
+
+def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=None, *, method=1,
+            s=4, tol=1e-6, maxit=1000, in_s=1, in_it=0, in_tol=0.1, preconditioner=0, degree=0,
+            n_ritz=32, inner_precision=64) -> Result:
+    """x = pp_idrs(K, b[, P, center, foci]) (RPP_IDRS, pp_idrs_module.f90:118-162);
+    the command-line options of initialize.inc:4-31 are keyword arguments."""
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.empty_like(b)
+    o = PPOptions(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
+                  inner_precision)
+    rep = PPReport()
+    f = None if foci is None else np.ascontiguousarray(foci, dtype=np.float64)
+    _check(lib().idrs_rpp_idrs(K.handle, _p(b), P.handle if P else None, _ref_dbl(center), _p(f),
+                               C.byref(o), C.byref(rep), _p(x)))
+    return Result(x=x, flag=rep.flag, iterations=rep.iterations,
+                  ritz_iterations=rep.ritz_iterations, nritz=rep.nritz,
+                  relres=rep.relres_solver, relres_original=rep.relres_original,
+                  foci=tuple(rep.foci), center=rep.center, seconds_setup=rep.seconds_setup,
+                  seconds_solve=rep.seconds_solve, seconds_total=rep.seconds_total)

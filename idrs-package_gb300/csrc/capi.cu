@@ -1,0 +1,1108 @@
+// capi.cu -- the extern "C" boundary (include/idrs_gb300.h).
+#include <algorithm>
+#include <chrono>
+#include <complex>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <vector>
+
+#include "../../include/idrs_gb300.h"
+#include "idrs_gpu.cuh"
+#include "setup.h"
+
+using namespace idrs;
+
+struct idrs_user_matrix_s : UserMatrix {};
+struct idrs_matrix_s : Operator {};
+
+namespace {
+
+using cd = std::complex<double>;
+
+struct arg_error : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct unsupported_error : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+template <class F>
+int guard(F&& f) {
+  try {
+    return f();
+  } catch (const cuda_error& e) {
+    set_error(std::string(cudaGetErrorString(e.code)) + " (" + e.where + ")");
+    return e.code == cudaErrorMemoryAllocation ? IDRS_ERR_ALLOC : IDRS_ERR_CUDA;
+  } catch (const arg_error& e) {
+    set_error(e.what());
+    return IDRS_ERR_ARG;
+  } catch (const unsupported_error& e) {
+    set_error(e.what());
+    return IDRS_ERR_UNSUPPORTED;
+  } catch (const std::bad_alloc&) {
+    set_error("host allocation failed");
+    return IDRS_ERR_ALLOC;
+  } catch (const std::exception& e) {
+    set_error(e.what());
+    return IDRS_ERR_ARG;
+  }
+}
+
+#define REQUIRE(cond, msg) \
+  do {                     \
+    if (!(cond)) throw arg_error(msg); \
+  } while (0)
+
+void init_runtime() {
+  static bool done = false;
+  if (done) return;
+  done = true;
+  int dev = 0;
+  IDRS_CUDA(cudaGetDevice(&dev));
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+}
+
+// device buffer owned for the duration of one call
+struct DBuf {
+  void* p = nullptr;
+  cudaStream_t st = nullptr;
+  DBuf() = default;
+  DBuf(size_t bytes, cudaStream_t s) : st(s) {
+    IDRS_CUDA(cudaMallocAsync(&p, std::max<size_t>(bytes, 16), s));
+  }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), st(o.st) { o.p = nullptr; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) {
+      if (p) cudaFreeAsync(p, st);
+      p = o.p; st = o.st; o.p = nullptr;
+    }
+    return *this;
+  }
+  ~DBuf() { if (p) cudaFreeAsync(p, st); }
+  template <class T> T* as() const { return (T*)p; }
+};
+
+void* upload(const void* h, size_t bytes) {
+  void* d = nullptr;
+  IDRS_CUDA(cudaMalloc(&d, std::max<size_t>(bytes, 16)));
+  if (h && bytes) IDRS_CUDA(cudaMemcpy(d, h, bytes, cudaMemcpyHostToDevice));
+  return d;
+}
+
+int crs_group(long nnz, long nrows) {
+  double mean = nrows > 0 ? (double)nnz / nrows : 1.0;
+  int g = 2;
+  while (g < 32 && g < mean) g *= 2;
+  return g;
+}
+
+// Vector staging for host-pointer mode: uploads `in`, gives a device pointer,
+// and downloads to `out` on finish().
+struct Staged {
+  Operator* A;
+  size_t bytes;
+  std::vector<DBuf> bufs;
+  Staged(Operator* a, size_t b) : A(a), bytes(b) {}
+  const void* in(const void* h) {
+    if (!h) return nullptr;
+    if (A->device_pointers) return h;
+    bufs.emplace_back(bytes, A->stream);
+    IDRS_CUDA(cudaMemcpyAsync(bufs.back().p, h, bytes, cudaMemcpyHostToDevice, A->stream));
+    return bufs.back().p;
+  }
+  void* out(void* h) {
+    if (A->device_pointers) return h;
+    bufs.emplace_back(bytes, A->stream);
+    return bufs.back().p;
+  }
+  void finish(void* h, const void* d) {
+    if (A->device_pointers || !h) return;
+    IDRS_CUDA(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, A->stream));
+  }
+};
+
+const void* find_shadow(Operator* A, int s) {
+  for (auto& p : A->shadows)
+    if (p.first == s) return p.second;
+  return nullptr;
+}
+
+// ----------------------------------------------------------------- diagonal
+template <class V>
+__global__ void k_diag_crs(int n, const int* rp, const int* ci, const V* val, V* D) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x) {
+    V d = V(0.0);
+    for (int k = rp[i]; k < rp[i + 1]; ++k)
+      if (ci[k] == i) d = d + val[k];
+    D[i] = d;
+  }
+}
+template <class V>
+__global__ void k_diag_cds(int n, int hb, const V* band, V* D) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x)
+    D[i] = band[i + (long)n * hb];
+}
+template <class V>
+__global__ void k_diag_dense(int n, const V* mat, V* D) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x)
+    D[i] = mat[i + (long)n * i];
+}
+template <class V>
+__global__ void k_diag_fix(int n, V* D, V shift) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x) {
+    V d = D[i];
+    if (d == V(0.0)) d = V(1.0);  // where (D == 0) D = 1 (user_module.f90:1043-1045)
+    D[i] = d - shift;
+  }
+}
+
+template <class V>
+void diagonal_into(const UserMatrix& K, V* D, cudaStream_t st) {
+  int n = K.nrows;
+  switch (K.format) {
+    case FMT_CRS:
+    case FMT_COO: k_diag_crs<V><<<stream_grid(n), kThreads, 0, st>>>(n, K.row_ptr, K.col_ind, (const V*)K.val, D); break;
+    case FMT_CDS: k_diag_cds<V><<<stream_grid(n), kThreads, 0, st>>>(n, K.half_band, (const V*)K.band, D); break;
+    case FMT_DENSE: k_diag_dense<V><<<stream_grid(n), kThreads, 0, st>>>(n, (const V*)K.mat, D); break;
+    default: throw unsupported_error("diagonal: unsupported format");
+  }
+  IDRS_LAUNCH_CHECK();
+}
+__global__ void k_promote(long n, const double* a, c128* b) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x) b[i] = c128(a[i], 0.0);
+}
+
+// Diagonal of K (complex if K is complex or `want_cplx`), D==0 -> 1, minus shift.
+void* make_diagonal(const UserMatrix& K, bool want_cplx, c128 shift, bool* is_cplx) {
+  int n = K.nrows;
+  bool cplx = want_cplx || K.vals == 2;
+  *is_cplx = cplx;
+  void* D = nullptr;
+  IDRS_CUDA(cudaMalloc(&D, (cplx ? 16 : 8) * (size_t)std::max(n, 1)));
+  cudaStream_t st = nullptr;
+  if (cplx) {
+    if (K.vals == 2) {
+      diagonal_into<c128>(K, (c128*)D, st);
+    } else {
+      double* tmp = nullptr;
+      IDRS_CUDA(cudaMalloc(&tmp, 8 * (size_t)std::max(n, 1)));
+      diagonal_into<double>(K, tmp, st);
+      k_promote<<<stream_grid(n), kThreads, 0, st>>>(n, tmp, (c128*)D);
+      IDRS_CUDA(cudaDeviceSynchronize());
+      cudaFree(tmp);
+    }
+    k_diag_fix<c128><<<stream_grid(n), kThreads, 0, st>>>(n, (c128*)D, shift);
+  } else {
+    diagonal_into<double>(K, (double*)D, st);
+    k_diag_fix<double><<<stream_grid(n), kThreads, 0, st>>>(n, (double*)D, shift.x);
+  }
+  IDRS_LAUNCH_CHECK();
+  IDRS_CUDA(cudaDeviceSynchronize());
+  return D;
+}
+
+
+// -------------------------------------------------- polynomial set-up
+int set_preconditioner(Operator* A, int preconditioner, int degree, const double* foci,
+                       const double* center, const double* H, int ldh, int nh) {
+  REQUIRE(preconditioner >= 0 && preconditioner <= 3, "illegal value for preconditioner");
+  REQUIRE(degree >= 0 && degree <= 62, "illegal polynomial degree");
+  A->preconditioner = preconditioner;
+  A->degree = (preconditioner == 0) ? 0 : degree;
+  A->alpha_p.assign(A->degree + 1, c128(1.0, 0.0));
+  if (A->degree == 0) return IDRS_OK;
+  if (!A->cplx) {
+    std::vector<double> al(A->degree + 1);
+    int st = 0;
+    if (preconditioner == 1) {
+      double c;
+      if (center) c = *center - A->seed.x;
+      else if (H) analyse_spectrum(H, ldh, nh, nullptr, &c, nullptr);
+      else c = 1.0;
+      st = neumann(A->degree, c, al.data());
+    } else if (preconditioner == 2) {
+      double f[2];
+      if (foci) { f[0] = foci[0] - A->seed.x; f[1] = foci[1] - A->seed.x; }
+      else if (H) analyse_spectrum(H, ldh, nh, f, nullptr, nullptr);
+      else { f[0] = 0.25; f[1] = 1.75; }
+      st = chebyshev(A->degree, f, al.data());
+    } else {
+      REQUIRE(H, "the Hessenberg preconditioner needs H");
+      st = compute_alpha(A->degree, H, ldh, nh, al.data());
+    }
+    REQUIRE(st == 0, "Hessenberg matrix too small for polynomial degree");
+    for (int i = 0; i <= A->degree; ++i) A->alpha_p[i] = c128(al[i], 0.0);
+  } else {
+    std::vector<cd> al(A->degree + 1);
+    cd seed(A->seed.x, A->seed.y);
+    int st = 0;
+    std::vector<cd> Hc;
+    if (H) {
+      Hc.resize((size_t)ldh * nh);
+      for (size_t i = 0; i < Hc.size(); ++i) Hc[i] = cd(H[2 * i], H[2 * i + 1]);
+    }
+    if (preconditioner == 1) {
+      cd c;
+      if (center) c = cd(center[0], center[1]) - seed;
+      else if (H) analyse_spectrum(Hc.data(), ldh, nh, nullptr, &c, nullptr);
+      else c = 1.0;
+      st = neumann(A->degree, c, al.data());
+    } else if (preconditioner == 2) {
+      cd f[2];
+      if (foci) { f[0] = cd(foci[0], foci[1]) - seed; f[1] = cd(foci[2], foci[3]) - seed; }
+      else if (H) analyse_spectrum(Hc.data(), ldh, nh, f, nullptr, nullptr);
+      else { f[0] = 0.25; f[1] = 1.75; }
+      st = chebyshev(A->degree, f, al.data());
+    } else {
+      REQUIRE(H, "the Hessenberg preconditioner needs H");
+      st = compute_alpha(A->degree, Hc.data(), ldh, nh, al.data());
+    }
+    REQUIRE(st == 0, "Hessenberg matrix too small for polynomial degree");
+    for (int i = 0; i <= A->degree; ++i) A->alpha_p[i] = c128(al[i].real(), al[i].imag());
+  }
+  return IDRS_OK;
+}
+
+// ---------------------------------------------------------------- solvers
+template <class T>
+int run_idrs(Operator* A, const double* b, int s, Operator* M1, const double* tolerance,
+             const int* maximum_iterations, const int* variant, int* flag, double* relres,
+             int* iterations, const double* x0, const double* U0, const double* omega, int n_omega,
+             double* resvec, int resvec_len, double* H, int ldh, int nritz, double* x) {
+  using W = typename traits<T>::wide;
+  REQUIRE(A && b && x, "idrs: A, b and x are required");
+  REQUIRE(s >= 1, "idrs: s must be positive");
+  if (s > MAXS) throw unsupported_error("idrs: s > 16 is not supported by the GPU path");
+  SolveOpts o;
+  if (tolerance) {
+    REQUIRE(*tolerance >= 0, "Illegal value for parameter tolerance");
+    o.tol = *tolerance;
+  }
+  const long n = A->n();
+  o.maxit = maximum_iterations ? *maximum_iterations : (int)std::min<long>(2 * n, 1000);
+  o.method = variant ? *variant : 1;
+  REQUIRE(o.method >= 1 && o.method <= 4, "idrs: variant must be 1..4");
+  REQUIRE(o.method == 1 || s == 1, "idrs: variants 2-4 use s = 1");
+  if (flag) *flag = -1;
+  if (relres) *relres = 1.0;
+  if (iterations) *iterations = 0;
+  if (resvec) REQUIRE(o.maxit + 1 <= resvec_len, "Length of vector with residual norms too small, should be maxit+1");
+  bool out_H = (H != nullptr) && nritz > 0;
+  if (H && nritz > 0) REQUIRE(ldh == nritz + 1, "Second dimension of H incompatible, with first");
+  cudaStream_t st = A->stream;
+  Staged sv(A, sizeof(T) * n);
+  const T* d_b = (const T*)sv.in(b);
+  const T* d_x0 = (const T*)sv.in(x0);
+  T* d_x = (T*)sv.out(x);
+  Staged su(A, sizeof(T) * n * s);
+  const T* d_U0 = (const T*)su.in(U0);
+  DBuf d_res, d_H, d_om;
+  if (resvec) { d_res = DBuf(sizeof(double) * resvec_len, st); IDRS_CUDA(cudaMemsetAsync(d_res.p, 0, sizeof(double) * resvec_len, st)); }
+  if (out_H) { d_H = DBuf(sizeof(W) * ldh * nritz, st); IDRS_CUDA(cudaMemsetAsync(d_H.p, 0, sizeof(W) * ldh * nritz, st)); }
+  if (omega && n_omega > 0) {
+    d_om = DBuf(sizeof(W) * n_omega, st);
+    IDRS_CUDA(cudaMemcpyAsync(d_om.p, omega, sizeof(W) * n_omega, cudaMemcpyHostToDevice, st));
+  }
+  o.M1 = M1;
+  o.x0 = d_x0;
+  o.U0 = d_U0;
+  o.omega = d_om.p;
+  o.n_omega = n_omega;
+  o.resvec = d_res.as<double>();
+  o.resvec_len = resvec_len;
+  o.H = out_H ? d_H.p : nullptr;
+  o.ldH = ldh;
+  o.nritz = out_H ? nritz : 0;
+  o.PT = find_shadow(A, s);
+  IdrsGpu<T> solver(*A, 64, s, o.method);
+  solver.solve(d_b, d_x, o);
+  auto h = solver.state();
+  sv.finish(x, d_x);
+  if (resvec) IDRS_CUDA(cudaMemcpyAsync(resvec, d_res.p, sizeof(double) * resvec_len, cudaMemcpyDeviceToHost, st));
+  if (out_H) IDRS_CUDA(cudaMemcpyAsync(H, d_H.p, sizeof(W) * ldh * nritz, cudaMemcpyDeviceToHost, st));
+  IDRS_CUDA(cudaStreamSynchronize(st));
+  if (flag) *flag = h.info;
+  if (relres) *relres = h.relres;
+  if (iterations) *iterations = h.iter;
+  return IDRS_OK;
+}
+
+template <class T, class Tin>
+void run_qmr_typed(Operator* A, int s, const T* d_b, T* d_x, SolveOpts& o, int* flag,
+                   double* relres, int* iterations) {
+  QmrGpu<T, Tin> solver(*A, s, o);
+  solver.solve(d_b, d_x, o);
+  auto h = solver.state();
+  if (flag) *flag = h.info;
+  if (relres) *relres = h.relres;
+  if (iterations) *iterations = h.iter;
+}
+
+template <class T, class Tlow>
+int run_qmridr(Operator* A, const double* b, int s, Operator* M1, const double* tolerance,
+               const int* maximum_iterations, int* flag, double* relres, int* iterations,
+               const int* inner_s, const double* inner_tolerance, const int* inner_iterations,
+               const double* x0, const double* omega, int n_omega, double* resvec,
+               int resvec_len, const int* inner_precision, double* x) {
+  using W = typename traits<T>::wide;
+  REQUIRE(A && b && x, "qmridr: A, b and x are required");
+  REQUIRE(s >= 1, "qmridr: s must be positive");
+  if (s > MAXS) throw unsupported_error("qmridr: s > 16 is not supported by the GPU path");
+  SolveOpts o;
+  if (tolerance) {
+    REQUIRE(*tolerance >= 0, "Illegal value for parameter tolerance");
+    o.tol = *tolerance;
+  }
+  const long n = A->n();
+  o.maxit = maximum_iterations ? *maximum_iterations : (int)std::min<long>(2 * n, 1000);
+  o.in_s = inner_s ? *inner_s : 4;
+  REQUIRE(o.in_s >= 1, "Illegal value for parameter inner_s");
+  if (o.in_s > MAXS) throw unsupported_error("qmridr: inner_s > 16 is not supported by the GPU path");
+  o.in_tol = inner_tolerance ? *inner_tolerance : kInnerTolDefault;
+  REQUIRE(o.in_tol >= 0, "Illegal value for parameter inner_tolerance");
+  o.in_it = inner_iterations ? *inner_iterations : 0;
+  o.in_prec = inner_precision ? *inner_precision : 64;
+  REQUIRE(o.in_prec == 64 || o.in_prec == 32, "inner_precision must be 64 or 32");
+  if (flag) *flag = -1;
+  if (relres) *relres = 1.0;
+  if (iterations) *iterations = 0;
+  if (resvec) REQUIRE(o.maxit + 1 <= resvec_len, "Length of vector with residual norms too small, should be maxit+1");
+  cudaStream_t st = A->stream;
+  Staged sv(A, sizeof(T) * n);
+  const T* d_b = (const T*)sv.in(b);
+  const T* d_x0 = (const T*)sv.in(x0);
+  T* d_x = (T*)sv.out(x);
+  DBuf d_res, d_om;
+  if (resvec) { d_res = DBuf(sizeof(double) * resvec_len, st); IDRS_CUDA(cudaMemsetAsync(d_res.p, 0, sizeof(double) * resvec_len, st)); }
+  if (omega && n_omega > 0) {
+    d_om = DBuf(sizeof(W) * n_omega, st);
+    IDRS_CUDA(cudaMemcpyAsync(d_om.p, omega, sizeof(W) * n_omega, cudaMemcpyHostToDevice, st));
+  }
+  o.M1 = M1;
+  o.x0 = d_x0;
+  o.omega = d_om.p;
+  o.n_omega = n_omega;
+  o.resvec = d_res.as<double>();
+  o.resvec_len = resvec_len;
+  o.PT = find_shadow(A, s);
+  if (o.in_it > 0 && o.in_prec == 32) run_qmr_typed<T, Tlow>(A, s, d_b, d_x, o, flag, relres, iterations);
+  else run_qmr_typed<T, T>(A, s, d_b, d_x, o, flag, relres, iterations);
+  sv.finish(x, d_x);
+  if (resvec) IDRS_CUDA(cudaMemcpyAsync(resvec, d_res.p, sizeof(double) * resvec_len, cudaMemcpyDeviceToHost, st));
+  IDRS_CUDA(cudaStreamSynchronize(st));
+  return IDRS_OK;
+}
+
+template <class W> struct TStoreVals {
+  W* out; int cnt;
+  __device__ void operator()(const W* v) const { for (int q = 0; q < cnt; ++q) out[q] = v[q]; }
+};
+template <class T>
+struct BDotc {
+  const T* u; const T* v;
+  using Shared = NoShared;
+  __device__ void prepare(Shared&) const {}
+  template <int ND, class A>
+  __device__ void operator()(long i, Shared&, A (&acc)[ND]) const { acc_add(acc[0], conj_(u[i]) * v[i]); }
+};
+
+static int precon_common(int which, idrs_user_matrix K, c128 shift, bool want_cplx, idrs_user_matrix* P) {
+  REQUIRE(K && P, "real_precon: bad arguments");
+  if (which != 0 && which != 1) throw unsupported_error("precon: only which_precon 0 and 1 (diagonal scaling) are supported");
+  auto* M = new idrs_user_matrix_s();
+  M->format = FMT_CDS;
+  M->which_precon = which;
+  M->nrows = K->nrows;
+  M->ncols = K->ncols;
+  if (which == 1) {
+    if (K->format == FMT_STENCIL7) {
+      M->diag_uniform = true;
+      c128 d(K->st[0], 0.0);
+      if (d == c128(0.0)) d = c128(1.0);
+      M->diag_u = d - shift;
+      M->diag_cplx = (M->diag_u.y != 0.0);
+    } else {
+      bool cplx = false;
+      M->diag = make_diagonal(*K, want_cplx || shift.y != 0.0, shift, &cplx);
+      M->diag_cplx = cplx;
+    }
+  }
+  *P = M;
+  return IDRS_OK;
+}
+
+static int diag_out(idrs_user_matrix K, double* D, bool cplx) {
+  REQUIRE(K && D, "diagonal: bad arguments");
+  int n = K->nrows;
+  if (K->format == FMT_STENCIL7) {
+    for (int i = 0; i < n; ++i) {
+      double d = K->st[0] == 0.0 ? 1.0 : K->st[0];
+      if (cplx) { D[2 * i] = d; D[2 * i + 1] = 0.0; } else D[i] = d;
+    }
+    return IDRS_OK;
+  }
+  bool is_c = false;
+  void* d = make_diagonal(*K, cplx, c128(0.0), &is_c);
+  if (!cplx && is_c) { cudaFree(d); throw arg_error("real_diagonal of a complex matrix"); }
+  IDRS_CUDA(cudaMemcpy(D, d, (cplx ? 16 : 8) * (size_t)n, cudaMemcpyDeviceToHost));
+  cudaFree(d);
+  return IDRS_OK;
+}
+
+static int user_mv(idrs_user_matrix K, const double* v, double* w, bool cplx) {
+  REQUIRE(K && v && w, "user_mv: bad arguments");
+  MatView M = K->view64();
+  size_t vb = (cplx ? 16 : 8) * (size_t)K->ncols, wb = (cplx ? 16 : 8) * (size_t)K->nrows;
+  void *dv = upload(v, vb), *dw = nullptr;
+  IDRS_CUDA(cudaMalloc(&dw, std::max<size_t>(wb, 16)));
+  if (cplx) spmv<c128>(M, (const c128*)dv, (c128*)dw, c128(1.0), c128(0.0), nullptr, nullptr, nullptr);
+  else spmv<double>(M, (const double*)dv, (double*)dw, 1.0, 0.0, nullptr, nullptr, nullptr);
+  IDRS_CUDA(cudaMemcpy(w, dw, wb, cudaMemcpyDeviceToHost));
+  cudaFree(dv);
+  cudaFree(dw);
+  return IDRS_OK;
+}
+
+static int ms_parameters(idrs_matrix A, int n_sigma, const double* sigma, double* sigma_p, bool cplx) {
+  REQUIRE(A && sigma && sigma_p && n_sigma >= 1, "ms_parameters: bad arguments");
+  REQUIRE(A->cplx == cplx, "ms_parameters: real/complex mismatch");
+  int d = A->degree;
+  A->n_sigma = n_sigma;
+  A->alpha_s.assign((size_t)(d + 1) * n_sigma, c128(0.0));
+  for (int i = 0; i < n_sigma; ++i) {
+    cd ss = (cplx ? cd(sigma[2 * i], sigma[2 * i + 1]) : cd(sigma[i], 0.0)) - cd(A->seed.x, A->seed.y);
+    cd sp;
+    if (d > 0) {
+      std::vector<cd> as(d + 1);
+      as[d] = cd(A->alpha_p[d].x, A->alpha_p[d].y);
+      for (int k = d - 1; k >= 0; --k) as[k] = cd(A->alpha_p[k].x, A->alpha_p[k].y) + ss * as[k + 1];
+      for (int k = 0; k <= d; ++k) A->alpha_s[k + (size_t)(d + 1) * i] = c128(as[k].real(), as[k].imag());
+      sp = ss * as[0];
+    } else {
+      sp = ss;
+    }
+    if (cplx) { sigma_p[2 * i] = sp.real(); sigma_p[2 * i + 1] = sp.imag(); }
+    else sigma_p[i] = sp.real();
+  }
+  return IDRS_OK;
+}
+
+template <class T>
+static int matvec_t(idrs_matrix A, const double* v, double* w) {
+  REQUIRE(A && v && w, "matvec: bad arguments");
+  long n = A->n();
+  Staged sv(A, sizeof(T) * n);
+  const T* dv = (const T*)sv.in(v);
+  T* dw = (T*)sv.out(w);
+  DBuf t1(sizeof(T) * n, A->stream), t2(sizeof(T) * n, A->stream);
+  op_chain<T>(A->view(64), A->alpha_p, A->degree, dv, dw, t1.as<T>(), t2.as<T>(), nullptr, A->stream, T(1), T(0), nullptr);
+  sv.finish(w, dw);
+  IDRS_CUDA(cudaStreamSynchronize(A->stream));
+  return IDRS_OK;
+}
+
+template <class T>
+static int precon_t(idrs_matrix A, const double* v, double* w) {
+  REQUIRE(A && v && w, "precon: bad arguments");
+  long n = A->n();
+  Staged sv(A, sizeof(T) * n);
+  const T* dv = (const T*)sv.in(v);
+  T* dw = (T*)sv.out(w);
+  op_precon<T>(*A, 64, dv, dw, nullptr, A->stream);
+  sv.finish(w, dw);
+  IDRS_CUDA(cudaStreamSynchronize(A->stream));
+  return IDRS_OK;
+}
+
+template <class T>
+static int scaleback_t(idrs_matrix A, const double* y, double* x) {
+  REQUIRE(A && y && x, "scaleback: bad arguments");
+  long n = A->n();
+  Staged sv(A, sizeof(T) * n);
+  const T* dy = (const T*)sv.in(y);
+  T* dx = (T*)sv.out(x);
+  DBuf t1(sizeof(T) * n, A->stream), t2(sizeof(T) * n, A->stream);
+  op_scaleback<T>(*A, 64, A->alpha_p, A->degree, dy, dx, t1.as<T>(), t2.as<T>(), nullptr, A->stream);
+  sv.finish(x, dx);
+  IDRS_CUDA(cudaStreamSynchronize(A->stream));
+  return IDRS_OK;
+}
+
+template <class T>
+static int ms_scaleback_t(idrs_matrix A, int n_sigma, const double* y, double* x) {
+  REQUIRE(A && y && x && n_sigma >= 1, "ms_scaleback: bad arguments");
+  REQUIRE(A->degree == 0 || A->n_sigma == n_sigma, "ms_scaleback: call ms_parameters with these shifts first");
+  long n = A->n();
+  Staged sv(A, sizeof(T) * n * n_sigma);
+  const T* dy = (const T*)sv.in(y);
+  T* dx = (T*)sv.out(x);
+  DBuf t1(sizeof(T) * n, A->stream), t2(sizeof(T) * n, A->stream);
+  int d = A->degree;
+  for (int i = 0; i < n_sigma; ++i) {
+    std::vector<c128> al(A->alpha_s.begin() + (size_t)(d + 1) * i, A->alpha_s.begin() + (size_t)(d + 1) * (i + 1));
+    if (d == 0) al.assign(1, c128(1.0));
+    op_scaleback<T>(*A, 64, al, d, dy + n * i, dx + n * i, t1.as<T>(), t2.as<T>(), nullptr, A->stream);
+  }
+  sv.finish(x, dx);
+  IDRS_CUDA(cudaStreamSynchronize(A->stream));
+  return IDRS_OK;
+}
+
+template <class T>
+static int norm_t(idrs_matrix A, const double* u, const double* v, double* out, bool dot) {
+  using W = typename traits<T>::wide;
+  REQUIRE(A && u && out && (!dot || v), "norm/inprod: bad arguments");
+  long n = A->n();
+  Staged sv(A, sizeof(T) * n);
+  const T* du = (const T*)sv.in(u);
+  const T* dv = dot ? (const T*)sv.in(v) : nullptr;
+  DBuf res(sizeof(W), A->stream);
+  if (dot) launch_fused<1, T>(n, BDotc<T>{du, dv}, TStoreVals<W>{res.as<W>(), 1}, A->red, nullptr, A->stream);
+  else launch_fused<1, T>(n, BNorm<T>{du}, TStoreVals<W>{res.as<W>(), 1}, A->red, nullptr, A->stream);
+  W h;
+  IDRS_CUDA(cudaMemcpyAsync(&h, res.p, sizeof(W), cudaMemcpyDeviceToHost, A->stream));
+  IDRS_CUDA(cudaStreamSynchronize(A->stream));
+  if (dot) {
+    out[0] = real_(h);
+    if (traits<T>::is_cplx) out[1] = imag_(h);
+  } else {
+    out[0] = std::sqrt(real_(h));
+  }
+  return IDRS_OK;
+}
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+int idrs_real_diagonal(idrs_user_matrix K, double* D) { return guard([&] { return diag_out(K, D, false); }); }
+
+int idrs_complex_diagonal(idrs_user_matrix K, double* D) { return guard([&] { return diag_out(K, D, true); }); }
+
+int idrs_ruser_mv(idrs_user_matrix K, const double* v, double* w) { return guard([&] { return user_mv(K, v, w, false); }); }
+
+int idrs_cuser_mv(idrs_user_matrix K, const double* v, double* w) { return guard([&] { return user_mv(K, v, w, true); }); }
+
+int idrs_real_ms_parameters(idrs_matrix A, int n_sigma, const double* sigma, double* sigma_p) {
+  return guard([&] { return ms_parameters(A, n_sigma, sigma, sigma_p, false); });
+}
+
+int idrs_complex_ms_parameters(idrs_matrix A, int n_sigma, const double* sigma, double* sigma_p) {
+  return guard([&] { return ms_parameters(A, n_sigma, sigma, sigma_p, true); });
+}
+
+int idrs_rmatvec(idrs_matrix A, const double* v, double* w) {
+  return guard([&] { REQUIRE(A && !A->cplx, "rmatvec: real handle required"); return matvec_t<double>(A, v, w); });
+}
+
+int idrs_cmatvec(idrs_matrix A, const double* v, double* w) {
+  return guard([&] { REQUIRE(A && A->cplx, "cmatvec: complex handle required"); return matvec_t<c128>(A, v, w); });
+}
+
+int idrs_rprecon(idrs_matrix A, const double* v, double* w) {
+  return guard([&] { REQUIRE(A && !A->cplx, "rprecon: real handle required"); return precon_t<double>(A, v, w); });
+}
+
+int idrs_cprecon(idrs_matrix A, const double* v, double* w) {
+  return guard([&] { REQUIRE(A && A->cplx, "cprecon: complex handle required"); return precon_t<c128>(A, v, w); });
+}
+
+int idrs_rscaleback(idrs_matrix A, const double* b, const double* y, double* x) {
+  (void)b;
+  return guard([&] { REQUIRE(A && !A->cplx, "rscaleback: real handle required"); return scaleback_t<double>(A, y, x); });
+}
+
+int idrs_cscaleback(idrs_matrix A, const double* b, const double* y, double* x) {
+  (void)b;
+  return guard([&] { REQUIRE(A && A->cplx, "cscaleback: complex handle required"); return scaleback_t<c128>(A, y, x); });
+}
+
+int idrs_ms_rscaleback(idrs_matrix A, int n_sigma, const double* sigma, const double* b,
+                       const double* y, double* x) {
+  (void)sigma; (void)b;
+  return guard([&] { REQUIRE(A && !A->cplx, "ms_rscaleback: real handle required"); return ms_scaleback_t<double>(A, n_sigma, y, x); });
+}
+
+int idrs_ms_cscaleback(idrs_matrix A, int n_sigma, const double* sigma, const double* b,
+                       const double* y, double* x) {
+  (void)sigma; (void)b;
+  return guard([&] { REQUIRE(A && A->cplx, "ms_cscaleback: complex handle required"); return ms_scaleback_t<c128>(A, n_sigma, y, x); });
+}
+
+int idrs_rnorm(idrs_matrix A, const double* w, double* norm) { return guard([&] { return norm_t<double>(A, w, nullptr, norm, false); }); }
+
+int idrs_cnorm(idrs_matrix A, const double* w, double* norm) { return guard([&] { return norm_t<c128>(A, w, nullptr, norm, false); }); }
+
+int idrs_rinprod(idrs_matrix A, const double* u, const double* v, double* uv) { return guard([&] { return norm_t<double>(A, u, v, uv, true); }); }
+
+int idrs_cinprod(idrs_matrix A, const double* u, const double* v, double* uv) { return guard([&] { return norm_t<c128>(A, u, v, uv, true); }); }
+
+const char* idrs_last_error(void) { return idrs::last_error(); }
+int idrs_version(void) { return 10000; }
+
+int idrs_crs_format(int nrows, int ncols, const int* row_ptr, const int* col_ind,
+                    const double* rval, const double* cval, idrs_user_matrix* K) {
+  return guard([&] {
+    REQUIRE(K && row_ptr && nrows >= 0 && ncols >= 0, "crs_format: bad arguments");
+    init_runtime();
+    long base = row_ptr[0];
+    long nnz = (long)row_ptr[nrows] - base;
+    REQUIRE(nnz >= 0 && (nnz == 0 || col_ind), "crs_format: bad row pointers");
+    std::vector<int> rp(nrows + 1), ci(std::max<long>(nnz, 1));
+    for (int i = 0; i <= nrows; ++i) {
+      rp[i] = (int)(row_ptr[i] - base);
+      if (i > 0) REQUIRE(rp[i] >= rp[i - 1], "crs_format: row pointers must not decrease");
+    }
+    for (long k = 0; k < nnz; ++k) {
+      int c = col_ind[k] - 1;
+      REQUIRE(c >= 0 && c < ncols, "crs_format: column index out of range");
+      ci[k] = c;
+    }
+    auto* M = new idrs_user_matrix_s();
+    M->format = FMT_CRS;
+    M->nrows = nrows;
+    M->ncols = ncols;
+    M->nnz = nnz;
+    M->row_ptr = (int*)upload(rp.data(), sizeof(int) * (nrows + 1));
+    M->col_ind = (int*)upload(ci.data(), sizeof(int) * nnz);
+    if (cval) {
+      M->vals = 2;
+      M->val = upload(cval, 16 * (size_t)nnz);
+    } else {
+      M->vals = 1;
+      if (rval) M->val = upload(rval, 8 * (size_t)nnz);
+      else {
+        std::vector<double> ones(std::max<long>(nnz, 1), 1.0);
+        M->val = upload(ones.data(), 8 * (size_t)nnz);
+      }
+    }
+    M->group = crs_group(nnz, nrows);
+    *K = M;
+    return IDRS_OK;
+  });
+}
+
+int idrs_coo_format(int nrows, int ncols, int nnz, const int* indx, const int* jndx,
+                    const double* rval, const double* cval, idrs_user_matrix* K) {
+  return guard([&] {
+    REQUIRE(K && nrows >= 0 && ncols >= 0 && nnz >= 0 && (nnz == 0 || (indx && jndx)),
+            "coo_format: bad arguments");
+    init_runtime();
+    // stable counting sort by row: rows keep the caller's order of entries
+    std::vector<int> cnt(nrows + 1, 0);
+    for (int k = 0; k < nnz; ++k) {
+      REQUIRE(indx[k] >= 1 && indx[k] <= nrows && jndx[k] >= 1 && jndx[k] <= ncols,
+              "coo_format: index out of range");
+      cnt[indx[k]]++;
+    }
+    for (int i = 0; i < nrows; ++i) cnt[i + 1] += cnt[i];
+    std::vector<int> pos(cnt.begin(), cnt.end() - 1), ci(std::max(nnz, 1));
+    size_t vs = cval ? 2 : 1;
+    std::vector<double> val(std::max<size_t>((size_t)nnz * vs, 1), 1.0);
+    for (int k = 0; k < nnz; ++k) {
+      int p = pos[indx[k] - 1]++;
+      ci[p] = jndx[k] - 1;
+      if (cval) { val[2 * p] = cval[2 * k]; val[2 * p + 1] = cval[2 * k + 1]; }
+      else if (rval) val[p] = rval[k];
+    }
+    auto* M = new idrs_user_matrix_s();
+    M->format = FMT_COO;
+    M->nrows = nrows;
+    M->ncols = ncols;
+    M->nnz = nnz;
+    M->row_ptr = (int*)upload(cnt.data(), sizeof(int) * (nrows + 1));
+    M->col_ind = (int*)upload(ci.data(), sizeof(int) * nnz);
+    M->vals = cval ? 2 : 1;
+    M->val = upload(val.data(), 8 * vs * (size_t)nnz);
+    M->group = crs_group(nnz, nrows);
+    *K = M;
+    return IDRS_OK;
+  });
+}
+
+int idrs_cds_format(int nrows, int ncols, int half_band, const double* rband, const double* cband,
+                    idrs_user_matrix* K) {
+  return guard([&] {
+    REQUIRE(K && nrows >= 0 && half_band >= 0 && half_band < std::max(nrows, 1),
+            "cds_format: bad arguments");
+    init_runtime();
+    size_t cnt = (size_t)nrows * (2 * half_band + 1);
+    auto* M = new idrs_user_matrix_s();
+    M->format = FMT_CDS;
+    M->nrows = nrows;
+    M->ncols = ncols;
+    M->half_band = half_band;
+    if (cband) { M->vals = 2; M->band = upload(cband, 16 * cnt); }
+    else {
+      M->vals = 1;
+      if (rband) M->band = upload(rband, 8 * cnt);
+      else { std::vector<double> ones(std::max<size_t>(cnt, 1), 1.0); M->band = upload(ones.data(), 8 * cnt); }
+    }
+    *K = M;
+    return IDRS_OK;
+  });
+}
+
+int idrs_dense_format(int nrows, int ncols, const double* rmat, const double* cmat,
+                      idrs_user_matrix* K) {
+  return guard([&] {
+    REQUIRE(K && nrows >= 0 && ncols >= 0 && (rmat || cmat), "dense_format: bad arguments");
+    init_runtime();
+    size_t cnt = (size_t)nrows * ncols;
+    auto* M = new idrs_user_matrix_s();
+    M->format = FMT_DENSE;
+    M->nrows = nrows;
+    M->ncols = ncols;
+    if (cmat) { M->vals = 2; M->mat = upload(cmat, 16 * cnt); }
+    else { M->vals = 1; M->mat = upload(rmat, 8 * cnt); }
+    *K = M;
+    return IDRS_OK;
+  });
+}
+
+int idrs_stencil7_format(int nx, int ny, int nz, const double* coef, idrs_user_matrix* K) {
+  return guard([&] {
+    REQUIRE(K && coef && nx >= 1 && ny >= 1 && nz >= 1, "stencil7_format: bad arguments");
+    REQUIRE((long)nx * ny * nz < (1L << 31), "stencil7_format: grid too large");
+    init_runtime();
+    auto* M = new idrs_user_matrix_s();
+    M->format = FMT_STENCIL7;
+    M->nrows = M->ncols = nx * ny * nz;
+    M->nx = nx; M->ny = ny; M->nz = nz;
+    for (int i = 0; i < 7; ++i) M->st[i] = coef[i];
+    *K = M;
+    return IDRS_OK;
+  });
+}
+
+int idrs_real_precon(int which_precon, idrs_user_matrix K, const double* shift, idrs_user_matrix* P) {
+  return guard([&] { return precon_common(which_precon, K, c128(shift ? *shift : 0.0, 0.0), false, P); });
+}
+int idrs_complex_precon(int which_precon, idrs_user_matrix K, const double* shift, idrs_user_matrix* P) {
+  return guard([&] {
+    c128 sh = shift ? c128(shift[0], shift[1]) : c128(0.0);
+    return precon_common(which_precon, K, sh, true, P);
+  });
+}
+
+int idrs_user_matrix_free(idrs_user_matrix K) {
+  return guard([&] {
+    if (K) user_matrix_release(K);
+    return IDRS_OK;
+  });
+}
+
+int idrs_matrix_create(idrs_user_matrix K, idrs_user_matrix P, int is_complex, const double* seed,
+                       idrs_matrix* A) {
+  return guard([&] {
+    REQUIRE(K && A, "matrix_create: bad arguments");
+    REQUIRE(K->nrows == K->ncols, "matrix_create: K must be square");
+    REQUIRE(!P || P->nrows == K->nrows, "matrix_create: P size mismatch");
+    init_runtime();
+    auto* M = new idrs_matrix_s();
+    M->K = K;
+    K->refcount++;
+    if (P) { M->P = P; P->refcount++; }
+    M->cplx = is_complex != 0;
+    if (seed) M->seed = M->cplx ? c128(seed[0], seed[1]) : c128(seed[0], 0.0);
+    REQUIRE(M->cplx || K->vals != 2, "matrix_create: complex matrix in a real problem");
+    IDRS_CUDA(cudaStreamCreateWithFlags(&M->stream, cudaStreamNonBlocking));
+    M->own_stream = true;
+    M->alpha_p.assign(1, c128(1.0));
+    M->red = alloc_redbuf(M->stream);
+    int st = build_operator(M);
+    if (st != 0) {
+      std::string msg = idrs::last_error();
+      operator_free(M);
+      delete M;
+      set_error(msg);
+      return st == 5 ? IDRS_ERR_UNSUPPORTED : IDRS_ERR_ARG;
+    }
+    IDRS_CUDA(cudaStreamSynchronize(M->stream));
+    *A = M;
+    return IDRS_OK;
+  });
+}
+
+int idrs_matrix_free(idrs_matrix A) {
+  return guard([&] {
+    if (A) {
+      operator_free(A);
+      delete A;
+    }
+    return IDRS_OK;
+  });
+}
+
+int idrs_matrix_set_stream(idrs_matrix A, void* cuda_stream) {
+  return guard([&] {
+    REQUIRE(A, "set_stream: bad handle");
+    IDRS_CUDA(cudaStreamSynchronize(A->stream));
+    if (A->own_stream) cudaStreamDestroy(A->stream);
+    A->stream = (cudaStream_t)cuda_stream;
+    A->own_stream = false;
+    return IDRS_OK;
+  });
+}
+
+int idrs_matrix_set_pointer_mode(idrs_matrix A, int mode) {
+  return guard([&] {
+    REQUIRE(A && (mode == IDRS_POINTER_HOST || mode == IDRS_POINTER_DEVICE), "set_pointer_mode: bad arguments");
+    A->device_pointers = (mode == IDRS_POINTER_DEVICE);
+    return IDRS_OK;
+  });
+}
+
+int idrs_matrix_set_shadow(idrs_matrix A, int s, const double* PT) {
+  return guard([&] {
+    REQUIRE(A && s >= 1, "set_shadow: bad arguments");
+    for (auto it = A->shadows.begin(); it != A->shadows.end(); ++it)
+      if (it->first == s) { cudaFree(it->second); A->shadows.erase(it); break; }
+    if (PT) {
+      size_t bytes = (A->cplx ? 16 : 8) * (size_t)s * A->n();
+      A->shadows.emplace_back(s, upload(PT, bytes));
+    }
+    return IDRS_OK;
+  });
+}
+
+int idrs_real_preconditioner(idrs_matrix A, int preconditioner, int degree, const double* foci,
+                             const double* center, const double* H, int ldh, int nh) {
+  return guard([&] {
+    REQUIRE(A && !A->cplx, "real_preconditioner: real matrix handle required");
+    return set_preconditioner(A, preconditioner, degree, foci, center, H, ldh, nh);
+  });
+}
+int idrs_complex_preconditioner(idrs_matrix A, int preconditioner, int degree, const double* foci,
+                                const double* center, const double* H, int ldh, int nh) {
+  return guard([&] {
+    REQUIRE(A && A->cplx, "complex_preconditioner: complex matrix handle required");
+    return set_preconditioner(A, preconditioner, degree, foci, center, H, ldh, nh);
+  });
+}
+
+int idrs_matrix_get_alpha(idrs_matrix A, double* alpha, int* degree) {
+  return guard([&] {
+    REQUIRE(A, "get_alpha: bad handle");
+    if (degree) *degree = A->degree;
+    if (alpha)
+      for (int i = 0; i <= A->degree; ++i) {
+        if (A->cplx) { alpha[2 * i] = A->alpha_p[i].x; alpha[2 * i + 1] = A->alpha_p[i].y; }
+        else alpha[i] = A->alpha_p[i].x;
+      }
+    return IDRS_OK;
+  });
+}
+
+int idrs_time_matvec(idrs_matrix A, int prec, int warmup, int reps, double* ms_per_product,
+                     double* ms_per_launch) {
+  return guard([&] {
+    REQUIRE(A && (prec == 64 || prec == 32) && reps >= 1 && warmup >= 0, "time_matvec: bad arguments");
+    long n = A->n();
+    cudaStream_t st = A->stream;
+    size_t es = (A->cplx ? 2 : 1) * (prec == 64 ? 8 : 4);
+    DBuf v(es * n, st), w(es * n, st), t1(es * n, st), t2(es * n, st);
+    IDRS_CUDA(cudaMemsetAsync(v.p, 0, es * n, st));
+    const MatView& M = A->view(prec);
+    auto once = [&] {
+      if (prec == 64 && !A->cplx)
+        op_chain<double>(M, A->alpha_p, A->degree, v.as<double>(), w.as<double>(), t1.as<double>(), t2.as<double>(), nullptr, st, 1.0, 0.0, nullptr);
+      else if (prec == 32 && !A->cplx)
+        op_chain<float>(M, A->alpha_p, A->degree, v.as<float>(), w.as<float>(), t1.as<float>(), t2.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
+      else if (prec == 64)
+        op_chain<c128>(M, A->alpha_p, A->degree, v.as<c128>(), w.as<c128>(), t1.as<c128>(), t2.as<c128>(), nullptr, st, c128(1.0), c128(0.0), nullptr);
+      else
+        op_chain<c64>(M, A->alpha_p, A->degree, v.as<c64>(), w.as<c64>(), t1.as<c64>(), t2.as<c64>(), nullptr, st, c64(1.0f), c64(0.0f), nullptr);
+    };
+    for (int i = 0; i < warmup; ++i) once();
+    cudaEvent_t e0, e1;
+    IDRS_CUDA(cudaEventCreate(&e0));
+    IDRS_CUDA(cudaEventCreate(&e1));
+    IDRS_CUDA(cudaEventRecord(e0, st));
+    for (int i = 0; i < reps; ++i) once();
+    IDRS_CUDA(cudaEventRecord(e1, st));
+    IDRS_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    IDRS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms_per_product) *ms_per_product = ms / reps;
+    if (ms_per_launch) *ms_per_launch = ms / reps / (A->degree + 1);
+    return IDRS_OK;
+  });
+}
+
+int idrs_ridrs(idrs_matrix A, const double* b, int s, idrs_matrix M1, const double* tolerance,
+               const int* maximum_iterations, const int* variant, int* flag, double* relres,
+               int* iterations, const double* x0, const double* U0, const double* omega,
+               int n_omega, double* resvec, int resvec_len, double* H, int ldh, int nritz,
+               double* x) {
+  return guard([&] {
+    REQUIRE(A && !A->cplx, "ridrs: real matrix handle required");
+    return run_idrs<double>(A, b, s, M1, tolerance, maximum_iterations, variant, flag, relres,
+                            iterations, x0, U0, omega, n_omega, resvec, resvec_len, H, ldh, nritz, x);
+  });
+}
+int idrs_cidrs(idrs_matrix A, const double* b, int s, idrs_matrix M1, const double* tolerance,
+               const int* maximum_iterations, const int* variant, int* flag, double* relres,
+               int* iterations, const double* x0, const double* U0, const double* omega,
+               int n_omega, double* resvec, int resvec_len, double* H, int ldh, int nritz,
+               double* x) {
+  return guard([&] {
+    REQUIRE(A && A->cplx, "cidrs: complex matrix handle required");
+    return run_idrs<c128>(A, b, s, M1, tolerance, maximum_iterations, variant, flag, relres,
+                          iterations, x0, U0, omega, n_omega, resvec, resvec_len, H, ldh, nritz, x);
+  });
+}
+
+int idrs_rqmridr(idrs_matrix A, const double* b, int s, idrs_matrix M1, const double* tolerance,
+                 const int* maximum_iterations, int* flag, double* relres, int* iterations,
+                 const int* inner_s, const double* inner_tolerance, const int* inner_iterations,
+                 const double* x0, const double* omega, int n_omega, double* resvec,
+                 int resvec_len, const int* inner_precision, double* x) {
+  return guard([&] {
+    REQUIRE(A && !A->cplx, "rqmridr: real matrix handle required");
+    return run_qmridr<double, float>(A, b, s, M1, tolerance, maximum_iterations, flag, relres,
+                                     iterations, inner_s, inner_tolerance, inner_iterations, x0,
+                                     omega, n_omega, resvec, resvec_len, inner_precision, x);
+  });
+}
+int idrs_cqmridr(idrs_matrix A, const double* b, int s, idrs_matrix M1, const double* tolerance,
+                 const int* maximum_iterations, int* flag, double* relres, int* iterations,
+                 const int* inner_s, const double* inner_tolerance, const int* inner_iterations,
+                 const double* x0, const double* omega, int n_omega, double* resvec,
+                 int resvec_len, const int* inner_precision, double* x) {
+  return guard([&] {
+    REQUIRE(A && A->cplx, "cqmridr: complex matrix handle required");
+    return run_qmridr<c128, c64>(A, b, s, M1, tolerance, maximum_iterations, flag, relres,
+                                 iterations, inner_s, inner_tolerance, inner_iterations, x0,
+                                 omega, n_omega, resvec, resvec_len, inner_precision, x);
+  });
+}
+
+int idrs_ridrs_ritz(idrs_matrix A, const double* b, int s, const double* tolerance,
+                    const int* maximum_iterations, int* flag, double* relres, int* iterations,
+                    const double* x0, double* H, int ldh, int nh, int* nritz, double* x) {
+  return guard([&] {
+    REQUIRE(A && !A->cplx && b && x, "ridrs_ritz: bad arguments");
+    long n = A->n();
+    int maxit = maximum_iterations ? *maximum_iterations : (int)std::min<long>(2 * n, 1000);
+    REQUIRE(maxit >= 1, "ridrs_ritz: maximum_iterations must be positive");
+    std::vector<double> Hf((size_t)(maxit + 1) * maxit, 0.0);
+    std::vector<double> zeros;
+    const double* xs = x0;
+    if (!xs && !A->device_pointers) { zeros.assign(n, 0.0); xs = zeros.data(); }
+    int conv = -1, iter = 0, one = 1;
+    double rel = 1.0;
+    std::vector<double> resnrm(maxit + 1);
+    int st = run_idrs<double>(A, b, s, nullptr, tolerance, &maxit, &one, &conv, &rel, &iter, xs,
+                              nullptr, nullptr, 0, resnrm.data(), maxit + 1, Hf.data(), maxit + 1,
+                              maxit, x);
+    if (st) return st;
+    if (flag) *flag = conv;
+    if (relres) *relres = rel;
+    if (iterations) *iterations = iter;
+    if (nritz) *nritz = (iter / (s + 1)) * s + iter % (s + 1);
+    if (H) {
+      REQUIRE((long)ldh * nh <= (long)(maxit + 1) * maxit && ldh <= maxit + 1 && nh <= maxit,
+              "Dimensions of Hessenberg matrix too large");
+      for (int j = 0; j < nh; ++j)
+        for (int i = 0; i < ldh; ++i) H[i + (size_t)ldh * j] = Hf[i + (size_t)(maxit + 1) * j];
+    }
+    return IDRS_OK;
+  });
+}
+
+int idrs_rpp_idrs(idrs_user_matrix K, const double* b, idrs_user_matrix P, const double* center,
+                  const double* foci, const idrs_pp_options* opt, idrs_pp_report* report,
+                  double* x) {
+  return guard([&] {
+    REQUIRE(K && b && opt && x, "rpp_idrs: bad arguments");
+    using clk = std::chrono::steady_clock;
+    auto t0 = clk::now();
+    idrs_matrix A = nullptr;
+    int st = idrs_matrix_create(K, P, 0, nullptr, &A);
+    if (st) return st;
+    std::unique_ptr<idrs_matrix_s, int (*)(idrs_matrix)> guardA(A, idrs_matrix_free);
+    long n = A->n();
+    const int s = opt->s;
+    REQUIRE(s >= 1, "rpp_idrs: s must be positive");
+    int preconditioner = opt->degree == 0 ? 0 : opt->preconditioner;
+    bool estimate = preconditioner != 0;
+    if (preconditioner == 1 && center) estimate = false;
+    if (preconditioner == 2 && foci) estimate = false;
+    cudaStream_t cs = A->stream;
+    DBuf d_b(8 * n, cs), d_x0(8 * n, cs), d_y(8 * n, cs), d_x(8 * n, cs);
+    IDRS_CUDA(cudaMemcpyAsync(d_b.p, b, 8 * n, cudaMemcpyHostToDevice, cs));
+    IDRS_CUDA(cudaMemsetAsync(d_x0.p, 0, 8 * n, cs));
+    A->device_pointers = true;
+    idrs_pp_report rep{};
+    double tol = opt->tol;
+    if (estimate) {
+      int ini_iter = opt->n_ritz + opt->n_ritz / s;
+      int ldh = ini_iter + 1;
+      std::vector<double> H((size_t)ldh * ini_iter, 0.0);
+      int flag = -1, iter = 0, nr = 0;
+      double rel = 1;
+      st = idrs_ridrs_ritz(A, d_b.as<double>(), s, &tol, &ini_iter, &flag, &rel, &iter,
+                           d_x0.as<double>(), H.data(), ldh, ini_iter, &nr, d_x0.as<double>());
+      if (st) return st;
+      rep.ritz_iterations = iter;
+      rep.nritz = nr;
+      analyse_spectrum(H.data(), ldh, nr, rep.foci, &rep.center, nullptr);
+      set_preconditioner(A, preconditioner, opt->degree, nullptr, nullptr, H.data(), ldh, nr);
+    } else {
+      double f[2] = {0.15, 1.85}, c = 1.0;
+      if (foci) { f[0] = foci[0]; f[1] = foci[1]; }
+      if (center) c = *center;
+      rep.foci[0] = f[0]; rep.foci[1] = f[1]; rep.center = c;
+      set_preconditioner(A, preconditioner, opt->degree, f, &c, nullptr, 0, 0);
+    }
+    IDRS_CUDA(cudaStreamSynchronize(cs));
+    auto t1 = clk::now();
+    int maxit = opt->maxit;
+    if (opt->method == 0) {
+      int in_s = opt->in_s, in_it = opt->in_it, prec = opt->inner_precision ? opt->inner_precision : 64;
+      double in_tol = opt->in_tol;
+      st = idrs_rqmridr(A, d_b.as<double>(), s, nullptr, &tol, &maxit, &rep.flag, &rep.relres_solver,
+                        &rep.iterations, &in_s, &in_tol, &in_it, d_x0.as<double>(), nullptr, 0,
+                        nullptr, 0, &prec, d_y.as<double>());
+    } else {
+      int variant = opt->method == 2 ? 2 : 1;
+      st = idrs_ridrs(A, d_b.as<double>(), s, nullptr, &tol, &maxit, &variant, &rep.flag,
+                      &rep.relres_solver, &rep.iterations, d_x0.as<double>(), nullptr, nullptr, 0,
+                      nullptr, 0, nullptr, 0, 0, d_y.as<double>());
+    }
+    if (st) return st;
+    // x = scaleback(A, b, y); relres on the original system (run_idrs.inc:113-120)
+    DBuf t1b(8 * n, cs), t2b(8 * n, cs), r(8 * n, cs), res(8, cs);
+    op_scaleback<double>(*A, 64, A->alpha_p, A->degree, d_y.as<double>(), d_x.as<double>(),
+                         t1b.as<double>(), t2b.as<double>(), nullptr, cs);
+    spmv<double>(A->k64, d_x.as<double>(), r.as<double>(), -1.0, 1.0, d_b.as<double>(), nullptr, cs);
+    launch_fused<1, double>(n, BNorm<double>{r.as<double>()}, TStoreVals<double>{res.as<double>(), 1}, A->red, nullptr, cs);
+    double rr = 0, bb = 0;
+    IDRS_CUDA(cudaMemcpyAsync(&rr, res.p, 8, cudaMemcpyDeviceToHost, cs));
+    launch_fused<1, double>(n, BNorm<double>{d_b.as<double>()}, TStoreVals<double>{res.as<double>(), 1}, A->red, nullptr, cs);
+    IDRS_CUDA(cudaStreamSynchronize(cs));
+    IDRS_CUDA(cudaMemcpyAsync(&bb, res.p, 8, cudaMemcpyDeviceToHost, cs));
+    IDRS_CUDA(cudaMemcpyAsync(x, d_x.p, 8 * n, cudaMemcpyDeviceToHost, cs));
+    IDRS_CUDA(cudaStreamSynchronize(cs));
+    rep.relres_original = std::sqrt(rr) / std::sqrt(bb);
+    auto t2 = clk::now();
+    rep.seconds_setup = std::chrono::duration<double>(t1 - t0).count();
+    rep.seconds_solve = std::chrono::duration<double>(t2 - t1).count();
+    rep.seconds_total = std::chrono::duration<double>(t2 - t0).count();
+    if (report) *report = rep;
+    return IDRS_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,668 @@
+// matrix.cu -- SpMV kernels (stencil, CRS, CDS, dense), the scaled operator
+// build and the Horner chain of the polynomial preconditioner.
+#include <algorithm>
+#include <mutex>
+
+#include "matrix.cuh"
+
+namespace idrs {
+
+// ---------------------------------------------------------------------------
+// runtime basics
+// ---------------------------------------------------------------------------
+static thread_local std::string g_error;
+void set_error(const std::string& msg) { g_error = msg; }
+const char* last_error() { return g_error.c_str(); }
+
+int num_sms() {
+  static int sms = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+      sms = 152;
+  });
+  return sms;
+}
+
+RedBuf alloc_redbuf(cudaStream_t st) {
+  RedBuf rb{nullptr, nullptr};
+  IDRS_CUDA(cudaMallocAsync((void**)&rb.ticket, sizeof(unsigned int) * 32, st));
+  IDRS_CUDA(cudaMemsetAsync(rb.ticket, 0, sizeof(unsigned int) * 32, st));
+  IDRS_CUDA(cudaMallocAsync(&rb.partials, (size_t)kMaxRedBlocks * kMaxND * sizeof(c128), st));
+  return rb;
+}
+void free_redbuf(RedBuf rb, cudaStream_t st) {
+  if (rb.ticket) cudaFreeAsync(rb.ticket, st);
+  if (rb.partials) cudaFreeAsync(rb.partials, st);
+}
+
+// ---------------------------------------------------------------------------
+// small generic helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double shfl_x(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ float shfl_x(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ c128 shfl_x(c128 v, int m) { return c128(shfl_x(v.x, m), shfl_x(v.y, m)); }
+__device__ __forceinline__ c64 shfl_x(c64 v, int m) { return c64(shfl_x(v.x, m), shfl_x(v.y, m)); }
+
+template <class V, class T> __device__ __forceinline__ T mulvt(V a, T b) { return a * b; }
+
+MatView UserMatrix::view64() const {
+  MatView v;
+  v.format = format;
+  v.nrows = nrows;
+  v.ncols = ncols;
+  v.nnz = nnz;
+  v.rp = row_ptr;
+  v.ci = col_ind;
+  v.hb = half_band;
+  v.nx = nx; v.ny = ny; v.nz = nz;
+  for (int i = 0; i < 7; ++i) v.st[i] = st[i];
+  v.vcplx = (vals == 2);
+  v.group = group;
+  if (format == FMT_CRS || format == FMT_COO) v.val = val;
+  else if (format == FMT_CDS) v.val = band;
+  else if (format == FMT_DENSE) v.val = mat;
+  return v;
+}
+
+long UserMatrix::bytes() const {
+  size_t vs = (vals == 2) ? 16 : 8;
+  switch (format) {
+    case FMT_CRS: case FMT_COO: return (long)(4 * (nrows + 1) + nnz * (4 + vs));
+    case FMT_CDS: return (long)nrows * (2 * half_band + 1) * vs;
+    case FMT_DENSE: return (long)nrows * ncols * vs;
+    default: return 0;
+  }
+}
+
+void user_matrix_release(UserMatrix* K) {
+  if (!K) return;
+  if (--K->refcount > 0) return;
+  cudaFree(K->row_ptr); cudaFree(K->col_ind); cudaFree(K->val); cudaFree(K->band);
+  cudaFree(K->mat); cudaFree(K->diag);
+  delete K;
+}
+
+// ---------------------------------------------------------------------------
+// SpMV kernels.  All compute y = a * (M x) + cv * v and return at once when
+// *skip is non-zero (solver already stopped on the device).
+// ---------------------------------------------------------------------------
+
+// Matrix-free 7-point stencil (E/STENCIL/user_module.f90:155-160): 2-D thread
+// tiles in x-y march along z keeping x(z-1), x(z), x(z+1) in registers; the
+// x/y neighbours come from L1/L2.  Dirichlet zero outside the grid.
+template <class T, class R>
+__global__ void __launch_bounds__(256) k_stencil7(int nx, int ny, int nz, int zc, R c0, R cw, R ce,
+                                                  R cs, R cn, R cf, R cb, const T* __restrict__ x,
+                                                  T* __restrict__ y, T a, T cv,
+                                                  const T* __restrict__ v,
+                                                  const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const int z0 = blockIdx.z * zc;
+  const int z1 = min(nz, z0 + zc);
+  const long plane = (long)nx * ny;
+  long p = i + (long)nx * (j + (long)ny * z0);
+  T xm = z0 > 0 ? x[p - plane] : T(0);
+  T xc = x[p];
+  for (int z = z0; z < z1; ++z, p += plane) {
+    T xp = (z + 1 < nz) ? x[p + plane] : T(0);
+    T xw = i > 0 ? x[p - 1] : T(0);
+    T xe = i < nx - 1 ? x[p + 1] : T(0);
+    T xs = j > 0 ? x[p - nx] : T(0);
+    T xn = j < ny - 1 ? x[p + nx] : T(0);
+    T s = c0 * xc + cw * xw + ce * xe + cs * xs + cn * xn + cf * xm + cb * xp;
+    T out = a * s;
+    if (v) out = out + cv * v[p];
+    y[p] = out;
+    xm = xc;
+    xc = xp;
+  }
+}
+
+// CRS, G lanes per row (G | 32).  Warp-uniform loop so the shuffles are
+// always executed by the full warp.
+template <int G, class T, class V>
+__global__ void __launch_bounds__(256) k_crs(int nrows, const int* __restrict__ rp,
+                                             const int* __restrict__ ci, const V* __restrict__ val,
+                                             const T* __restrict__ x, T* __restrict__ y, T a, T cv,
+                                             const T* __restrict__ v,
+                                             const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  constexpr int RPW = 32 / G;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / G;
+  const int gl = lane & (G - 1);
+  const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const long nwarps = (gridDim.x * (long)blockDim.x) >> 5;
+  for (long base = warp * RPW; base < nrows; base += nwarps * RPW) {
+    const long row = base + sub;
+    T sum = T(0);
+    if (row < nrows) {
+      const int beg = rp[row], end = rp[row + 1];
+      for (int k = beg + gl; k < end; k += G) sum = sum + mulvt(val[k], x[ci[k]]);
+    }
+#pragma unroll
+    for (int m = G / 2; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
+    if (row < nrows && gl == 0) {
+      T out = a * sum;
+      if (v) out = out + cv * v[row];
+      y[row] = out;
+    }
+  }
+}
+
+// CDS: w(i) = sum_d band(i,d) * x(i+d)  (user_module.f90:728-733)
+template <class T, class V>
+__global__ void __launch_bounds__(256) k_cds(int n, int hb, const V* __restrict__ band,
+                                             const T* __restrict__ x, T* __restrict__ y, T a, T cv,
+                                             const T* __restrict__ v, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x) {
+    T s = T(0);
+    for (int d = -hb; d <= hb; ++d) {
+      long j = i + d;
+      if (j >= 0 && j < n) s = s + mulvt(band[i + (long)n * (d + hb)], x[j]);
+    }
+    T out = a * s;
+    if (v) out = out + cv * v[i];
+    y[i] = out;
+  }
+}
+
+// Dense column-major (user_module.f90:587-606), one thread per row.
+template <class T, class V>
+__global__ void __launch_bounds__(256) k_dense(int nrows, int ncols, const V* __restrict__ mat,
+                                               const T* __restrict__ x, T* __restrict__ y, T a,
+                                               T cv, const T* __restrict__ v,
+                                               const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nrows; i += gridDim.x * (long)blockDim.x) {
+    T s = T(0);
+    for (long j = 0; j < ncols; ++j) s = s + mulvt(mat[i + (long)nrows * j], x[j]);
+    T out = a * s;
+    if (v) out = out + cv * v[i];
+    y[i] = out;
+  }
+}
+
+template <class T, class V>
+static void launch_crs(const MatView& M, const V* val, const T* x, T* y, T a, T cv, const T* v,
+                       const int* skip, cudaStream_t st) {
+  long rows_per_block = kThreads / M.group;
+  long need = (M.nrows + rows_per_block - 1) / rows_per_block;
+  int grid = (int)std::max(1L, std::min(need, (long)num_sms() * 8));
+  switch (M.group) {
+    case 2: k_crs<2><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip); break;
+    case 4: k_crs<4><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip); break;
+    case 8: k_crs<8><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip); break;
+    case 16: k_crs<16><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip); break;
+    default: k_crs<32><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip); break;
+  }
+}
+
+template <class T, class V>
+static void launch_valued(const MatView& M, const V* val, const T* x, T* y, T a, T cv, const T* v,
+                          const int* skip, cudaStream_t st) {
+  switch (M.format) {
+    case FMT_CRS:
+    case FMT_COO:
+      launch_crs<T, V>(M, val, x, y, a, cv, v, skip, st);
+      break;
+    case FMT_CDS:
+      k_cds<T, V><<<stream_grid(M.nrows), kThreads, 0, st>>>(M.nrows, M.hb, val, x, y, a, cv, v, skip);
+      break;
+    case FMT_DENSE:
+      k_dense<T, V><<<stream_grid(M.nrows), kThreads, 0, st>>>(M.nrows, M.ncols, val, x, y, a, cv, v, skip);
+      break;
+    default:
+      throw std::runtime_error("spmv: unsupported format");
+  }
+}
+
+template <class T>
+static void launch_stencil(const MatView& M, const T* x, T* y, T a, T cv, const T* v,
+                           const int* skip, cudaStream_t st) {
+  using R = typename traits<T>::real;
+  dim3 blk(32, 8, 1);
+  int gx = (M.nx + 31) / 32, gy = (M.ny + 7) / 8;
+  long xy = (long)gx * gy;
+  long target = (long)num_sms() * 8;
+  int zc = (int)std::max(1L, std::min((long)M.nz, (M.nz * xy + target - 1) / target));
+  if (zc < 4 && M.nz >= 4) zc = 4;  // keep some register reuse along z
+  int gz = (M.nz + zc - 1) / zc;
+  k_stencil7<T, R><<<dim3(gx, gy, gz), blk, 0, st>>>(
+      M.nx, M.ny, M.nz, zc, R(M.st[0]), R(M.st[1]), R(M.st[2]), R(M.st[3]), R(M.st[4]),
+      R(M.st[5]), R(M.st[6]), x, y, a, cv, v, skip);
+}
+
+template <>
+void spmv<double>(const MatView& M, const double* x, double* y, double a, double cv,
+                  const double* v, const int* skip, cudaStream_t st) {
+  if (M.format == FMT_STENCIL7) launch_stencil<double>(M, x, y, a, cv, v, skip, st);
+  else if (M.vcplx) throw std::runtime_error("spmv: complex matrix applied to a real vector");
+  else launch_valued<double, double>(M, (const double*)M.val, x, y, a, cv, v, skip, st);
+  IDRS_LAUNCH_CHECK();
+}
+template <>
+void spmv<float>(const MatView& M, const float* x, float* y, float a, float cv, const float* v,
+                 const int* skip, cudaStream_t st) {
+  if (M.format == FMT_STENCIL7) launch_stencil<float>(M, x, y, a, cv, v, skip, st);
+  else if (M.vcplx) throw std::runtime_error("spmv: complex matrix applied to a real vector");
+  else launch_valued<float, float>(M, (const float*)M.val, x, y, a, cv, v, skip, st);
+  IDRS_LAUNCH_CHECK();
+}
+template <>
+void spmv<c128>(const MatView& M, const c128* x, c128* y, c128 a, c128 cv, const c128* v,
+                const int* skip, cudaStream_t st) {
+  if (M.format == FMT_STENCIL7) launch_stencil<c128>(M, x, y, a, cv, v, skip, st);
+  else if (M.vcplx) launch_valued<c128, c128>(M, (const c128*)M.val, x, y, a, cv, v, skip, st);
+  else launch_valued<c128, double>(M, (const double*)M.val, x, y, a, cv, v, skip, st);
+  IDRS_LAUNCH_CHECK();
+}
+template <>
+void spmv<c64>(const MatView& M, const c64* x, c64* y, c64 a, c64 cv, const c64* v,
+               const int* skip, cudaStream_t st) {
+  if (M.format == FMT_STENCIL7) launch_stencil<c64>(M, x, y, a, cv, v, skip, st);
+  else if (M.vcplx) launch_valued<c64, c64>(M, (const c64*)M.val, x, y, a, cv, v, skip, st);
+  else launch_valued<c64, float>(M, (const float*)M.val, x, y, a, cv, v, skip, st);
+  IDRS_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Horner chain (rpolpre + real_mv, matrix_module.f90:152-167, 266-284)
+// ---------------------------------------------------------------------------
+template <class T> static inline T narrow_c(c128 v) { return narrow<T>(v); }
+
+template <class T>
+void op_chain(const MatView& Ks, const std::vector<c128>& alpha, int degree, const T* v, T* w,
+              T* t1, T* t2, const int* skip, cudaStream_t st, T fa, T fcv, const T* fv) {
+  if (degree == 0) {
+    spmv<T>(Ks, v, w, fa, fcv, fv, skip, st);
+    return;
+  }
+  // u_{d-1} = Ks (alpha_d v) + alpha_{d-1} v
+  spmv<T>(Ks, v, t1, narrow_c<T>(alpha[degree]), narrow_c<T>(alpha[degree - 1]), v, skip, st);
+  T* cur = t1;
+  T* nxt = t2;
+  for (int k = degree - 2; k >= 0; --k) {
+    spmv<T>(Ks, cur, nxt, T(1), narrow_c<T>(alpha[k]), v, skip, st);
+    std::swap(cur, nxt);
+  }
+  spmv<T>(Ks, cur, w, fa, fcv, fv, skip, st);
+}
+
+// ---------------------------------------------------------------------------
+// elementwise kernels
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_copy(long n, const T* __restrict__ a, T* __restrict__ b, const int* skip) {
+  if (skip && *skip) return;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x) b[i] = a[i];
+}
+template <class T, class D>
+__global__ void k_scale_vec(long n, const D* __restrict__ d, const T* __restrict__ a, T* __restrict__ b,
+                            const int* skip) {
+  if (skip && *skip) return;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x)
+    b[i] = mulvt(d[i], a[i]);
+}
+template <class T>
+__global__ void k_scale_uniform(long n, T d, const T* __restrict__ a, T* __restrict__ b, const int* skip) {
+  if (skip && *skip) return;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x)
+    b[i] = d * a[i];
+}
+template <class Tin, class Tout>
+__global__ void k_convert(long n, const Tin* __restrict__ a, Tout* __restrict__ b, const int* skip) {
+  if (skip && *skip) return;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x)
+    b[i] = Tout(a[i]);
+}
+
+template <class T>
+void vec_copy(long n, const T* a, T* b, const int* skip, cudaStream_t st) {
+  if (a == b) return;
+  k_copy<T><<<stream_grid(n), kThreads, 0, st>>>(n, a, b, skip);
+  IDRS_LAUNCH_CHECK();
+}
+template <class Tin, class Tout>
+void vec_convert(long n, const Tin* a, Tout* b, const int* skip, cudaStream_t st) {
+  k_convert<Tin, Tout><<<stream_grid(n), kThreads, 0, st>>>(n, a, b, skip);
+  IDRS_LAUNCH_CHECK();
+}
+
+template <class T> struct real_of_prec;
+template <> struct real_of_prec<double> { using R = double; using C = c128; };
+template <> struct real_of_prec<c128> { using R = double; using C = c128; };
+template <> struct real_of_prec<float> { using R = float; using C = c64; };
+template <> struct real_of_prec<c64> { using R = float; using C = c64; };
+
+template <class T>
+void vec_scale_vec(long n, const void* d, bool dcplx, const T* a, T* b, const int* skip,
+                   cudaStream_t st) {
+  using R = typename real_of_prec<T>::R;
+  using C = typename real_of_prec<T>::C;
+  if constexpr (traits<T>::is_cplx) {
+    if (dcplx) k_scale_vec<T, C><<<stream_grid(n), kThreads, 0, st>>>(n, (const C*)d, a, b, skip);
+    else k_scale_vec<T, R><<<stream_grid(n), kThreads, 0, st>>>(n, (const R*)d, a, b, skip);
+  } else {
+    if (dcplx) throw std::runtime_error("complex diagonal scaling of a real vector");
+    k_scale_vec<T, R><<<stream_grid(n), kThreads, 0, st>>>(n, (const R*)d, a, b, skip);
+  }
+  IDRS_LAUNCH_CHECK();
+}
+
+template <class T>
+void op_precon(Operator& A, int prec, const T* v, T* w, const int* skip, cudaStream_t st) {
+  long n = A.n();
+  if (A.dkind == 0) {
+    vec_copy<T>(n, v, w, skip, st);
+  } else if (A.dkind == 1) {
+    k_scale_uniform<T><<<stream_grid(n), kThreads, 0, st>>>(n, narrow<T>(A.dinv_u), v, w, skip);
+    IDRS_LAUNCH_CHECK();
+  } else {
+    if (prec == 32 && !A.dinv32) A.view(32);
+    vec_scale_vec<T>(n, prec == 32 ? A.dinv32 : A.dinv64, A.dinv_cplx, v, w, skip, st);
+  }
+}
+
+template <class T>
+void op_scaleback(Operator& A, int prec, const std::vector<c128>& alpha, int degree, const T* y,
+                  T* x, T* t1, T* t2, const int* skip, cudaStream_t st) {
+  const MatView& Ks = A.view(prec);
+  long n = A.n();
+  if (degree == 0) {
+    op_precon<T>(A, prec, y, x, skip, st);
+    return;
+  }
+  T du = (A.dkind == 1) ? narrow<T>(A.dinv_u) : T(1);
+  const T* cur = y;
+  T* bufs[2] = {t1, t2};
+  int nb = 0;
+  for (int k = degree - 1; k >= 0; --k) {
+    T a = (k == degree - 1) ? narrow<T>(alpha[degree]) : T(1);
+    T cv = narrow<T>(alpha[k]);
+    T* dst;
+    if (k == 0 && A.dkind != 2) {
+      dst = x;
+      if (A.dkind == 1) { a = a * du; cv = cv * du; }
+    } else {
+      dst = bufs[nb];
+      nb ^= 1;
+    }
+    spmv<T>(Ks, cur, dst, a, cv, y, skip, st);
+    cur = dst;
+  }
+  if (A.dkind == 2) {
+    if (prec == 32 && !A.dinv32) A.view(32);
+    vec_scale_vec<T>(n, prec == 32 ? A.dinv32 : A.dinv64, A.dinv_cplx, cur, x, skip, st);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// operator build: Ks = (K - seed I) D^-1 folded into a scaled copy
+// ---------------------------------------------------------------------------
+template <class V, class D>
+__global__ void k_scale_crs(int nrows, const int* rp, const int* ci, const V* val, const D* dinv,
+                            V seed, V* out, int* missing_diag) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nrows; i += gridDim.x * (long)blockDim.x) {
+    bool found = false;
+    for (int k = rp[i]; k < rp[i + 1]; ++k) {
+      int j = ci[k];
+      V a = val ? val[k] : V(1);
+      if (j == i && !found) { a = a - seed; found = true; }
+      out[k] = dinv ? mulvt(dinv[j], a) : a;
+    }
+    if (!found && seed != V(0)) atomicAdd(missing_diag, 1);
+  }
+}
+template <class V, class D>
+__global__ void k_scale_cds(int n, int hb, const V* band, const D* dinv, V seed, V* out) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x)
+    for (int d = -hb; d <= hb; ++d) {
+      long j = i + d;
+      long k = i + (long)n * (d + hb);
+      V a = band ? band[k] : V(1);
+      if (d == 0) a = a - seed;
+      out[k] = (dinv && j >= 0 && j < n) ? mulvt(dinv[j], a) : a;
+    }
+}
+template <class V, class D>
+__global__ void k_scale_dense(int nrows, int ncols, const V* mat, const D* dinv, V seed, V* out) {
+  long tot = (long)nrows * ncols;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < tot; k += gridDim.x * (long)blockDim.x) {
+    long i = k % nrows, j = k / nrows;
+    V a = mat[k];
+    if (i == j) a = a - seed;
+    out[k] = dinv ? mulvt(dinv[j], a) : a;
+  }
+}
+template <class D>
+__global__ void k_invert(long n, const D* d, D* out) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x)
+    out[i] = D(1) / d[i];
+}
+__global__ void k_c2r(long n, const c128* a, double* b) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x) b[i] = a[i].x;
+}
+__global__ void k_r2c(long n, const double* a, c128* b) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x) b[i] = c128(a[i], 0.0);
+}
+
+template <class V, class D>
+static void scale_values(const UserMatrix& K, const void* kval, const D* dinv, V seed, V* out,
+                         cudaStream_t st, int* d_missing) {
+  switch (K.format) {
+    case FMT_CRS:
+    case FMT_COO:
+      k_scale_crs<V, D><<<stream_grid(K.nrows), kThreads, 0, st>>>(K.nrows, K.row_ptr, K.col_ind,
+                                                                   (const V*)kval, dinv, seed, out, d_missing);
+      break;
+    case FMT_CDS:
+      k_scale_cds<V, D><<<stream_grid(K.nrows), kThreads, 0, st>>>(K.nrows, K.half_band, (const V*)kval,
+                                                                   dinv, seed, out);
+      break;
+    case FMT_DENSE:
+      k_scale_dense<V, D><<<stream_grid((long)K.nrows * K.ncols), kThreads, 0, st>>>(
+          K.nrows, K.ncols, (const V*)kval, dinv, seed, out);
+      break;
+  }
+  IDRS_LAUNCH_CHECK();
+}
+
+static long value_count(const UserMatrix& K) {
+  switch (K.format) {
+    case FMT_CRS: case FMT_COO: return K.nnz;
+    case FMT_CDS: return (long)K.nrows * (2 * K.half_band + 1);
+    case FMT_DENSE: return (long)K.nrows * K.ncols;
+    default: return 0;
+  }
+}
+static const void* value_ptr(const UserMatrix& K) {
+  switch (K.format) {
+    case FMT_CRS: case FMT_COO: return K.val;
+    case FMT_CDS: return K.band;
+    case FMT_DENSE: return K.mat;
+    default: return nullptr;
+  }
+}
+
+int build_operator(Operator* A) {
+  UserMatrix& K = *A->K;
+  cudaStream_t st = A->stream;
+  long n = K.nrows;
+  if (A->ks_val64) { cudaFreeAsync(A->ks_val64, st); A->ks_val64 = nullptr; }
+  if (A->ks_val32) { cudaFreeAsync(A->ks_val32, st); A->ks_val32 = nullptr; }
+  if (A->dinv64) { cudaFreeAsync(A->dinv64, st); A->dinv64 = nullptr; }
+  if (A->dinv32) { cudaFreeAsync(A->dinv32, st); A->dinv32 = nullptr; }
+  A->k64 = K.view64();
+  A->ks64 = A->k64;
+  A->ks32 = MatView();
+  A->dkind = 0;
+  A->dinv_u = c128(1.0, 0.0);
+  A->dinv_cplx = false;
+  // diagonal scaling
+  if (A->P && A->P->which_precon == 1) {
+    UserMatrix& P = *A->P;
+    if (P.diag_uniform) {
+      A->dkind = 1;
+      A->dinv_u = c128(1.0, 0.0) / P.diag_u;
+      if (!A->cplx && A->dinv_u.y != 0.0) { set_error("complex diagonal on a real problem"); return 1; }
+    } else {
+      A->dkind = 2;
+      A->dinv_cplx = P.diag_cplx;
+      if (!A->cplx && P.diag_cplx) { set_error("complex diagonal on a real problem"); return 1; }
+      size_t es = P.diag_cplx ? 16 : 8;
+      IDRS_CUDA(cudaMallocAsync(&A->dinv64, es * n, st));
+      if (P.diag_cplx) k_invert<c128><<<stream_grid(n), kThreads, 0, st>>>(n, (const c128*)P.diag, (c128*)A->dinv64);
+      else k_invert<double><<<stream_grid(n), kThreads, 0, st>>>(n, (const double*)P.diag, (double*)A->dinv64);
+      IDRS_LAUNCH_CHECK();
+    }
+  }
+  bool seeded = (A->seed.x != 0.0 || A->seed.y != 0.0);
+  if (!A->cplx && A->seed.y != 0.0) { set_error("complex seed on a real problem"); return 1; }
+  if (K.format == FMT_STENCIL7) {
+    if (A->dkind == 2) { set_error("stencil operator: only a constant diagonal scaling is supported"); return 5; }
+    if (A->seed.y != 0.0 || A->dinv_u.y != 0.0) { set_error("stencil operator: complex seed/scaling unsupported"); return 5; }
+    double du = A->dinv_u.x;
+    A->ks64.st[0] = (K.st[0] - A->seed.x) * du;
+    for (int i = 1; i < 7; ++i) A->ks64.st[i] = K.st[i] * du;
+    return 0;
+  }
+  if (A->dkind == 0 && !seeded) return 0;  // Ks == K
+  // scaled copy of the values
+  long cnt = value_count(K);
+  bool dvec_cplx = (A->dkind == 2 && A->dinv_cplx) || (A->dkind == 1 && A->dinv_u.y != 0.0);
+  bool out_cplx = (K.vals == 2) || dvec_cplx || A->seed.y != 0.0;
+  // uniform scaling is applied through a temporary constant vector for simplicity
+  void* dtmp = nullptr;
+  const void* dptr = A->dinv64;
+  bool dcplx = A->dinv_cplx;
+  if (A->dkind == 1) {
+    size_t es = dvec_cplx ? 16 : 8;
+    IDRS_CUDA(cudaMallocAsync(&dtmp, es * std::max<long>(n, 1), st));
+    if (dvec_cplx) {
+      std::vector<c128> h(n, A->dinv_u);
+      IDRS_CUDA(cudaMemcpyAsync(dtmp, h.data(), es * n, cudaMemcpyHostToDevice, st));
+      IDRS_CUDA(cudaStreamSynchronize(st));
+    } else {
+      std::vector<double> h(n, A->dinv_u.x);
+      IDRS_CUDA(cudaMemcpyAsync(dtmp, h.data(), es * n, cudaMemcpyHostToDevice, st));
+      IDRS_CUDA(cudaStreamSynchronize(st));
+    }
+    dptr = dtmp;
+    dcplx = dvec_cplx;
+  }
+  int* d_missing = nullptr;
+  IDRS_CUDA(cudaMallocAsync((void**)&d_missing, sizeof(int), st));
+  IDRS_CUDA(cudaMemsetAsync(d_missing, 0, sizeof(int), st));
+  const void* kval = value_ptr(K);
+  void* kval_tmp = nullptr;
+  if (out_cplx) {
+    IDRS_CUDA(cudaMallocAsync(&A->ks_val64, 16 * std::max<long>(cnt, 1), st));
+    const c128* kv = (const c128*)kval;
+    if (K.vals == 1 && kval) {  // promote real values
+      IDRS_CUDA(cudaMallocAsync(&kval_tmp, 16 * std::max<long>(cnt, 1), st));
+      k_r2c<<<stream_grid(cnt), kThreads, 0, st>>>(cnt, (const double*)kval, (c128*)kval_tmp);
+      kv = (const c128*)kval_tmp;
+    }
+    if (dptr && !dcplx) scale_values<c128, double>(K, kv, (const double*)dptr, A->seed, (c128*)A->ks_val64, st, d_missing);
+    else scale_values<c128, c128>(K, kv, (const c128*)dptr, A->seed, (c128*)A->ks_val64, st, d_missing);
+  } else {
+    IDRS_CUDA(cudaMallocAsync(&A->ks_val64, 8 * std::max<long>(cnt, 1), st));
+    scale_values<double, double>(K, kval, (const double*)dptr, A->seed.x, (double*)A->ks_val64, st, d_missing);
+  }
+  int missing = 0;
+  IDRS_CUDA(cudaMemcpyAsync(&missing, d_missing, sizeof(int), cudaMemcpyDeviceToHost, st));
+  IDRS_CUDA(cudaStreamSynchronize(st));
+  cudaFreeAsync(d_missing, st);
+  if (dtmp) cudaFreeAsync(dtmp, st);
+  if (kval_tmp) cudaFreeAsync(kval_tmp, st);
+  if (missing) {
+    set_error("seed shift needs every diagonal entry present in the sparsity pattern");
+    return 5;
+  }
+  A->ks64.val = A->ks_val64;
+  A->ks64.vcplx = out_cplx;
+  return 0;
+}
+
+template <class Tin, class Tout>
+__global__ void k_narrow(long n, const Tin* a, Tout* b) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x)
+    b[i] = narrow<Tout>(widen(a[i]));
+}
+
+const MatView& Operator::view(int prec) {
+  if (prec != 32) return ks64;
+  if (ks32.format != FMT_NONE) return ks32;
+  ks32 = ks64;
+  cudaStream_t st = stream;
+  if (ks64.format != FMT_STENCIL7) {
+    long cnt = value_count(*K);
+    if (ks64.vcplx) {
+      IDRS_CUDA(cudaMallocAsync(&ks_val32, 8 * std::max<long>(cnt, 1), st));
+      k_narrow<c128, c64><<<stream_grid(cnt), kThreads, 0, st>>>(cnt, (const c128*)ks64.val, (c64*)ks_val32);
+    } else {
+      IDRS_CUDA(cudaMallocAsync(&ks_val32, 4 * std::max<long>(cnt, 1), st));
+      k_narrow<double, float><<<stream_grid(cnt), kThreads, 0, st>>>(cnt, (const double*)ks64.val, (float*)ks_val32);
+    }
+    IDRS_LAUNCH_CHECK();
+    ks32.val = ks_val32;
+  }
+  if (dkind == 2 && !dinv32) {
+    long nn = n();
+    if (dinv_cplx) {
+      IDRS_CUDA(cudaMallocAsync(&dinv32, 8 * nn, st));
+      k_narrow<c128, c64><<<stream_grid(nn), kThreads, 0, st>>>(nn, (const c128*)dinv64, (c64*)dinv32);
+    } else {
+      IDRS_CUDA(cudaMallocAsync(&dinv32, 4 * nn, st));
+      k_narrow<double, float><<<stream_grid(nn), kThreads, 0, st>>>(nn, (const double*)dinv64, (float*)dinv32);
+    }
+    IDRS_LAUNCH_CHECK();
+  }
+  return ks32;
+}
+
+void operator_free(Operator* A) {
+  cudaStream_t st = A->stream;
+  if (A->ks_val64) cudaFreeAsync(A->ks_val64, st);
+  if (A->ks_val32) cudaFreeAsync(A->ks_val32, st);
+  if (A->dinv64) cudaFreeAsync(A->dinv64, st);
+  if (A->dinv32) cudaFreeAsync(A->dinv32, st);
+  for (auto& p : A->shadows) cudaFreeAsync(p.second, st);
+  A->shadows.clear();
+  free_redbuf(A->red, st);
+  cudaStreamSynchronize(st);
+  if (A->own_stream) cudaStreamDestroy(st);
+  user_matrix_release(A->K);
+  user_matrix_release(A->P);
+}
+
+// ---------------------------------------------------------------------------
+// explicit instantiations
+// ---------------------------------------------------------------------------
+#define IDRS_INST(T)                                                                              \
+  template void op_chain<T>(const MatView&, const std::vector<c128>&, int, const T*, T*, T*, T*,   \
+                            const int*, cudaStream_t, T, T, const T*);                            \
+  template void op_scaleback<T>(Operator&, int, const std::vector<c128>&, int, const T*, T*, T*,  \
+                                T*, const int*, cudaStream_t);                                     \
+  template void op_precon<T>(Operator&, int, const T*, T*, const int*, cudaStream_t);             \
+  template void vec_copy<T>(long, const T*, T*, const int*, cudaStream_t);                        \
+  template void vec_scale_vec<T>(long, const void*, bool, const T*, T*, const int*, cudaStream_t);
+IDRS_INST(double)
+IDRS_INST(float)
+IDRS_INST(c128)
+IDRS_INST(c64)
+#undef IDRS_INST
+template void vec_convert<double, float>(long, const double*, float*, const int*, cudaStream_t);
+template void vec_convert<float, double>(long, const float*, double*, const int*, cudaStream_t);
+template void vec_convert<c128, c64>(long, const c128*, c64*, const int*, cudaStream_t);
+template void vec_convert<c64, c128>(long, const c64*, c128*, const int*, cudaStream_t);
+
+}  // namespace idrs

@@ -1,0 +1,152 @@
+// matrix.cuh -- device user_matrix, the composed operator and its SpMV chain.
+//
+// user_matrix (M/PP_MATRIX/user_module.f90:134-167) lives in HBM in one of
+// the formats DENSE, CRS, COO (stored row-sorted, i.e. CRS with a stable
+// order inside each row), CDS, or the matrix-free 7-point stencil of
+// E/STENCIL/user_module.f90.  Indices are 0-based int32.
+//
+// type(matrix) (M/PP_MATRIX/matrix_module.f90:38-81) becomes `Operator`:
+// the solver product A*v = K D^-1 p(K D^-1) v of rmatvec (:152-167), with
+// the diagonal scaling D (user preconditioner, which_precon = 1) and the
+// real seed shift folded into a scaled copy Ks = (K - seed I) D^-1 made once
+// at set-up, and the polynomial evaluated by Horner with every step fused
+// into one SpMV kernel: w_new = Ks w + alpha_k v (the epilogue).  So one
+// solver matvec with a degree-d polynomial is d+1 SpMV launches and no
+// separate vector passes.
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace idrs {
+
+enum Format { FMT_NONE = 0, FMT_DENSE = 1, FMT_CRS = 2, FMT_COO = 3, FMT_CDS = 4, FMT_STENCIL7 = 5 };
+
+// Read-only view of one matrix in one precision (values double/c128 for
+// prec 64, float/c64 for prec 32; `vcplx` tells whether values are complex).
+struct MatView {
+  int format = FMT_NONE;
+  int nrows = 0, ncols = 0;
+  long nnz = 0;
+  const int* rp = nullptr;
+  const int* ci = nullptr;
+  const void* val = nullptr;
+  bool vcplx = false;
+  int hb = 0;  // CDS half band
+  int nx = 0, ny = 0, nz = 0;
+  double st[7] = {0, 0, 0, 0, 0, 0, 0};  // stencil c,w,e,s,n,f,b
+  int group = 8;                          // CRS lanes per row
+};
+
+struct UserMatrix {
+  int format = FMT_NONE;
+  int which_precon = 0;
+  int nrows = 0, ncols = 0;
+  int vals = 1;  // 0 pattern, 1 real, 2 complex
+  long nnz = 0;
+  int* row_ptr = nullptr;  // CRS / sorted COO
+  int* col_ind = nullptr;
+  void* val = nullptr;     // double or c128
+  int half_band = 0;
+  void* band = nullptr;    // CDS, column-major nrows x (2hb+1)
+  void* mat = nullptr;     // dense, column-major
+  int nx = 0, ny = 0, nz = 0;
+  double st[7] = {0, 0, 0, 0, 0, 0, 0};
+  void* diag = nullptr;    // which_precon == 1: diagonal D (double or c128)
+  bool diag_cplx = false;
+  bool diag_uniform = false;  // D constant (stencil): value in diag_u
+  c128 diag_u;
+  int group = 8;
+  int refcount = 1;
+
+  MatView view64() const;
+  long bytes() const;
+};
+
+void user_matrix_release(UserMatrix* K);
+
+// The composed operator of type(matrix).
+struct Operator {
+  UserMatrix* K = nullptr;
+  UserMatrix* P = nullptr;  // diagonal preconditioner or null
+  bool cplx = false;        // vectors complex?
+  c128 seed;                // rseed / cseed
+  int preconditioner = 0, degree = 0;
+  std::vector<c128> alpha_p;  // 0..degree
+  int n_sigma = 0;
+  std::vector<c128> alpha_s;  // (degree+1) x n_sigma
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  bool device_pointers = false;
+
+  // scaled operator Ks = (K - seed I) D^-1
+  MatView ks64, ks32;         // ks32 built lazily
+  void* ks_val64 = nullptr;   // owned scaled values (CRS/COO/CDS/dense)
+  void* ks_val32 = nullptr;
+  int dkind = 0;              // 0: no scaling, 1: uniform, 2: vector
+  c128 dinv_u;                // uniform D^-1
+  void* dinv64 = nullptr;     // vector D^-1 (double or c128)
+  void* dinv32 = nullptr;
+  bool dinv_cplx = false;
+  MatView k64;                // unscaled K (original system residual)
+
+  // injected shadow spaces, keyed by s
+  std::vector<std::pair<int, void*>> shadows;  // device PT (s x n), wide type
+
+  // reduction scratch for kernels launched on this operator's stream
+  RedBuf red{nullptr, nullptr};
+
+  int n() const { return K->nrows; }
+  const MatView& view(int prec);
+};
+
+int build_operator(Operator* A);  // (re)builds the scaled data; returns status
+void operator_free(Operator* A);
+RedBuf alloc_redbuf(cudaStream_t st);
+void free_redbuf(RedBuf rb, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// SpMV with the fused epilogue  y = a * (M x) + cv * v   (v may be null)
+// ---------------------------------------------------------------------------
+template <class T>
+void spmv(const MatView& M, const T* x, T* y, T a, T cv, const T* v, const int* skip,
+          cudaStream_t st);
+
+// w = Ks p(Ks) v, then the final product gets the epilogue
+//   w = fa * (Ks u) + fcv * fv.
+// t1, t2: scratch vectors (length n).  alpha: polynomial coefficients (host).
+template <class T>
+void op_chain(const MatView& Ks, const std::vector<c128>& alpha, int degree, const T* v, T* w,
+              T* t1, T* t2, const int* skip, cudaStream_t st, T fa = T(1), T fcv = T(0),
+              const T* fv = nullptr);
+
+// x = D^-1 p(Ks) y   (scaleback of matrix_module.f90:831-849 without deflation)
+template <class T>
+void op_scaleback(Operator& A, int prec, const std::vector<c128>& alpha, int degree,
+                  const T* y, T* x, T* t1, T* t2, const int* skip, cudaStream_t st);
+
+// w = D^-1 v  (operator / of matrix_module.f90:306-352 for a standard system)
+template <class T>
+void op_precon(Operator& A, int prec, const T* v, T* w, const int* skip, cudaStream_t st);
+
+// elementwise helpers
+template <class T> void vec_copy(long n, const T* a, T* b, const int* skip, cudaStream_t st);
+template <class T> void vec_scale_vec(long n, const void* d, bool dcplx, const T* a, T* b,
+                                      const int* skip, cudaStream_t st);
+template <class Tin, class Tout>
+void vec_convert(long n, const Tin* a, Tout* b, const int* skip, cudaStream_t st);
+
+// uniform [0,1) generator shared with the oracle (splitmix64 of the index)
+__host__ __device__ inline uint64_t splitmix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__host__ __device__ inline double uniform01(uint64_t seed, uint64_t index) {
+  uint64_t z = splitmix64(index ^ splitmix64(seed));
+  return (double)(z >> 11) * 0x1.0p-53;
+}
+
+}  // namespace idrs

@@ -1,0 +1,231 @@
+/*
+ * idrs_gb300.h -- C ABI of the GB300-native IDRS solve path.
+ *
+ * Drop-in boundary for the Fortran 2018 API of the IDRS package
+ * (mbvangijzen/IDRS-package).  Each entry point names the Fortran interface
+ * it replaces (path:line in the IDRS package; M/ = IDRS/MODULES).  A Fortran
+ * ISO_C_BINDING module (idrs-package_gb300/fortran/idrs_gb300_module.f90)
+ * binds these with the reference's module and routine names.
+ *
+ * Conventions
+ *  - Every function returns an int status: IDRS_OK (0) or an error code; the
+ *    message of the last error on the calling thread is idrs_last_error().
+ *    The library never aborts the process (the reference's `error stop`
+ *    becomes a status code; the Fortran shim turns it back into error stop).
+ *  - Fortran OPTIONAL arguments are pointers: NULL means "not present", which
+ *    is what an OPTIONAL dummy of a BIND(C) interface passes when absent.
+ *  - Real vectors are double*, complex vectors are double* holding
+ *    interleaved (re, im) pairs (Fortran complex(real64), C99 double _Complex).
+ *  - Index arrays are 1-based int32, as in the Fortran API.
+ *  - Vector arguments of the solver, matvec and scaleback calls are host
+ *    pointers by default (copied in and out, never retained).  After
+ *    idrs_matrix_set_pointer_mode(A, IDRS_POINTER_DEVICE) they are device
+ *    pointers on the current CUDA device.
+ *  - One CUDA stream per idrs_matrix handle (idrs_matrix_set_stream).
+ *  - Small matrices (H, U0, multishift x(n, n_sigma), resvec(maxit+1,
+ *    n_sigma)) are column-major like Fortran.
+ */
+#ifndef IDRS_GB300_H
+#define IDRS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IDRS_OK 0
+#define IDRS_ERR_ARG 1         /* illegal argument (reference: error stop / stop) */
+#define IDRS_ERR_CUDA 2        /* CUDA runtime error */
+#define IDRS_ERR_ALLOC 3       /* out of device or host memory */
+#define IDRS_ERR_STATE 4       /* handle used in the wrong state */
+#define IDRS_ERR_UNSUPPORTED 5 /* valid in the reference, not in this build */
+
+#define IDRS_POINTER_HOST 0
+#define IDRS_POINTER_DEVICE 1
+
+/* type(user_matrix): M/PP_MATRIX/user_module.f90:134-167 */
+typedef struct idrs_user_matrix_s *idrs_user_matrix;
+/* type(matrix): M/PP_MATRIX/matrix_module.f90:38-81 */
+typedef struct idrs_matrix_s *idrs_matrix;
+
+const char *idrs_last_error(void);
+int idrs_version(void);
+
+/* ---------------------------------------------------------------------- */
+/* user_module                                                            */
+/* ---------------------------------------------------------------------- */
+
+/* crs_format(nrows, ncols, row_ptr, col_ind[, rval, ival, cval]):
+ * user_module.f90:829-863.  rval (real) or cval (complex) or neither
+ * (pattern only, all values 1). */
+int idrs_crs_format(int nrows, int ncols, const int *row_ptr, const int *col_ind,
+                    const double *rval, const double *cval, idrs_user_matrix *K);
+/* coo_format(nrows, ncols, nnz, indx, jndx[, rval, ival, cval]): user_module.f90:865-898 */
+int idrs_coo_format(int nrows, int ncols, int nnz, const int *indx, const int *jndx,
+                    const double *rval, const double *cval, idrs_user_matrix *K);
+/* cds_format(nrows, ncols, half_band[, rband, iband, cband]): user_module.f90:932-958.
+ * band(nrows, -half_band:half_band) column-major. */
+int idrs_cds_format(int nrows, int ncols, int half_band, const double *rband,
+                    const double *cband, idrs_user_matrix *K);
+/* dense_format([rmat, imat, cmat]): user_module.f90:900-930 (column-major) */
+int idrs_dense_format(int nrows, int ncols, const double *rmat, const double *cmat,
+                      idrs_user_matrix *K);
+/* Matrix-free 7-point stencil user_matrix of E/STENCIL/user_module.f90:39-187
+ * (Dirichlet boundaries, x fastest).  coef = {c, w, e, s, n, f, b}. */
+int idrs_stencil7_format(int nx, int ny, int nz, const double *coef, idrs_user_matrix *K);
+/* REAL_PRECON(which_precon, K[, M, C, shift]): user_module.f90:1327-1463.
+ * which_precon 0 (none) or 1 (diagonal scaling, D(K) - shift). */
+int idrs_real_precon(int which_precon, idrs_user_matrix K, const double *shift,
+                     idrs_user_matrix *P);
+/* COMPLEX_PRECON: user_module.f90:1465-1603 (shift = {re, im}) */
+int idrs_complex_precon(int which_precon, idrs_user_matrix K, const double *shift,
+                        idrs_user_matrix *P);
+/* real_diagonal(K) / complex_diagonal(K): user_module.f90:960-1047, 1049-1136 */
+int idrs_real_diagonal(idrs_user_matrix K, double *D);
+int idrs_complex_diagonal(idrs_user_matrix K, double *D);
+/* operator(*) of user_matrix: ruser_mv / cuser_mv, user_module.f90:182-241 (host vectors) */
+int idrs_ruser_mv(idrs_user_matrix K, const double *v, double *w);
+int idrs_cuser_mv(idrs_user_matrix K, const double *v, double *w);
+int idrs_user_matrix_free(idrs_user_matrix K);
+
+/* ---------------------------------------------------------------------- */
+/* matrix_module                                                          */
+/* ---------------------------------------------------------------------- */
+
+/* A%K = K, A%P = P, A%rseed/cseed = seed: M/PP_IDRS/real_matrix.inc:9-58.
+ * is_complex selects the real (r*) or complex (c*) specifics; seed = {re[, im]}. */
+int idrs_matrix_create(idrs_user_matrix K, idrs_user_matrix P, int is_complex,
+                       const double *seed, idrs_matrix *A);
+int idrs_matrix_free(idrs_matrix A);
+int idrs_matrix_set_stream(idrs_matrix A, void *cuda_stream);
+int idrs_matrix_set_pointer_mode(idrs_matrix A, int mode);
+/* Injects the shadow space used by solves with this s (row j of PT is
+ * PT + j*n, real or interleaved complex).  PT = NULL removes it.  The
+ * reference draws P from gfortran's RANDOM_NUMBER (idrs_module.f90:839-937);
+ * without an injected P this library draws it from a documented seeded
+ * generator (splitmix64), shared with the CPU oracle. */
+int idrs_matrix_set_shadow(idrs_matrix A, int s, const double *PT);
+
+/* real_preconditioner(A, preconditioner, degree[, foci, center, H]):
+ * matrix_module.f90:551-635.  preconditioner 0 none, 1 Neumann, 2 Chebyshev,
+ * 3 Hessenberg.  H(ldh, nh) column-major. */
+int idrs_real_preconditioner(idrs_matrix A, int preconditioner, int degree, const double *foci,
+                             const double *center, const double *H, int ldh, int nh);
+/* complex_preconditioner: matrix_module.f90:637-722 (complex foci[2], center, H) */
+int idrs_complex_preconditioner(idrs_matrix A, int preconditioner, int degree,
+                                const double *foci, const double *center, const double *H,
+                                int ldh, int nh);
+/* Polynomial coefficients alpha_p(0:degree) currently held by A. */
+int idrs_matrix_get_alpha(idrs_matrix A, double *alpha, int *degree);
+/* ms_parameters(A, sigma, sigma_p): matrix_module.f90:402-549 */
+int idrs_real_ms_parameters(idrs_matrix A, int n_sigma, const double *sigma, double *sigma_p);
+int idrs_complex_ms_parameters(idrs_matrix A, int n_sigma, const double *sigma,
+                               double *sigma_p);
+/* operator(*): rmatvec / cmatvec, matrix_module.f90:135-167 */
+int idrs_rmatvec(idrs_matrix A, const double *v, double *w);
+int idrs_cmatvec(idrs_matrix A, const double *v, double *w);
+/* operator(/): rprecon / cprecon, matrix_module.f90:306-400  (w = v/A) */
+int idrs_rprecon(idrs_matrix A, const double *v, double *w);
+int idrs_cprecon(idrs_matrix A, const double *v, double *w);
+/* scaleback(A, b, y): matrix_module.f90:811-849 */
+int idrs_rscaleback(idrs_matrix A, const double *b, const double *y, double *x);
+int idrs_cscaleback(idrs_matrix A, const double *b, const double *y, double *x);
+/* scaleback(A, sigma, b, y) (multishift): matrix_module.f90:724-809 */
+int idrs_ms_rscaleback(idrs_matrix A, int n_sigma, const double *sigma, const double *b,
+                       const double *y, double *x);
+int idrs_ms_cscaleback(idrs_matrix A, int n_sigma, const double *sigma, const double *b,
+                       const double *y, double *x);
+
+/* Measurement helper (no counterpart in the reference): runs `reps` products
+ * w = A*v of the operator chain (degree+1 SpMV launches) in precision prec
+ * (64 or 32) on A's stream, after `warmup` untimed ones, on internal vectors
+ * of length n, and returns the CUDA-event time per product and per launch.
+ * Each vector is larger than the GPU's L2 for n >= 2^24 (fp64). */
+int idrs_time_matvec(idrs_matrix A, int prec, int warmup, int reps, double *ms_per_product,
+                     double *ms_per_launch);
+
+/* ---------------------------------------------------------------------- */
+/* idrs_module                                                            */
+/* ---------------------------------------------------------------------- */
+
+/* x = IDRS(A, b, s[, M1, tolerance, maximum_iterations, variant, flag, relres,
+ *          iterations, x0, U0, omega, resvec, H]):
+ * RIDRS idrs_module.f90:180-251, CIDRS :107-178, body M/IDRS/idrs.inc.
+ * U0(n, s) column-major; omega(n_omega); resvec(resvec_len >= maxit+1);
+ * H(nritz+1, nritz) column-major with ldh = nritz+1. */
+int idrs_ridrs(idrs_matrix A, const double *b, int s, idrs_matrix M1, const double *tolerance,
+               const int *maximum_iterations, const int *variant, int *flag, double *relres,
+               int *iterations, const double *x0, const double *U0, const double *omega,
+               int n_omega, double *resvec, int resvec_len, double *H, int ldh, int nritz,
+               double *x);
+int idrs_cidrs(idrs_matrix A, const double *b, int s, idrs_matrix M1, const double *tolerance,
+               const int *maximum_iterations, const int *variant, int *flag, double *relres,
+               int *iterations, const double *x0, const double *U0, const double *omega,
+               int n_omega, double *resvec, int resvec_len, double *H, int ldh, int nritz,
+               double *x);
+
+/* x = QMRIDR(A, b, s[, M1, tolerance, maximum_iterations, flag, relres,
+ *            iterations, inner_s, inner_tolerance, inner_iterations, x0, omega,
+ *            resvec]): RQMRIDR idrs_module.f90:331-408, CQMRIDR :253-329,
+ * body M/IDRS/qmridr.inc.  inner_precision (new, optional): 64 (default) or
+ * 32 -- the inner IDR(inner_s) and its operator run in fp32 (complex64). */
+int idrs_rqmridr(idrs_matrix A, const double *b, int s, idrs_matrix M1,
+                 const double *tolerance, const int *maximum_iterations, int *flag,
+                 double *relres, int *iterations, const int *inner_s,
+                 const double *inner_tolerance, const int *inner_iterations, const double *x0,
+                 const double *omega, int n_omega, double *resvec, int resvec_len,
+                 const int *inner_precision, double *x);
+int idrs_cqmridr(idrs_matrix A, const double *b, int s, idrs_matrix M1,
+                 const double *tolerance, const int *maximum_iterations, int *flag,
+                 double *relres, int *iterations, const int *inner_s,
+                 const double *inner_tolerance, const int *inner_iterations, const double *x0,
+                 const double *omega, int n_omega, double *resvec, int resvec_len,
+                 const int *inner_precision, double *x);
+
+/* NORM(w): idrs_module.f90:787-811;  INPROD(u, v): idrs_module.f90:813-837 */
+int idrs_rnorm(idrs_matrix A, const double *w, double *norm);
+int idrs_cnorm(idrs_matrix A, const double *w, double *norm);
+int idrs_rinprod(idrs_matrix A, const double *u, const double *v, double *uv);
+int idrs_cinprod(idrs_matrix A, const double *u, const double *v, double *uv);
+
+/* x = IDRS_RITZ(A, b, s[, M, tolerance, maximum_iterations, variant, flag,
+ *               relres, iterations, x0, ..., H]): ritz_module.f90:389-556
+ * (the Hessenberg output; recycling U0/omega outputs are not provided).
+ * H(ldh, nh) receives Hf(1:ldh, 1:nh); *nritz = (iter/(s+1))*s + mod(iter,s+1). */
+int idrs_ridrs_ritz(idrs_matrix A, const double *b, int s, const double *tolerance,
+                    const int *maximum_iterations, int *flag, double *relres, int *iterations,
+                    const double *x0, double *H, int ldh, int nh, int *nritz, double *x);
+
+/* ---------------------------------------------------------------------- */
+/* pp_idrs: M/PP_IDRS/pp_idrs_module.f90:118-162 (RPP_IDRS) with            */
+/* real_matrix.inc, real_preconditioner.inc:10-34 and run_idrs.inc:9-60.  */
+/* The reference reads its options from the command line                 */
+/* (initialize.inc:4-31); here they are a struct.                         */
+/* ---------------------------------------------------------------------- */
+typedef struct idrs_pp_options {
+  int method;          /* 1 idrs, 2 bicgstab, 0 qmridr */
+  int s;
+  double tol;
+  int maxit;
+  int in_s, in_it;
+  double in_tol;
+  int preconditioner;  /* 0 none, 1 neumann, 2 chebyshev, 3 hessenberg */
+  int degree;
+  int n_ritz;          /* -ritz (default 32) */
+  int inner_precision; /* 64 or 32 */
+} idrs_pp_options;
+
+typedef struct idrs_pp_report {
+  int flag, iterations, ritz_iterations, nritz;
+  double relres_solver, relres_original;
+  double foci[2], center;
+  double seconds_setup, seconds_solve, seconds_total;
+} idrs_pp_report;
+
+int idrs_rpp_idrs(idrs_user_matrix K, const double *b, idrs_user_matrix P, const double *center,
+                  const double *foci, const idrs_pp_options *opt, idrs_pp_report *report,
+                  double *x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

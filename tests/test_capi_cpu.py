@@ -1,0 +1,39 @@
+"""C ABI checks that need no GPU: the library loads, exports every function
+include/idrs_gb300.h declares, and rejects bad arguments before touching the
+device."""
+import ctypes as C
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "idrs_gb300.h")
+
+
+def _declared():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^(?:int|const char \*)\s*(idrs_\w+)\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol(pkg):
+    lib_path = pkg.build_recipe.build()
+    lib = C.CDLL(lib_path)
+    names = _declared()
+    assert len(names) >= 40
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_prototypes_cover_the_header(pkg):
+    assert set(_declared()) <= set(pkg.api._PROTOS)
+
+
+def test_argument_errors_without_gpu(pkg):
+    lib = pkg.load()
+    h = C.c_void_p()
+    st = lib.idrs_crs_format(-1, 3, None, None, None, None, C.byref(h))
+    assert st == pkg.api.IDRS_ERR_ARG
+    assert b"crs_format" in lib.idrs_last_error()
+    st = lib.idrs_stencil7_format(0, 3, 3, None, C.byref(h))
+    assert st == pkg.api.IDRS_ERR_ARG
+    assert lib.idrs_matrix_create(None, None, 0, None, C.byref(h)) == pkg.api.IDRS_ERR_ARG
+    assert lib.idrs_version() >= 10000

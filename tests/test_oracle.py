@@ -1,0 +1,161 @@
+"""The oracle (CPU restatement) against the golden fixtures and the
+reference's own known-answer examples.  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+
+
+@pytest.fixture(scope="module")
+def P(pkg):
+    return pkg.problems
+
+
+def _toeplitz_real(O, P):
+    rp, ci, vals, b = P.toeplitz_real()
+    return O.Matrix(O.crs_format(60, 60, rp, ci, vals)), b
+
+
+def _toeplitz_complex(O, P):
+    rp, ci, vals, b = P.toeplitz_complex()
+    return O.Matrix(O.crs_format(200, 200, rp, ci, vals), cplx=True), b
+
+
+def test_bicgstab_variant_matches_scipy_real(oracle, P):
+    """IDRS variant 2 is BiCGSTAB (idrs_module.f90:13-15): its residual after
+    every omega step follows scipy's bicgstab (tests/golden)."""
+    d = np.load(os.path.join(GOLD, "bicgstab_toeplitz_real.npz"))
+    A, b = _toeplitz_real(oracle, P)
+    r = oracle.idrs(A, b, 1, variant=2, tolerance=1e-14, maximum_iterations=80, resvec_len=81)
+    k = 12
+    ours = r.resvec[2:2 * k + 1:2]
+    np.testing.assert_allclose(ours, d["resnorm"][:k], rtol=1e-10)
+    assert abs(r.resvec[0] - d["normb"]) <= 1e-14 * d["normb"]
+
+
+def test_bicgstab_variant_matches_scipy_complex(oracle, P):
+    d = np.load(os.path.join(GOLD, "bicgstab_toeplitz_complex.npz"))
+    A, b = _toeplitz_complex(oracle, P)
+    r = oracle.idrs(A, b, 1, variant=2, tolerance=1e-14, maximum_iterations=80, resvec_len=81)
+    k = 8
+    np.testing.assert_allclose(r.resvec[2:2 * k + 1:2], d["resnorm"][:k], rtol=1e-9)
+
+
+@pytest.mark.parametrize("s", [1, 2, 4, 8])
+def test_finite_termination_real_toeplitz(oracle, P, s):
+    """E/TOEPLITZ/toeplitz.f90:134-138: IDR(s) terminates within N + N/s."""
+    A, b = _toeplitz_real(oracle, P)
+    r = oracle.idrs(A, b, s, tolerance=1e-8, maximum_iterations=4000)
+    assert r.flag == 0
+    assert r.iterations <= 60 + 60 // s
+    assert r.relres < 1e-8
+    q = oracle.qmridr(A, b, s, tolerance=1e-8, maximum_iterations=4000)
+    assert q.flag == 0 and q.iterations <= 60 + 60 // s and q.relres < 1e-8
+
+
+@pytest.mark.parametrize("s", [1, 2, 4, 8, 16, 32, 64])
+def test_complex_toeplitz_accuracy(oracle, P, s):
+    """E/TOEPLITZ/toeplitz.f90:20-93: tol 1e-12, flag 0."""
+    A, b = _toeplitz_complex(oracle, P)
+    r = oracle.idrs(A, b, s, tolerance=1e-12, maximum_iterations=4000)
+    assert r.flag == 0 and r.relres < 1e-12
+    q = oracle.qmridr(A, b, s, tolerance=1e-12, maximum_iterations=4000)
+    assert q.flag == 0 and q.relres < 1e-12
+
+
+def test_chebyshev_and_neumann_polynomials(oracle):
+    """matrix_module.f90:851-1019: r(t) = 1 - t p(t) equals the closed-form
+    Chebyshev / Neumann residual polynomial."""
+    g = np.load(os.path.join(GOLD, "poly.npz"))
+    t = g["t"]
+    for d in (1, 2, 4, 8, 12):
+        a = oracle.chebyshev(d, g["foci"])
+        r = 1 - t * np.polyval(a[::-1], t)
+        np.testing.assert_allclose(r, g[f"cheb_{d}"], atol=1e-9)
+    for d in (1, 3, 6):
+        a = oracle.neumann(d, float(g["center"]))
+        r = 1 - t * np.polyval(a[::-1], t)
+        np.testing.assert_allclose(r, g[f"neu_{d}"], atol=1e-12)
+
+
+def test_qr_eig_and_solve(oracle):
+    """dense_la_module.f90: QR_eig against numpy eigenvalues, SOLVE against
+    numpy.linalg.solve, GROT in BLAS rotg style."""
+    g = np.load(os.path.join(GOLD, "dense.npz"))
+    e, conv = oracle.qr_eig(g["H"])
+    assert conv == 12
+    ref = g["eig"]
+    for z in ref:
+        assert np.min(np.abs(e - z)) < 1e-10 * max(1.0, abs(z))
+    np.testing.assert_allclose(oracle.solve(g["M"], g["rhs"]), g["x"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(oracle.solve(g["Mc"], g["rhsc"]), g["xc"], rtol=1e-12, atol=1e-12)
+    c, s, r = oracle.grot(3.0, 4.0)
+    assert (c, s, r) == pytest.approx((0.6, 0.8, 5.0))
+    assert oracle.grot(0.0, 2.0) == (0.0, 1.0, 2.0)
+
+
+def test_known_solution_cdr(oracle, P):
+    """b = A*1 => x = 1 (E/RANDOM/band_real.f90:77-79 style) on the 3-D
+    convection-diffusion operator, CRS and stencil formats agree."""
+    n = 10
+    coef = P.cdr_coefficients(n)
+    rp, ci, vals = P.stencil_to_crs(n, n, n, coef)
+    K = oracle.crs_format(n ** 3, n ** 3, rp, ci, vals)
+    S = oracle.stencil7_format(n, n, n, coef)
+    v = np.random.default_rng(1).standard_normal(n ** 3)
+    np.testing.assert_allclose(K.mv(v), S.mv(v), rtol=1e-13, atol=1e-9)
+    np.testing.assert_allclose(S.mv(v), P.stencil_apply(n, n, n, coef, v), rtol=1e-13, atol=1e-9)
+    b = K.mv(np.ones(n ** 3))
+    r = oracle.idrs(oracle.Matrix(K), b, 4, tolerance=1e-10)
+    assert r.flag == 0
+    np.testing.assert_allclose(r.x, 1.0, atol=1e-8)
+
+
+def test_problem_sizes(P):
+    """The 64^3 CRS operator has the nonzero count of the benchmark config."""
+    rp, ci, vals = P.stencil_to_crs(64, 64, 64, P.cdr_coefficients(64))
+    assert rp[-1] - 1 == 1_810_432
+    c = P.cdr_coefficients(64)
+    h = 1 / 65
+    assert c[0] == pytest.approx(6 / h**2)
+    assert c[2] == pytest.approx(-1 / h**2 + 5 / h)
+    assert c[1] == pytest.approx(-1 / h**2 - 5 / h)
+
+
+def test_flags_and_errors(oracle, P):
+    A, b = _toeplitz_real(oracle, P)
+    r = oracle.idrs(A, b, 4, tolerance=1e-12, maximum_iterations=5)
+    assert r.flag == 1 and r.iterations == 5
+    with pytest.raises(ValueError):
+        oracle.idrs(A, b, 4, tolerance=-1.0)
+    r = oracle.idrs(A, np.zeros(60), 4)
+    assert r.flag == 0 and r.iterations == 0
+
+
+def test_pp_idrs_pipeline(oracle, P):
+    """PP_IDRS with Ritz-estimated Chebyshev(8) and diagonal scaling."""
+    n = 12
+    coef = P.cdr_coefficients(n)
+    S = oracle.stencil7_format(n, n, n, coef)
+    D = oracle.real_precon(1, S)
+    b = S.mv(np.ones(n ** 3))
+    r = oracle.pp_idrs(S, b, P=D, method=0, s=8, tol=1e-8, preconditioner=2, degree=8, n_ritz=20)
+    assert r.flag == 0 and r.relres_original < 1e-8 * 1.0001 or r.relres_original < 2e-8
+    np.testing.assert_allclose(r.x, 1.0, atol=1e-6)
+
+
+def test_multishift_oracle(oracle, P):
+    """MSIDRS / MSQMRIDR on a small shifted Laplacian: every shifted system's
+    true residual meets the tolerance."""
+    n = 8
+    K = oracle.stencil7_format(n, n, n, P.laplace_coefficients(n))
+    A = oracle.Matrix(K, cplx=True)
+    sig, _ = P.multishift_shifts(n, n_shifts=4, lo=0.1, hi=0.9)
+    b = P.complex_unit_normal(n ** 3)
+    r = oracle.msidrs(A, b, sig, 4, tolerance=1e-8, maximum_iterations=2000)
+    assert r.flag == 0 and np.max(r.relres) < 1e-8
+    q = oracle.msqmridr(A, b, sig, 4, tolerance=1e-8, maximum_iterations=2000)
+    assert q.flag == 0 and np.max(q.relres) < 1e-8
