@@ -47,6 +47,7 @@ _dp = C.POINTER(C.c_double)
 _PROTOS = {
     "idrs_last_error": (C.c_char_p, []),
     "idrs_version": (_i, []),
+    "idrs_launch_count": (C.c_long, []),
     "idrs_crs_format": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp]),
     "idrs_coo_format": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "idrs_cds_format": (_i, [_i, _i, _i, _vp, _vp, _vp]),
@@ -99,7 +100,7 @@ class PPOptions(C.Structure):
     _fields_ = [("method", C.c_int), ("s", C.c_int), ("tol", C.c_double), ("maxit", C.c_int),
                 ("in_s", C.c_int), ("in_it", C.c_int), ("in_tol", C.c_double),
                 ("preconditioner", C.c_int), ("degree", C.c_int), ("n_ritz", C.c_int),
-                ("inner_precision", C.c_int)]
+                ("inner_precision", C.c_int), ("device_pointers", C.c_int)]
 
 
 class PPReport(C.Structure):
@@ -154,10 +155,13 @@ def _ref_dbl(v):
     return None if v is None else C.byref(C.c_double(float(v)))
 
 
-def _arr(a, cplx):
+def _arr(a, cplx, n=None):
     if a is None:
         return None
-    return np.ascontiguousarray(a, dtype=np.complex128 if cplx else np.float64)
+    a = np.ascontiguousarray(a, dtype=np.complex128 if cplx else np.float64)
+    if n is not None and a.size != n:
+        raise ValueError(f"vector of length {a.size} where {n} entries are required")
+    return a
 
 
 class Result(dict):
@@ -171,6 +175,8 @@ class Result(dict):
 class UserMatrix:
     """type(user_matrix) (M/PP_MATRIX/user_module.f90:134-167), device resident."""
 
+    __array_ufunc__ = None  # `v * K`, `v / K` must not broadcast element-wise
+
     def __init__(self, handle, nrows, ncols, cplx):
         self.handle, self.nrows, self.ncols, self.cplx = handle, nrows, ncols, cplx
 
@@ -183,7 +189,7 @@ class UserMatrix:
     def __mul__(self, v):
         """K*v: ruser_mv / cuser_mv (user_module.f90:182-241)."""
         cplx = self.cplx or np.iscomplexobj(v)
-        v = _arr(v, cplx)
+        v = _arr(v, cplx, self.ncols)
         w = np.empty(self.nrows, dtype=v.dtype)
         fn = lib().idrs_cuser_mv if cplx else lib().idrs_ruser_mv
         _check(fn(self.handle, _p(v), _p(w)))
@@ -295,6 +301,8 @@ class Matrix:
     """type(matrix) (M/PP_MATRIX/matrix_module.f90:38-81): K, the diagonal
     preconditioner P, the seed shift and the polynomial preconditioner."""
 
+    __array_ufunc__ = None  # `v / A` must reach __rtruediv__ with the whole vector
+
     def __init__(self, K: UserMatrix, P: UserMatrix | None = None, seed=None, complex=False):
         self.K, self.P, self.cplx, self.n = K, P, bool(complex), K.nrows
         sd = None if seed is None else np.array([np.real(seed), np.imag(seed)], dtype=np.float64)
@@ -363,7 +371,7 @@ class Matrix:
 
     def __mul__(self, v):
         """A*v: rmatvec / cmatvec (matrix_module.f90:135-167)."""
-        v = _arr(v, self.cplx)
+        v = _arr(v, self.cplx, self.n)
         w = np.empty_like(v)
         fn = lib().idrs_cmatvec if self.cplx else lib().idrs_rmatvec
         _check(fn(self.handle, _p(v), _p(w)))
@@ -371,7 +379,7 @@ class Matrix:
 
     def __rtruediv__(self, v):
         """v/A: rprecon / cprecon (matrix_module.f90:306-400)."""
-        v = _arr(v, self.cplx)
+        v = _arr(v, self.cplx, self.n)
         w = np.empty_like(v)
         fn = lib().idrs_cprecon if self.cplx else lib().idrs_rprecon
         _check(fn(self.handle, _p(v), _p(w)))
@@ -379,8 +387,8 @@ class Matrix:
 
     def scaleback(self, b, y):
         """scaleback(A, b, y) (matrix_module.f90:811-849)."""
-        y = _arr(y, self.cplx)
-        b = _arr(b, self.cplx)
+        y = _arr(y, self.cplx, self.n)
+        b = _arr(b, self.cplx, self.n)
         x = np.empty_like(y)
         fn = lib().idrs_cscaleback if self.cplx else lib().idrs_rscaleback
         _check(fn(self.handle, _p(b), _p(y), _p(x)))
@@ -389,6 +397,8 @@ class Matrix:
     def ms_scaleback(self, sigma, b, Y):
         """scaleback(A, sigma, b, y) (matrix_module.f90:724-809); Y is n x n_sigma."""
         Y = np.asfortranarray(Y, dtype=self.dtype)
+        if Y.ndim != 2 or Y.shape[0] != self.n:
+            raise ValueError("Y must be n x n_sigma")
         X = np.empty_like(Y, order="F")
         sg = np.ascontiguousarray(sigma, dtype=self.dtype)
         b = _arr(b, self.cplx)
@@ -403,7 +413,7 @@ class Matrix:
 def _solver_common(A: Matrix, b):
     if A.device_pointers:
         raise ValueError("the numpy mirror works in host-pointer mode")
-    return _arr(b, A.cplx)
+    return _arr(b, A.cplx, A.n)
 
 
 def IDRS(A: Matrix, b, s, M1: Matrix | None = None, tolerance=None, maximum_iterations=None,
@@ -417,8 +427,10 @@ def IDRS(A: Matrix, b, s, M1: Matrix | None = None, tolerance=None, maximum_iter
     maxit = maximum_iterations if maximum_iterations is not None else min(2 * n, 1000)
     x = np.empty_like(b)
     flag, relres, iters = C.c_int(), C.c_double(), C.c_int()
-    x0a = _arr(x0, A.cplx)
+    x0a = _arr(x0, A.cplx, n)
     U0a = None if U0 is None else np.asfortranarray(U0, dtype=A.dtype)
+    if U0a is not None and U0a.shape != (n, s):
+        raise ValueError("U0 must be n x s")
     om = _arr(omega, A.cplx)
     rv = np.zeros(maxit + 1) if resvec else None
     Hm = np.zeros((H + 1, H), dtype=A.dtype, order="F") if H else None
@@ -445,7 +457,7 @@ def QMRIDR(A: Matrix, b, s, M1: Matrix | None = None, tolerance=None, maximum_it
     maxit = maximum_iterations if maximum_iterations is not None else min(2 * n, 1000)
     x = np.empty_like(b)
     flag, relres, iters = C.c_int(), C.c_double(), C.c_int()
-    x0a = _arr(x0, A.cplx)
+    x0a = _arr(x0, A.cplx, n)
     om = _arr(omega, A.cplx)
     rv = np.zeros(maxit + 1) if resvec else None
     fn = lib().idrs_cqmridr if A.cplx else lib().idrs_rqmridr
@@ -461,7 +473,7 @@ def QMRIDR(A: Matrix, b, s, M1: Matrix | None = None, tolerance=None, maximum_it
 
 
 def NORM(A: Matrix, w) -> float:
-    w = _arr(w, A.cplx)
+    w = _arr(w, A.cplx, A.n)
     out = np.zeros(1)
     fn = lib().idrs_cnorm if A.cplx else lib().idrs_rnorm
     _check(fn(A.handle, _p(w), _p(out)))
@@ -469,8 +481,8 @@ def NORM(A: Matrix, w) -> float:
 
 
 def INPROD(A: Matrix, u, v):
-    u = _arr(u, A.cplx)
-    v = _arr(v, A.cplx)
+    u = _arr(u, A.cplx, A.n)
+    v = _arr(v, A.cplx, A.n)
     out = np.zeros(2)
     fn = lib().idrs_cinprod if A.cplx else lib().idrs_rinprod
     _check(fn(A.handle, _p(u), _p(v), _p(out)))
@@ -487,7 +499,7 @@ def IDRS_RITZ(A: Matrix, b, s, tolerance=None, maximum_iterations=None, x0=None,
         Hm = np.zeros(H_shape, order="F")
     _check(lib().idrs_ridrs_ritz(A.handle, _p(b), int(s), _ref_dbl(tolerance),
                                  _ref_int(maximum_iterations), C.byref(flag), C.byref(relres),
-                                 C.byref(iters), _p(_arr(x0, False)), _p(Hm),
+                                 C.byref(iters), _p(_arr(x0, False, A.n)), _p(Hm),
                                  0 if Hm is None else H_shape[0], 0 if Hm is None else H_shape[1],
                                  C.byref(nritz), _p(x)))
     r = Result(x=x, flag=flag.value, relres=relres.value, iterations=iters.value, nritz=nritz.value)
@@ -498,18 +510,27 @@ def IDRS_RITZ(A: Matrix, b, s, tolerance=None, maximum_iterations=None, x0=None,
 
 def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=None, *, method=1,
             s=4, tol=1e-6, maxit=1000, in_s=1, in_it=0, in_tol=0.1, preconditioner=0, degree=0,
-            n_ritz=32, inner_precision=64) -> Result:
+            n_ritz=32, inner_precision=64, x_out=None) -> Result:
     """x = pp_idrs(K, b[, P, center, foci]) (RPP_IDRS, pp_idrs_module.f90:118-162);
-    the command-line options of initialize.inc:4-31 are keyword arguments."""
-    b = np.ascontiguousarray(b, dtype=np.float64)
-    x = np.empty_like(b)
+    the command-line options of initialize.inc:4-31 are keyword arguments.
+
+    b may be a numpy array (host) or an int device address; with a device b,
+    x_out must be the device address of the solution vector."""
+    dev = isinstance(b, int)
+    if dev:
+        if not isinstance(x_out, int):
+            raise ValueError("a device b needs a device x_out")
+        x = x_out
+    else:
+        b = _arr(b, False, K.nrows)
+        x = np.empty_like(b)
     o = PPOptions(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
-                  inner_precision)
+                  inner_precision, int(dev))
     rep = PPReport()
     f = None if foci is None else np.ascontiguousarray(foci, dtype=np.float64)
     _check(lib().idrs_rpp_idrs(K.handle, _p(b), P.handle if P else None, _ref_dbl(center), _p(f),
                                C.byref(o), C.byref(rep), _p(x)))
-    return Result(x=x, flag=rep.flag, iterations=rep.iterations,
+    return Result(x=None if dev else x, flag=rep.flag, iterations=rep.iterations,
                   ritz_iterations=rep.ritz_iterations, nritz=rep.nritz,
                   relres=rep.relres_solver, relres_original=rep.relres_original,
                   foci=tuple(rep.foci), center=rep.center, seconds_setup=rep.seconds_setup,

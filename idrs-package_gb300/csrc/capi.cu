@@ -97,8 +97,11 @@ void* upload(const void* h, size_t bytes) {
   return d;
 }
 
+// Lanes per row of the CRS kernel: one thread per row for short rows (no
+// FP64 shuffle additions), otherwise a power-of-two sub-warp.
 int crs_group(long nnz, long nrows) {
   double mean = nrows > 0 ? (double)nnz / nrows : 1.0;
+  if (mean <= 16.0) return 1;
   int g = 2;
   while (g < 32 && g < mean) g *= 2;
   return g;
@@ -196,6 +199,7 @@ void* make_diagonal(const UserMatrix& K, bool want_cplx, c128 shift, bool* is_cp
       IDRS_CUDA(cudaMalloc(&tmp, 8 * (size_t)std::max(n, 1)));
       diagonal_into<double>(K, tmp, st);
       k_promote<<<stream_grid(n), kThreads, 0, st>>>(n, tmp, (c128*)D);
+      IDRS_LAUNCH_CHECK();
       IDRS_CUDA(cudaDeviceSynchronize());
       cudaFree(tmp);
     }
@@ -646,6 +650,7 @@ int idrs_rinprod(idrs_matrix A, const double* u, const double* v, double* uv) { 
 int idrs_cinprod(idrs_matrix A, const double* u, const double* v, double* uv) { return guard([&] { return norm_t<c128>(A, u, v, uv, true); }); }
 
 const char* idrs_last_error(void) { return idrs::last_error(); }
+long idrs_launch_count(void) { return idrs::launch_count(); }
 int idrs_version(void) { return 10000; }
 
 int idrs_crs_format(int nrows, int ncols, const int* row_ptr, const int* col_ind,
@@ -1040,8 +1045,17 @@ int idrs_rpp_idrs(idrs_user_matrix K, const double* b, idrs_user_matrix P, const
     if (preconditioner == 1 && center) estimate = false;
     if (preconditioner == 2 && foci) estimate = false;
     cudaStream_t cs = A->stream;
-    DBuf d_b(8 * n, cs), d_x0(8 * n, cs), d_y(8 * n, cs), d_x(8 * n, cs);
-    IDRS_CUDA(cudaMemcpyAsync(d_b.p, b, 8 * n, cudaMemcpyHostToDevice, cs));
+    const bool dev = opt->device_pointers != 0;
+    DBuf hb_buf, hx_buf, d_x0(8 * n, cs), d_y(8 * n, cs);
+    const double* pb = b;
+    double* px = x;
+    if (!dev) {
+      hb_buf = DBuf(8 * n, cs);
+      hx_buf = DBuf(8 * n, cs);
+      IDRS_CUDA(cudaMemcpyAsync(hb_buf.p, b, 8 * n, cudaMemcpyHostToDevice, cs));
+      pb = hb_buf.as<double>();
+      px = hx_buf.as<double>();
+    }
     IDRS_CUDA(cudaMemsetAsync(d_x0.p, 0, 8 * n, cs));
     A->device_pointers = true;
     idrs_pp_report rep{};
@@ -1052,7 +1066,7 @@ int idrs_rpp_idrs(idrs_user_matrix K, const double* b, idrs_user_matrix P, const
       std::vector<double> H((size_t)ldh * ini_iter, 0.0);
       int flag = -1, iter = 0, nr = 0;
       double rel = 1;
-      st = idrs_ridrs_ritz(A, d_b.as<double>(), s, &tol, &ini_iter, &flag, &rel, &iter,
+      st = idrs_ridrs_ritz(A, pb, s, &tol, &ini_iter, &flag, &rel, &iter,
                            d_x0.as<double>(), H.data(), ldh, ini_iter, &nr, d_x0.as<double>());
       if (st) return st;
       rep.ritz_iterations = iter;
@@ -1072,28 +1086,28 @@ int idrs_rpp_idrs(idrs_user_matrix K, const double* b, idrs_user_matrix P, const
     if (opt->method == 0) {
       int in_s = opt->in_s, in_it = opt->in_it, prec = opt->inner_precision ? opt->inner_precision : 64;
       double in_tol = opt->in_tol;
-      st = idrs_rqmridr(A, d_b.as<double>(), s, nullptr, &tol, &maxit, &rep.flag, &rep.relres_solver,
+      st = idrs_rqmridr(A, pb, s, nullptr, &tol, &maxit, &rep.flag, &rep.relres_solver,
                         &rep.iterations, &in_s, &in_tol, &in_it, d_x0.as<double>(), nullptr, 0,
                         nullptr, 0, &prec, d_y.as<double>());
     } else {
       int variant = opt->method == 2 ? 2 : 1;
-      st = idrs_ridrs(A, d_b.as<double>(), s, nullptr, &tol, &maxit, &variant, &rep.flag,
+      st = idrs_ridrs(A, pb, s, nullptr, &tol, &maxit, &variant, &rep.flag,
                       &rep.relres_solver, &rep.iterations, d_x0.as<double>(), nullptr, nullptr, 0,
                       nullptr, 0, nullptr, 0, 0, d_y.as<double>());
     }
     if (st) return st;
     // x = scaleback(A, b, y); relres on the original system (run_idrs.inc:113-120)
     DBuf t1b(8 * n, cs), t2b(8 * n, cs), r(8 * n, cs), res(8, cs);
-    op_scaleback<double>(*A, 64, A->alpha_p, A->degree, d_y.as<double>(), d_x.as<double>(),
+    op_scaleback<double>(*A, 64, A->alpha_p, A->degree, d_y.as<double>(), px,
                          t1b.as<double>(), t2b.as<double>(), nullptr, cs);
-    spmv<double>(A->k64, d_x.as<double>(), r.as<double>(), -1.0, 1.0, d_b.as<double>(), nullptr, cs);
+    spmv<double>(A->k64, px, r.as<double>(), -1.0, 1.0, pb, nullptr, cs);
     launch_fused<1, double>(n, BNorm<double>{r.as<double>()}, TStoreVals<double>{res.as<double>(), 1}, A->red, nullptr, cs);
     double rr = 0, bb = 0;
     IDRS_CUDA(cudaMemcpyAsync(&rr, res.p, 8, cudaMemcpyDeviceToHost, cs));
-    launch_fused<1, double>(n, BNorm<double>{d_b.as<double>()}, TStoreVals<double>{res.as<double>(), 1}, A->red, nullptr, cs);
+    launch_fused<1, double>(n, BNorm<double>{pb}, TStoreVals<double>{res.as<double>(), 1}, A->red, nullptr, cs);
     IDRS_CUDA(cudaStreamSynchronize(cs));
     IDRS_CUDA(cudaMemcpyAsync(&bb, res.p, 8, cudaMemcpyDeviceToHost, cs));
-    IDRS_CUDA(cudaMemcpyAsync(x, d_x.p, 8 * n, cudaMemcpyDeviceToHost, cs));
+    if (!dev) IDRS_CUDA(cudaMemcpyAsync(x, px, 8 * n, cudaMemcpyDeviceToHost, cs));
     IDRS_CUDA(cudaStreamSynchronize(cs));
     rep.relres_original = std::sqrt(rr) / std::sqrt(bb);
     auto t2 = clk::now();

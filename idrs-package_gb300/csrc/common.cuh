@@ -167,7 +167,13 @@ struct cuda_error {
     if (e__ != cudaSuccess) throw ::idrs::cuda_error{e__, std::string(#call) + " @ " \
                                                      __FILE__ ":" + std::to_string(__LINE__)}; \
   } while (0)
-#define IDRS_LAUNCH_CHECK() IDRS_CUDA(cudaPeekAtLastError())
+void count_launch();
+long launch_count();
+#define IDRS_LAUNCH_CHECK()   \
+  do {                        \
+    ::idrs::count_launch();   \
+    IDRS_CUDA(cudaPeekAtLastError()); \
+  } while (0)
 
 // ---------------------------------------------------------------------------
 // launch geometry: 152 SMs on GB300; grids are multiples of the SM count.

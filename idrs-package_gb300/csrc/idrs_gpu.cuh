@@ -508,11 +508,12 @@ struct BMgs {
   T* gn; const T* y; const T* gnext; bool div_by_om; int prev; const QmrState<W>* st;
   struct Shared { T c; };
   __device__ void prepare(Shared& sh) const {
-    if (threadIdx.x == 0) sh.c = div_by_om ? narrow<T>(st->om) : narrow<T>(st->beta[prev]);
+    // v/om as v*(1/om): one FP64 multiply per element instead of a division
+    if (threadIdx.x == 0) sh.c = div_by_om ? narrow<T>(W(1.0) / st->om) : narrow<T>(st->beta[prev]);
   }
   template <int ND, class A>
   __device__ void operator()(long i, Shared& sh, A (&acc)[ND]) const {
-    T g = div_by_om ? gn[i] - y[i] / sh.c : gn[i] - y[i] * sh.c;
+    T g = gn[i] - y[i] * sh.c;
     gn[i] = g;
     if (gnext) acc_add(acc[0], conj_(gnext[i]) * g);
     else acc_add(acc[0], abs2_(g));
@@ -524,23 +525,23 @@ struct BMgs {
 template <class T, class W>
 struct BQw {
   const T* vt; T* wpool; long ld; int wmap[MAXS + 1]; int s; T* x; T* gn; const T* PT; const QmrState<W>* st;
-  struct Shared { T rs[MAXS + 1]; T rd; T phi; typename traits<T>::real normg; };
+  struct Shared { T rs[MAXS + 1]; T rd; T phi; typename traits<T>::real inorm; };
   __device__ void prepare(Shared& sh) const {
     for (int q = threadIdx.x; q <= s; q += blockDim.x) sh.rs[q] = narrow<T>(st->rs[q]);
     if (threadIdx.x == 0) {
-      sh.rd = narrow<T>(st->rs[s + 1]);
+      sh.rd = narrow<T>(W(1.0) / st->rs[s + 1]);  // reciprocals: no per-element divisions
       sh.phi = narrow<T>(st->phi_n);
-      sh.normg = (typename traits<T>::real)st->normg;
+      sh.inorm = (typename traits<T>::real)(1.0 / st->normg);
     }
   }
   template <int ND, class A>
   __device__ void operator()(long i, Shared& sh, A (&acc)[ND]) const {
     T a = T(0);
     for (int q = 0; q <= s; ++q) a = a + wpool[wmap[q] * ld + i] * sh.rs[q];
-    T wn = (vt[i] - a) / sh.rd;
+    T wn = (vt[i] - a) * sh.rd;
     wpool[wmap[0] * ld + i] = wn;
     x[i] = x[i] + sh.phi * wn;
-    T g = gn[i] / sh.normg;
+    T g = gn[i] * sh.inorm;
     gn[i] = g;
 #pragma unroll
     for (int d = 0; d < ND; ++d)
@@ -551,11 +552,11 @@ struct BQw {
 template <class T, class W>
 struct BQstart {
   T* gn; const T* PT; long ld; int s; const QmrState<W>* st;
-  struct Shared { typename traits<T>::real normg; };
-  __device__ void prepare(Shared& sh) const { if (threadIdx.x == 0) sh.normg = (typename traits<T>::real)st->normg; }
+  struct Shared { typename traits<T>::real inorm; };
+  __device__ void prepare(Shared& sh) const { if (threadIdx.x == 0) sh.inorm = (typename traits<T>::real)(1.0 / st->normg); }
   template <int ND, class A>
   __device__ void operator()(long i, Shared& sh, A (&acc)[ND]) const {
-    T g = gn[i] / sh.normg;
+    T g = gn[i] * sh.inorm;
     gn[i] = g;
 #pragma unroll
     for (int d = 0; d < ND; ++d)

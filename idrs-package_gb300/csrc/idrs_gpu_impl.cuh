@@ -106,15 +106,17 @@ void IdrsGpu<T>::solve(const T* b, T* x, const SolveOpts& o) {
   // maxit <= 0 never ends the reference loop by count; the host then relies
   // on the device stop flag alone.
   const int max_cycles = o.inner ? (maxit + s) / (s + 1) : (maxit > 0 ? maxit / (s + 1) + 2 : 1 << 30);
+  // One cycle of look-ahead: cycle c is queued before the host waits for the
+  // stop flag of cycle c-1, so the GPU never waits for the host.  An inner
+  // solve polls too (its outer iteration waits for its result anyway) so that
+  // it launches no cycles beyond the one after convergence.
   for (int c = 0; c < max_cycles; ++c) {
     enqueue_cycle(b, x, o, c, inispace);
-    if (!o.inner) {
-      IDRS_CUDA(cudaMemcpyAsync(&h_stop[c & 1], stop, sizeof(int), cudaMemcpyDeviceToHost, st));
-      IDRS_CUDA(cudaEventRecord(ev[c & 1], st));
-      if (c >= 1) {
-        IDRS_CUDA(cudaEventSynchronize(ev[(c - 1) & 1]));
-        if (h_stop[(c - 1) & 1]) break;
-      }
+    IDRS_CUDA(cudaMemcpyAsync(&h_stop[c & 1], stop, sizeof(int), cudaMemcpyDeviceToHost, st));
+    IDRS_CUDA(cudaEventRecord(ev[c & 1], st));
+    if (c >= 1) {
+      IDRS_CUDA(cudaEventSynchronize(ev[(c - 1) & 1]));
+      if (h_stop[(c - 1) & 1]) break;
     }
   }
   if (!o.inner) {

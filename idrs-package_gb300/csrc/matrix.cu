@@ -1,6 +1,7 @@
 // matrix.cu -- SpMV kernels (stencil, CRS, CDS, dense), the scaled operator
 // build and the Horner chain of the polynomial preconditioner.
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 
 #include "matrix.cuh"
@@ -11,6 +12,9 @@ namespace idrs {
 // runtime basics
 // ---------------------------------------------------------------------------
 static thread_local std::string g_error;
+static std::atomic<long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 void set_error(const std::string& msg) { g_error = msg; }
 const char* last_error() { return g_error.c_str(); }
 
@@ -92,8 +96,11 @@ void user_matrix_release(UserMatrix* K) {
 
 // Matrix-free 7-point stencil (E/STENCIL/user_module.f90:155-160): 2-D thread
 // tiles in x-y march along z keeping x(z-1), x(z), x(z+1) in registers; the
-// x/y neighbours come from L1/L2.  Dirichlet zero outside the grid.
-template <class T, class R>
+// x/y neighbours come from L1/L2.  Dirichlet zero outside the grid.  GB300's
+// FP64 pipe is narrow, so the fp64 form spends as few FP64 instructions as
+// possible: the epilogue scale is folded into the coefficients on the host
+// (SCALE == false) and the sum is one multiply plus an FMA chain.
+template <class T, class R, bool SCALE>
 __global__ void __launch_bounds__(256) k_stencil7(int nx, int ny, int nz, int zc, R c0, R cw, R ce,
                                                   R cs, R cn, R cf, R cb, const T* __restrict__ x,
                                                   T* __restrict__ y, T a, T cv,
@@ -116,7 +123,7 @@ __global__ void __launch_bounds__(256) k_stencil7(int nx, int ny, int nz, int zc
     T xs = j > 0 ? x[p - nx] : T(0);
     T xn = j < ny - 1 ? x[p + nx] : T(0);
     T s = c0 * xc + cw * xw + ce * xe + cs * xs + cn * xn + cf * xm + cb * xp;
-    T out = a * s;
+    T out = SCALE ? a * s : s;
     if (v) out = out + cv * v[p];
     y[p] = out;
     xm = xc;
@@ -153,6 +160,26 @@ __global__ void __launch_bounds__(256) k_crs(int nrows, const int* __restrict__ 
       if (v) out = out + cv * v[row];
       y[row] = out;
     }
+  }
+}
+
+// CRS, one thread per row: no cross-lane reduction, so a row of k nonzeros
+// costs k FMAs (the FP64 pipe of GB300 is the limit of short-row fp64 SpMV).
+template <class T, class V>
+__global__ void __launch_bounds__(256) k_crs_row(int nrows, const int* __restrict__ rp,
+                                                 const int* __restrict__ ci, const V* __restrict__ val,
+                                                 const T* __restrict__ x, T* __restrict__ y, T a, T cv,
+                                                 const T* __restrict__ v,
+                                                 const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  for (long row = blockIdx.x * (long)blockDim.x + threadIdx.x; row < nrows;
+       row += gridDim.x * (long)blockDim.x) {
+    const int beg = rp[row], end = rp[row + 1];
+    T sum = T(0);
+    for (int k = beg; k < end; ++k) sum = sum + mulvt(val[k], x[ci[k]]);
+    T out = a * sum;
+    if (v) out = out + cv * v[row];
+    y[row] = out;
   }
 }
 
@@ -196,6 +223,10 @@ static void launch_crs(const MatView& M, const V* val, const T* x, T* y, T a, T 
   long rows_per_block = kThreads / M.group;
   long need = (M.nrows + rows_per_block - 1) / rows_per_block;
   int grid = (int)std::max(1L, std::min(need, (long)num_sms() * 8));
+  if (M.group == 1) {
+    k_crs_row<T, V><<<stream_grid(M.nrows), kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip);
+    return;
+  }
   switch (M.group) {
     case 2: k_crs<2><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip); break;
     case 4: k_crs<4><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip); break;
@@ -235,9 +266,18 @@ static void launch_stencil(const MatView& M, const T* x, T* y, T a, T cv, const 
   int zc = (int)std::max(1L, std::min((long)M.nz, (M.nz * xy + target - 1) / target));
   if (zc < 4 && M.nz >= 4) zc = 4;  // keep some register reuse along z
   int gz = (M.nz + zc - 1) / zc;
-  k_stencil7<T, R><<<dim3(gx, gy, gz), blk, 0, st>>>(
-      M.nx, M.ny, M.nz, zc, R(M.st[0]), R(M.st[1]), R(M.st[2]), R(M.st[3]), R(M.st[4]),
-      R(M.st[5]), R(M.st[6]), x, y, a, cv, v, skip);
+  dim3 grid(gx, gy, gz);
+  const bool real_a = (imag_(a) == 0);
+  if (real_a) {  // fold the real scale into the coefficients
+    double ar = (double)real_(a);
+    k_stencil7<T, R, false><<<grid, blk, 0, st>>>(
+        M.nx, M.ny, M.nz, zc, R(ar * M.st[0]), R(ar * M.st[1]), R(ar * M.st[2]), R(ar * M.st[3]),
+        R(ar * M.st[4]), R(ar * M.st[5]), R(ar * M.st[6]), x, y, a, cv, v, skip);
+  } else {
+    k_stencil7<T, R, true><<<grid, blk, 0, st>>>(
+        M.nx, M.ny, M.nz, zc, R(M.st[0]), R(M.st[1]), R(M.st[2]), R(M.st[3]), R(M.st[4]),
+        R(M.st[5]), R(M.st[6]), x, y, a, cv, v, skip);
+  }
 }
 
 template <>
@@ -569,6 +609,7 @@ int build_operator(Operator* A) {
     if (K.vals == 1 && kval) {  // promote real values
       IDRS_CUDA(cudaMallocAsync(&kval_tmp, 16 * std::max<long>(cnt, 1), st));
       k_r2c<<<stream_grid(cnt), kThreads, 0, st>>>(cnt, (const double*)kval, (c128*)kval_tmp);
+      IDRS_LAUNCH_CHECK();
       kv = (const c128*)kval_tmp;
     }
     if (dptr && !dcplx) scale_values<c128, double>(K, kv, (const double*)dptr, A->seed, (c128*)A->ks_val64, st, d_missing);

@@ -49,6 +49,9 @@ typedef struct idrs_matrix_s *idrs_matrix;
 
 const char *idrs_last_error(void);
 int idrs_version(void);
+/* Number of CUDA kernels this library has launched in this process
+ * (measurement helper; no counterpart in the reference). */
+long idrs_launch_count(void);
 
 /* ---------------------------------------------------------------------- */
 /* user_module                                                            */
@@ -212,6 +215,7 @@ typedef struct idrs_pp_options {
   int degree;
   int n_ritz;          /* -ritz (default 32) */
   int inner_precision; /* 64 or 32 */
+  int device_pointers; /* 1: b and x are device pointers */
 } idrs_pp_options;
 
 typedef struct idrs_pp_report {

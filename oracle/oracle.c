@@ -716,8 +716,17 @@ int or_idrs_ritz_r(const or_mat *A, int n, const double *b, int s, const or_opts
 /* PP_IDRS (real, single rhs): M/PP_IDRS/pp_idrs_module.f90:118-162 with    */
 /* real_matrix.inc, real_preconditioner.inc:10-34 and run_idrs.inc:9-60.    */
 /* ------------------------------------------------------------------------ */
+static double or_wtime(void) {
+#ifdef _OPENMP
+  return omp_get_wtime();
+#else
+  return 0.0;
+#endif
+}
+
 int or_pp_idrs_r(const or_umat *K, const or_umat *P, int n, const double *b, or_pp_args *a,
                  double *x) {
+  double t0 = or_wtime();
   or_mat *A;
   or_matrix_create(K, P, NULL, 0, &A);
   double *x0 = calloc(n, sizeof(double)), *y = malloc(sizeof(double) * n),
@@ -753,6 +762,8 @@ int or_pp_idrs_r(const or_umat *K, const or_umat *P, int n, const double *b, or_
     a->foci_used[0] = f[0]; a->foci_used[1] = f[1]; a->center_used = c;
     st = or_real_preconditioner(A, preconditioner, a->degree, f, &c, NULL, 0, 0);
   }
+  double t1 = or_wtime();
+  a->seconds_setup = t1 - t0;
   if (st == OR_OK) {
     for (int i = 0; i <= A->degree && i < 64; ++i) a->alpha_p[i] = A->ralpha_p ? A->ralpha_p[i] : 1.;
     or_opts o; memset(&o, 0, sizeof o);
@@ -773,6 +784,7 @@ int or_pp_idrs_r(const or_umat *K, const or_umat *P, int n, const double *b, or_
     for (int i = 0; i < n; ++i) t[i] = b[i] - t[i];
     a->relres_original = or_norm_r(n, t) / or_norm_r(n, b);
   }
+  a->seconds_solve = or_wtime() - t1;
   free(x0); free(y); free(t);
   or_matrix_free(A);
   return st;

@@ -180,6 +180,7 @@ typedef struct or_pp_args {
   double relres_solver, relres_original;
   double foci_used[2], center_used;
   double alpha_p[64];
+  double seconds_setup, seconds_solve; /* wall clock of the set-up and the solve */
 } or_pp_args;
 int or_pp_idrs_r(const or_umat *K, const or_umat *P, int n, const double *b, or_pp_args *a,
                  double *x);

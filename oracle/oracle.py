@@ -62,6 +62,7 @@ class PPArgs(C.Structure):
         ("relres_solver", C.c_double), ("relres_original", C.c_double),
         ("foci_used", C.c_double * 2), ("center_used", C.c_double),
         ("alpha_p", C.c_double * 64),
+        ("seconds_setup", C.c_double), ("seconds_solve", C.c_double),
     ]
 
 
@@ -514,7 +515,8 @@ def pp_idrs(K: UserMatrix, b, *, P: UserMatrix | None = None, method=1, s=4, tol
     return Result(x=x, flag=a.flag, iterations=a.iterations, ritz_iterations=a.ritz_iterations,
                   nritz=a.nritz_used, relres=a.relres_solver, relres_original=a.relres_original,
                   foci=tuple(a.foci_used), center=a.center_used,
-                  alpha_p=np.array(a.alpha_p[: degree + 1]))
+                  alpha_p=np.array(a.alpha_p[: degree + 1]),
+                  seconds_setup=a.seconds_setup, seconds_solve=a.seconds_solve)
 
 
 def crs_transpose(K: UserMatrix) -> UserMatrix:

@@ -11,7 +11,7 @@ HEADER = os.path.join(ROOT, "include", "idrs_gb300.h")
 
 def _declared():
     src = open(HEADER).read()
-    return sorted(set(re.findall(r"^(?:int|const char \*)\s*(idrs_\w+)\(", src, re.M)))
+    return sorted(set(re.findall(r"^(?:int|long|const char \*)\s*(idrs_\w+)\(", src, re.M)))
 
 
 def test_library_exports_every_declared_symbol(pkg):
