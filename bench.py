@@ -43,7 +43,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--grid", type=int, default=256)
-    p.add_argument("--in-it", type=int, default=1000)
+    p.add_argument("--in-it", type=int, default=500)
     p.add_argument("--in-tol", type=float, default=1e-2)
     p.add_argument("--in-s", type=int, default=4)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -143,9 +143,11 @@ def make_problem(pkg, n):
 
 
 def solve_kw(mode, args):
-    kw = dict(method=0, s=8, maxit=3000, preconditioner=2, degree=8, n_ritz=20)
+    kw = dict(method=0, s=8, maxit=1500, preconditioner=2, degree=8, n_ritz=20)
     if mode == "mixed":
-        kw.update(in_s=args.in_s, in_it=args.in_it, in_tol=args.in_tol, inner_precision=32)
+        # outer iterations are refinement steps: a handful suffice; the bound
+        # keeps a misconfigured inner solve from running for long
+        kw.update(maxit=60, in_s=args.in_s, in_it=args.in_it, in_tol=args.in_tol, inner_precision=32)
     return kw
 
 

@@ -222,7 +222,20 @@ int set_preconditioner(Operator* A, int preconditioner, int degree, const double
   A->preconditioner = preconditioner;
   A->degree = (preconditioner == 0) ? 0 : degree;
   A->alpha_p.assign(A->degree + 1, c128(1.0, 0.0));
+  A->jac = JacobiCols();
   if (A->degree == 0) return IDRS_OK;
+  // keeps the tridiagonal Jacobi matrix for the stable fp32 evaluation
+  auto keep_jacobi = [&](const std::vector<cd>& J) {
+    const int d = A->degree, ld = d + 2;
+    A->jac.a.assign(d + 1, c128(0.0));
+    A->jac.b.assign(d + 1, c128(0.0));
+    A->jac.c.assign(d + 1, c128(0.0));
+    for (int i = 1; i <= d + 1; ++i) {
+      if (i >= 2) A->jac.a[i - 1] = c128(J[(i - 2) + (size_t)ld * (i - 1)].real(), J[(i - 2) + (size_t)ld * (i - 1)].imag());
+      A->jac.b[i - 1] = c128(J[(i - 1) + (size_t)ld * (i - 1)].real(), J[(i - 1) + (size_t)ld * (i - 1)].imag());
+      A->jac.c[i - 1] = c128(J[i + (size_t)ld * (i - 1)].real(), J[i + (size_t)ld * (i - 1)].imag());
+    }
+  };
   if (!A->cplx) {
     std::vector<double> al(A->degree + 1);
     int st = 0;
@@ -232,12 +245,15 @@ int set_preconditioner(Operator* A, int preconditioner, int degree, const double
       else if (H) analyse_spectrum(H, ldh, nh, nullptr, &c, nullptr);
       else c = 1.0;
       st = neumann(A->degree, c, al.data());
+      keep_jacobi(neumann_jacobi(A->degree, cd(c, 0.0)));
     } else if (preconditioner == 2) {
       double f[2];
       if (foci) { f[0] = foci[0] - A->seed.x; f[1] = foci[1] - A->seed.x; }
       else if (H) analyse_spectrum(H, ldh, nh, f, nullptr, nullptr);
       else { f[0] = 0.25; f[1] = 1.75; }
       st = chebyshev(A->degree, f, al.data());
+      cd fc[2] = {cd(f[0], 0.0), cd(f[1], 0.0)};
+      keep_jacobi(chebyshev_jacobi(A->degree, fc));
     } else {
       REQUIRE(H, "the Hessenberg preconditioner needs H");
       st = compute_alpha(A->degree, H, ldh, nh, al.data());
@@ -259,12 +275,14 @@ int set_preconditioner(Operator* A, int preconditioner, int degree, const double
       else if (H) analyse_spectrum(Hc.data(), ldh, nh, nullptr, &c, nullptr);
       else c = 1.0;
       st = neumann(A->degree, c, al.data());
+      keep_jacobi(neumann_jacobi(A->degree, c));
     } else if (preconditioner == 2) {
       cd f[2];
       if (foci) { f[0] = cd(foci[0], foci[1]) - seed; f[1] = cd(foci[2], foci[3]) - seed; }
       else if (H) analyse_spectrum(Hc.data(), ldh, nh, f, nullptr, nullptr);
       else { f[0] = 0.25; f[1] = 1.75; }
       st = chebyshev(A->degree, f, al.data());
+      keep_jacobi(chebyshev_jacobi(A->degree, f));
     } else {
       REQUIRE(H, "the Hessenberg preconditioner needs H");
       st = compute_alpha(A->degree, Hc.data(), ldh, nh, al.data());
@@ -914,16 +932,21 @@ int idrs_time_matvec(idrs_matrix A, int prec, int warmup, int reps, double* ms_p
     long n = A->n();
     cudaStream_t st = A->stream;
     size_t es = (A->cplx ? 2 : 1) * (prec == 64 ? 8 : 4);
-    DBuf v(es * n, st), w(es * n, st), t1(es * n, st), t2(es * n, st);
+    DBuf v(es * n, st), w(es * n, st), t1(es * n, st), t2(es * n, st), t3(es * n, st);
     IDRS_CUDA(cudaMemsetAsync(v.p, 0, es * n, st));
     const MatView& M = A->view(prec);
+    const bool recur = (prec == 32 && A->jac.valid());
     auto once = [&] {
       if (prec == 64 && !A->cplx)
         op_chain<double>(M, A->alpha_p, A->degree, v.as<double>(), w.as<double>(), t1.as<double>(), t2.as<double>(), nullptr, st, 1.0, 0.0, nullptr);
+      else if (prec == 32 && !A->cplx && recur)
+        op_chain_recur<float>(M, A->jac, A->degree, v.as<float>(), w.as<float>(), t1.as<float>(), t2.as<float>(), t3.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
       else if (prec == 32 && !A->cplx)
         op_chain<float>(M, A->alpha_p, A->degree, v.as<float>(), w.as<float>(), t1.as<float>(), t2.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
       else if (prec == 64)
         op_chain<c128>(M, A->alpha_p, A->degree, v.as<c128>(), w.as<c128>(), t1.as<c128>(), t2.as<c128>(), nullptr, st, c128(1.0), c128(0.0), nullptr);
+      else if (recur)
+        op_chain_recur<c64>(M, A->jac, A->degree, v.as<c64>(), w.as<c64>(), t1.as<c64>(), t2.as<c64>(), t3.as<c64>(), nullptr, st, c64(1.0f), c64(0.0f), nullptr);
       else
         op_chain<c64>(M, A->alpha_p, A->degree, v.as<c64>(), w.as<c64>(), t1.as<c64>(), t2.as<c64>(), nullptr, st, c64(1.0f), c64(0.0f), nullptr);
     };

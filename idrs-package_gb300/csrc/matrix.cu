@@ -104,7 +104,8 @@ template <class T, class R, bool SCALE>
 __global__ void __launch_bounds__(256) k_stencil7(int nx, int ny, int nz, int zc, R c0, R cw, R ce,
                                                   R cs, R cn, R cf, R cb, const T* __restrict__ x,
                                                   T* __restrict__ y, T a, T cv,
-                                                  const T* __restrict__ v,
+                                                  const T* __restrict__ v, T cu,
+                                                  const T* __restrict__ u,
                                                   const int* __restrict__ skip) {
   if (skip && *skip) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -124,6 +125,7 @@ __global__ void __launch_bounds__(256) k_stencil7(int nx, int ny, int nz, int zc
     T xn = j < ny - 1 ? x[p + nx] : T(0);
     T s = c0 * xc + cw * xw + ce * xe + cs * xs + cn * xn + cf * xm + cb * xp;
     T out = SCALE ? a * s : s;
+    if (u) out = out + cu * u[p];
     if (v) out = out + cv * v[p];
     y[p] = out;
     xm = xc;
@@ -137,7 +139,8 @@ template <int G, class T, class V>
 __global__ void __launch_bounds__(256) k_crs(int nrows, const int* __restrict__ rp,
                                              const int* __restrict__ ci, const V* __restrict__ val,
                                              const T* __restrict__ x, T* __restrict__ y, T a, T cv,
-                                             const T* __restrict__ v,
+                                             const T* __restrict__ v, T cx, T cu,
+                                             const T* __restrict__ u,
                                              const int* __restrict__ skip) {
   if (skip && *skip) return;
   constexpr int RPW = 32 / G;
@@ -157,6 +160,8 @@ __global__ void __launch_bounds__(256) k_crs(int nrows, const int* __restrict__ 
     for (int m = G / 2; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
     if (row < nrows && gl == 0) {
       T out = a * sum;
+      if (cx != T(0)) out = out + cx * x[row];
+      if (u) out = out + cu * u[row];
       if (v) out = out + cv * v[row];
       y[row] = out;
     }
@@ -169,7 +174,8 @@ template <class T, class V>
 __global__ void __launch_bounds__(256) k_crs_row(int nrows, const int* __restrict__ rp,
                                                  const int* __restrict__ ci, const V* __restrict__ val,
                                                  const T* __restrict__ x, T* __restrict__ y, T a, T cv,
-                                                 const T* __restrict__ v,
+                                                 const T* __restrict__ v, T cx, T cu,
+                                                 const T* __restrict__ u,
                                                  const int* __restrict__ skip) {
   if (skip && *skip) return;
   for (long row = blockIdx.x * (long)blockDim.x + threadIdx.x; row < nrows;
@@ -178,6 +184,8 @@ __global__ void __launch_bounds__(256) k_crs_row(int nrows, const int* __restric
     T sum = T(0);
     for (int k = beg; k < end; ++k) sum = sum + mulvt(val[k], x[ci[k]]);
     T out = a * sum;
+    if (cx != T(0)) out = out + cx * x[row];
+    if (u) out = out + cu * u[row];
     if (v) out = out + cv * v[row];
     y[row] = out;
   }
@@ -187,7 +195,8 @@ __global__ void __launch_bounds__(256) k_crs_row(int nrows, const int* __restric
 template <class T, class V>
 __global__ void __launch_bounds__(256) k_cds(int n, int hb, const V* __restrict__ band,
                                              const T* __restrict__ x, T* __restrict__ y, T a, T cv,
-                                             const T* __restrict__ v, const int* __restrict__ skip) {
+                                             const T* __restrict__ v, T cx, T cu,
+                                             const T* __restrict__ u, const int* __restrict__ skip) {
   if (skip && *skip) return;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x) {
     T s = T(0);
@@ -196,6 +205,8 @@ __global__ void __launch_bounds__(256) k_cds(int n, int hb, const V* __restrict_
       if (j >= 0 && j < n) s = s + mulvt(band[i + (long)n * (d + hb)], x[j]);
     }
     T out = a * s;
+    if (cx != T(0)) out = out + cx * x[i];
+    if (u) out = out + cu * u[i];
     if (v) out = out + cv * v[i];
     y[i] = out;
   }
@@ -205,13 +216,16 @@ __global__ void __launch_bounds__(256) k_cds(int n, int hb, const V* __restrict_
 template <class T, class V>
 __global__ void __launch_bounds__(256) k_dense(int nrows, int ncols, const V* __restrict__ mat,
                                                const T* __restrict__ x, T* __restrict__ y, T a,
-                                               T cv, const T* __restrict__ v,
+                                               T cv, const T* __restrict__ v, T cx, T cu,
+                                               const T* __restrict__ u,
                                                const int* __restrict__ skip) {
   if (skip && *skip) return;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nrows; i += gridDim.x * (long)blockDim.x) {
     T s = T(0);
     for (long j = 0; j < ncols; ++j) s = s + mulvt(mat[i + (long)nrows * j], x[j]);
     T out = a * s;
+    if (cx != T(0)) out = out + cx * x[i];
+    if (u) out = out + cu * u[i];
     if (v) out = out + cv * v[i];
     y[i] = out;
   }
@@ -219,36 +233,36 @@ __global__ void __launch_bounds__(256) k_dense(int nrows, int ncols, const V* __
 
 template <class T, class V>
 static void launch_crs(const MatView& M, const V* val, const T* x, T* y, T a, T cv, const T* v,
-                       const int* skip, cudaStream_t st) {
+                       T cx, T cu, const T* u, const int* skip, cudaStream_t st) {
   long rows_per_block = kThreads / M.group;
   long need = (M.nrows + rows_per_block - 1) / rows_per_block;
   int grid = (int)std::max(1L, std::min(need, (long)num_sms() * 8));
   if (M.group == 1) {
-    k_crs_row<T, V><<<stream_grid(M.nrows), kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip);
+    k_crs_row<T, V><<<stream_grid(M.nrows), kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip);
     return;
   }
   switch (M.group) {
-    case 2: k_crs<2><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip); break;
-    case 4: k_crs<4><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip); break;
-    case 8: k_crs<8><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip); break;
-    case 16: k_crs<16><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip); break;
-    default: k_crs<32><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, skip); break;
+    case 2: k_crs<2><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
+    case 4: k_crs<4><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
+    case 8: k_crs<8><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
+    case 16: k_crs<16><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
+    default: k_crs<32><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
   }
 }
 
 template <class T, class V>
 static void launch_valued(const MatView& M, const V* val, const T* x, T* y, T a, T cv, const T* v,
-                          const int* skip, cudaStream_t st) {
+                          T cx, T cu, const T* u, const int* skip, cudaStream_t st) {
   switch (M.format) {
     case FMT_CRS:
     case FMT_COO:
-      launch_crs<T, V>(M, val, x, y, a, cv, v, skip, st);
+      launch_crs<T, V>(M, val, x, y, a, cv, v, cx, cu, u, skip, st);
       break;
     case FMT_CDS:
-      k_cds<T, V><<<stream_grid(M.nrows), kThreads, 0, st>>>(M.nrows, M.hb, val, x, y, a, cv, v, skip);
+      k_cds<T, V><<<stream_grid(M.nrows), kThreads, 0, st>>>(M.nrows, M.hb, val, x, y, a, cv, v, cx, cu, u, skip);
       break;
     case FMT_DENSE:
-      k_dense<T, V><<<stream_grid(M.nrows), kThreads, 0, st>>>(M.nrows, M.ncols, val, x, y, a, cv, v, skip);
+      k_dense<T, V><<<stream_grid(M.nrows), kThreads, 0, st>>>(M.nrows, M.ncols, val, x, y, a, cv, v, cx, cu, u, skip);
       break;
     default:
       throw std::runtime_error("spmv: unsupported format");
@@ -256,8 +270,8 @@ static void launch_valued(const MatView& M, const V* val, const T* x, T* y, T a,
 }
 
 template <class T>
-static void launch_stencil(const MatView& M, const T* x, T* y, T a, T cv, const T* v,
-                           const int* skip, cudaStream_t st) {
+static void launch_stencil(const MatView& M, const T* x, T* y, T a, T cv, const T* v, T cx, T cu,
+                           const T* u, const int* skip, cudaStream_t st) {
   using R = typename traits<T>::real;
   dim3 blk(32, 8, 1);
   int gx = (M.nx + 31) / 32, gy = (M.ny + 7) / 8;
@@ -267,50 +281,44 @@ static void launch_stencil(const MatView& M, const T* x, T* y, T a, T cv, const 
   if (zc < 4 && M.nz >= 4) zc = 4;  // keep some register reuse along z
   int gz = (M.nz + zc - 1) / zc;
   dim3 grid(gx, gy, gz);
-  const bool real_a = (imag_(a) == 0);
-  if (real_a) {  // fold the real scale into the coefficients
+  const bool real_a = (imag_(a) == 0) && (imag_(cx) == 0);
+  if (real_a) {  // fold the real scale (and the centre term cx*x) into the coefficients
     double ar = (double)real_(a);
+    double c0 = ar * M.st[0] + (double)real_(cx);
     k_stencil7<T, R, false><<<grid, blk, 0, st>>>(
-        M.nx, M.ny, M.nz, zc, R(ar * M.st[0]), R(ar * M.st[1]), R(ar * M.st[2]), R(ar * M.st[3]),
-        R(ar * M.st[4]), R(ar * M.st[5]), R(ar * M.st[6]), x, y, a, cv, v, skip);
+        M.nx, M.ny, M.nz, zc, R(c0), R(ar * M.st[1]), R(ar * M.st[2]), R(ar * M.st[3]),
+        R(ar * M.st[4]), R(ar * M.st[5]), R(ar * M.st[6]), x, y, a, cv, v, cu, u, skip);
   } else {
+    if (cx != T(0)) throw std::runtime_error("stencil: complex centre term unsupported");
     k_stencil7<T, R, true><<<grid, blk, 0, st>>>(
         M.nx, M.ny, M.nz, zc, R(M.st[0]), R(M.st[1]), R(M.st[2]), R(M.st[3]), R(M.st[4]),
-        R(M.st[5]), R(M.st[6]), x, y, a, cv, v, skip);
+        R(M.st[5]), R(M.st[6]), x, y, a, cv, v, cu, u, skip);
   }
 }
 
-template <>
-void spmv<double>(const MatView& M, const double* x, double* y, double a, double cv,
-                  const double* v, const int* skip, cudaStream_t st) {
-  if (M.format == FMT_STENCIL7) launch_stencil<double>(M, x, y, a, cv, v, skip, st);
-  else if (M.vcplx) throw std::runtime_error("spmv: complex matrix applied to a real vector");
-  else launch_valued<double, double>(M, (const double*)M.val, x, y, a, cv, v, skip, st);
+template <class T>
+void spmv_ex(const MatView& M, const T* x, T* y, const Epi<T>& e, const int* skip, cudaStream_t st) {
+  using R = typename traits<T>::real;
+  using C = cplx<R>;
+  if (M.format == FMT_STENCIL7) {
+    launch_stencil<T>(M, x, y, e.a, e.cv, e.v, e.cx, e.cu, e.u, skip, st);
+  } else if (M.vcplx) {
+    if constexpr (traits<T>::is_cplx) launch_valued<T, C>(M, (const C*)M.val, x, y, e.a, e.cv, e.v, e.cx, e.cu, e.u, skip, st);
+    else throw std::runtime_error("spmv: complex matrix applied to a real vector");
+  } else {
+    launch_valued<T, R>(M, (const R*)M.val, x, y, e.a, e.cv, e.v, e.cx, e.cu, e.u, skip, st);
+  }
   IDRS_LAUNCH_CHECK();
 }
-template <>
-void spmv<float>(const MatView& M, const float* x, float* y, float a, float cv, const float* v,
-                 const int* skip, cudaStream_t st) {
-  if (M.format == FMT_STENCIL7) launch_stencil<float>(M, x, y, a, cv, v, skip, st);
-  else if (M.vcplx) throw std::runtime_error("spmv: complex matrix applied to a real vector");
-  else launch_valued<float, float>(M, (const float*)M.val, x, y, a, cv, v, skip, st);
-  IDRS_LAUNCH_CHECK();
-}
-template <>
-void spmv<c128>(const MatView& M, const c128* x, c128* y, c128 a, c128 cv, const c128* v,
-                const int* skip, cudaStream_t st) {
-  if (M.format == FMT_STENCIL7) launch_stencil<c128>(M, x, y, a, cv, v, skip, st);
-  else if (M.vcplx) launch_valued<c128, c128>(M, (const c128*)M.val, x, y, a, cv, v, skip, st);
-  else launch_valued<c128, double>(M, (const double*)M.val, x, y, a, cv, v, skip, st);
-  IDRS_LAUNCH_CHECK();
-}
-template <>
-void spmv<c64>(const MatView& M, const c64* x, c64* y, c64 a, c64 cv, const c64* v,
-               const int* skip, cudaStream_t st) {
-  if (M.format == FMT_STENCIL7) launch_stencil<c64>(M, x, y, a, cv, v, skip, st);
-  else if (M.vcplx) launch_valued<c64, c64>(M, (const c64*)M.val, x, y, a, cv, v, skip, st);
-  else launch_valued<c64, float>(M, (const float*)M.val, x, y, a, cv, v, skip, st);
-  IDRS_LAUNCH_CHECK();
+
+template <class T>
+void spmv(const MatView& M, const T* x, T* y, T a, T cv, const T* v, const int* skip,
+          cudaStream_t st) {
+  Epi<T> e;
+  e.a = a;
+  e.cv = cv;
+  e.v = v;
+  spmv_ex<T>(M, x, y, e, skip, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -334,6 +342,63 @@ void op_chain(const MatView& Ks, const std::vector<c128>& alpha, int degree, con
     std::swap(cur, nxt);
   }
   spmv<T>(Ks, cur, w, fa, fcv, fv, skip, st);
+}
+
+// A p(A) v with p evaluated through the three-term recurrence of its
+// tridiagonal Jacobi matrix (Chebyshev / Neumann, matrix_module.f90:851-941)
+// instead of monomial Horner.  With r_i(t) = 1 - t p_i(t) and column i of J
+// holding (a_i, b_i, c_i) = (J(i-1,i), J(i,i), J(i+1,i)), a_i + b_i + c_i = 0:
+//   y_0 = 0,  y_1 = -v / c_1,
+//   y_i = (A y_{i-1} - b_i y_{i-1} - a_i y_{i-2} - v) / c_i ,  i = 2..d+1
+// and p(A) v = y_{d+1}.  The iterates stay of the size of A^-1 v, so the fp32
+// form keeps its accuracy where the monomial coefficients (|alpha| ~ 10^3-10^4
+// with alternating signs for a degree-8 Chebyshev polynomial) cancel.
+template <class T>
+void op_chain_recur(const MatView& Ks, const JacobiCols& J, int degree, const T* v, T* w, T* t1,
+                    T* t2, T* t3, const int* skip, cudaStream_t st, T fa, T fcv, const T* fv) {
+  if (degree == 0) {
+    spmv<T>(Ks, v, w, fa, fcv, fv, skip, st);
+    return;
+  }
+  auto C = [](c128 z) { return narrow<T>(z); };
+  // y_1 = -v/c_1 ; y_2 = (A y_1 - b_2 y_1 - v)/c_2 read from v alone
+  T* buf[3] = {t1, t2, t3};
+  const T* ym2 = nullptr;  // y_{i-2}
+  const T* ym1 = nullptr;  // y_{i-1}
+  {
+    c128 c1 = J.c[0], b2 = J.b[1], c2 = J.c[1];
+    c128 s1 = c128(-1.0) / c1;  // y_1 = s1 v
+    Epi<T> e;
+    e.a = C(s1 / c2);            // (A y_1)/c2
+    e.cx = C((c128(0.0) - b2 * s1 - c128(1.0)) / c2);  // (-b2 y_1 - v)/c2, y_1 and v share v
+    spmv_ex<T>(Ks, v, buf[0], e, skip, st);
+    ym2 = nullptr;
+    ym1 = buf[0];
+    // y_1 itself is s1*v: keep it implicit, the next step needs y_{i-2} = y_1
+  }
+  int nb = 1;
+  for (int i = 3; i <= degree + 1; ++i) {
+    c128 ai = J.a[i - 1], bi = J.b[i - 1], ci = J.c[i - 1];
+    Epi<T> e;
+    e.a = C(c128(1.0) / ci);
+    e.cx = C(c128(0.0) - bi / ci);
+    e.cv = C(c128(-1.0) / ci);
+    e.v = v;
+    if (i == 3) {  // y_{i-2} = y_1 = s1 v: fold into the v term
+      c128 s1 = c128(-1.0) / J.c[0];
+      e.cv = C((c128(-1.0) - ai * s1) / ci);
+    } else if (ai != c128(0.0)) {  // Neumann: a_i = 0, no y_{i-2} read
+      e.cu = C(c128(0.0) - ai / ci);
+      e.u = ym2;
+    }
+    T* out = buf[nb % 3];
+    spmv_ex<T>(Ks, ym1, out, e, skip, st);
+    ym2 = ym1;
+    ym1 = out;
+    ++nb;
+  }
+  (void)ym2;
+  spmv<T>(Ks, ym1, w, fa, fcv, fv, skip, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -689,6 +754,10 @@ void operator_free(Operator* A) {
 // explicit instantiations
 // ---------------------------------------------------------------------------
 #define IDRS_INST(T)                                                                              \
+  template void spmv<T>(const MatView&, const T*, T*, T, T, const T*, const int*, cudaStream_t);    \
+  template void spmv_ex<T>(const MatView&, const T*, T*, const Epi<T>&, const int*, cudaStream_t); \
+  template void op_chain_recur<T>(const MatView&, const JacobiCols&, int, const T*, T*, T*, T*, T*, \
+                                  const int*, cudaStream_t, T, T, const T*);                       \
   template void op_chain<T>(const MatView&, const std::vector<c128>&, int, const T*, T*, T*, T*,   \
                             const int*, cudaStream_t, T, T, const T*);                            \
   template void op_scaleback<T>(Operator&, int, const std::vector<c128>&, int, const T*, T*, T*,  \

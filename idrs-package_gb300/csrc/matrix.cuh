@@ -39,6 +39,21 @@ struct MatView {
   int group = 8;                          // CRS lanes per row
 };
 
+// Three diagonals of a tridiagonal Jacobi matrix J((d+2) x (d+1)):
+// a[i-1] = J(i-1,i), b[i-1] = J(i,i), c[i-1] = J(i+1,i), i = 1..d+1.
+struct JacobiCols {
+  std::vector<c128> a, b, c;
+  bool valid() const { return !c.empty(); }
+};
+
+// SpMV epilogue: y = a*(M x) + cx*x + cu*u + cv*v   (u, v may be null)
+template <class T>
+struct Epi {
+  T a = T(1), cx = T(0), cu = T(0), cv = T(0);
+  const T* u = nullptr;
+  const T* v = nullptr;
+};
+
 struct UserMatrix {
   int format = FMT_NONE;
   int which_precon = 0;
@@ -74,6 +89,7 @@ struct Operator {
   c128 seed;                // rseed / cseed
   int preconditioner = 0, degree = 0;
   std::vector<c128> alpha_p;  // 0..degree
+  JacobiCols jac;             // tridiagonal Jacobi matrix of the polynomial (Chebyshev/Neumann)
   int n_sigma = 0;
   std::vector<c128> alpha_s;  // (degree+1) x n_sigma
   cudaStream_t stream = nullptr;
@@ -112,6 +128,15 @@ void free_redbuf(RedBuf rb, cudaStream_t st);
 template <class T>
 void spmv(const MatView& M, const T* x, T* y, T a, T cv, const T* v, const int* skip,
           cudaStream_t st);
+template <class T>
+void spmv_ex(const MatView& M, const T* x, T* y, const Epi<T>& e, const int* skip, cudaStream_t st);
+
+// w = fa * Ks p(Ks) v + fcv * fv with p from its Jacobi three-term recurrence
+// (numerically stable; used by the fp32 inner solves).  t1..t3: scratch.
+template <class T>
+void op_chain_recur(const MatView& Ks, const JacobiCols& J, int degree, const T* v, T* w, T* t1,
+                    T* t2, T* t3, const int* skip, cudaStream_t st, T fa = T(1), T fcv = T(0),
+                    const T* fv = nullptr);
 
 // w = Ks p(Ks) v, then the final product gets the epilogue
 //   w = fa * (Ks u) + fcv * fv.

@@ -38,21 +38,22 @@ static int compute_alpha_t(int degree, const S* H, int ldh, int nh, S* alpha) {
   return 0;
 }
 
-// rneumann / cneumann: matrix_module.f90:851-901
+// Jacobi matrix of the Neumann residual polynomials: matrix_module.f90:851-875
 template <class S>
-static int neumann_t(int degree, S center, S* alpha) {
+static std::vector<S> neumann_jacobi_t(int degree, S center) {
   const int ld = degree + 2;
   std::vector<S> J((size_t)ld * (degree + 1), S(0.0));
   for (int i = 1; i <= degree + 1; ++i) {
     J[(i - 1) + (size_t)ld * (i - 1)] = center;
     J[i + (size_t)ld * (i - 1)] = -center;
   }
-  return compute_alpha_t<S>(degree, J.data(), ld, degree + 1, alpha);
+  return J;
 }
 
-// rchebyshev / cchebyshev: matrix_module.f90:903-981
+// Jacobi matrix of the shifted and scaled Chebyshev residual polynomials:
+// matrix_module.f90:903-941
 template <class S>
-static int chebyshev_t(int degree, const S* foci, S* alpha) {
+static std::vector<S> chebyshev_jacobi_t(int degree, const S* foci) {
   S theta = (foci[0] + foci[1]) / 2.0;
   S delta = (foci[0] - foci[1]) / 2.0;
   S sigma = theta / delta;
@@ -67,7 +68,18 @@ static int chebyshev_t(int degree, const S* foci, S* alpha) {
     J[i + (size_t)ld * (i - 1)] = -delta * sigma + delta * rho / 2.0;
     rho = S(1.0) / (2.0 * sigma - rho);
   }
-  return compute_alpha_t<S>(degree, J.data(), ld, degree + 1, alpha);
+  return J;
+}
+
+template <class S>
+static int neumann_t(int degree, S center, S* alpha) {
+  auto J = neumann_jacobi_t<S>(degree, center);
+  return compute_alpha_t<S>(degree, J.data(), degree + 2, degree + 1, alpha);
+}
+template <class S>
+static int chebyshev_t(int degree, const S* foci, S* alpha) {
+  auto J = chebyshev_jacobi_t<S>(degree, foci);
+  return compute_alpha_t<S>(degree, J.data(), degree + 2, degree + 1, alpha);
 }
 
 int compute_alpha(int degree, const double* H, int ldh, int nh, double* a) { return compute_alpha_t(degree, H, ldh, nh, a); }
@@ -76,6 +88,8 @@ int neumann(int degree, double c, double* a) { return neumann_t(degree, c, a); }
 int neumann(int degree, cd c, cd* a) { return neumann_t(degree, c, a); }
 int chebyshev(int degree, const double* f, double* a) { return chebyshev_t(degree, f, a); }
 int chebyshev(int degree, const cd* f, cd* a) { return chebyshev_t(degree, f, a); }
+std::vector<cd> neumann_jacobi(int degree, cd center) { return neumann_jacobi_t<cd>(degree, center); }
+std::vector<cd> chebyshev_jacobi(int degree, const cd* foci) { return chebyshev_jacobi_t<cd>(degree, foci); }
 
 // CQR_factorization with refine = 2: dense_la_module.f90:42-83
 static int cqr_factorization(int m, const cd* V, int ldv, cd* Q, cd* R) {

@@ -1,6 +1,7 @@
 // setup.h -- host set-up arithmetic of the polynomial preconditioners.
 #pragma once
 #include <complex>
+#include <vector>
 
 namespace idrs {
 int compute_alpha(int degree, const double* H, int ldh, int nh, double* alpha);
@@ -9,6 +10,10 @@ int neumann(int degree, double center, double* alpha);
 int neumann(int degree, std::complex<double> center, std::complex<double>* alpha);
 int chebyshev(int degree, const double* foci, double* alpha);
 int chebyshev(int degree, const std::complex<double>* foci, std::complex<double>* alpha);
+// Jacobi matrices ((degree+2) x (degree+1), column-major) of the residual
+// polynomials; real problems pass real values with zero imaginary parts.
+std::vector<std::complex<double>> neumann_jacobi(int degree, std::complex<double> center);
+std::vector<std::complex<double>> chebyshev_jacobi(int degree, const std::complex<double>* foci);
 void qr_eig(const double* H, int ldh, int n, std::complex<double>* eig, int* converged);
 void qr_eig(const std::complex<double>* H, int ldh, int n, std::complex<double>* eig, int* converged);
 void analyse_spectrum(const double* H, int ldh, int n, double* foci, double* center, double* shift);

@@ -282,3 +282,19 @@ def test_pp_idrs_matches_oracle(gpu, oracle, P):
     np.testing.assert_allclose(g.foci, o.foci, rtol=1e-6)
     assert g.relres_original <= 1e-8 * 1.01
     assert _rel(g.x, o.x) <= 1e-7
+
+
+def test_mixed_precision_with_chebyshev(gpu, P):
+    """fp32 inner IDR(4) on a Chebyshev(8)-preconditioned operator (the
+    polynomial evaluated by its stable Jacobi recurrence) inside the FP64
+    QMRIDR(8): converges to 1e-8 in a few outer iterations."""
+    n = 32
+    coef = P.cdr_coefficients(n)
+    N = n ** 3
+    K = gpu.stencil7_format(n, n, n, coef)
+    b = K * np.ones(N)
+    r = gpu.PP_IDRS(K, b, P=gpu.real_precon(1, K), method=0, s=8, tol=1e-8, maxit=60, preconditioner=2,
+                    degree=8, n_ritz=20, in_s=4, in_it=300, in_tol=1e-2, inner_precision=32)
+    assert r.flag == 0 and r.iterations <= 10
+    assert r.relres_original <= 1.01e-8
+    np.testing.assert_allclose(r.x, 1.0, atol=1e-6)
