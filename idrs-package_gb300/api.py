@@ -91,6 +91,7 @@ _PROTOS = {
     "idrs_cnorm": (_i, [_vp, _vp, _vp]),
     "idrs_rinprod": (_i, [_vp, _vp, _vp, _vp]),
     "idrs_cinprod": (_i, [_vp, _vp, _vp, _vp]),
+    "idrs_rinprod_noalloc": (_i, [C.c_long, _vp, _vp, _vp, _vp]),
     "idrs_ridrs_ritz": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp]),
     "idrs_rpp_idrs": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }

@@ -190,6 +190,18 @@ int idrs_cnorm(idrs_matrix A, const double *w, double *norm);
 int idrs_rinprod(idrs_matrix A, const double *u, const double *v, double *uv);
 int idrs_cinprod(idrs_matrix A, const double *u, const double *v, double *uv);
 
+/* INPROD(u, v) = sum u_i v_i of two real device vectors of length n, written
+ * to the device double *uv, without allocating any device memory.  No
+ * counterpart in the reference: it serves callers that cannot call
+ * cudaMalloc (their device memory belongs to another allocator, or their
+ * policy forbids allocating after start-up).  Its scratch is a static
+ * 128 KiB device array held by every GPU that loads this library, so n is
+ * limited to 67,108,864 (IDRS_ERR_ARG beyond).  The first call on each device
+ * performs a one-time set-up; make it before any stream capture.  The call
+ * is asynchronous on `stream` (a cudaStream_t, NULL for the default stream);
+ * calls that overlap on the GPU share the scratch and race. */
+int idrs_rinprod_noalloc(long n, const double *u, const double *v, double *uv, void *stream);
+
 /* x = IDRS_RITZ(A, b, s[, M, tolerance, maximum_iterations, variant, flag,
  *               relres, iterations, x0, ..., H]): ritz_module.f90:389-556
  * (the Hessenberg output; recycling U0/omega outputs are not provided).
