@@ -9,7 +9,8 @@ The names, argument meanings and error behaviour follow the Fortran modules
   matrix_module : Matrix (type(matrix)), real_preconditioner /
                   complex_preconditioner, ms_parameters, A * v, v / A,
                   scaleback
-  idrs_module   : IDRS, QMRIDR, NORM, INPROD (and IDRS_RITZ, PP_IDRS)
+  idrs_module   : IDRS, QMRIDR, MSIDRS, MSQMRIDR, NORM, INPROD (and IDRS_RITZ,
+                  PP_IDRS)
 
 Every call goes through libidrs_gb300.so (CUDA, sm_103a).  There is no CPU
 fallback: importing this module raises if the library is missing, and a
@@ -87,6 +88,14 @@ _PROTOS = {
                           _i, _vp, _i, _vp, _vp]),
     "idrs_cqmridr": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                           _i, _vp, _i, _vp, _vp]),
+    "idrs_rmsidrs": (_i, [_vp, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp,
+                          _i, _vp, _vp]),
+    "idrs_cmsidrs": (_i, [_vp, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp,
+                          _i, _vp, _vp]),
+    "idrs_rmsqmridr": (_i, [_vp, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                            _vp, _i, _vp, _i, _vp, _vp]),
+    "idrs_cmsqmridr": (_i, [_vp, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                            _vp, _i, _vp, _i, _vp, _vp]),
     "idrs_rnorm": (_i, [_vp, _vp, _vp]),
     "idrs_cnorm": (_i, [_vp, _vp, _vp]),
     "idrs_rinprod": (_i, [_vp, _vp, _vp, _vp]),
@@ -468,6 +477,70 @@ def QMRIDR(A: Matrix, b, s, M1: Matrix | None = None, tolerance=None, maximum_it
               _p(om), 0 if om is None else len(om), _p(rv), 0 if rv is None else len(rv),
               _ref_int(inner_precision), _p(x)))
     r = Result(x=x, flag=flag.value, relres=relres.value, iterations=iters.value)
+    if rv is not None:
+        r["resvec"] = rv
+    return r
+
+
+def _shifts(A: Matrix, sigma):
+    sig = np.ascontiguousarray(np.atleast_1d(sigma), dtype=np.complex128 if A.cplx else np.float64)
+    if sig.ndim != 1 or len(sig) < 1:
+        raise IDRSError(IDRS_ERR_ARG, "sigma must be a non-empty vector of shifts")
+    return sig
+
+
+def MSIDRS(A: Matrix, b, sigma, s, M1: Matrix | None = None, tolerance=None,
+           maximum_iterations=None, variant=None, omega=None, resvec=False,
+           colfac=False) -> Result:
+    """x(:, k) = MSIDRS(A, b, sigma, s, ...) (RMSIDRS/CMSIDRS, idrs_module.f90:572-713):
+    (A - sigma_k I) x_k = b for every shift; relres has one entry per shift."""
+    b = _solver_common(A, b)
+    n = len(b)
+    sig = _shifts(A, sigma)
+    ns = len(sig)
+    maxit = maximum_iterations if maximum_iterations is not None else min(2 * n, 1000)
+    x = np.empty((n, ns), dtype=b.dtype, order="F")
+    flag, iters = C.c_int(), C.c_int()
+    relres = np.ones(ns)
+    om = _arr(omega, A.cplx)
+    rv = np.zeros((maxit + 1, ns), order="F") if resvec else None
+    cf = np.empty(ns, dtype=b.dtype) if colfac else None
+    fn = lib().idrs_cmsidrs if A.cplx else lib().idrs_rmsidrs
+    _check(fn(A.handle, _p(b), ns, _p(sig), int(s), M1.handle if M1 else None,
+              _ref_dbl(tolerance), _ref_int(maximum_iterations), _ref_int(variant),
+              C.byref(flag), _p(relres), C.byref(iters), _p(om), 0 if om is None else len(om),
+              _p(rv), 0 if rv is None else maxit + 1, _p(cf), _p(x)))
+    r = Result(x=x, flag=flag.value, relres=relres, iterations=iters.value)
+    if rv is not None:
+        r["resvec"] = rv
+    if cf is not None:
+        r["colfac"] = cf
+    return r
+
+
+def MSQMRIDR(A: Matrix, b, sigma, s, M1: Matrix | None = None, tolerance=None,
+             maximum_iterations=None, inner_s=None, inner_tolerance=None,
+             inner_iterations=None, omega=None, resvec=False, inner_precision=None) -> Result:
+    """x(:, k) = MSQMRIDR(A, b, sigma, s, ...) (RMSQMRIDR/CMSQMRIDR,
+    idrs_module.f90:410-570).  inner_precision=32 runs the inner MSIDRS in
+    fp32 / complex64."""
+    b = _solver_common(A, b)
+    n = len(b)
+    sig = _shifts(A, sigma)
+    ns = len(sig)
+    maxit = maximum_iterations if maximum_iterations is not None else min(2 * n, 1000)
+    x = np.empty((n, ns), dtype=b.dtype, order="F")
+    flag, iters = C.c_int(), C.c_int()
+    relres = np.ones(ns)
+    om = _arr(omega, A.cplx)
+    rv = np.zeros((maxit + 1, ns), order="F") if resvec else None
+    fn = lib().idrs_cmsqmridr if A.cplx else lib().idrs_rmsqmridr
+    _check(fn(A.handle, _p(b), ns, _p(sig), int(s), M1.handle if M1 else None,
+              _ref_dbl(tolerance), _ref_int(maximum_iterations), C.byref(flag), _p(relres),
+              C.byref(iters), _ref_int(inner_s), _ref_dbl(inner_tolerance),
+              _ref_int(inner_iterations), _p(om), 0 if om is None else len(om), _p(rv),
+              0 if rv is None else maxit + 1, _ref_int(inner_precision), _p(x)))
+    r = Result(x=x, flag=flag.value, relres=relres, iterations=iters.value)
     if rv is not None:
         r["resvec"] = rv
     return r

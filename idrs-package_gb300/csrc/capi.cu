@@ -10,6 +10,7 @@
 
 #include "../../include/idrs_gb300.h"
 #include "idrs_gpu.cuh"
+#include "ms_gpu.cuh"
 #include "setup.h"
 
 using namespace idrs;
@@ -420,6 +421,144 @@ int run_qmridr(Operator* A, const double* b, int s, Operator* M1, const double* 
   sv.finish(x, d_x);
   if (resvec) IDRS_CUDA(cudaMemcpyAsync(resvec, d_res.p, sizeof(double) * resvec_len, cudaMemcpyDeviceToHost, st));
   IDRS_CUDA(cudaStreamSynchronize(st));
+  return IDRS_OK;
+}
+
+// ------------------------------------------------------------- multishift
+// Shifts and user omegas arrive as host arrays of the vector kind; x is
+// n x n_sigma column-major; resvec(resvec_len, n_sigma) column-major.
+template <class T>
+struct MsCommon {
+  using W = typename traits<T>::wide;
+  DBuf d_sigma, d_res, d_om;
+  void setup(Operator* A, int n_sigma, const double* sigma, const double* omega, int n_omega,
+             double* resvec, int resvec_len, int maxit, SolveOpts& o) {
+    cudaStream_t st = A->stream;
+    d_sigma = DBuf(sizeof(W) * n_sigma, st);
+    IDRS_CUDA(cudaMemcpyAsync(d_sigma.p, sigma, sizeof(W) * n_sigma, cudaMemcpyHostToDevice, st));
+    if (resvec) {
+      REQUIRE(maxit + 1 <= resvec_len, "Length of vector with residual norms too small, should be maxit+1");
+      size_t bytes = sizeof(double) * (size_t)resvec_len * n_sigma;
+      d_res = DBuf(bytes, st);
+      IDRS_CUDA(cudaMemsetAsync(d_res.p, 0, bytes, st));
+    }
+    if (omega && n_omega > 0) {
+      d_om = DBuf(sizeof(W) * n_omega, st);
+      IDRS_CUDA(cudaMemcpyAsync(d_om.p, omega, sizeof(W) * n_omega, cudaMemcpyHostToDevice, st));
+    }
+    o.omega = d_om.p;
+    o.n_omega = (omega && n_omega > 0) ? n_omega : 0;
+    o.resvec = d_res.as<double>();
+    o.resvec_len = resvec_len;
+  }
+  void finish(Operator* A, int n_sigma, double* resvec, int resvec_len) {
+    if (resvec)
+      IDRS_CUDA(cudaMemcpyAsync(resvec, d_res.p, sizeof(double) * (size_t)resvec_len * n_sigma,
+                                cudaMemcpyDeviceToHost, A->stream));
+  }
+};
+
+template <class T>
+int run_msidrs(Operator* A, const double* b, int n_sigma, const double* sigma, int s, Operator* M1,
+               const double* tolerance, const int* maximum_iterations, const int* variant,
+               int* flag, double* relres, int* iterations, const double* omega, int n_omega,
+               double* resvec, int resvec_len, double* colfac, double* x) {
+  using W = typename traits<T>::wide;
+  REQUIRE(A && b && sigma && x, "msidrs: A, b, sigma and x are required");
+  REQUIRE(s >= 1, "msidrs: s must be positive");
+  REQUIRE(n_sigma >= 1, "msidrs: at least one shift is required");
+  if (s > MAXS) throw unsupported_error("msidrs: s > 16 is not supported by the GPU path");
+  if (n_sigma > MAXSIG) throw unsupported_error("msidrs: more than 64 shifts are not supported by the GPU path");
+  SolveOpts o;
+  if (tolerance) {
+    REQUIRE(*tolerance >= 0, "Illegal value for parameter tolerance");
+    o.tol = *tolerance;
+  }
+  const long n = A->n();
+  o.maxit = maximum_iterations ? *maximum_iterations : (int)std::min<long>(2 * n, 1000);
+  o.method = variant ? *variant : 1;
+  REQUIRE(o.method == 1 || o.method == 2, "msidrs: variant must be 1 (msidrs) or 2 (msbicgstab)");
+  REQUIRE(o.method == 1 || s == 1, "msidrs: variant 2 uses one shadow vector (s = 1)");
+  if (flag) *flag = -1;
+  if (relres) for (int k = 0; k < n_sigma; ++k) relres[k] = 1.0;
+  if (iterations) *iterations = 0;
+  MsCommon<T> mc;
+  mc.setup(A, n_sigma, sigma, omega, n_omega, resvec, resvec_len, o.maxit, o);
+  Staged sv(A, sizeof(T) * n), sx(A, sizeof(T) * n * n_sigma);
+  const T* d_b = (const T*)sv.in(b);
+  T* d_x = (T*)sx.out(x);
+  o.M1 = M1;
+  o.PT = find_shadow(A, s);
+  o.inner = false;
+  MsIdrsGpu<T> solver(*A, 64, s, n_sigma, o.method);
+  solver.solve(d_b, mc.d_sigma.template as<W>(), d_x, o);
+  auto h = solver.state();
+  if (flag) *flag = h.info;
+  if (iterations) *iterations = h.iter;
+  if (relres) for (int k = 0; k < n_sigma; ++k) relres[k] = h.normr[k] / h.normb;
+  if (colfac) std::memcpy(colfac, h.phi, sizeof(W) * n_sigma);
+  sx.finish(x, d_x);
+  mc.finish(A, n_sigma, resvec, resvec_len);
+  IDRS_CUDA(cudaStreamSynchronize(A->stream));
+  return IDRS_OK;
+}
+
+template <class T, class Tin>
+void run_msqmr_typed(Operator* A, int s, int n_sigma, const T* d_b, const typename traits<T>::wide* d_sigma,
+                     T* d_x, SolveOpts& o, int* flag, double* relres, int* iterations) {
+  MsQmrGpu<T, Tin> solver(*A, s, n_sigma, o);
+  solver.solve(d_b, d_sigma, d_x, o);
+  auto h = solver.state();
+  if (flag) *flag = h.info;
+  if (iterations) *iterations = h.iter;
+  if (relres) for (int k = 0; k < n_sigma; ++k) relres[k] = h.normr[k] / h.normb;
+}
+
+template <class T, class Tlow>
+int run_msqmridr(Operator* A, const double* b, int n_sigma, const double* sigma, int s, Operator* M1,
+                 const double* tolerance, const int* maximum_iterations, int* flag, double* relres,
+                 int* iterations, const int* inner_s, const double* inner_tolerance,
+                 const int* inner_iterations, const double* omega, int n_omega, double* resvec,
+                 int resvec_len, const int* inner_precision, double* x) {
+  using W = typename traits<T>::wide;
+  REQUIRE(A && b && sigma && x, "msqmridr: A, b, sigma and x are required");
+  REQUIRE(s >= 1, "msqmridr: s must be positive");
+  REQUIRE(n_sigma >= 1, "msqmridr: at least one shift is required");
+  if (s > MAXS) throw unsupported_error("msqmridr: s > 16 is not supported by the GPU path");
+  if (n_sigma + 1 > MAXSIG) throw unsupported_error("msqmridr: more than 63 shifts are not supported by the GPU path");
+  SolveOpts o;
+  if (tolerance) {
+    REQUIRE(*tolerance >= 0, "Illegal value for parameter tolerance");
+    o.tol = *tolerance;
+  }
+  const long n = A->n();
+  o.maxit = maximum_iterations ? *maximum_iterations : (int)std::min<long>(2 * n, 1000);
+  o.in_s = inner_s ? *inner_s : 4;
+  REQUIRE(o.in_s >= 1, "Illegal value for parameter inner_s");
+  if (o.in_s > MAXS) throw unsupported_error("msqmridr: inner_s > 16 is not supported by the GPU path");
+  o.in_tol = inner_tolerance ? *inner_tolerance : kInnerTolDefault;
+  REQUIRE(o.in_tol >= 0, "Illegal value for parameter inner_tolerance");
+  o.in_it = inner_iterations ? *inner_iterations : 0;
+  o.in_prec = inner_precision ? *inner_precision : 64;
+  REQUIRE(o.in_prec == 64 || o.in_prec == 32, "inner_precision must be 64 or 32");
+  if (flag) *flag = -1;
+  if (relres) for (int k = 0; k < n_sigma; ++k) relres[k] = 1.0;
+  if (iterations) *iterations = 0;
+  MsCommon<T> mc;
+  mc.setup(A, n_sigma, sigma, omega, n_omega, resvec, resvec_len, o.maxit, o);
+  Staged sv(A, sizeof(T) * n), sx(A, sizeof(T) * n * n_sigma);
+  const T* d_b = (const T*)sv.in(b);
+  T* d_x = (T*)sx.out(x);
+  o.M1 = M1;
+  o.PT = find_shadow(A, s);
+  const W* d_sigma = mc.d_sigma.template as<W>();
+  if (o.in_it > 0 && o.in_prec == 32)
+    run_msqmr_typed<T, Tlow>(A, s, n_sigma, d_b, d_sigma, d_x, o, flag, relres, iterations);
+  else
+    run_msqmr_typed<T, T>(A, s, n_sigma, d_b, d_sigma, d_x, o, flag, relres, iterations);
+  sx.finish(x, d_x);
+  mc.finish(A, n_sigma, resvec, resvec_len);
+  IDRS_CUDA(cudaStreamSynchronize(A->stream));
   return IDRS_OK;
 }
 
@@ -1013,6 +1152,57 @@ int idrs_cqmridr(idrs_matrix A, const double* b, int s, idrs_matrix M1, const do
     return run_qmridr<c128, c64>(A, b, s, M1, tolerance, maximum_iterations, flag, relres,
                                  iterations, inner_s, inner_tolerance, inner_iterations, x0,
                                  omega, n_omega, resvec, resvec_len, inner_precision, x);
+  });
+}
+
+int idrs_rmsidrs(idrs_matrix A, const double* b, int n_sigma, const double* sigma, int s,
+                 idrs_matrix M1, const double* tolerance, const int* maximum_iterations,
+                 const int* variant, int* flag, double* relres, int* iterations,
+                 const double* omega, int n_omega, double* resvec, int resvec_len, double* colfac,
+                 double* x) {
+  return guard([&] {
+    REQUIRE(A && !A->cplx, "rmsidrs: real matrix handle required");
+    return run_msidrs<double>(A, b, n_sigma, sigma, s, M1, tolerance, maximum_iterations, variant,
+                              flag, relres, iterations, omega, n_omega, resvec, resvec_len, colfac, x);
+  });
+}
+int idrs_cmsidrs(idrs_matrix A, const double* b, int n_sigma, const double* sigma, int s,
+                 idrs_matrix M1, const double* tolerance, const int* maximum_iterations,
+                 const int* variant, int* flag, double* relres, int* iterations,
+                 const double* omega, int n_omega, double* resvec, int resvec_len, double* colfac,
+                 double* x) {
+  return guard([&] {
+    REQUIRE(A && A->cplx, "cmsidrs: complex matrix handle required");
+    return run_msidrs<c128>(A, b, n_sigma, sigma, s, M1, tolerance, maximum_iterations, variant,
+                            flag, relres, iterations, omega, n_omega, resvec, resvec_len, colfac, x);
+  });
+}
+int idrs_rmsqmridr(idrs_matrix A, const double* b, int n_sigma, const double* sigma, int s,
+                   idrs_matrix M1, const double* tolerance, const int* maximum_iterations,
+                   int* flag, double* relres, int* iterations, const int* inner_s,
+                   const double* inner_tolerance, const int* inner_iterations,
+                   const double* omega, int n_omega, double* resvec, int resvec_len,
+                   const int* inner_precision, double* x) {
+  return guard([&] {
+    REQUIRE(A && !A->cplx, "rmsqmridr: real matrix handle required");
+    return run_msqmridr<double, float>(A, b, n_sigma, sigma, s, M1, tolerance, maximum_iterations,
+                                       flag, relres, iterations, inner_s, inner_tolerance,
+                                       inner_iterations, omega, n_omega, resvec, resvec_len,
+                                       inner_precision, x);
+  });
+}
+int idrs_cmsqmridr(idrs_matrix A, const double* b, int n_sigma, const double* sigma, int s,
+                   idrs_matrix M1, const double* tolerance, const int* maximum_iterations,
+                   int* flag, double* relres, int* iterations, const int* inner_s,
+                   const double* inner_tolerance, const int* inner_iterations,
+                   const double* omega, int n_omega, double* resvec, int resvec_len,
+                   const int* inner_precision, double* x) {
+  return guard([&] {
+    REQUIRE(A && A->cplx, "cmsqmridr: complex matrix handle required");
+    return run_msqmridr<c128, c64>(A, b, n_sigma, sigma, s, M1, tolerance, maximum_iterations,
+                                   flag, relres, iterations, inner_s, inner_tolerance,
+                                   inner_iterations, omega, n_omega, resvec, resvec_len,
+                                   inner_precision, x);
   });
 }
 

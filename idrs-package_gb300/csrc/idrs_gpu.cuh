@@ -487,9 +487,9 @@ class IdrsGpu {
 // ---------------------------------------------------------------------------
 // QMRIDR(s) bodies and tails (qmridr.inc:129-254)
 // ---------------------------------------------------------------------------
-template <class T, class W>
+template <class T, class W, class S = QmrState<W>>
 struct BQv {  // v = gn - sum_i gamma_i G_i (logical G_1..G_s)
-  const T* gn; const T* pool; long ld; int gmap[MAXS]; int s; T* v; const QmrState<W>* st;
+  const T* gn; const T* pool; long ld; int gmap[MAXS]; int s; T* v; const S* st;
   struct Shared { T g[MAXS]; };
   __device__ void prepare(Shared& sh) const {
     for (int q = threadIdx.x; q < s; q += blockDim.x) sh.g[q] = narrow<T>(st->gamma[q]);
@@ -504,9 +504,9 @@ struct BQv {  // v = gn - sum_i gamma_i G_i (logical G_1..G_s)
 
 // One modified Gram-Schmidt pass: gn' = gn - c*y (c = 1/om on y = v with a
 // division, or beta_prev on y = G_prev); acc0 = (G_next, gn') or |gn'|^2.
-template <class T, class W>
+template <class T, class W, class S = QmrState<W>>
 struct BMgs {
-  T* gn; const T* y; const T* gnext; bool div_by_om; int prev; const QmrState<W>* st;
+  T* gn; const T* y; const T* gnext; bool div_by_om; int prev; const S* st;
   struct Shared { T c; };
   __device__ void prepare(Shared& sh) const {
     // v/om as v*(1/om): one FP64 multiply per element instead of a division
@@ -550,9 +550,9 @@ struct BQw {
   }
 };
 // gn /= normg; acc_j = PT_j . gn   (start of the iteration loop)
-template <class T, class W>
+template <class T, class W, class S = QmrState<W>>
 struct BQstart {
-  T* gn; const T* PT; long ld; int s; const QmrState<W>* st;
+  T* gn; const T* PT; long ld; int s; const S* st;
   struct Shared { typename traits<T>::real inorm; };
   __device__ void prepare(Shared& sh) const { if (threadIdx.x == 0) sh.inorm = (typename traits<T>::real)(1.0 / st->normg); }
   template <int ND, class A>

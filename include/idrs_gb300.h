@@ -184,6 +184,46 @@ int idrs_cqmridr(idrs_matrix A, const double *b, int s, idrs_matrix M1,
                  const double *omega, int n_omega, double *resvec, int resvec_len,
                  const int *inner_precision, double *x);
 
+/* x(n, n_sigma) = MSIDRS(A, b, sigma, s[, M1, tolerance, maximum_iterations,
+ *                 variant, flag, relres, iterations, omega, resvec, colfac]):
+ * RMSIDRS idrs_module.f90:572-641, CMSIDRS :643-713, body M/IDRS/msidrs.inc.
+ * Solves (A - sigma_k I) x_k = b for every shift.  sigma(n_sigma) and
+ * omega(n_omega) have the kind of b (complex: interleaved re/im);
+ * relres(n_sigma); resvec(resvec_len, n_sigma) column-major with
+ * resvec_len >= maxit+1; colfac(n_sigma) of the kind of b; x column-major.
+ * variant 1: MSIDRS(s), 2: MSBiCGSTAB (s = 1).  n_sigma <= 64. */
+int idrs_rmsidrs(idrs_matrix A, const double *b, int n_sigma, const double *sigma, int s,
+                 idrs_matrix M1, const double *tolerance, const int *maximum_iterations,
+                 const int *variant, int *flag, double *relres, int *iterations,
+                 const double *omega, int n_omega, double *resvec, int resvec_len, double *colfac,
+                 double *x);
+int idrs_cmsidrs(idrs_matrix A, const double *b, int n_sigma, const double *sigma, int s,
+                 idrs_matrix M1, const double *tolerance, const int *maximum_iterations,
+                 const int *variant, int *flag, double *relres, int *iterations,
+                 const double *omega, int n_omega, double *resvec, int resvec_len, double *colfac,
+                 double *x);
+
+/* x(n, n_sigma) = MSQMRIDR(A, b, sigma, s[, M1, tolerance, maximum_iterations,
+ *                   flag, relres, iterations, inner_s, inner_tolerance,
+ *                   inner_iterations, omega, resvec]):
+ * RMSQMRIDR idrs_module.f90:491-570, CMSQMRIDR :410-489, body
+ * M/IDRS/msqmridr.inc.  With inner_iterations > 0 each iteration runs
+ * MSIDRS(inner_s) on the shifts [sigma, 0] as flexible preconditioner;
+ * inner_precision (new, optional): 64 (default) or 32 -- that inner solve and
+ * its operator run in fp32 (complex64).  n_sigma <= 63. */
+int idrs_rmsqmridr(idrs_matrix A, const double *b, int n_sigma, const double *sigma, int s,
+                   idrs_matrix M1, const double *tolerance, const int *maximum_iterations,
+                   int *flag, double *relres, int *iterations, const int *inner_s,
+                   const double *inner_tolerance, const int *inner_iterations,
+                   const double *omega, int n_omega, double *resvec, int resvec_len,
+                   const int *inner_precision, double *x);
+int idrs_cmsqmridr(idrs_matrix A, const double *b, int n_sigma, const double *sigma, int s,
+                   idrs_matrix M1, const double *tolerance, const int *maximum_iterations,
+                   int *flag, double *relres, int *iterations, const int *inner_s,
+                   const double *inner_tolerance, const int *inner_iterations,
+                   const double *omega, int n_omega, double *resvec, int resvec_len,
+                   const int *inner_precision, double *x);
+
 /* NORM(w): idrs_module.f90:787-811;  INPROD(u, v): idrs_module.f90:813-837 */
 int idrs_rnorm(idrs_matrix A, const double *w, double *norm);
 int idrs_cnorm(idrs_matrix A, const double *w, double *norm);
