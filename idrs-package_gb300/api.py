@@ -96,6 +96,9 @@ _PROTOS = {
                             _vp, _i, _vp, _i, _vp, _vp]),
     "idrs_cmsqmridr": (_i, [_vp, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                             _vp, _i, _vp, _i, _vp, _vp]),
+    "idrs_crs_transpose": (_i, [_vp, _vp]),
+    "idrs_rsparse_outer_grad": (_i, [_vp, _vp, _vp, _vp]),
+    "idrs_radjoint": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "idrs_rnorm": (_i, [_vp, _vp, _vp]),
     "idrs_cnorm": (_i, [_vp, _vp, _vp]),
     "idrs_rinprod": (_i, [_vp, _vp, _vp, _vp]),
@@ -187,8 +190,9 @@ class UserMatrix:
 
     __array_ufunc__ = None  # `v * K`, `v / K` must not broadcast element-wise
 
-    def __init__(self, handle, nrows, ncols, cplx):
+    def __init__(self, handle, nrows, ncols, cplx, nnz=None):
         self.handle, self.nrows, self.ncols, self.cplx = handle, nrows, ncols, cplx
+        self.nnz = nnz
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -226,7 +230,7 @@ def crs_format(nrows, ncols, row_ptr, col_ind, rval=None, ival=None, cval=None) 
     rv, cv = _values(rval, cval)
     h = C.c_void_p()
     _check(lib().idrs_crs_format(int(nrows), int(ncols), _p(rp), _p(ci), _p(rv), _p(cv), C.byref(h)))
-    return UserMatrix(h.value, nrows, ncols, cv is not None)
+    return UserMatrix(h.value, nrows, ncols, cv is not None, nnz=int(rp[nrows] - rp[0]))
 
 
 def coo_format(nrows, ncols, nnz, indx, jndx, rval=None, ival=None, cval=None) -> UserMatrix:
@@ -543,6 +547,46 @@ def MSQMRIDR(A: Matrix, b, sigma, s, M1: Matrix | None = None, tolerance=None,
     r = Result(x=x, flag=flag.value, relres=relres, iterations=iters.value)
     if rv is not None:
         r["resvec"] = rv
+    return r
+
+
+# ------------------------------------------------------------------ adjoint
+def crs_transpose(K: UserMatrix) -> UserMatrix:
+    """K^T as a CRS user_matrix built on the device (no reference counterpart)."""
+    h = C.c_void_p()
+    _check(lib().idrs_crs_transpose(K.handle, C.byref(h)))
+    return UserMatrix(h.value, K.ncols, K.nrows, K.cplx, nnz=K.nnz)
+
+
+def sparse_outer_grad(A: Matrix, lam, x):
+    """grad[p] = -lam_i x_j over the stored entries of A's CRS matrix, in storage order."""
+    if A.K.nnz is None:
+        raise IDRSError(IDRS_ERR_ARG, "sparse_outer_grad: CRS matrix required")
+    lam = _arr(lam, False, A.n)
+    x = _arr(x, False, A.n)
+    g = np.empty(A.K.nnz)
+    _check(lib().idrs_rsparse_outer_grad(A.handle, _p(lam), _p(x), _p(g)))
+    return g
+
+
+def ADJOINT(AT: Matrix, K: UserMatrix, x, g, s, tolerance=None, maximum_iterations=None,
+            grad=True) -> Result:
+    """Backward step of A x = b for a scalar loss with dL/dx = g: IDR(s) on the
+    adjoint operator AT (from crs_transpose(K)) gives lambda = dL/db; grad is
+    dL/dK over K's stored entries, -lambda_i x_j."""
+    if K.nnz is None:
+        raise IDRSError(IDRS_ERR_ARG, "ADJOINT: K must be a CRS user_matrix")
+    x = _arr(x, False, AT.n)
+    g = _arr(g, False, AT.n)
+    lam = np.empty(AT.n)
+    gr = np.empty(K.nnz) if grad else None
+    flag, relres, iters = C.c_int(), C.c_double(), C.c_int()
+    _check(lib().idrs_radjoint(AT.handle, K.handle, _p(x), _p(g), int(s), _ref_dbl(tolerance),
+                               _ref_int(maximum_iterations), C.byref(flag), C.byref(relres),
+                               C.byref(iters), _p(lam), _p(gr)))
+    r = Result(lam=lam, flag=flag.value, relres=relres.value, iterations=iters.value)
+    if gr is not None:
+        r["grad"] = gr
     return r
 
 

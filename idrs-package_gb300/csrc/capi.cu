@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/idrs_gb300.h"
+#include "adjoint.h"
 #include "idrs_gpu.cuh"
 #include "ms_gpu.cuh"
 #include "setup.h"
@@ -1203,6 +1204,81 @@ int idrs_cmsqmridr(idrs_matrix A, const double* b, int n_sigma, const double* si
                                    flag, relres, iterations, inner_s, inner_tolerance,
                                    inner_iterations, omega, n_omega, resvec, resvec_len,
                                    inner_precision, x);
+  });
+}
+
+// ------------------------------------------------------------------ adjoint
+int idrs_crs_transpose(idrs_user_matrix K, idrs_user_matrix* KT) {
+  return guard([&] {
+    REQUIRE(K && KT, "crs_transpose: K and KT are required");
+    REQUIRE(K->format == FMT_CRS, "crs_transpose: CRS matrix required");
+    init_runtime();
+    auto* M = new idrs_user_matrix_s();
+    try {
+      crs_transpose(*K, *M, nullptr);
+    } catch (...) {
+      delete M;
+      throw;
+    }
+    *KT = M;
+    return IDRS_OK;
+  });
+}
+
+int idrs_rsparse_outer_grad(idrs_matrix A, const double* lambda, const double* x, double* grad) {
+  return guard([&] {
+    REQUIRE(A && lambda && x && grad, "sparse_outer_grad: bad arguments");
+    REQUIRE(A->K->format == FMT_CRS && A->K->vals != 2, "sparse_outer_grad: real CRS matrix required");
+    const long n = A->n();
+    Staged sv(A, sizeof(double) * n), sg(A, sizeof(double) * A->K->nnz);
+    const double* d_l = (const double*)sv.in(lambda);
+    const double* d_x = (const double*)sv.in(x);
+    double* d_g = (double*)sg.out(grad);
+    sparse_outer_grad(*A->K, d_l, d_x, d_g, A->stream);
+    sg.finish(grad, d_g);
+    IDRS_CUDA(cudaStreamSynchronize(A->stream));
+    return IDRS_OK;
+  });
+}
+
+int idrs_radjoint(idrs_matrix AT, idrs_user_matrix K, const double* x, const double* g, int s,
+                  const double* tolerance, const int* maximum_iterations, int* flag,
+                  double* relres, int* iterations, double* lambda, double* grad) {
+  return guard([&] {
+    REQUIRE(AT && !AT->cplx && K && x && g && lambda, "radjoint: AT, K, x, g and lambda are required");
+    REQUIRE(K->format == FMT_CRS && K->vals != 2, "radjoint: K must be a real CRS matrix");
+    REQUIRE(K->nrows == AT->n() && K->ncols == AT->n(), "radjoint: K and AT differ in size");
+    REQUIRE(s >= 1, "radjoint: s must be positive");
+    if (s > MAXS) throw unsupported_error("radjoint: s > 16 is not supported by the GPU path");
+    SolveOpts o;
+    if (tolerance) {
+      REQUIRE(*tolerance >= 0, "Illegal value for parameter tolerance");
+      o.tol = *tolerance;
+    }
+    const long n = AT->n();
+    o.maxit = maximum_iterations ? *maximum_iterations : (int)std::min<long>(2 * n, 1000);
+    o.PT = find_shadow(AT, s);
+    cudaStream_t st = AT->stream;
+    Staged sv(AT, sizeof(double) * n), sg(AT, sizeof(double) * K->nnz);
+    const double* d_g = (const double*)sv.in(g);
+    const double* d_x = (const double*)sv.in(x);
+    double* d_lam = (double*)sv.out(lambda);
+    double* d_grad = grad ? (double*)sg.out(grad) : nullptr;
+    DBuf mu(sizeof(double) * n, st), t1(sizeof(double) * n, st), t2(sizeof(double) * n, st);
+    // A^T mu = g with IDR(s) on the adjoint operator, then lambda = scaleback(AT, g, mu)
+    IdrsGpu<double> solver(*AT, 64, s, 1);
+    solver.solve(d_g, mu.as<double>(), o);
+    op_scaleback<double>(*AT, 64, AT->alpha_p, AT->degree, mu.as<double>(), d_lam, t1.as<double>(),
+                         t2.as<double>(), nullptr, st);
+    if (d_grad) sparse_outer_grad(*K, d_lam, d_x, d_grad, st);
+    auto h = solver.state();
+    sv.finish(lambda, d_lam);
+    if (d_grad) sg.finish(grad, d_grad);
+    IDRS_CUDA(cudaStreamSynchronize(st));
+    if (flag) *flag = h.info;
+    if (relres) *relres = h.relres;
+    if (iterations) *iterations = h.iter;
+    return IDRS_OK;
   });
 }
 

@@ -10,8 +10,9 @@
 ! argument order and optional arguments are those of
 !     M/PP_MATRIX/user_module.f90:829-958, 1327-1463
 !     M/PP_MATRIX/matrix_module.f90:135-167, 306-352, 551-635, 811-849
-!     M/IDRS/idrs_module.f90:66-103, 107-408, 787-837
-! (IDRS package paths, M/ = IDRS/MODULES).  Status codes of the C ABI become
+!     M/IDRS/idrs_module.f90:66-103, 107-408, 410-713, 787-837
+! (IDRS package paths, M/ = IDRS/MODULES).  Beyond the reference: the adjoint
+! path (crs_transpose, idrs_backward) for gradients of a scalar loss.  Status codes of the C ABI become
 ! `error stop` with the library's message, as the reference stops on illegal
 ! arguments.  Index arrays are 1-based, as in the reference.
 !
@@ -27,11 +28,12 @@ module idrs_gb300_module
    public :: user_matrix, matrix, crs_format, coo_format, cds_format, stencil7_format
    public :: real_precon, make_matrix, real_preconditioner, scaleback
    public :: operator(*), operator(/)
-   public :: IDRS, QMRIDR, NORM, INPROD
+   public :: IDRS, QMRIDR, MSIDRS, MSQMRIDR, NORM, INPROD
+   public :: crs_transpose, idrs_backward
 
    type :: user_matrix
       type(c_ptr) :: h = c_null_ptr
-      integer     :: nrows = 0, ncols = 0
+      integer     :: nrows = 0, ncols = 0, nnz = 0
    end type user_matrix
 
    type :: matrix
@@ -50,6 +52,12 @@ module idrs_gb300_module
    end interface
    interface QMRIDR
       module procedure RQMRIDR
+   end interface
+   interface MSIDRS
+      module procedure RMSIDRS
+   end interface
+   interface MSQMRIDR
+      module procedure RMSQMRIDR
    end interface
    interface NORM
       module procedure RNORM
@@ -174,6 +182,54 @@ module idrs_gb300_module
          real(c_double), intent(out), optional :: resvec(*)
          real(c_double), intent(out) :: x(*)
       end function
+      integer(c_int) function c_rmsidrs(A, b, n_sigma, sigma, s, M1, tolerance, &
+            maximum_iterations, variant, flag, relres, iterations, omega, n_omega, resvec, &
+            resvec_len, colfac, x) bind(C, name='idrs_rmsidrs')
+         import :: c_int, c_double, c_ptr
+         type(c_ptr), value :: A, M1
+         real(c_double), intent(in) :: b(*), sigma(*)
+         integer(c_int), value :: n_sigma, s, n_omega, resvec_len
+         real(c_double), intent(in), optional :: tolerance
+         integer(c_int), intent(in), optional :: maximum_iterations, variant
+         integer(c_int), intent(out), optional :: flag, iterations
+         real(c_double), intent(out), optional :: relres(*), resvec(*), colfac(*)
+         real(c_double), intent(in), optional :: omega(*)
+         real(c_double), intent(out) :: x(*)
+      end function
+      integer(c_int) function c_rmsqmridr(A, b, n_sigma, sigma, s, M1, tolerance, &
+            maximum_iterations, flag, relres, iterations, inner_s, inner_tolerance, &
+            inner_iterations, omega, n_omega, resvec, resvec_len, inner_precision, x) &
+            bind(C, name='idrs_rmsqmridr')
+         import :: c_int, c_double, c_ptr
+         type(c_ptr), value :: A, M1
+         real(c_double), intent(in) :: b(*), sigma(*)
+         integer(c_int), value :: n_sigma, s, n_omega, resvec_len
+         real(c_double), intent(in), optional :: tolerance, inner_tolerance
+         integer(c_int), intent(in), optional :: maximum_iterations, inner_s, inner_iterations
+         integer(c_int), intent(in), optional :: inner_precision
+         integer(c_int), intent(out), optional :: flag, iterations
+         real(c_double), intent(out), optional :: relres(*), resvec(*)
+         real(c_double), intent(in), optional :: omega(*)
+         real(c_double), intent(out) :: x(*)
+      end function
+      integer(c_int) function c_crs_transpose(K, KT) bind(C, name='idrs_crs_transpose')
+         import :: c_int, c_ptr
+         type(c_ptr), value :: K
+         type(c_ptr), intent(out) :: KT
+      end function
+      integer(c_int) function c_radjoint(AT, K, x, g, s, tolerance, maximum_iterations, flag, &
+            relres, iterations, lambda, grad) bind(C, name='idrs_radjoint')
+         import :: c_int, c_double, c_ptr
+         type(c_ptr), value :: AT, K
+         real(c_double), intent(in) :: x(*), g(*)
+         integer(c_int), value :: s
+         real(c_double), intent(in), optional :: tolerance
+         integer(c_int), intent(in), optional :: maximum_iterations
+         integer(c_int), intent(out), optional :: flag, iterations
+         real(c_double), intent(out), optional :: relres
+         real(c_double), intent(out) :: lambda(*)
+         real(c_double), intent(out), optional :: grad(*)
+      end function
       integer(c_int) function c_rnorm(A, w, nrm) bind(C, name='idrs_rnorm')
          import :: c_int, c_double, c_ptr
          type(c_ptr), value :: A
@@ -225,6 +281,7 @@ contains
       end if
       A%nrows = nrows
       A%ncols = ncols
+      A%nnz = row_ptr(nrows+1) - row_ptr(1)
    end function crs_format
 
    function coo_format(nrows, ncols, nnz, indx, jndx, rval, ival, cval) result(A)
@@ -414,6 +471,95 @@ contains
            iterations, inner_s, inner_tolerance, inner_iterations, x0, omega, n_omega, resvec, &
            nres, inner_precision, x))
    end function RQMRIDR
+
+   function RMSIDRS(A, b, sigma, s, M1, tolerance, maximum_iterations, variant, flag, relres, &
+                    iterations, omega, resvec, colfac) result(x)
+      ! RMSIDRS, idrs_module.f90:572-641
+      type(matrix), intent(in) :: A
+      real(c_double), intent(in) :: b(:), sigma(:)
+      integer, intent(in) :: s
+      type(matrix), intent(in), optional :: M1
+      real(c_double), intent(in), optional :: tolerance
+      integer, intent(in), optional :: maximum_iterations, variant
+      integer, intent(out), optional :: flag, iterations
+      real(c_double), intent(out), optional :: relres(size(sigma)), colfac(size(sigma))
+      real(c_double), intent(in), optional :: omega(:)
+      real(c_double), intent(out), optional :: resvec(:,:)
+      real(c_double) :: x(size(b), size(sigma))
+      type(c_ptr) :: m1h
+      integer :: n_omega, nres
+      m1h = c_null_ptr
+      if (present(M1)) m1h = M1%h
+      n_omega = 0
+      if (present(omega)) n_omega = size(omega)
+      nres = 0
+      if (present(resvec)) nres = size(resvec, 1)
+      call check(c_rmsidrs(A%h, b, size(sigma), sigma, s, m1h, tolerance, maximum_iterations, &
+           variant, flag, relres, iterations, omega, n_omega, resvec, nres, colfac, x))
+   end function RMSIDRS
+
+   function RMSQMRIDR(A, b, sigma, s, M1, tolerance, maximum_iterations, flag, relres, &
+                      iterations, inner_s, inner_tolerance, inner_iterations, omega, resvec, &
+                      inner_precision) result(x)
+      ! RMSQMRIDR, idrs_module.f90:491-570
+      type(matrix), intent(in) :: A
+      real(c_double), intent(in) :: b(:), sigma(:)
+      integer, intent(in) :: s
+      type(matrix), intent(in), optional :: M1
+      real(c_double), intent(in), optional :: tolerance, inner_tolerance
+      integer, intent(in), optional :: maximum_iterations, inner_s, inner_iterations
+      integer, intent(in), optional :: inner_precision
+      integer, intent(out), optional :: flag, iterations
+      real(c_double), intent(out), optional :: relres(size(sigma))
+      real(c_double), intent(in), optional :: omega(:)
+      real(c_double), intent(out), optional :: resvec(:,:)
+      real(c_double) :: x(size(b), size(sigma))
+      type(c_ptr) :: m1h
+      integer :: n_omega, nres
+      m1h = c_null_ptr
+      if (present(M1)) m1h = M1%h
+      n_omega = 0
+      if (present(omega)) n_omega = size(omega)
+      nres = 0
+      if (present(resvec)) nres = size(resvec, 1)
+      call check(c_rmsqmridr(A%h, b, size(sigma), sigma, s, m1h, tolerance, maximum_iterations, &
+           flag, relres, iterations, inner_s, inner_tolerance, inner_iterations, omega, n_omega, &
+           resvec, nres, inner_precision, x))
+   end function RMSQMRIDR
+
+   ! ---------------------------------------------------------------- adjoint
+   function crs_transpose(K) result(KT)
+      ! K^T as a new CRS user_matrix, built on the device
+      type(user_matrix), intent(in) :: K
+      type(user_matrix) :: KT
+      call check(c_crs_transpose(K%h, KT%h))
+      KT%nrows = K%ncols
+      KT%ncols = K%nrows
+      KT%nnz = K%nnz
+   end function crs_transpose
+
+   subroutine idrs_backward(AT, K, x, dLdx, s, dLdb, dLdK, tolerance, maximum_iterations, &
+                            flag, relres, iterations)
+      ! Backward step of A x = b, A = K (CRS), for a scalar loss L(x):
+      ! AT lambda = dL/dx with IDR(s) on the adjoint operator AT (built from
+      ! crs_transpose(K)), dL/db = lambda, dL/dK(p) = -lambda(i) x(j) over K's
+      ! stored entries p = (i, j) in storage order.
+      type(matrix), intent(in) :: AT
+      type(user_matrix), intent(in) :: K
+      real(c_double), intent(in) :: x(:), dLdx(:)
+      integer, intent(in) :: s
+      real(c_double), intent(out) :: dLdb(:)
+      real(c_double), intent(out), optional :: dLdK(:)
+      real(c_double), intent(in), optional :: tolerance
+      integer, intent(in), optional :: maximum_iterations
+      integer, intent(out), optional :: flag, iterations
+      real(c_double), intent(out), optional :: relres
+      if (present(dLdK)) then
+         if (size(dLdK) /= K%nnz) error stop "idrs_backward: dLdK must have one entry per nonzero of K"
+      end if
+      call check(c_radjoint(AT%h, K%h, x, dLdx, s, tolerance, maximum_iterations, flag, relres, &
+           iterations, dLdb, dLdK))
+   end subroutine idrs_backward
 
    function RNORM(A, w) result(nrm)
       type(matrix), intent(in) :: A

@@ -224,6 +224,27 @@ int idrs_cmsqmridr(idrs_matrix A, const double *b, int n_sigma, const double *si
                    const double *omega, int n_omega, double *resvec, int resvec_len,
                    const int *inner_precision, double *x);
 
+/* ---------------------------------------------------------------------- */
+/* Adjoint (backward) path of A x = b with a real CRS matrix A = K.  No    */
+/* counterpart in the reference, which has no adjoint (its compliance      */
+/* sensitivities, E/TOP/top_opt.f90:209-224, are written by hand for a     */
+/* self-adjoint problem).  For a scalar loss L(x):                         */
+/*   K^T lambda = dL/dx,  dL/db = lambda,  dL/dK_ij = -lambda_i x_j.       */
+/* ---------------------------------------------------------------------- */
+/* K^T as a new CRS user_matrix (device; stable: ascending rows of K). */
+int idrs_crs_transpose(idrs_user_matrix K, idrs_user_matrix *KT);
+/* grad(nnz) = -lambda_i x_j over the stored entries of A's CRS matrix K, in
+ * K's storage order; vectors follow A's pointer mode and stream. */
+int idrs_rsparse_outer_grad(idrs_matrix A, const double *lambda, const double *x, double *grad);
+/* One backward step: IDR(s) on the adjoint operator AT (built from K^T,
+ * optionally with its own preconditioner and seed) for AT lambda = g
+ * (g = dL/dx), lambda = scaleback(AT, g, mu); then, if grad is given,
+ * grad(nnz) = -lambda_i x_j over K's pattern.  flag/relres/iterations are
+ * those of the adjoint solve.  Pointer mode and stream are AT's. */
+int idrs_radjoint(idrs_matrix AT, idrs_user_matrix K, const double *x, const double *g, int s,
+                  const double *tolerance, const int *maximum_iterations, int *flag,
+                  double *relres, int *iterations, double *lambda, double *grad);
+
 /* NORM(w): idrs_module.f90:787-811;  INPROD(u, v): idrs_module.f90:813-837 */
 int idrs_rnorm(idrs_matrix A, const double *w, double *norm);
 int idrs_cnorm(idrs_matrix A, const double *w, double *norm);

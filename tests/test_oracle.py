@@ -159,3 +159,48 @@ def test_multishift_oracle(oracle, P):
     assert r.flag == 0 and np.max(r.relres) < 1e-8
     q = oracle.msqmridr(A, b, sig, 4, tolerance=1e-8, maximum_iterations=2000)
     assert q.flag == 0 and np.max(q.relres) < 1e-8
+
+
+def test_adjoint_oracle(oracle, P):
+    """The FP64 reference gradient: transposed CRS equals the dense transpose,
+    lambda solves A^T lambda = x - x_t, and -lambda_i x_j matches central
+    differences of L = 1/2 ||x - x_t||^2 on a few entries (dense FP64 solves)."""
+    n = 6
+    N = n ** 3
+    coef = P.cdr_coefficients(n)
+    rp, ci, vals = P.stencil_to_crs(n, n, n, coef)
+    rows = np.repeat(np.arange(N), np.diff(rp))
+    D = np.zeros((N, N))
+    D[rows, ci - 1] = vals
+    Ko = oracle.crs_format(N, N, rp, ci, vals)
+    KT = oracle.crs_transpose(Ko)
+    v = np.random.default_rng(0).standard_normal(N)
+    np.testing.assert_allclose(KT.mv(v), D.T @ v, rtol=1e-13, atol=1e-12)
+    rng = np.random.default_rng(1)
+    b, xt = rng.standard_normal(N), rng.standard_normal(N)
+    x = oracle.idrs(oracle.Matrix(Ko), b, 4, tolerance=1e-13).x
+    lam = oracle.idrs(oracle.Matrix(KT), x - xt, 4, tolerance=1e-13).x
+    g = oracle.sparse_outer_grad(Ko, lam, x, len(vals))
+    np.testing.assert_array_equal(g, -lam[rows] * x[ci - 1])
+    eps = 1e-6
+    res = x - xt
+
+    def central(dp, dm):
+        # L(+) - L(-) with d = x(+-) - x, rearranged so no large losses cancel
+        return (res @ (dp - dm) + 0.5 * (dp @ dp - dm @ dm)) / (2 * eps)
+
+    for p in (0, 17, 333, len(vals) - 1):
+        i, j = rows[p], ci[p] - 1
+        d = []
+        for sgn in (1.0, -1.0):
+            Dp = D.copy()
+            Dp[i, j] += sgn * eps
+            rhs = np.zeros(N)
+            rhs[i] = -sgn * eps * x[j]
+            d.append(np.linalg.solve(Dp, rhs))
+        assert abs(central(*d) - g[p]) <= 1e-5 * abs(g[p])
+    for k in (3, 100):
+        e = np.zeros(N)
+        e[k] = eps
+        fd = central(np.linalg.solve(D, e), np.linalg.solve(D, -e))
+        assert abs(fd - lam[k]) <= 1e-5 * abs(lam[k])
