@@ -133,6 +133,67 @@ __global__ void __launch_bounds__(256) k_stencil7(int nx, int ny, int nz, int zc
   }
 }
 
+// fp32 stencil, four x-points per thread (float4): a warp covers 128
+// consecutive x-points of one row, the x-neighbours come from the adjacent
+// lanes by shuffles (the two row ends of a warp from L1), the y-neighbours
+// are float4 loads of the rows of the neighbouring warps (L1 hits), and the
+// z-neighbours stay in registers while the block marches along z.  One
+// 16-byte load per operand and point quadruple instead of seven scalar loads
+// per point.  Needs nx % 4 == 0 and 16-byte aligned vectors (checked by the
+// launcher).  SCALE == false form: a and the centre term are folded into the
+// coefficients.
+constexpr int kF4Rows = 8;
+
+__device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+__global__ void __launch_bounds__(32 * kF4Rows) k_stencil7_f4(
+    int nx, int ny, int nz, int zc, float c0, float cw, float ce, float cs, float cn, float cf,
+    float cb, const float* __restrict__ x, float* __restrict__ y, float cv,
+    const float* __restrict__ v, float cu, const float* __restrict__ u,
+    const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  const int lane = threadIdx.x;
+  const int i0 = (blockIdx.x * 32 + lane) * 4;
+  const int j = blockIdx.y * kF4Rows + threadIdx.y;
+  const int z0 = blockIdx.z * zc;
+  const int z1 = min(nz, z0 + zc);
+  const bool in = (i0 < nx) && (j < ny);
+  const long plane = (long)nx * ny;
+  long p = (long)j * nx + i0 + plane * z0;
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 xm = (in && z0 > 0) ? ld4(x + p - plane) : zero;
+  float4 xc = in ? ld4(x + p) : zero;
+  for (int z = z0; z < z1; ++z, p += plane) {
+    const float4 xp = (in && z + 1 < nz) ? ld4(x + p + plane) : zero;
+    const float4 xs = (in && j > 0) ? ld4(x + p - nx) : zero;
+    const float4 xn = (in && j + 1 < ny) ? ld4(x + p + nx) : zero;
+    float left = __shfl_up_sync(0xffffffffu, xc.w, 1);
+    float right = __shfl_down_sync(0xffffffffu, xc.x, 1);
+    if (lane == 0) left = (in && i0 > 0) ? __ldg(x + p - 1) : 0.f;
+    if (lane == 31) right = (in && i0 + 4 < nx) ? __ldg(x + p + 4) : 0.f;
+    if (in) {
+      float4 r;
+      r.x = c0 * xc.x + cw * left + ce * xc.y + cs * xs.x + cn * xn.x + cf * xm.x + cb * xp.x;
+      r.y = c0 * xc.y + cw * xc.x + ce * xc.z + cs * xs.y + cn * xn.y + cf * xm.y + cb * xp.y;
+      r.z = c0 * xc.z + cw * xc.y + ce * xc.w + cs * xs.z + cn * xn.z + cf * xm.z + cb * xp.z;
+      r.w = c0 * xc.w + cw * xc.z + ce * right + cs * xs.w + cn * xn.w + cf * xm.w + cb * xp.w;
+      if (u) {
+        const float4 uu = ld4(u + p);
+        r.x += cu * uu.x; r.y += cu * uu.y; r.z += cu * uu.z; r.w += cu * uu.w;
+      }
+      if (v) {
+        const float4 vv = ld4(v + p);
+        r.x += cv * vv.x; r.y += cv * vv.y; r.z += cv * vv.z; r.w += cv * vv.w;
+      }
+      *reinterpret_cast<float4*>(y + p) = r;
+    }
+    xm = xc;
+    xc = xp;
+  }
+}
+
+static inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
 // CRS, G lanes per row (G | 32).  Warp-uniform loop so the shuffles are
 // always executed by the full warp.
 template <int G, class T, class V>
@@ -282,6 +343,22 @@ static void launch_stencil(const MatView& M, const T* x, T* y, T a, T cv, const 
   int gz = (M.nz + zc - 1) / zc;
   dim3 grid(gx, gy, gz);
   const bool real_a = (imag_(a) == 0) && (imag_(cx) == 0);
+  if constexpr (std::is_same<T, float>::value) {
+    if (M.nx % 4 == 0 && aligned16(x) && aligned16(y) && aligned16(u) && aligned16(v)) {
+      dim3 blk4(32, kF4Rows, 1);
+      int gx4 = (M.nx + 127) / 128, gy4 = (M.ny + kF4Rows - 1) / kF4Rows;
+      long xy4 = (long)gx4 * gy4;
+      int zc4 = (int)std::max(1L, std::min((long)M.nz, (M.nz * xy4 + target - 1) / target));
+      if (zc4 < 4 && M.nz >= 4) zc4 = 4;
+      dim3 grid4(gx4, gy4, (M.nz + zc4 - 1) / zc4);
+      const double ar = (double)a;
+      k_stencil7_f4<<<grid4, blk4, 0, st>>>(
+          M.nx, M.ny, M.nz, zc4, float(ar * M.st[0] + (double)cx), float(ar * M.st[1]),
+          float(ar * M.st[2]), float(ar * M.st[3]), float(ar * M.st[4]), float(ar * M.st[5]),
+          float(ar * M.st[6]), x, y, cv, v, cu, u, skip);
+      return;
+    }
+  }
   if (real_a) {  // fold the real scale (and the centre term cx*x) into the coefficients
     double ar = (double)real_(a);
     double c0 = ar * M.st[0] + (double)real_(cx);
