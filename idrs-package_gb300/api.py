@@ -96,6 +96,7 @@ _PROTOS = {
                             _vp, _i, _vp, _i, _vp, _vp]),
     "idrs_cmsqmridr": (_i, [_vp, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                             _vp, _i, _vp, _i, _vp, _vp]),
+    "idrs_solve_stats": (_i, [_vp, _vp, _vp, _vp]),
     "idrs_crs_transpose": (_i, [_vp, _vp]),
     "idrs_rsparse_outer_grad": (_i, [_vp, _vp, _vp, _vp]),
     "idrs_radjoint": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -121,7 +122,8 @@ class PPReport(C.Structure):
                 ("nritz", C.c_int), ("relres_solver", C.c_double),
                 ("relres_original", C.c_double), ("foci", C.c_double * 2), ("center", C.c_double),
                 ("seconds_setup", C.c_double), ("seconds_solve", C.c_double),
-                ("seconds_total", C.c_double)]
+                ("seconds_total", C.c_double), ("inner_solves", C.c_int),
+                ("inner_iterations", C.c_int), ("inner_max", C.c_int)]
 
 
 def load(path: str | None = None):
@@ -652,4 +654,6 @@ def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=Non
                   ritz_iterations=rep.ritz_iterations, nritz=rep.nritz,
                   relres=rep.relres_solver, relres_original=rep.relres_original,
                   foci=tuple(rep.foci), center=rep.center, seconds_setup=rep.seconds_setup,
-                  seconds_solve=rep.seconds_solve, seconds_total=rep.seconds_total)
+                  seconds_solve=rep.seconds_solve, seconds_total=rep.seconds_total,
+                  inner_solves=rep.inner_solves, inner_iterations=rep.inner_iterations,
+                  inner_max=rep.inner_max)

@@ -365,6 +365,9 @@ void run_qmr_typed(Operator* A, int s, const T* d_b, T* d_x, SolveOpts& o, int* 
   QmrGpu<T, Tin> solver(*A, s, o);
   solver.solve(d_b, d_x, o);
   auto h = solver.state();
+  A->last_inner_calls = h.inner_calls;
+  A->last_inner_total = h.inner_total;
+  A->last_inner_max = h.inner_max;
   if (flag) *flag = h.info;
   if (relres) *relres = h.relres;
   if (iterations) *iterations = h.iter;
@@ -1207,6 +1210,16 @@ int idrs_cmsqmridr(idrs_matrix A, const double* b, int n_sigma, const double* si
   });
 }
 
+int idrs_solve_stats(idrs_matrix A, int* inner_solves, int* inner_iterations, int* inner_max) {
+  return guard([&] {
+    REQUIRE(A, "solve_stats: matrix handle required");
+    if (inner_solves) *inner_solves = A->last_inner_calls;
+    if (inner_iterations) *inner_iterations = A->last_inner_total;
+    if (inner_max) *inner_max = A->last_inner_max;
+    return IDRS_OK;
+  });
+}
+
 // ------------------------------------------------------------------ adjoint
 int idrs_crs_transpose(idrs_user_matrix K, idrs_user_matrix* KT) {
   return guard([&] {
@@ -1378,6 +1391,9 @@ int idrs_rpp_idrs(idrs_user_matrix K, const double* b, idrs_user_matrix P, const
       st = idrs_rqmridr(A, pb, s, nullptr, &tol, &maxit, &rep.flag, &rep.relres_solver,
                         &rep.iterations, &in_s, &in_tol, &in_it, d_x0.as<double>(), nullptr, 0,
                         nullptr, 0, &prec, d_y.as<double>());
+      rep.inner_solves = A->last_inner_calls;
+      rep.inner_iterations = A->last_inner_total;
+      rep.inner_max = A->last_inner_max;
     } else {
       int variant = opt->method == 2 ? 2 : 1;
       st = idrs_ridrs(A, pb, s, nullptr, &tol, &maxit, &variant, &rep.flag,

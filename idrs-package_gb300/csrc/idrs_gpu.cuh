@@ -50,6 +50,7 @@ struct IdrsState {
 template <class W>
 struct QmrState {
   int info, stop, early, iter, jj, maxit, s, n_omega;
+  int inner_calls, inner_total, inner_max;  // statistics of the inner solves
   double tol, tolb, normb, normg, normr, kappa, relres;
   W om, phi_n, phi_n1;
   W M[MAXS * MAXS];
@@ -718,6 +719,16 @@ template <class W> struct TQmrFinal {  // qmridr.inc:256-262
     st->relres = st->normr / st->normb;
   }
 };
+
+// adds the iteration count of the inner solve that just ran (skipped once the
+// outer solve has stopped: the inner state was not re-initialised then)
+template <class W, class Win>
+__global__ void k_inner_stats(QmrState<W>* st, const IdrsState<Win>* in) {
+  if (st->stop) return;
+  st->inner_calls += 1;
+  st->inner_total += in->iter;
+  st->inner_max = max(st->inner_max, in->iter);
+}
 
 template <class T, class Tin>
 class QmrGpu {

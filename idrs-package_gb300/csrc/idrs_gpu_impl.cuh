@@ -297,6 +297,8 @@ void QmrGpu<T, Tin>::solve(const T* b, T* x, const SolveOpts& o) {
           inner->solve(v_in, vt_in, io);
           vec_convert<Tin, T>(n, vt_in, vt, stop, st);
         }
+        k_inner_stats<<<1, 1, 0, st>>>(d_st, inner->d_st);
+        IDRS_LAUNCH_CHECK();
         vtptr = vt;
       }
       matvec(vtptr, gn, stop, T(1), T(0), nullptr);

@@ -146,7 +146,7 @@ constexpr int kF4Rows = 8;
 
 __device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
-__global__ void __launch_bounds__(32 * kF4Rows) k_stencil7_f4(
+__global__ void __launch_bounds__(32 * kF4Rows, 4) k_stencil7_f4(
     int nx, int ny, int nz, int zc, float c0, float cw, float ce, float cs, float cn, float cf,
     float cb, const float* __restrict__ x, float* __restrict__ y, float cv,
     const float* __restrict__ v, float cu, const float* __restrict__ u,
@@ -161,10 +161,18 @@ __global__ void __launch_bounds__(32 * kF4Rows) k_stencil7_f4(
   const long plane = (long)nx * ny;
   long p = (long)j * nx + i0 + plane * z0;
   const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  // software pipeline: the HBM streams (plane z+2 of x, plane z+1 of u and v)
+  // are requested one iteration ahead of their use
   float4 xm = (in && z0 > 0) ? ld4(x + p - plane) : zero;
   float4 xc = in ? ld4(x + p) : zero;
+  float4 xp = (in && z0 + 1 < nz) ? ld4(x + p + plane) : zero;
+  float4 uc = (in && u) ? ld4(u + p) : zero;
+  float4 vc = (in && v) ? ld4(v + p) : zero;
   for (int z = z0; z < z1; ++z, p += plane) {
-    const float4 xp = (in && z + 1 < nz) ? ld4(x + p + plane) : zero;
+    const bool more = z + 1 < z1;
+    const float4 xpp = (in && z + 2 < nz) ? ld4(x + p + 2 * plane) : zero;
+    const float4 un = (in && u && more) ? ld4(u + p + plane) : zero;
+    const float4 vn = (in && v && more) ? ld4(v + p + plane) : zero;
     const float4 xs = (in && j > 0) ? ld4(x + p - nx) : zero;
     const float4 xn = (in && j + 1 < ny) ? ld4(x + p + nx) : zero;
     float left = __shfl_up_sync(0xffffffffu, xc.w, 1);
@@ -177,18 +185,15 @@ __global__ void __launch_bounds__(32 * kF4Rows) k_stencil7_f4(
       r.y = c0 * xc.y + cw * xc.x + ce * xc.z + cs * xs.y + cn * xn.y + cf * xm.y + cb * xp.y;
       r.z = c0 * xc.z + cw * xc.y + ce * xc.w + cs * xs.z + cn * xn.z + cf * xm.z + cb * xp.z;
       r.w = c0 * xc.w + cw * xc.z + ce * right + cs * xs.w + cn * xn.w + cf * xm.w + cb * xp.w;
-      if (u) {
-        const float4 uu = ld4(u + p);
-        r.x += cu * uu.x; r.y += cu * uu.y; r.z += cu * uu.z; r.w += cu * uu.w;
-      }
-      if (v) {
-        const float4 vv = ld4(v + p);
-        r.x += cv * vv.x; r.y += cv * vv.y; r.z += cv * vv.z; r.w += cv * vv.w;
-      }
+      if (u) { r.x += cu * uc.x; r.y += cu * uc.y; r.z += cu * uc.z; r.w += cu * uc.w; }
+      if (v) { r.x += cv * vc.x; r.y += cv * vc.y; r.z += cv * vc.z; r.w += cv * vc.w; }
       *reinterpret_cast<float4*>(y + p) = r;
     }
     xm = xc;
     xc = xp;
+    xp = xpp;
+    uc = un;
+    vc = vn;
   }
 }
 

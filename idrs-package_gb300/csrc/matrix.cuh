@@ -113,6 +113,9 @@ struct Operator {
   // reduction scratch for kernels launched on this operator's stream
   RedBuf red{nullptr, nullptr};
 
+  // statistics of the last flexible (QMRIDR) solve with inner iterations
+  int last_inner_calls = 0, last_inner_total = 0, last_inner_max = 0;
+
   int n() const { return K->nrows; }
   const MatView& view(int prec);
 };

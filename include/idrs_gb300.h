@@ -224,6 +224,11 @@ int idrs_cmsqmridr(idrs_matrix A, const double *b, int n_sigma, const double *si
                    const double *omega, int n_omega, double *resvec, int resvec_len,
                    const int *inner_precision, double *x);
 
+/* Statistics of the last QMRIDR solve with inner iterations on handle A (new,
+ * no reference counterpart): number of inner solves, their total and largest
+ * iteration counts. */
+int idrs_solve_stats(idrs_matrix A, int *inner_solves, int *inner_iterations, int *inner_max);
+
 /* ---------------------------------------------------------------------- */
 /* Adjoint (backward) path of A x = b with a real CRS matrix A = K.  No    */
 /* counterpart in the reference, which has no adjoint (its compliance      */
@@ -296,6 +301,7 @@ typedef struct idrs_pp_report {
   double relres_solver, relres_original;
   double foci[2], center;
   double seconds_setup, seconds_solve, seconds_total;
+  int inner_solves, inner_iterations, inner_max;  /* flexible QMRIDR: inner IDR(s) statistics */
 } idrs_pp_report;
 
 int idrs_rpp_idrs(idrs_user_matrix K, const double *b, idrs_user_matrix P, const double *center,
