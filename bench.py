@@ -44,11 +44,16 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--grid", type=int, default=256)
     p.add_argument("--in-it", type=int, default=500)
-    p.add_argument("--in-tol", type=float, default=1e-3)
+    p.add_argument("--in-tol", type=float, default=3e-3)
     p.add_argument("--in-s", type=int, default=4)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--profile", choices=["solve", "chain32", "chain64"], default=None,
                    help="profiling driver: one mixed solve, or the fp32/fp64 Chebyshev(8) chain alone")
+    p.add_argument("--workload", choices=["cdr256", "pagerank", "multishift", "adjoint"], default="cdr256",
+                   help="cdr256: the headline line; the others measure the remaining configurations "
+                        "(PageRank 4M, complex multishift 128^3, adjoint 128^3) and print one JSON line each")
+    p.add_argument("--fd-samples", type=int, default=64,
+                   help="adjoint workload: finite-difference samples of b and of A's nonzeros (each)")
     return p.parse_args()
 
 
@@ -384,10 +389,251 @@ def run_profile(args):
         print(json.dumps({"profile": args.profile, "grid": n, "ms_per_product": ms, "ms_per_launch": msl}))
 
 
+# ------------------------------------------------------- other configurations
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def _timed_call(fn, steps=1):
+    import torch
+    out, ts = None, []
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) / 1e3)
+    return out, statistics.mean(ts)
+
+
+def run_pagerank(args):
+    """(I - alpha P^T) x = (1-alpha)/N 1, alpha 0.85, N = 4,194,304 nodes with
+    Zipf(2.1) in-link counts scaled to mean 12 (seed 2024, rule in
+    problems.zipf_row_lengths), uniform random columns (pagerank.f90:87-179).
+    IDR(2) and IDR(8) in FP64, and the mixed form (FP32 inner IDR(s), FP32
+    SpMV, under FP64 QMRIDR(s)), tol 1e-10; CRS SpMV GB/s."""
+    import torch
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    P = pkg.problems
+    n = 4194304
+    t0 = time.perf_counter()
+    rp, ci, vals, b = P.pagerank_crs(n)
+    gen = time.perf_counter() - t0
+    nnz = len(vals)
+    K = pkg.crs_format(n, n, rp, ci, rval=vals)
+    A = pkg.Matrix(K)
+    b_dev = torch.from_numpy(b).cuda()
+    x_dev = torch.empty(n, dtype=torch.float64, device="cuda")
+    A.set_pointer_mode(pkg.POINTER_DEVICE)
+    tol = 1e-10
+    res = {}
+    launches0 = pkg.lib().idrs_launch_count()
+    for s in (2, 8):
+        import ctypes as C
+        flag, relres, iters = C.c_int(), C.c_double(), C.c_int()
+        tl, mx = C.c_double(tol), C.c_int(1000)
+
+        def solve64():
+            pkg.api._check(pkg.lib().idrs_ridrs(A.handle, b_dev.data_ptr(), s, None, C.byref(tl), C.byref(mx),
+                                                None, C.byref(flag), C.byref(relres), C.byref(iters), None,
+                                                None, None, 0, None, 0, None, 0, 0, x_dev.data_ptr()))
+            return flag.value, relres.value, iters.value
+        solve64()
+        (f, r, it), sec = _timed_call(solve64, max(1, args.steps))
+        res[f"idr{s}_fp64"] = {"seconds": round(sec, 5), "flag": f, "relres": r, "iterations": it}
+        in_s, in_it, in_tol, prec = C.c_int(s), C.c_int(100), C.c_double(1e-3), C.c_int(32)
+
+        def solve_mixed():
+            pkg.api._check(pkg.lib().idrs_rqmridr(A.handle, b_dev.data_ptr(), s, None, C.byref(tl), C.byref(mx),
+                                                  C.byref(flag), C.byref(relres), C.byref(iters), C.byref(in_s),
+                                                  C.byref(in_tol), C.byref(in_it), None, None, 0, None, 0,
+                                                  C.byref(prec), x_dev.data_ptr()))
+            return flag.value, relres.value, iters.value
+        solve_mixed()
+        (f, r, it), sec = _timed_call(solve_mixed, max(1, args.steps))
+        ist = (C.c_int(), C.c_int(), C.c_int())
+        pkg.lib().idrs_solve_stats(A.handle, C.byref(ist[0]), C.byref(ist[1]), C.byref(ist[2]))
+        res[f"idr{s}_mixed"] = {"seconds": round(sec, 5), "flag": f, "relres": r, "outer_iterations": it,
+                                "inner_iterations": ist[1].value, "inner": f"IDR({s}) fp32, in_tol 1e-3"}
+    A.set_pointer_mode(pkg.POINTER_HOST)
+    ms64, _ = A.time_matvec(64, 5, 20)
+    ms32, _ = A.time_matvec(32, 5, 20)
+    bytes64 = 12.0 * nnz + 4.0 * (n + 1) + 16.0 * n
+    bytes32 = 8.0 * nnz + 4.0 * (n + 1) + 8.0 * n
+    hbm = float(_peaks().get("hbm_gbs", 6800.0))
+    line = {"workload": "pagerank4m_idr2_idr8_tol1e-10", "N": n, "nnz": nnz, "alpha": 0.85,
+            "row_lengths": "Zipf(2.1) scaled to mean 12, seed 2024 (max %d)" % int(np.diff(rp).max() - 1),
+            "generation_seconds": round(gen, 2), "results": res,
+            "spmv": {"fp64_ms": ms64, "fp64_GBps": round(bytes64 / (ms64 * 1e-3) / 1e9, 1),
+                     "fp32_ms": ms32, "fp32_GBps": round(bytes32 / (ms32 * 1e-3) / 1e9, 1),
+                     "peak_GBps": hbm, "fp64_frac": round(bytes64 / (ms64 * 1e-3) / 1e9 / hbm, 3),
+                     "algorithmic_bytes": "fp64 12 nnz + 4(N+1) + 16 N; fp32 8 nnz + 4(N+1) + 8 N"},
+            "gpu_launches": int(pkg.lib().idrs_launch_count() - launches0)}
+    print(json.dumps(line), flush=True)
+
+
+def run_multishift(args):
+    """(K - sigma_k I) x_k = b, K the 7-point Dirichlet Laplacian on 128^3,
+    16 shifts sigma_k = (2 pi f_k)^2 (1 - 0.05i) spanning [0.1, 4] lambda_max,
+    b a seeded unit complex normal vector; MSQMRIDR(4) alone and with MSIDRS(4)
+    inner in complex128 / complex64, Neumann polynomial variants.  Reports time
+    per outer iteration and the residuals reached within fixed iteration
+    budgets (the strongly indefinite low shifts do not converge with these
+    methods, as in the reference's algorithm)."""
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    P = pkg.problems
+    n = 128
+    N = n ** 3
+    K = pkg.stencil7_format(n, n, n, P.laplace_coefficients(n))
+    sig, lam = P.multishift_shifts(n, n_shifts=16)
+    b = P.complex_unit_normal(N)
+    A = pkg.Matrix(K, complex=True)
+    out = {}
+
+    def rec(name, fn):
+        r, sec = _timed_call(fn)
+        rr = np.asarray(r.relres)
+        out[name] = {"seconds": round(sec, 4), "flag": r.flag, "iterations": r.iterations,
+                     "ms_per_iteration": round(1e3 * sec / max(r.iterations, 1), 4),
+                     "converged_shifts": int(np.sum(rr <= 1e-8)),
+                     "relres": [float("%.2e" % v) for v in rr]}
+    pkg.MSQMRIDR(A, b, sig, 4, tolerance=1e-8, maximum_iterations=20)  # warm-up
+    rec("msqmridr4_fp64", lambda: pkg.MSQMRIDR(A, b, sig, 4, tolerance=1e-8, maximum_iterations=1000))
+    rec("msidrs4_fp64", lambda: pkg.MSIDRS(A, b, sig, 4, tolerance=1e-8, maximum_iterations=1000))
+    for prec in (64, 32):
+        rec(f"msqmridr4_nested_msidrs4_c{'128' if prec == 64 else '64'}",
+            lambda: pkg.MSQMRIDR(A, b, sig, 4, tolerance=1e-8, maximum_iterations=40, inner_s=4,
+                                 inner_iterations=20, inner_tolerance=0.1, inner_precision=prec))
+    An = pkg.Matrix(K, complex=True)
+    An.preconditioner(1, 4, center=lam / 2)
+    sp = An.ms_parameters(sig)
+    rec("neumann4_msqmridr4", lambda: pkg.MSQMRIDR(An, b, sp, 4, tolerance=1e-8, maximum_iterations=500))
+    # the shifts the methods can reach (Re sigma > lambda_max): time to 1e-8
+    sd, _ = P.multishift_shifts(n, n_shifts=16, lo=1.2, hi=4.0)
+    rd, sec = _timed_call(lambda: pkg.MSQMRIDR(A, b, sd, 4, tolerance=1e-8, maximum_iterations=1000))
+    out["definite_shifts_msqmridr4_to_1e-8"] = {"seconds": round(sec, 4), "flag": rd.flag,
+                                                "iterations": rd.iterations,
+                                                "relres_max": float(np.max(rd.relres))}
+    for prec in (64, 32):
+        r, sec = _timed_call(lambda: pkg.MSQMRIDR(A, b, sd, 4, tolerance=1e-8, maximum_iterations=200, inner_s=4,
+                                                   inner_iterations=20, inner_tolerance=0.1,
+                                                   inner_precision=prec))
+        out[f"definite_shifts_nested_c{'128' if prec == 64 else '64'}"] = {
+            "seconds": round(sec, 4), "flag": r.flag, "iterations": r.iterations,
+            "relres_max": float(np.max(r.relres))}
+    # algorithmic bytes of one MSQMRIDR(4) iteration's all-shift pass (BMsqW,
+    # c128): per shift read 5 W columns + vtilde share, write wn, read/write x
+    bytes_w = 16.0 * N * (16 * (5 + 1 + 2) + 2 + 4)
+    print(json.dumps({"workload": "multishift_laplace128_16shifts_msqmridr4", "N": N, "n_shifts": 16,
+                      "lambda_max": lam, "results": out,
+                      "msqmridr_shift_pass_bytes": bytes_w}), flush=True)
+
+
+def run_adjoint(args):
+    """L = 1/2 ||x - x_t||^2, A x = b, A the 128^3 convection-diffusion CRS
+    (nnz 14,581,760), x_t and b seeded N(0,1); IDR(4) forward and IDR(4) on
+    A^T backward (tol 1e-10), dL/db = lambda, dL/dA_ij = -lambda_i x_j;
+    forward + backward timed for 8 right-hand sides; central differences
+    (eps 1e-6) on random entries of b and of A's nonzeros."""
+    import torch
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    P = pkg.problems
+    n = 128
+    N = n ** 3
+    rp, ci, vals = P.stencil_to_crs(n, n, n, P.cdr_coefficients(n))
+    nnz = len(vals)
+    K = pkg.crs_format(N, N, rp, ci, rval=vals)
+    A = pkg.Matrix(K)
+    KT = pkg.crs_transpose(K)
+    AT = pkg.Matrix(KT)
+    tol = 1e-10
+    rng = np.random.default_rng(2025)
+    B = rng.standard_normal((8, N))
+    XT = rng.standard_normal((8, N))
+    pkg.IDRS(A, B[0], 4, tolerance=1e-6)  # warm-up
+
+    def fwd_bwd():
+        outs = []
+        for r in range(8):
+            f = pkg.IDRS(A, B[r], 4, tolerance=tol, maximum_iterations=4000)
+            a = pkg.ADJOINT(AT, K, f.x, f.x - XT[r], 4, tolerance=tol, maximum_iterations=4000)
+            outs.append((f, a))
+        return outs
+    outs, sec = _timed_call(fwd_bwd)
+    f0, a0 = outs[0]
+    # gradient kernel alone
+    lam = torch.from_numpy(a0.lam).cuda()
+    xx = torch.from_numpy(f0.x).cuda()
+    gr = torch.empty(nnz, dtype=torch.float64, device="cuda")
+    A.set_pointer_mode(pkg.POINTER_DEVICE)
+    import ctypes as C
+
+    def gk():
+        pkg.api._check(pkg.lib().idrs_rsparse_outer_grad(A.handle, lam.data_ptr(), xx.data_ptr(), gr.data_ptr()))
+    gk()
+    _, t_g = _timed_call(lambda: [gk() for _ in range(20)])
+    A.set_pointer_mode(pkg.POINTER_HOST)
+    t_g /= 20
+    g_bytes = 12.0 * nnz + 4.0 * (N + 1) + 16.0 * N
+    hbm = float(_peaks().get("hbm_gbs", 6800.0))
+    # central differences (cancellation-free form, one perturbed solve each)
+    x, res = f0.x, f0.x - XT[0]
+    eps, ftol = 1e-6, 1e-12
+    rows = np.repeat(np.arange(N), np.diff(rp))
+
+    def solve(Am, rhs):
+        return pkg.IDRS(Am, rhs, 4, tolerance=ftol, maximum_iterations=6000).x
+
+    def central(dp, dm):
+        return (res @ (dp - dm) + 0.5 * (dp @ dp - dm @ dm)) / (2 * eps)
+    errs_b, errs_a = [], []
+    t0 = time.perf_counter()
+    for k in rng.choice(N, args.fd_samples, replace=False):
+        e = np.zeros(N)
+        e[k] = eps
+        fd = central(solve(A, e), solve(A, -e))
+        errs_b.append(abs(fd - a0.lam[k]) / abs(a0.lam[k]))
+    for p in rng.choice(nnz, args.fd_samples, replace=False):
+        i, j = rows[p], ci[p] - 1
+        d = []
+        for sgn in (1.0, -1.0):
+            v2 = vals.copy()
+            v2[p] += sgn * eps
+            Ap = pkg.Matrix(pkg.crs_format(N, N, rp, ci, rval=v2))
+            rhs = np.zeros(N)
+            rhs[i] = -sgn * eps * x[j]
+            d.append(solve(Ap, rhs))
+        fd = central(*d)
+        errs_a.append(abs(fd - a0.grad[p]) / abs(a0.grad[p]))
+    fd_sec = time.perf_counter() - t0
+    print(json.dumps({
+        "workload": "adjoint_cdr128_crs_idr4_tol1e-10_8rhs", "N": N, "nnz": nnz,
+        "forward_backward_8rhs_seconds": round(sec, 4),
+        "per_rhs": [{"fwd_it": f.iterations, "fwd_relres": f.relres, "adj_it": a.iterations,
+                     "adj_relres": a.relres} for f, a in outs],
+        "gradient_kernel": {"ms": round(t_g * 1e3, 4), "GBps": round(g_bytes / t_g / 1e9, 1),
+                            "frac": round(g_bytes / t_g / 1e9 / hbm, 3),
+                            "algorithmic_bytes": "12 nnz + 4(N+1) + 16 N"},
+        "finite_differences": {"eps": eps, "samples_b": len(errs_b), "samples_A": len(errs_a),
+                               "max_rel_err_b": max(errs_b), "max_rel_err_A": max(errs_a),
+                               "seconds": round(fd_sec, 1)}}), flush=True)
+
+
 def main():
     args = parse()
     if args.profile:
         run_profile(args)
+        return
+    if args.workload != "cdr256":
+        {"pagerank": run_pagerank, "multishift": run_multishift, "adjoint": run_adjoint}[args.workload](args)
         return
     rank, world, dist = dist_init(args.gpus)
     if args.impl == "reference":

@@ -19,6 +19,7 @@
 // order (coalesced col_ind / grad traffic), finding each entry's row by a
 // binary search in shared memory.
 #include <stdexcept>
+#include <vector>
 
 #include "adjoint.h"
 
@@ -213,12 +214,17 @@ void crs_transpose(const UserMatrix& K, UserMatrix& Tm, cudaStream_t st) {
     }
     for (int* p : {cnt, cursor, keyT, keyS, rowidx}) IDRS_CUDA(cudaFreeAsync(p, st));
     IDRS_CUDA(cudaStreamSynchronize(st));
+    std::vector<int> rp_host(m + 1);
+    IDRS_CUDA(cudaMemcpy(rp_host.data(), T->row_ptr, sizeof(int) * (m + 1), cudaMemcpyDeviceToHost));
+    build_row_plan(*T, rp_host.data());
   } catch (...) {
     for (int* p : {cnt, cursor, keyT, keyS, rowidx})
       if (p) cudaFreeAsync(p, st);
     cudaFree(T->row_ptr); cudaFree(T->col_ind); cudaFree(T->val);
+    cudaFree(T->long_rows); cudaFree(T->seg_ptr); cudaFree(T->partial);
     T->row_ptr = T->col_ind = nullptr;
-    T->val = nullptr;
+    T->long_rows = T->seg_ptr = nullptr;
+    T->val = T->partial = nullptr;
     throw;
   }
 }

@@ -851,6 +851,7 @@ int idrs_crs_format(int nrows, int ncols, const int* row_ptr, const int* col_ind
       }
     }
     M->group = crs_group(nnz, nrows);
+    build_row_plan(*M, rp.data());
     *K = M;
     return IDRS_OK;
   });
@@ -889,6 +890,7 @@ int idrs_coo_format(int nrows, int ncols, int nnz, const int* indx, const int* j
     M->vals = cval ? 2 : 1;
     M->val = upload(val.data(), 8 * vs * (size_t)nnz);
     M->group = crs_group(nnz, nrows);
+    build_coo_rows(*M, cnt.data());
     *K = M;
     return IDRS_OK;
   });
