@@ -47,7 +47,7 @@ def parse():
     p.add_argument("--in-tol", type=float, default=3e-3)
     p.add_argument("--in-s", type=int, default=4)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--profile", choices=["solve", "chain32", "chain64"], default=None,
+    p.add_argument("--profile", choices=["solve", "chain32", "chain64", "spmv_pagerank", "grad128"], default=None,
                    help="profiling driver: one mixed solve, or the fp32/fp64 Chebyshev(8) chain alone")
     p.add_argument("--workload", choices=["cdr256", "pagerank", "multishift", "adjoint"], default="cdr256",
                    help="cdr256: the headline line; the others measure the remaining configurations "
@@ -380,6 +380,26 @@ def run_profile(args):
         r = pkg.PP_IDRS(K, K * np.ones(n ** 3), P=D, tol=TOL, **solve_kw("mixed", args))
         print(json.dumps({"profile": "solve", "grid": n, "flag": r.flag, "outer": r.iterations,
                           "relres_original": r.relres_original}))
+    elif args.profile == "spmv_pagerank":
+        rp, ci, vals, b = pkg.problems.pagerank_crs(4194304)
+        A = pkg.Matrix(pkg.crs_format(4194304, 4194304, rp, ci, rval=vals))
+        ms64, _ = A.time_matvec(64, 3, 5)
+        ms32, _ = A.time_matvec(32, 3, 5)
+        print(json.dumps({"profile": "spmv_pagerank", "ms64": ms64, "ms32": ms32}))
+    elif args.profile == "grad128":
+        import torch
+        P = pkg.problems
+        rp, ci, vals = P.stencil_to_crs(128, 128, 128, P.cdr_coefficients(128))
+        N = 128 ** 3
+        A = pkg.Matrix(pkg.crs_format(N, N, rp, ci, rval=vals))
+        A.set_pointer_mode(pkg.POINTER_DEVICE)
+        lam = torch.randn(N, dtype=torch.float64, device="cuda")
+        x = torch.randn(N, dtype=torch.float64, device="cuda")
+        g = torch.empty(len(vals), dtype=torch.float64, device="cuda")
+        for _ in range(8):
+            pkg.api._check(pkg.lib().idrs_rsparse_outer_grad(A.handle, lam.data_ptr(), x.data_ptr(), g.data_ptr()))
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "grad128", "nnz": len(vals)}))
     else:
         K, D = make_problem(pkg, n)
         A = pkg.Matrix(K, P=D)

@@ -74,12 +74,6 @@ MatView UserMatrix::view64() const {
   for (int i = 0; i < 7; ++i) v.st[i] = st[i];
   v.vcplx = (vals == 2);
   v.group = group;
-  v.plan_th = plan_th;
-  v.n_long = n_long;
-  v.n_seg = n_seg;
-  v.long_rows = long_rows;
-  v.seg_ptr = seg_ptr;
-  v.partial = partial;
   v.ri = row_ind;
   v.n_empty = n_empty;
   v.empty_rows = empty_rows;
@@ -105,39 +99,15 @@ void user_matrix_release(UserMatrix* K) {
   if (--K->refcount > 0) return;
   cudaFree(K->row_ptr); cudaFree(K->col_ind); cudaFree(K->val); cudaFree(K->band);
   cudaFree(K->mat); cudaFree(K->diag);
-  cudaFree(K->long_rows); cudaFree(K->seg_ptr); cudaFree(K->partial);
   cudaFree(K->row_ind); cudaFree(K->empty_rows); cudaFree(K->carry);
   delete K;
 }
 
-void build_row_plan(UserMatrix& M, const int* rp) {
-  M.plan_th = 32 * std::max(M.group, 1);
-  std::vector<int> rows, segp(1, 0);
-  for (int i = 0; i < M.nrows; ++i) {
-    const long len = (long)rp[i + 1] - rp[i];
-    if (len > M.plan_th) {
-      rows.push_back(i);
-      segp.push_back(segp.back() + (int)((len + kSegNnz - 1) / kSegNnz));
-    }
-  }
-  if (rows.empty()) return;
-  M.n_long = (int)rows.size();
-  M.n_seg = segp.back();
-  IDRS_CUDA(cudaMalloc((void**)&M.long_rows, sizeof(int) * rows.size()));
-  IDRS_CUDA(cudaMemcpy(M.long_rows, rows.data(), sizeof(int) * rows.size(), cudaMemcpyHostToDevice));
-  IDRS_CUDA(cudaMalloc((void**)&M.seg_ptr, sizeof(int) * segp.size()));
-  IDRS_CUDA(cudaMemcpy(M.seg_ptr, segp.data(), sizeof(int) * segp.size(), cudaMemcpyHostToDevice));
-  IDRS_CUDA(cudaMalloc(&M.partial, 16 * (size_t)M.n_seg));
-}
-
-void build_coo_rows(UserMatrix& M, const int* rp) {
-  std::vector<int> ri(std::max<long>(M.nnz, 1)), empty;
-  for (int i = 0; i < M.nrows; ++i) {
+// empty rows and the carries of the nonzero-balanced segmented reduction
+static void build_seg_reduce(UserMatrix& M, const int* rp) {
+  std::vector<int> empty;
+  for (int i = 0; i < M.nrows; ++i)
     if (rp[i + 1] == rp[i]) empty.push_back(i);
-    for (int k = rp[i]; k < rp[i + 1]; ++k) ri[k] = i;
-  }
-  IDRS_CUDA(cudaMalloc((void**)&M.row_ind, sizeof(int) * ri.size()));
-  IDRS_CUDA(cudaMemcpy(M.row_ind, ri.data(), sizeof(int) * ri.size(), cudaMemcpyHostToDevice));
   M.n_empty = (int)empty.size();
   if (!empty.empty()) {
     IDRS_CUDA(cudaMalloc((void**)&M.empty_rows, sizeof(int) * empty.size()));
@@ -145,6 +115,26 @@ void build_coo_rows(UserMatrix& M, const int* rp) {
   }
   const long warps = (M.nnz + kCooWarpNnz - 1) / kCooWarpNnz;
   IDRS_CUDA(cudaMalloc(&M.carry, 2 * 16 * (size_t)std::max<long>(warps, 1)));
+}
+
+void build_row_plan(UserMatrix& M, const int* rp) {
+  // rows far longer than the lanes given to a row would serialise a warp:
+  // such matrices use the nonzero-balanced segmented reduction instead
+  const long th = 32L * std::max(M.group, 1);
+  for (int i = 0; i < M.nrows; ++i)
+    if ((long)rp[i + 1] - rp[i] > th) {
+      build_seg_reduce(M, rp);
+      return;
+    }
+}
+
+void build_coo_rows(UserMatrix& M, const int* rp) {
+  std::vector<int> ri(std::max<long>(M.nnz, 1));
+  for (int i = 0; i < M.nrows; ++i)
+    for (int k = rp[i]; k < rp[i + 1]; ++k) ri[k] = i;
+  IDRS_CUDA(cudaMalloc((void**)&M.row_ind, sizeof(int) * ri.size()));
+  IDRS_CUDA(cudaMemcpy(M.row_ind, ri.data(), sizeof(int) * ri.size(), cudaMemcpyHostToDevice));
+  build_seg_reduce(M, rp);
 }
 
 // ---------------------------------------------------------------------------
@@ -265,7 +255,7 @@ __global__ void __launch_bounds__(256) k_crs(int nrows, const int* __restrict__ 
                                              const T* __restrict__ x, T* __restrict__ y, T a, T cv,
                                              const T* __restrict__ v, T cx, T cu,
                                              const T* __restrict__ u,
-                                             const int* __restrict__ skip, int max_len) {
+                                             const int* __restrict__ skip) {
   if (skip && *skip) return;
   constexpr int RPW = 32 / G;
   const int lane = threadIdx.x & 31;
@@ -276,12 +266,10 @@ __global__ void __launch_bounds__(256) k_crs(int nrows, const int* __restrict__ 
   for (long base = warp * RPW; base < nrows; base += nwarps * RPW) {
     const long row = base + sub;
     T sum = T(0);
-    bool mine = row < nrows;
+    const bool mine = row < nrows;
     if (mine) {
       const int beg = rp[row], end = rp[row + 1];
-      mine = (end - beg) <= max_len;  // longer rows: segment kernels
-      if (mine)
-        for (int k = beg + gl; k < end; k += G) sum = sum + mulvt(val[k], x[ci[k]]);
+      for (int k = beg + gl; k < end; k += G) sum = sum + mulvt(val[k], x[ci[k]]);
     }
 #pragma unroll
     for (int m = G / 2; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
@@ -303,12 +291,11 @@ __global__ void __launch_bounds__(256) k_crs_row(int nrows, const int* __restric
                                                  const T* __restrict__ x, T* __restrict__ y, T a, T cv,
                                                  const T* __restrict__ v, T cx, T cu,
                                                  const T* __restrict__ u,
-                                                 const int* __restrict__ skip, int max_len) {
+                                                 const int* __restrict__ skip) {
   if (skip && *skip) return;
   for (long row = blockIdx.x * (long)blockDim.x + threadIdx.x; row < nrows;
        row += gridDim.x * (long)blockDim.x) {
     const int beg = rp[row], end = rp[row + 1];
-    if (end - beg > max_len) continue;  // written by the segment kernels
     T sum = T(0);
     for (int k = beg; k < end; ++k) sum = sum + mulvt(val[k], x[ci[k]]);
     T out = a * sum;
@@ -329,85 +316,65 @@ __device__ __forceinline__ T epilogue(T sum, long row, T a, T cv, const T* __res
   return out;
 }
 
-// CRS long rows, one warp per segment of kSegNnz nonzeros: partial sums.
-template <class T, class V>
-__global__ void __launch_bounds__(256) k_crs_seg(int n_seg, int n_long, const int* __restrict__ long_rows,
-                                                 const int* __restrict__ seg_ptr,
-                                                 const int* __restrict__ rp, const int* __restrict__ ci,
-                                                 const V* __restrict__ val, const T* __restrict__ x,
-                                                 T* __restrict__ partial, const int* __restrict__ skip) {
-  if (skip && *skip) return;
-  const int lane = threadIdx.x & 31;
-  const long g = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
-  if (g >= n_seg) return;  // whole warp
-  int lo = 0, hi = n_long;  // seg_ptr[lo] <= g < seg_ptr[hi]
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (seg_ptr[mid] <= g) lo = mid; else hi = mid;
+// Row index of an entry for the segmented reduction: stored (COO) or found
+// by binary search in the row pointers (CRS with skewed rows).
+struct RowsStored {
+  const int* __restrict__ ri;
+  const int* __restrict__ rp;
+  __device__ int find(long k) const { return ri[k]; }
+  __device__ int at(long k, int, int) const { return ri[k]; }
+  __device__ bool first_open(long beg, int row_first) const { return beg > 0 && ri[beg - 1] == row_first; }
+  __device__ bool last_open(long end, long nnz, int row_last) const { return end < nnz && ri[end] == row_last; }
+};
+struct RowsSearch {
+  const int* __restrict__ rp;
+  int nrows;
+  // the row holding entry k: the largest r in [lo, hi] with rp[r] <= k
+  __device__ int at(long k, int lo, int hi) const {
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (rp[mid] <= k) lo = mid; else hi = mid - 1;
+    }
+    return lo;
   }
-  const int row = long_rows[lo];
-  const long beg = rp[row] + (g - seg_ptr[lo]) * (long)kSegNnz;
-  const long end = min((long)rp[row + 1], beg + kSegNnz);
-  T sum = T(0);
-  for (long k = beg + lane; k < end; k += 32) sum = sum + mulvt(val[k], x[ci[k]]);
-#pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
-  if (lane == 0) partial[g] = sum;
-}
+  __device__ int find(long k) const { return at(k, 0, nrows - 1); }
+  __device__ bool first_open(long beg, int row_first) const { return rp[row_first] < beg; }
+  __device__ bool last_open(long end, long, int row_last) const { return rp[row_last + 1] > end; }
+};
 
-// CRS long rows: one warp per row adds its segments in a fixed order.
-template <class T>
-__global__ void __launch_bounds__(256) k_crs_fin(int n_long, const int* __restrict__ long_rows,
-                                                 const int* __restrict__ seg_ptr,
-                                                 const T* __restrict__ partial, const T* __restrict__ x,
-                                                 T* __restrict__ y, T a, T cv, const T* __restrict__ v, T cx,
-                                                 T cu, const T* __restrict__ u, const int* __restrict__ skip) {
-  if (skip && *skip) return;
-  const int lane = threadIdx.x & 31;
-  const long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
-  if (w >= n_long) return;
-  T sum = T(0);
-  for (int g = seg_ptr[w] + lane; g < seg_ptr[w + 1]; g += 32) sum = sum + partial[g];
-#pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
-  if (lane == 0) {
-    const int row = long_rows[w];
-    y[row] = epilogue(sum, row, a, cv, v, cx, cu, u, x);
-  }
-}
-
-// COO, segmented reduction (user_module.f90:525-585 computes the same sums by
-// a serial scatter-add).  The entries are stored row-sorted (the caller's
-// order inside a row) with their row index; every warp takes a fixed share of
-// kCooWarpNnz entries, whatever the row lengths, and reduces them by row with
-// a shuffle-based segmented scan, 32 entries per round.  Rows that start and
-// end inside the share are written at once; the first row of a share, when it
-// began in an earlier share, leaves its partial sum in carry[2w]; the last
-// row, when it continues into a later share, leaves it in carry[2w+1] and
-// this warp owns it: k_coo_fix adds the later shares' partials in order.
-template <class T, class V>
-__global__ void __launch_bounds__(256) k_coo_seg(long nnz, long nwarps, const int* __restrict__ ri,
-                                                 const int* __restrict__ ci, const V* __restrict__ val,
-                                                 const T* __restrict__ x, T* __restrict__ y, T a, T cv,
-                                                 const T* __restrict__ v, T cx, T cu,
-                                                 const T* __restrict__ u, T* __restrict__ carry,
-                                                 const int* __restrict__ skip) {
+// Segmented-reduction SpMV for COO (user_module.f90:525-585 computes the same
+// sums by a serial scatter-add) and for CRS matrices with skewed rows.  The
+// entries are row-sorted (COO: the caller's order inside a row); every warp
+// takes a fixed share of kCooWarpNnz entries, whatever the row lengths, and
+// reduces them by row with a shuffle segmented scan, 32 entries per round.
+// Rows that start and end inside the share are written at once; the first
+// row of a share, when it began in an earlier share, leaves its partial sum
+// in carry[2w]; the last row, when it continues into a later share, leaves it
+// in carry[2w+1] and this share owns it: k_seg_fix adds the later shares'
+// partials in order.
+template <class T, class V, class Rows>
+__global__ void __launch_bounds__(256) k_seg_reduce(long nnz, long nwarps, Rows R,
+                                                    const int* __restrict__ ci, const V* __restrict__ val,
+                                                    const T* __restrict__ x, T* __restrict__ y, T a, T cv,
+                                                    const T* __restrict__ v, T cx, T cu,
+                                                    const T* __restrict__ u, T* __restrict__ carry,
+                                                    const int* __restrict__ skip) {
   if (skip && *skip) return;
   const int lane = threadIdx.x & 31;
   const long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
   if (w >= nwarps) return;  // whole warp
   const long beg = w * (long)kCooWarpNnz;
   const long end = min(nnz, beg + kCooWarpNnz);
-  const int row_first = ri[beg];
-  const int row_last = ri[end - 1];
-  const bool first_open = beg > 0 && ri[beg - 1] == row_first;
-  const bool last_open = end < nnz && ri[end] == row_last;
+  const int row_first = R.find(beg);
+  const int row_last = R.find(end - 1);
+  const bool first_open = R.first_open(beg, row_first);
+  const bool last_open = R.last_open(end, nnz, row_last);
   int crow = -1;  // row running across rounds and its sum so far
   T csum = T(0);
   for (long base = beg; base < end; base += 32) {
     const long k = base + lane;
     const bool valid = k < end;
-    const int r = valid ? ri[k] : -2 - lane;  // distinct sentinels for the tail
+    const int r = valid ? R.at(k, row_first, row_last) : -2 - lane;  // distinct sentinels for the tail
     T p = valid ? mulvt(val[k], x[ci[k]]) : T(0);
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
@@ -418,14 +385,14 @@ __global__ void __launch_bounds__(256) k_coo_seg(long nnz, long nwarps, const in
     if (r == crow) p = p + csum;
     // does this entry end its row inside the share?
     int rnext = __shfl_down_sync(0xffffffffu, r, 1);
-    if (lane == 31) rnext = (k + 1 < end) ? ri[k + 1] : -1;
+    if (lane == 31) rnext = (k + 1 < end) ? R.at(k + 1, row_first, row_last) : -1;
     const bool last_of_share = valid && (k + 1 == end);
     const bool seg_end = valid && (last_of_share || rnext != r);
     if (seg_end) {
       if (r == row_first && first_open) {
         carry[2 * w] = p;                    // continuation of an earlier share's row
       } else if (last_of_share && last_open) {
-        carry[2 * w + 1] = p;                // this share owns the row; k_coo_fix completes it
+        carry[2 * w + 1] = p;                // this share owns the row; k_seg_fix completes it
       } else {
         y[r] = epilogue(p, r, a, cv, v, cx, cu, u, x);
       }
@@ -435,10 +402,10 @@ __global__ void __launch_bounds__(256) k_coo_seg(long nnz, long nwarps, const in
   }
 }
 
-// COO rows spanning shares: the owning share (row started there and runs on)
-// adds the first-row partials of the following shares in order.
-template <class T>
-__global__ void __launch_bounds__(256) k_coo_fix(long nnz, long nwarps, const int* __restrict__ ri,
+// Rows spanning shares: the share where a row starts (and runs on) adds the
+// first-row partials of the following shares in order.
+template <class T, class Rows>
+__global__ void __launch_bounds__(256) k_seg_fix(long nnz, long nwarps, Rows R,
                                                  const int* __restrict__ rp, const T* __restrict__ carry,
                                                  const T* __restrict__ x, T* __restrict__ y, T a, T cv,
                                                  const T* __restrict__ v, T cx, T cu,
@@ -449,10 +416,10 @@ __global__ void __launch_bounds__(256) k_coo_fix(long nnz, long nwarps, const in
   if (w >= nwarps) return;
   const long beg = w * (long)kCooWarpNnz;
   const long end = min(nnz, beg + kCooWarpNnz);
-  const int row = ri[end - 1];
-  const bool last_open = end < nnz && ri[end] == row;
-  const bool first_open = beg > 0 && ri[beg - 1] == ri[beg];
-  if (!last_open || (first_open && ri[beg] == row)) return;  // not the owner
+  const int row = R.find(end - 1);
+  if (!R.last_open(end, nnz, row)) return;
+  const int row_first = R.find(beg);
+  if (row_first == row && R.first_open(beg, row_first)) return;  // middle share: not the owner
   const long wlast = ((long)rp[row + 1] - 1) / kCooWarpNnz;  // share holding the row's last entry
   T sum = T(0);
   for (long q = w + 1 + lane; q <= wlast; q += 32) sum = sum + carry[2 * q];
@@ -512,52 +479,51 @@ __global__ void __launch_bounds__(256) k_dense(int nrows, int ncols, const V* __
   }
 }
 
+template <class T, class V, class Rows>
+static void launch_seg_reduce(const MatView& M, Rows R, const V* val, const T* x, T* y, T a, T cv,
+                              const T* v, T cx, T cu, const T* u, const int* skip, cudaStream_t st) {
+  const long warps = (M.nnz + kCooWarpNnz - 1) / kCooWarpNnz;
+  if (warps > 0) {
+    const long blocks = (warps * 32 + kThreads - 1) / kThreads;
+    k_seg_reduce<T, V, Rows><<<(unsigned)blocks, kThreads, 0, st>>>(M.nnz, warps, R, M.ci, val, x, y, a, cv, v, cx,
+                                                                     cu, u, (T*)M.carry, skip);
+    IDRS_LAUNCH_CHECK();
+    k_seg_fix<T, Rows><<<(unsigned)blocks, kThreads, 0, st>>>(M.nnz, warps, R, M.rp, (const T*)M.carry, x, y, a,
+                                                              cv, v, cx, cu, u, skip);
+    IDRS_LAUNCH_CHECK();
+  }
+  if (M.n_empty > 0) {
+    k_empty_rows<T><<<stream_grid(M.n_empty), kThreads, 0, st>>>(M.n_empty, M.empty_rows, x, y, a, cv, v, cx, cu,
+                                                                 u, skip);
+    IDRS_LAUNCH_CHECK();
+  }
+}
+
 template <class T, class V>
 static void launch_crs(const MatView& M, const V* val, const T* x, T* y, T a, T cv, const T* v,
                        T cx, T cu, const T* u, const int* skip, cudaStream_t st) {
   if (M.format == FMT_COO && M.ri) {
-    const long warps = (M.nnz + kCooWarpNnz - 1) / kCooWarpNnz;
-    if (warps > 0) {
-      const long blocks = (warps * 32 + kThreads - 1) / kThreads;
-      k_coo_seg<T, V><<<(unsigned)blocks, kThreads, 0, st>>>(M.nnz, warps, M.ri, M.ci, val, x, y, a, cv, v, cx,
-                                                             cu, u, (T*)M.carry, skip);
-      IDRS_LAUNCH_CHECK();
-      k_coo_fix<T><<<(unsigned)blocks, kThreads, 0, st>>>(M.nnz, warps, M.ri, M.rp, (const T*)M.carry, x, y, a,
-                                                          cv, v, cx, cu, u, skip);
-      IDRS_LAUNCH_CHECK();
-    }
-    if (M.n_empty > 0) {
-      k_empty_rows<T><<<stream_grid(M.n_empty), kThreads, 0, st>>>(M.n_empty, M.empty_rows, x, y, a, cv, v, cx,
-                                                                   cu, u, skip);
-      IDRS_LAUNCH_CHECK();
-    }
+    launch_seg_reduce<T, V>(M, RowsStored{M.ri, M.rp}, val, x, y, a, cv, v, cx, cu, u, skip, st);
     return;
   }
-  const int max_len = (M.n_long > 0) ? M.plan_th : INT_MAX;
+  if (M.carry) {  // CRS with skewed rows: the same nonzero-balanced reduction
+    launch_seg_reduce<T, V>(M, RowsSearch{M.rp, M.nrows}, val, x, y, a, cv, v, cx, cu, u, skip, st);
+    return;
+  }
   long rows_per_block = kThreads / M.group;
   long need = (M.nrows + rows_per_block - 1) / rows_per_block;
   int grid = (int)std::max(1L, std::min(need, (long)num_sms() * 8));
   if (M.group == 1) {
     k_crs_row<T, V><<<stream_grid(M.nrows), kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu,
-                                                               u, skip, max_len);
+                                                               u, skip);
   } else {
     switch (M.group) {
-      case 2: k_crs<2><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip, max_len); break;
-      case 4: k_crs<4><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip, max_len); break;
-      case 8: k_crs<8><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip, max_len); break;
-      case 16: k_crs<16><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip, max_len); break;
-      default: k_crs<32><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip, max_len); break;
+      case 2: k_crs<2><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
+      case 4: k_crs<4><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
+      case 8: k_crs<8><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
+      case 16: k_crs<16><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
+      default: k_crs<32><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
     }
-  }
-  if (M.n_long > 0) {
-    IDRS_LAUNCH_CHECK();
-    const long sblocks = ((long)M.n_seg * 32 + kThreads - 1) / kThreads;
-    k_crs_seg<T, V><<<(unsigned)sblocks, kThreads, 0, st>>>(M.n_seg, M.n_long, M.long_rows, M.seg_ptr, M.rp, M.ci,
-                                                            val, x, (T*)M.partial, skip);
-    IDRS_LAUNCH_CHECK();
-    const long fblocks = ((long)M.n_long * 32 + kThreads - 1) / kThreads;
-    k_crs_fin<T><<<(unsigned)fblocks, kThreads, 0, st>>>(M.n_long, M.long_rows, M.seg_ptr, (const T*)M.partial, x,
-                                                         y, a, cv, v, cx, cu, u, skip);
   }
 }
 
@@ -933,12 +899,10 @@ int build_operator(Operator* A) {
   if (A->dinv64) { cudaFreeAsync(A->dinv64, st); A->dinv64 = nullptr; }
   if (A->dinv32) { cudaFreeAsync(A->dinv32, st); A->dinv32 = nullptr; }
   A->k64 = K.view64();
-  if (K.n_seg > 0 && !A->lb_partial) IDRS_CUDA(cudaMallocAsync(&A->lb_partial, 16 * (size_t)K.n_seg, st));
   if (K.carry && !A->lb_carry) {
     const long warps = (K.nnz + kCooWarpNnz - 1) / kCooWarpNnz;
     IDRS_CUDA(cudaMallocAsync(&A->lb_carry, 2 * 16 * (size_t)std::max<long>(warps, 1), st));
   }
-  A->k64.partial = A->lb_partial;
   A->k64.carry = A->lb_carry;
   A->ks64 = A->k64;
   A->ks32 = MatView();
@@ -1075,7 +1039,6 @@ void operator_free(Operator* A) {
   if (A->ks_val32) cudaFreeAsync(A->ks_val32, st);
   if (A->dinv64) cudaFreeAsync(A->dinv64, st);
   if (A->dinv32) cudaFreeAsync(A->dinv32, st);
-  if (A->lb_partial) cudaFreeAsync(A->lb_partial, st);
   if (A->lb_carry) cudaFreeAsync(A->lb_carry, st);
   for (auto& p : A->shadows) cudaFreeAsync(p.second, st);
   A->shadows.clear();

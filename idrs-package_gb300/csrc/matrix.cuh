@@ -37,21 +37,16 @@ struct MatView {
   int nx = 0, ny = 0, nz = 0;
   double st[7] = {0, 0, 0, 0, 0, 0, 0};  // stencil c,w,e,s,n,f,b
   int group = 8;                          // CRS lanes per row
-  // CRS long-row plan: rows longer than plan_th nonzeros are split into
-  // segments of kSegNnz, one warp each; partial sums in `partial`
-  int plan_th = 0, n_long = 0, n_seg = 0;
-  const int* long_rows = nullptr;
-  const int* seg_ptr = nullptr;
-  void* partial = nullptr;
-  // COO: row of every (row-sorted) entry, empty rows, per-warp carries
+  // nonzero-balanced segmented reduction (COO always; CRS with rows far
+  // longer than its lanes per row): row of every entry (COO), empty rows,
+  // per-warp carries
   const int* ri = nullptr;
   int n_empty = 0;
   const int* empty_rows = nullptr;
   void* carry = nullptr;
 };
 
-constexpr int kSegNnz = 256;       // CRS long-row segment (one warp)
-constexpr int kCooWarpNnz = 256;   // COO entries per warp (8 per lane)
+constexpr int kCooWarpNnz = 256;   // entries per warp of the segmented reduction (8 per lane)
 
 // Three diagonals of a tridiagonal Jacobi matrix J((d+2) x (d+1)):
 // a[i-1] = J(i-1,i), b[i-1] = J(i,i), c[i-1] = J(i+1,i), i = 1..d+1.
@@ -83,10 +78,6 @@ struct UserMatrix {
   int nx = 0, ny = 0, nz = 0;
   double st[7] = {0, 0, 0, 0, 0, 0, 0};
   // CRS / COO load-balancing data (see MatView)
-  int plan_th = 0, n_long = 0, n_seg = 0;
-  int* long_rows = nullptr;
-  int* seg_ptr = nullptr;
-  void* partial = nullptr;   // 16 B per segment
   int* row_ind = nullptr;    // COO
   int n_empty = 0;
   int* empty_rows = nullptr; // COO rows without entries
@@ -105,9 +96,9 @@ struct UserMatrix {
 void user_matrix_release(UserMatrix* K);
 
 // Load balancing of CRS / COO matrices (rp: host copy of the 0-based row
-// pointers).  CRS: rows with more than 32 * group nonzeros get a segment plan.
-// COO: row index of every entry, the list of empty rows and the carries of
-// the segmented reduction.
+// pointers).  CRS with a row longer than 32 * group nonzeros, and every COO
+// matrix, use the nonzero-balanced segmented reduction: the list of empty rows,
+// the per-warp carries and (COO) the row index of every entry.
 void build_row_plan(UserMatrix& M, const int* rp_host);
 void build_coo_rows(UserMatrix& M, const int* rp_host);
 
@@ -143,9 +134,8 @@ struct Operator {
   // reduction scratch for kernels launched on this operator's stream
   RedBuf red{nullptr, nullptr};
 
-  // private partial-sum / carry buffers of the load-balanced CRS / COO
-  // kernels (so that operators sharing a user_matrix may run concurrently)
-  void* lb_partial = nullptr;
+  // private carry buffer of the segmented reduction (so that operators
+  // sharing a user_matrix may run concurrently)
   void* lb_carry = nullptr;
 
   // statistics of the last flexible (QMRIDR) solve with inner iterations
