@@ -14,10 +14,11 @@
 // columns of K (7 for the stencil matrices, ~Poisson(12) for the PageRank
 // matrix), so it stays a small fraction of the transpose.
 //
-// Gradient: one block per 256 consecutive rows; the block loads its row
-// pointers into shared memory and its threads sweep the block's nonzeros in
-// order (coalesced col_ind / grad traffic), finding each entry's row by a
-// binary search in shared memory.
+// Gradient: one block per 256 consecutive rows; the block stages its row
+// pointers and lambda in shared memory, expands the local row id of each of
+// its nonzeros into shared memory (binary search instead when a block holds
+// more than 4096 nonzeros), and its threads sweep the nonzeros in order
+// (coalesced col_ind / grad traffic).
 #include <stdexcept>
 #include <vector>
 
@@ -141,6 +142,7 @@ __global__ void k_gather_T(long nnz, const int* __restrict__ keyS, const int* __
 }
 
 constexpr int kGradRows = 256;
+constexpr int kGradMaxNnz = 4096;  // nonzeros of a block whose local row ids fit in shared memory
 
 __global__ void __launch_bounds__(kGradRows) k_outer_grad(int n, const int* __restrict__ rp,
                                                           const int* __restrict__ ci,
@@ -149,12 +151,20 @@ __global__ void __launch_bounds__(kGradRows) k_outer_grad(int n, const int* __re
                                                           double* __restrict__ grad) {
   __shared__ int srp[kGradRows + 1];
   __shared__ double slam[kGradRows];
+  __shared__ unsigned char srow[kGradMaxNnz];  // local row (< 256) of each nonzero
   const int r0 = blockIdx.x * kGradRows;
   const int rows = min(kGradRows, n - r0);
   for (int t = threadIdx.x; t <= rows; t += blockDim.x) srp[t] = rp[r0 + t];
   for (int t = threadIdx.x; t < rows; t += blockDim.x) slam[t] = lambda[r0 + t];
   __syncthreads();
   const int p0 = srp[0], p1 = srp[rows];
+  if (p1 - p0 <= kGradMaxNnz) {  // uniform over the block
+    for (int t = threadIdx.x; t < rows; t += blockDim.x)
+      for (int q = srp[t]; q < srp[t + 1]; ++q) srow[q - p0] = (unsigned char)t;
+    __syncthreads();
+    for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) grad[p] = -slam[srow[p - p0]] * x[ci[p]];
+    return;
+  }
   for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
     int lo = 0, hi = rows;  // srp[lo] <= p < srp[hi]
     while (hi - lo > 1) {

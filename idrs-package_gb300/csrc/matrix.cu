@@ -317,14 +317,27 @@ __device__ __forceinline__ T epilogue(T sum, long row, T a, T cv, const T* __res
 }
 
 // Row index of an entry for the segmented reduction: stored (COO) or found
-// by binary search in the row pointers (CRS with skewed rows).
+// by binary search in the row pointers (CRS with skewed rows).  rows_of()
+// gives the rows of a lane's consecutive entries k0 .. k0+cnt-1.
 struct RowsStored {
   const int* __restrict__ ri;
   const int* __restrict__ rp;
   __device__ int find(long k) const { return ri[k]; }
-  __device__ int at(long k, int, int) const { return ri[k]; }
   __device__ bool first_open(long beg, int row_first) const { return beg > 0 && ri[beg - 1] == row_first; }
   __device__ bool last_open(long end, long nnz, int row_last) const { return end < nnz && ri[end] == row_last; }
+  template <int IT>
+  __device__ void rows_of(long k0, int cnt, int, int, int (&rows)[IT]) const {
+    if (cnt == IT && IT % 4 == 0) {
+#pragma unroll
+      for (int q = 0; q < IT / 4; ++q) {
+        const int4 r4 = __ldg(reinterpret_cast<const int4*>(ri + k0) + q);
+        rows[4 * q] = r4.x; rows[4 * q + 1] = r4.y; rows[4 * q + 2] = r4.z; rows[4 * q + 3] = r4.w;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < IT; ++j) rows[j] = (j < cnt) ? ri[k0 + j] : -1;
+    }
+  }
 };
 struct RowsSearch {
   const int* __restrict__ rp;
@@ -340,18 +353,72 @@ struct RowsSearch {
   __device__ int find(long k) const { return at(k, 0, nrows - 1); }
   __device__ bool first_open(long beg, int row_first) const { return rp[row_first] < beg; }
   __device__ bool last_open(long end, long, int row_last) const { return rp[row_last + 1] > end; }
+  template <int IT>
+  __device__ void rows_of(long k0, int cnt, int lo, int hi, int (&rows)[IT]) const {
+    int r = (cnt > 0) ? at(k0, lo, hi) : lo;
+#pragma unroll
+    for (int j = 0; j < IT; ++j) {
+      if (j < cnt) {
+        while (rp[r + 1] <= k0 + j) ++r;  // next non-empty row
+        rows[j] = r;
+      } else {
+        rows[j] = -1;
+      }
+    }
+  }
 };
+
+// ci and values of a lane's IT consecutive entries (16-byte loads when whole)
+template <int IT>
+__device__ __forceinline__ void load_cols(const int* __restrict__ ci, long k0, int cnt, int (&c)[IT]) {
+  if (cnt == IT && IT % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < IT / 4; ++q) {
+      const int4 c4 = __ldg(reinterpret_cast<const int4*>(ci + k0) + q);
+      c[4 * q] = c4.x; c[4 * q + 1] = c4.y; c[4 * q + 2] = c4.z; c[4 * q + 3] = c4.w;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < IT; ++j) c[j] = (j < cnt) ? ci[k0 + j] : 0;
+  }
+}
+template <int IT, class V>
+__device__ __forceinline__ void load_vals(const V* __restrict__ val, long k0, int cnt, V (&vv)[IT]) {
+  if constexpr (std::is_same<V, double>::value) {
+    if (cnt == IT && IT % 2 == 0) {
+#pragma unroll
+      for (int q = 0; q < IT / 2; ++q) {
+        const double2 d2 = __ldg(reinterpret_cast<const double2*>(val + k0) + q);
+        vv[2 * q] = d2.x; vv[2 * q + 1] = d2.y;
+      }
+      return;
+    }
+  } else if constexpr (std::is_same<V, float>::value) {
+    if (cnt == IT && IT % 4 == 0) {
+#pragma unroll
+      for (int q = 0; q < IT / 4; ++q) {
+        const float4 f4 = __ldg(reinterpret_cast<const float4*>(val + k0) + q);
+        vv[4 * q] = f4.x; vv[4 * q + 1] = f4.y; vv[4 * q + 2] = f4.z; vv[4 * q + 3] = f4.w;
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < IT; ++j) vv[j] = (j < cnt) ? val[k0 + j] : V(0);
+}
 
 // Segmented-reduction SpMV for COO (user_module.f90:525-585 computes the same
 // sums by a serial scatter-add) and for CRS matrices with skewed rows.  The
 // entries are row-sorted (COO: the caller's order inside a row); every warp
 // takes a fixed share of kCooWarpNnz entries, whatever the row lengths, and
-// reduces them by row with a shuffle segmented scan, 32 entries per round.
-// Rows that start and end inside the share are written at once; the first
-// row of a share, when it began in an earlier share, leaves its partial sum
-// in carry[2w]; the last row, when it continues into a later share, leaves it
-// in carry[2w+1] and this share owns it: k_seg_fix adds the later shares'
-// partials in order.
+// each lane IT consecutive ones: the lane sums its runs of equal rows
+// sequentially (one FMA per entry; GB300's FP64 pipe is narrow), rows that
+// start and end inside the lane are written at once, and one shuffle
+// segmented scan over the lanes' last runs joins rows that cross lanes.
+// A share's first row, when it began in an earlier share, leaves its partial
+// sum in carry[2w]; its last row, when it continues into a later share,
+// leaves it in carry[2w+1] and this share owns it: k_seg_fix adds the later
+// shares' partials in order.
 template <class T, class V, class Rows>
 __global__ void __launch_bounds__(256) k_seg_reduce(long nnz, long nwarps, Rows R,
                                                     const int* __restrict__ ci, const V* __restrict__ val,
@@ -360,6 +427,7 @@ __global__ void __launch_bounds__(256) k_seg_reduce(long nnz, long nwarps, Rows 
                                                     const T* __restrict__ u, T* __restrict__ carry,
                                                     const int* __restrict__ skip) {
   if (skip && *skip) return;
+  constexpr int IT = kCooWarpNnz / 32;
   const int lane = threadIdx.x & 31;
   const long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
   if (w >= nwarps) return;  // whole warp
@@ -369,36 +437,60 @@ __global__ void __launch_bounds__(256) k_seg_reduce(long nnz, long nwarps, Rows 
   const int row_last = R.find(end - 1);
   const bool first_open = R.first_open(beg, row_first);
   const bool last_open = R.last_open(end, nnz, row_last);
-  int crow = -1;  // row running across rounds and its sum so far
-  T csum = T(0);
-  for (long base = beg; base < end; base += 32) {
-    const long k = base + lane;
-    const bool valid = k < end;
-    const int r = valid ? R.at(k, row_first, row_last) : -2 - lane;  // distinct sentinels for the tail
-    T p = valid ? mulvt(val[k], x[ci[k]]) : T(0);
+  const long k0 = beg + (long)lane * IT;
+  const int cnt = (int)max(0L, min((long)IT, end - k0));
+  int rows[IT], cols[IT];
+  V vals[IT];
+  R.rows_of(k0, cnt, row_first, row_last, rows);
+  load_cols(ci, k0, cnt, cols);
+  load_vals(val, k0, cnt, vals);
+  T prod[IT];
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const T pu = shfl_up_t(p, d);
-      const int ru = __shfl_up_sync(0xffffffffu, r, d);
-      if (lane >= d && ru == r) p = p + pu;
-    }
-    if (r == crow) p = p + csum;
-    // does this entry end its row inside the share?
-    int rnext = __shfl_down_sync(0xffffffffu, r, 1);
-    if (lane == 31) rnext = (k + 1 < end) ? R.at(k + 1, row_first, row_last) : -1;
-    const bool last_of_share = valid && (k + 1 == end);
-    const bool seg_end = valid && (last_of_share || rnext != r);
-    if (seg_end) {
-      if (r == row_first && first_open) {
-        carry[2 * w] = p;                    // continuation of an earlier share's row
-      } else if (last_of_share && last_open) {
-        carry[2 * w + 1] = p;                // this share owns the row; k_seg_fix completes it
+  for (int j = 0; j < IT; ++j) prod[j] = (j < cnt) ? mulvt(vals[j], x[cols[j]]) : T(0);
+  // runs of equal rows inside the lane
+  const int head_row = (cnt > 0) ? rows[0] : -2 - lane;  // distinct sentinel for an empty lane
+  int cur = head_row;
+  T acc = T(0), head = T(0);
+  bool multi = false;
+#pragma unroll
+  for (int j = 0; j < IT; ++j) {
+    if (j < cnt) {
+      if (rows[j] != cur) {
+        if (!multi) {
+          head = acc;  // the lane's first run may continue an earlier lane's row
+          multi = true;
+        } else {
+          y[cur] = epilogue(acc, cur, a, cv, v, cx, cu, u, x);  // starts and ends in this lane
+        }
+        cur = rows[j];
+        acc = prod[j];
       } else {
-        y[r] = epilogue(p, r, a, cv, v, cx, cu, u, x);
+        acc = acc + prod[j];
       }
     }
-    crow = __shfl_sync(0xffffffffu, r, 31);
-    csum = shfl_idx_t(p, 31);  // lane 31 is valid unless the share ended
+  }
+  const int tail_row = cur;
+  // segmented inclusive scan of the lanes' last runs, keyed by their row
+  T sc = acc;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const T su = shfl_up_t(sc, d);
+    const int ku = __shfl_up_sync(0xffffffffu, tail_row, d);
+    if (lane >= d && ku == tail_row) sc = sc + su;
+  }
+  const T prev = shfl_up_t(sc, 1);
+  const int prev_row = __shfl_up_sync(0xffffffffu, tail_row, 1);
+  const int next_head = __shfl_down_sync(0xffffffffu, head_row, 1);
+  if (multi) {  // the head run ends inside this lane
+    const T tot = (lane > 0 && prev_row == head_row) ? head + prev : head;
+    if (head_row == row_first && first_open) carry[2 * w] = tot;
+    else y[head_row] = epilogue(tot, head_row, a, cv, v, cx, cu, u, x);
+  }
+  const bool last_lane = (cnt > 0) && (k0 + cnt == end);
+  if (cnt > 0 && (last_lane || next_head != tail_row)) {  // the tail run ends here
+    if (tail_row == row_first && first_open) carry[2 * w] = sc;
+    else if (last_lane && last_open) carry[2 * w + 1] = sc;
+    else y[tail_row] = epilogue(sc, tail_row, a, cv, v, cx, cu, u, x);
   }
 }
 
