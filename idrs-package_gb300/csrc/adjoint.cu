@@ -231,9 +231,10 @@ void crs_transpose(const UserMatrix& K, UserMatrix& Tm, cudaStream_t st) {
     for (int* p : {cnt, cursor, keyT, keyS, rowidx})
       if (p) cudaFreeAsync(p, st);
     cudaFree(T->row_ptr); cudaFree(T->col_ind); cudaFree(T->val);
-    cudaFree(T->empty_rows); cudaFree(T->carry);
-    T->row_ptr = T->col_ind = T->empty_rows = nullptr;
-    T->val = T->carry = nullptr;
+    cudaFree(T->med_rows); cudaFree(T->long_rows); cudaFree(T->seg_ptr); cudaFree(T->partial);
+    T->row_ptr = T->col_ind = T->med_rows = T->long_rows = T->seg_ptr = nullptr;
+    T->val = T->partial = nullptr;
+    T->n_med = T->n_long = T->n_seg = T->bin_short = 0;
     throw;
   }
 }

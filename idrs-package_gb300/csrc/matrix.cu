@@ -74,6 +74,14 @@ MatView UserMatrix::view64() const {
   for (int i = 0; i < 7; ++i) v.st[i] = st[i];
   v.vcplx = (vals == 2);
   v.group = group;
+  v.bin_short = bin_short;
+  v.n_med = n_med;
+  v.n_long = n_long;
+  v.n_seg = n_seg;
+  v.med_rows = med_rows;
+  v.long_rows = long_rows;
+  v.seg_ptr = seg_ptr;
+  v.partial = partial;
   v.ri = row_ind;
   v.n_empty = n_empty;
   v.empty_rows = empty_rows;
@@ -99,6 +107,7 @@ void user_matrix_release(UserMatrix* K) {
   if (--K->refcount > 0) return;
   cudaFree(K->row_ptr); cudaFree(K->col_ind); cudaFree(K->val); cudaFree(K->band);
   cudaFree(K->mat); cudaFree(K->diag);
+  cudaFree(K->med_rows); cudaFree(K->long_rows); cudaFree(K->seg_ptr); cudaFree(K->partial);
   cudaFree(K->row_ind); cudaFree(K->empty_rows); cudaFree(K->carry);
   delete K;
 }
@@ -117,15 +126,51 @@ static void build_seg_reduce(UserMatrix& M, const int* rp) {
   IDRS_CUDA(cudaMalloc(&M.carry, 2 * 16 * (size_t)std::max<long>(warps, 1)));
 }
 
+static int* upload_ints(const std::vector<int>& h) {
+  int* d = nullptr;
+  IDRS_CUDA(cudaMalloc((void**)&d, sizeof(int) * std::max<size_t>(h.size(), 1)));
+  if (!h.empty()) IDRS_CUDA(cudaMemcpy(d, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice));
+  return d;
+}
+
 void build_row_plan(UserMatrix& M, const int* rp) {
-  // rows far longer than the lanes given to a row would serialise a warp:
-  // such matrices use the nonzero-balanced segmented reduction instead
+  // rows far longer than the lanes given to a row would serialise a warp
   const long th = 32L * std::max(M.group, 1);
-  for (int i = 0; i < M.nrows; ++i)
-    if ((long)rp[i + 1] - rp[i] > th) {
-      build_seg_reduce(M, rp);
-      return;
+  bool skewed = false;
+  for (int i = 0; i < M.nrows && !skewed; ++i) skewed = (long)rp[i + 1] - rp[i] > th;
+  if (!skewed) return;
+  // one lane per row: short / middle / long bins; G lanes per row: rows up to 32 G / long
+  const long short_max = (M.group == 1) ? kBinShort : th;
+  const long med_max = (M.group == 1) ? kBinLong : th;
+  std::vector<std::pair<int, int>> med;  // (length, row)
+  std::vector<int> longr, segp(1, 0);
+  for (int i = 0; i < M.nrows; ++i) {
+    const long len = (long)rp[i + 1] - rp[i];
+    if (len <= short_max) continue;
+    if (len <= med_max) {
+      med.emplace_back((int)len, i);
+    } else {
+      longr.push_back(i);
+      segp.push_back(segp.back() + (int)((len + kBinLong - 1) / kBinLong));
     }
+  }
+  // longest first, rows ascending within a length: the rows of one warp have
+  // nearly equal lengths
+  std::stable_sort(med.begin(), med.end(), [](const std::pair<int, int>& a, const std::pair<int, int>& b) {
+    return a.first > b.first;
+  });
+  std::vector<int> medr(med.size());
+  for (size_t q = 0; q < med.size(); ++q) medr[q] = med[q].second;
+  M.bin_short = (int)short_max;
+  M.n_med = (int)medr.size();
+  M.n_long = (int)longr.size();
+  M.n_seg = segp.back();
+  if (M.n_med) M.med_rows = upload_ints(medr);
+  if (M.n_long) {
+    M.long_rows = upload_ints(longr);
+    M.seg_ptr = upload_ints(segp);
+    IDRS_CUDA(cudaMalloc(&M.partial, 16 * (size_t)M.n_seg));
+  }
 }
 
 void build_coo_rows(UserMatrix& M, const int* rp) {
@@ -255,7 +300,7 @@ __global__ void __launch_bounds__(256) k_crs(int nrows, const int* __restrict__ 
                                              const T* __restrict__ x, T* __restrict__ y, T a, T cv,
                                              const T* __restrict__ v, T cx, T cu,
                                              const T* __restrict__ u,
-                                             const int* __restrict__ skip) {
+                                             const int* __restrict__ skip, int max_len) {
   if (skip && *skip) return;
   constexpr int RPW = 32 / G;
   const int lane = threadIdx.x & 31;
@@ -266,10 +311,12 @@ __global__ void __launch_bounds__(256) k_crs(int nrows, const int* __restrict__ 
   for (long base = warp * RPW; base < nrows; base += nwarps * RPW) {
     const long row = base + sub;
     T sum = T(0);
-    const bool mine = row < nrows;
+    bool mine = row < nrows;
     if (mine) {
       const int beg = rp[row], end = rp[row + 1];
-      for (int k = beg + gl; k < end; k += G) sum = sum + mulvt(val[k], x[ci[k]]);
+      mine = (end - beg) <= max_len;  // longer rows: the bin kernels
+      if (mine)
+        for (int k = beg + gl; k < end; k += G) sum = sum + mulvt(val[k], x[ci[k]]);
     }
 #pragma unroll
     for (int m = G / 2; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
@@ -291,11 +338,12 @@ __global__ void __launch_bounds__(256) k_crs_row(int nrows, const int* __restric
                                                  const T* __restrict__ x, T* __restrict__ y, T a, T cv,
                                                  const T* __restrict__ v, T cx, T cu,
                                                  const T* __restrict__ u,
-                                                 const int* __restrict__ skip) {
+                                                 const int* __restrict__ skip, int max_len) {
   if (skip && *skip) return;
   for (long row = blockIdx.x * (long)blockDim.x + threadIdx.x; row < nrows;
        row += gridDim.x * (long)blockDim.x) {
     const int beg = rp[row], end = rp[row + 1];
+    if (end - beg > max_len) continue;  // written by the bin kernels
     T sum = T(0);
     for (int k = beg; k < end; ++k) sum = sum + mulvt(val[k], x[ci[k]]);
     T out = a * sum;
@@ -316,9 +364,90 @@ __device__ __forceinline__ T epilogue(T sum, long row, T a, T cv, const T* __res
   return out;
 }
 
-// Row index of an entry for the segmented reduction: stored (COO) or found
-// by binary search in the row pointers (CRS with skewed rows).  rows_of()
-// gives the rows of a lane's consecutive entries k0 .. k0+cnt-1.
+// CRS middle bin: G lanes per listed row (rows sorted by length, so the rows
+// of a warp need about the same number of steps).
+template <int G, class T, class V>
+__global__ void __launch_bounds__(256) k_crs_list(int nlist, const int* __restrict__ rows,
+                                                  const int* __restrict__ rp, const int* __restrict__ ci,
+                                                  const V* __restrict__ val, const T* __restrict__ x,
+                                                  T* __restrict__ y, T a, T cv, const T* __restrict__ v, T cx,
+                                                  T cu, const T* __restrict__ u, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  constexpr int RPW = 32 / G;
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / G;
+  const int gl = lane & (G - 1);
+  const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const long nwarps = (gridDim.x * (long)blockDim.x) >> 5;
+  for (long base = warp * RPW; base < nlist; base += nwarps * RPW) {
+    const long idx = base + sub;
+    T sum = T(0);
+    int row = 0;
+    if (idx < nlist) {
+      row = rows[idx];
+      const int beg = rp[row], end = rp[row + 1];
+#pragma unroll 4
+      for (int k = beg + gl; k < end; k += G) sum = sum + mulvt(val[k], x[ci[k]]);
+    }
+#pragma unroll
+    for (int m = G / 2; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
+    if (idx < nlist && gl == 0) y[row] = epilogue(sum, row, a, cv, v, cx, cu, u, x);
+  }
+}
+
+// CRS long bin: one warp per kBinLong-nonzero segment of a long row.
+template <class T, class V>
+__global__ void __launch_bounds__(256) k_crs_seg(int n_seg, int n_long, const int* __restrict__ long_rows,
+                                                 const int* __restrict__ seg_ptr,
+                                                 const int* __restrict__ rp, const int* __restrict__ ci,
+                                                 const V* __restrict__ val, const T* __restrict__ x,
+                                                 T* __restrict__ partial, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  const int lane = threadIdx.x & 31;
+  const long g = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  if (g >= n_seg) return;  // whole warp
+  int lo = 0, hi = n_long;  // seg_ptr[lo] <= g < seg_ptr[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (seg_ptr[mid] <= g) lo = mid; else hi = mid;
+  }
+  const int row = long_rows[lo];
+  const long beg = rp[row] + (g - seg_ptr[lo]) * (long)kBinLong;
+  const long end = min((long)rp[row + 1], beg + kBinLong);
+  T sum = T(0);
+#pragma unroll
+  for (int j = 0; j < kBinLong / 32; ++j) {
+    const long k = beg + lane + 32L * j;
+    if (k < end) sum = sum + mulvt(val[k], x[ci[k]]);
+  }
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
+  if (lane == 0) partial[g] = sum;
+}
+
+// CRS long bin: one warp per long row adds its segments in a fixed order.
+template <class T>
+__global__ void __launch_bounds__(256) k_crs_fin(int n_long, const int* __restrict__ long_rows,
+                                                 const int* __restrict__ seg_ptr,
+                                                 const T* __restrict__ partial, const T* __restrict__ x,
+                                                 T* __restrict__ y, T a, T cv, const T* __restrict__ v, T cx,
+                                                 T cu, const T* __restrict__ u, const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  const int lane = threadIdx.x & 31;
+  const long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  if (w >= n_long) return;
+  T sum = T(0);
+  for (int g = seg_ptr[w] + lane; g < seg_ptr[w + 1]; g += 32) sum = sum + partial[g];
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
+  if (lane == 0) {
+    const int row = long_rows[w];
+    y[row] = epilogue(sum, row, a, cv, v, cx, cu, u, x);
+  }
+}
+
+// Row index of an entry for the segmented reduction (stored with the COO
+// entries).  rows_of() gives the rows of a lane's entries k0 .. k0+cnt-1.
 struct RowsStored {
   const int* __restrict__ ri;
   const int* __restrict__ rp;
@@ -339,35 +468,6 @@ struct RowsStored {
     }
   }
 };
-struct RowsSearch {
-  const int* __restrict__ rp;
-  int nrows;
-  // the row holding entry k: the largest r in [lo, hi] with rp[r] <= k
-  __device__ int at(long k, int lo, int hi) const {
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (rp[mid] <= k) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-  }
-  __device__ int find(long k) const { return at(k, 0, nrows - 1); }
-  __device__ bool first_open(long beg, int row_first) const { return rp[row_first] < beg; }
-  __device__ bool last_open(long end, long, int row_last) const { return rp[row_last + 1] > end; }
-  template <int IT>
-  __device__ void rows_of(long k0, int cnt, int lo, int hi, int (&rows)[IT]) const {
-    int r = (cnt > 0) ? at(k0, lo, hi) : lo;
-#pragma unroll
-    for (int j = 0; j < IT; ++j) {
-      if (j < cnt) {
-        while (rp[r + 1] <= k0 + j) ++r;  // next non-empty row
-        rows[j] = r;
-      } else {
-        rows[j] = -1;
-      }
-    }
-  }
-};
-
 // ci and values of a lane's IT consecutive entries (16-byte loads when whole)
 template <int IT>
 __device__ __forceinline__ void load_cols(const int* __restrict__ ci, long k0, int cnt, int (&c)[IT]) {
@@ -408,7 +508,7 @@ __device__ __forceinline__ void load_vals(const V* __restrict__ val, long k0, in
 }
 
 // Segmented-reduction SpMV for COO (user_module.f90:525-585 computes the same
-// sums by a serial scatter-add) and for CRS matrices with skewed rows.  The
+// sums by a serial scatter-add).  The
 // entries are row-sorted (COO: the caller's order inside a row); every warp
 // takes a fixed share of kCooWarpNnz entries, whatever the row lengths, and
 // each lane IT consecutive ones: the lane sums its runs of equal rows
@@ -598,24 +698,37 @@ static void launch_crs(const MatView& M, const V* val, const T* x, T* y, T a, T 
     launch_seg_reduce<T, V>(M, RowsStored{M.ri, M.rp}, val, x, y, a, cv, v, cx, cu, u, skip, st);
     return;
   }
-  if (M.carry) {  // CRS with skewed rows: the same nonzero-balanced reduction
-    launch_seg_reduce<T, V>(M, RowsSearch{M.rp, M.nrows}, val, x, y, a, cv, v, cx, cu, u, skip, st);
-    return;
-  }
   long rows_per_block = kThreads / M.group;
   long need = (M.nrows + rows_per_block - 1) / rows_per_block;
   int grid = (int)std::max(1L, std::min(need, (long)num_sms() * 8));
+  const int max_len = (M.bin_short > 0) ? M.bin_short : INT_MAX;
   if (M.group == 1) {
     k_crs_row<T, V><<<stream_grid(M.nrows), kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu,
-                                                               u, skip);
+                                                               u, skip, max_len);
   } else {
     switch (M.group) {
-      case 2: k_crs<2><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
-      case 4: k_crs<4><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
-      case 8: k_crs<8><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
-      case 16: k_crs<16><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
-      default: k_crs<32><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip); break;
+      case 2: k_crs<2><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip, max_len); break;
+      case 4: k_crs<4><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip, max_len); break;
+      case 8: k_crs<8><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip, max_len); break;
+      case 16: k_crs<16><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip, max_len); break;
+      default: k_crs<32><<<grid, kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip, max_len); break;
     }
+  }
+  if (M.n_med > 0) {
+    IDRS_LAUNCH_CHECK();
+    const long mb = std::min(((long)M.n_med * kBinLanes + kThreads - 1) / kThreads, (long)num_sms() * 16);
+    k_crs_list<kBinLanes, T, V><<<(unsigned)std::max(mb, 1L), kThreads, 0, st>>>(
+        M.n_med, M.med_rows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip);
+  }
+  if (M.n_long > 0) {
+    IDRS_LAUNCH_CHECK();
+    const long sb = ((long)M.n_seg * 32 + kThreads - 1) / kThreads;
+    k_crs_seg<T, V><<<(unsigned)sb, kThreads, 0, st>>>(M.n_seg, M.n_long, M.long_rows, M.seg_ptr, M.rp, M.ci, val,
+                                                       x, (T*)M.partial, skip);
+    IDRS_LAUNCH_CHECK();
+    const long fb = ((long)M.n_long * 32 + kThreads - 1) / kThreads;
+    k_crs_fin<T><<<(unsigned)fb, kThreads, 0, st>>>(M.n_long, M.long_rows, M.seg_ptr, (const T*)M.partial, x, y,
+                                                    a, cv, v, cx, cu, u, skip);
   }
 }
 
@@ -995,6 +1108,8 @@ int build_operator(Operator* A) {
     const long warps = (K.nnz + kCooWarpNnz - 1) / kCooWarpNnz;
     IDRS_CUDA(cudaMallocAsync(&A->lb_carry, 2 * 16 * (size_t)std::max<long>(warps, 1), st));
   }
+  if (K.n_seg > 0 && !A->lb_partial) IDRS_CUDA(cudaMallocAsync(&A->lb_partial, 16 * (size_t)K.n_seg, st));
+  A->k64.partial = A->lb_partial;
   A->k64.carry = A->lb_carry;
   A->ks64 = A->k64;
   A->ks32 = MatView();
@@ -1131,6 +1246,7 @@ void operator_free(Operator* A) {
   if (A->ks_val32) cudaFreeAsync(A->ks_val32, st);
   if (A->dinv64) cudaFreeAsync(A->dinv64, st);
   if (A->dinv32) cudaFreeAsync(A->dinv32, st);
+  if (A->lb_partial) cudaFreeAsync(A->lb_partial, st);
   if (A->lb_carry) cudaFreeAsync(A->lb_carry, st);
   for (auto& p : A->shadows) cudaFreeAsync(p.second, st);
   A->shadows.clear();

@@ -37,9 +37,17 @@ struct MatView {
   int nx = 0, ny = 0, nz = 0;
   double st[7] = {0, 0, 0, 0, 0, 0, 0};  // stencil c,w,e,s,n,f,b
   int group = 8;                          // CRS lanes per row
-  // nonzero-balanced segmented reduction (COO always; CRS with rows far
-  // longer than its lanes per row): row of every entry (COO), empty rows,
-  // per-warp carries
+  // CRS with skewed rows: length bins.  Rows up to bin_short nonzeros stay
+  // with the row kernels; rows up to kBinLong in med_rows (sorted by length)
+  // get kBinLanes lanes each; longer rows are cut into kBinLong-nonzero warp
+  // segments whose partial sums are added per row in a fixed order.
+  int bin_short = 0, n_med = 0, n_long = 0, n_seg = 0;
+  const int* med_rows = nullptr;
+  const int* long_rows = nullptr;
+  const int* seg_ptr = nullptr;
+  void* partial = nullptr;
+  // COO: nonzero-balanced segmented reduction: row of every entry, empty
+  // rows, per-warp carries
   const int* ri = nullptr;
   int n_empty = 0;
   const int* empty_rows = nullptr;
@@ -47,6 +55,9 @@ struct MatView {
 };
 
 constexpr int kCooWarpNnz = 256;   // entries per warp of the segmented reduction (8 per lane)
+constexpr int kBinShort = 8;       // CRS length bins (rows with one lane per row)
+constexpr int kBinLanes = 8;       // lanes per row of the middle bin
+constexpr int kBinLong = 256;      // longer rows: warp segments of this many nonzeros
 
 // Three diagonals of a tridiagonal Jacobi matrix J((d+2) x (d+1)):
 // a[i-1] = J(i-1,i), b[i-1] = J(i,i), c[i-1] = J(i+1,i), i = 1..d+1.
@@ -78,6 +89,11 @@ struct UserMatrix {
   int nx = 0, ny = 0, nz = 0;
   double st[7] = {0, 0, 0, 0, 0, 0, 0};
   // CRS / COO load-balancing data (see MatView)
+  int bin_short = 0, n_med = 0, n_long = 0, n_seg = 0;
+  int* med_rows = nullptr;
+  int* long_rows = nullptr;
+  int* seg_ptr = nullptr;
+  void* partial = nullptr;   // 16 B per segment
   int* row_ind = nullptr;    // COO
   int n_empty = 0;
   int* empty_rows = nullptr; // COO rows without entries
@@ -96,9 +112,9 @@ struct UserMatrix {
 void user_matrix_release(UserMatrix* K);
 
 // Load balancing of CRS / COO matrices (rp: host copy of the 0-based row
-// pointers).  CRS with a row longer than 32 * group nonzeros, and every COO
-// matrix, use the nonzero-balanced segmented reduction: the list of empty rows,
-// the per-warp carries and (COO) the row index of every entry.
+// pointers).  CRS with a row longer than 32 * group nonzeros gets length bins
+// (see MatView); every COO matrix uses the nonzero-balanced segmented
+// reduction: the row index of every entry, the empty rows, the carries.
 void build_row_plan(UserMatrix& M, const int* rp_host);
 void build_coo_rows(UserMatrix& M, const int* rp_host);
 
@@ -134,8 +150,9 @@ struct Operator {
   // reduction scratch for kernels launched on this operator's stream
   RedBuf red{nullptr, nullptr};
 
-  // private carry buffer of the segmented reduction (so that operators
-  // sharing a user_matrix may run concurrently)
+  // private partial-sum / carry buffers of the load-balanced kernels (so that
+  // operators sharing a user_matrix may run concurrently)
+  void* lb_partial = nullptr;
   void* lb_carry = nullptr;
 
   // statistics of the last flexible (QMRIDR) solve with inner iterations
