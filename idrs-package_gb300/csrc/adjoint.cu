@@ -162,6 +162,7 @@ __global__ void __launch_bounds__(kGradRows) k_outer_grad(int n, const int* __re
     for (int t = threadIdx.x; t < rows; t += blockDim.x)
       for (int q = srp[t]; q < srp[t + 1]; ++q) srow[q - p0] = (unsigned char)t;
     __syncthreads();
+#pragma unroll 4
     for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) grad[p] = -slam[srow[p - p0]] * x[ci[p]];
     return;
   }

@@ -345,6 +345,7 @@ __global__ void __launch_bounds__(256) k_crs_row(int nrows, const int* __restric
     const int beg = rp[row], end = rp[row + 1];
     if (end - beg > max_len) continue;  // written by the bin kernels
     T sum = T(0);
+#pragma unroll 4
     for (int k = beg; k < end; ++k) sum = sum + mulvt(val[k], x[ci[k]]);
     T out = a * sum;
     if (cx != T(0)) out = out + cx * x[row];
