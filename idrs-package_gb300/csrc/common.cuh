@@ -189,9 +189,9 @@ inline int stream_grid(long n, int per_thread = 1) {
   long g = need < cap ? need : cap;
   return g < 1 ? 1 : (int)g;
 }
-inline int red_grid(long n) {
+inline int red_grid(long n, int blocks_per_sm = 4) {
   long need = (n + kThreads - 1) / kThreads;
-  long cap = (long)num_sms() * 4;
+  long cap = (long)num_sms() * blocks_per_sm;
   long g = need < cap ? need : cap;
   if (g > kMaxRedBlocks) g = kMaxRedBlocks;
   return g < 1 ? 1 : (int)g;

@@ -28,10 +28,23 @@ __global__ void __launch_bounds__(kThreads) k_fused(long n, Body body, Tail tail
 }
 
 // Launch with a compile-time reduction count ND (0: no reduction, no tail).
+// Reductions launch as many blocks as fit on the SMs at once (found once per
+// kernel from its register and shared-memory use), up to the partial slots.
+template <int ND, class T, class Body, class Tail>
+inline int resident_blocks() {
+  static const int per_sm = [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused<ND, T, Body, Tail>, kThreads, 0) != cudaSuccess)
+      b = 0;
+    return b > 0 ? b : 4;
+  }();
+  return per_sm;
+}
+
 template <int ND, class T, class Body, class Tail>
 inline void launch_fused(long n, const Body& body, const Tail& tail, RedBuf rb, const int* skip,
                          cudaStream_t st) {
-  int grid = (ND > 0) ? red_grid(n) : stream_grid(n);
+  int grid = (ND > 0) ? red_grid(n, resident_blocks<ND, T, Body, Tail>()) : stream_grid(n);
   k_fused<ND, T, Body, Tail><<<grid, kThreads, 0, st>>>(n, body, tail, rb, skip);
   IDRS_LAUNCH_CHECK();
 }
