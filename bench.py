@@ -43,7 +43,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--grid", type=int, default=256)
-    p.add_argument("--in-it", type=int, default=500)
+    p.add_argument("--in-it", type=int, default=250)
     p.add_argument("--in-tol", type=float, default=3e-3)
     p.add_argument("--in-s", type=int, default=4)
     p.add_argument("--no-cpu-baseline", action="store_true")
