@@ -73,6 +73,7 @@ _PROTOS = {
     "idrs_complex_ms_parameters": (_i, [_vp, _i, _vp, _vp]),
     "idrs_rmatvec": (_i, [_vp, _vp, _vp]),
     "idrs_cmatvec": (_i, [_vp, _vp, _vp]),
+    "idrs_rmatvec32": (_i, [_vp, _vp, _vp]),
     "idrs_rprecon": (_i, [_vp, _vp, _vp]),
     "idrs_cprecon": (_i, [_vp, _vp, _vp]),
     "idrs_rscaleback": (_i, [_vp, _vp, _vp, _vp]),
@@ -384,6 +385,15 @@ class Matrix:
         fn = lib().idrs_complex_ms_parameters if self.cplx else lib().idrs_real_ms_parameters
         _check(fn(self.handle, len(sigma), _p(sigma), _p(sp)))
         return sp
+
+    def matvec32(self, v):
+        """A*v evaluated in fp32 (the operator of the fp32 inner solves), widened to fp64."""
+        if self.cplx:
+            raise IDRSError(IDRS_ERR_UNSUPPORTED, "matvec32: real matrices only")
+        v = _arr(v, False, self.n)
+        w = np.empty_like(v)
+        _check(lib().idrs_rmatvec32(self.handle, _p(v), _p(w)))
+        return w
 
     def __mul__(self, v):
         """A*v: rmatvec / cmatvec (matrix_module.f90:135-167)."""

@@ -768,6 +768,30 @@ int idrs_rmatvec(idrs_matrix A, const double* v, double* w) {
   return guard([&] { REQUIRE(A && !A->cplx, "rmatvec: real handle required"); return matvec_t<double>(A, v, w); });
 }
 
+int idrs_rmatvec32(idrs_matrix A, const double* v, double* w) {
+  return guard([&] {
+    REQUIRE(A && !A->cplx && v && w, "rmatvec32: real handle, v and w required");
+    const long n = A->n();
+    cudaStream_t st = A->stream;
+    Staged sv(A, sizeof(double) * n);
+    const double* dv = (const double*)sv.in(v);
+    double* dw = (double*)sv.out(w);
+    DBuf v32(4 * n, st), w32(4 * n, st), t1(4 * n, st), t2(4 * n, st), t3(4 * n, st);
+    vec_convert<double, float>(n, dv, v32.as<float>(), nullptr, st);
+    const MatView& M = A->view(32);
+    if (A->jac.valid())
+      op_chain_recur<float>(M, A->jac, A->degree, v32.as<float>(), w32.as<float>(), t1.as<float>(),
+                            t2.as<float>(), t3.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
+    else
+      op_chain<float>(M, A->alpha_p, A->degree, v32.as<float>(), w32.as<float>(), t1.as<float>(),
+                      t2.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
+    vec_convert<float, double>(n, w32.as<float>(), dw, nullptr, st);
+    sv.finish(w, dw);
+    IDRS_CUDA(cudaStreamSynchronize(st));
+    return IDRS_OK;
+  });
+}
+
 int idrs_cmatvec(idrs_matrix A, const double* v, double* w) {
   return guard([&] { REQUIRE(A && A->cplx, "cmatvec: complex handle required"); return matvec_t<c128>(A, v, w); });
 }

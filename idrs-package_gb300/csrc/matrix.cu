@@ -292,6 +292,109 @@ __global__ void __launch_bounds__(32 * kF4Rows, 4) k_stencil7_f4(
 
 static inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
+// Two consecutive fp32 stencil steps in one pass (temporal blocking of the
+// polynomial chain):
+//   yA = S_a xin + cua u + cva v          (S_a: stencil with its scale folded in)
+//   yB = S_b yA  + cub xin + cvb vb
+// A block owns kX2Rows output rows of the full x extent (nx <= 256, four
+// x-points per thread) over zc planes.  Marching in z, it computes yA one
+// plane ahead for its rows plus one halo row on each side (recomputed, not
+// read back), keeps the last three yA planes in shared memory, and forms yB
+// from them, so yA never travels through HBM on its way into step B (it is
+// written out only when a later step reads it).  Per pair of steps it moves
+// xin, u, v, vb and the outputs once instead of twice: 5 vectors instead of 8
+// in the middle of a Chebyshev recurrence.
+struct St7 {
+  float c0, cw, ce, cs, cn, cf, cb;
+};
+constexpr int kX2Rows = 8;
+constexpr int kX2Halo = kX2Rows + 2;
+constexpr int kX2MaxNx = 256;
+
+__device__ __forceinline__ float4 st7_apply(const St7& c, float4 xm, float4 xc, float4 xp, float4 xs,
+                                            float4 xn, float left, float right) {
+  float4 r;
+  r.x = c.c0 * xc.x + c.cw * left + c.ce * xc.y + c.cs * xs.x + c.cn * xn.x + c.cf * xm.x + c.cb * xp.x;
+  r.y = c.c0 * xc.y + c.cw * xc.x + c.ce * xc.z + c.cs * xs.y + c.cn * xn.y + c.cf * xm.y + c.cb * xp.y;
+  r.z = c.c0 * xc.z + c.cw * xc.y + c.ce * xc.w + c.cs * xs.z + c.cn * xn.z + c.cf * xm.z + c.cb * xp.z;
+  r.w = c.c0 * xc.w + c.cw * xc.z + c.ce * right + c.cs * xs.w + c.cn * xn.w + c.cf * xm.w + c.cb * xp.w;
+  return r;
+}
+__device__ __forceinline__ void axpy4(float4& r, float a, float4 x) {
+  r.x += a * x.x; r.y += a * x.y; r.z += a * x.z; r.w += a * x.w;
+}
+
+__global__ void __launch_bounds__(64 * kX2Halo) k_stencil7_f4x2(
+    int nx, int ny, int nz, int zc, St7 ca, float cua, float cva, St7 cb, float cub, float cvb,
+    const float* __restrict__ xin, const float* __restrict__ u, const float* __restrict__ v,
+    const float* __restrict__ vb, float* __restrict__ ya, float* __restrict__ yb,
+    const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  __shared__ __align__(16) float sA[3][kX2Halo][kX2MaxNx];
+  const int tx = threadIdx.x;
+  const int lane = tx & 31;
+  const int ty = threadIdx.y;
+  const int i0 = tx * 4;
+  const int j = blockIdx.x * kX2Rows - 1 + ty;  // row of this thread (one halo row each side)
+  const int z0 = blockIdx.y * zc;
+  const int z1 = min(nz, z0 + zc);
+  const bool xok = i0 < nx;
+  const bool act = xok && j >= 0 && j < ny;
+  const bool interior = act && ty >= 1 && ty <= kX2Rows;
+  const long plane = (long)nx * ny;
+  const long roff = act ? (long)j * nx + i0 : 0;
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto ldx = [&](int z) -> float4 { return (act && z >= 0 && z < nz) ? ld4(xin + z * plane + roff) : zero; };
+  // step A at plane zp from xm = xin(zp-1), xc = xin(zp), xp = xin(zp+1) into slot zp mod 3
+  auto stepA = [&](int zp, float4 xm, float4 xc, float4 xp) {
+    float4 r = zero;
+    if (zp >= 0 && zp < nz) {  // uniform over the block
+      const long o = zp * plane + roff;
+      const float4 xs = (act && j > 0) ? ld4(xin + o - nx) : zero;
+      const float4 xn = (act && j + 1 < ny) ? ld4(xin + o + nx) : zero;
+      float left = __shfl_up_sync(0xffffffffu, xc.w, 1);
+      float right = __shfl_down_sync(0xffffffffu, xc.x, 1);
+      if (lane == 0) left = (act && i0 > 0) ? __ldg(xin + o - 1) : 0.f;
+      if (lane == 31) right = (act && i0 + 4 < nx) ? __ldg(xin + o + 4) : 0.f;
+      if (act) {
+        r = st7_apply(ca, xm, xc, xp, xs, xn, left, right);
+        if (u) axpy4(r, cua, ld4(u + o));
+        if (v) axpy4(r, cva, ld4(v + o));
+        if (ya && interior && zp >= z0 && zp < z1) *reinterpret_cast<float4*>(ya + o) = r;
+      }
+    }
+    if (xok) *reinterpret_cast<float4*>(&sA[(zp + 3) % 3][ty][i0]) = r;
+  };
+  float4 m = ldx(z0 - 2), c = ldx(z0 - 1), p = ldx(z0);
+  stepA(z0 - 1, m, c, p);
+  m = c; c = p; p = ldx(z0 + 1);
+  stepA(z0, m, c, p);
+  for (int z = z0; z < z1; ++z) {
+    const float4 xz = c;  // xin(z)
+    m = c; c = p; p = ldx(z + 2);
+    stepA(z + 1, m, c, p);
+    __syncthreads();
+    if (interior) {
+      const int s0 = (z + 2) % 3, s1 = z % 3, s2 = (z + 1) % 3;  // planes z-1, z, z+1
+      const float4 bm = *reinterpret_cast<const float4*>(&sA[s0][ty][i0]);
+      const float4 bc = *reinterpret_cast<const float4*>(&sA[s1][ty][i0]);
+      const float4 bp = *reinterpret_cast<const float4*>(&sA[s2][ty][i0]);
+      const float4 bs = *reinterpret_cast<const float4*>(&sA[s1][ty - 1][i0]);
+      const float4 bn = *reinterpret_cast<const float4*>(&sA[s1][ty + 1][i0]);
+      const float bl = (i0 > 0) ? sA[s1][ty][i0 - 1] : 0.f;
+      const float br = (i0 + 4 < nx) ? sA[s1][ty][i0 + 4] : 0.f;
+      float4 r = st7_apply(cb, bm, bc, bp, bs, bn, bl, br);
+      axpy4(r, cub, xz);
+      const long o = z * plane + roff;
+      if (vb) axpy4(r, cvb, ld4(vb + o));
+      *reinterpret_cast<float4*>(yb + o) = r;
+    }
+    __syncthreads();
+  }
+}
+
+
+
 // CRS, G lanes per row (G | 32).  Warp-uniform loop so the shuffles are
 // always executed by the full warp.
 template <int G, class T, class V>
@@ -843,6 +946,63 @@ void op_chain(const MatView& Ks, const std::vector<c128>& alpha, int degree, con
   spmv<T>(Ks, cur, w, fa, fcv, fv, skip, st);
 }
 
+// One step of a polynomial chain: out = Epi(Ks in).
+template <class T>
+struct ChainStep {
+  const T* in;
+  T* out;
+  Epi<T> e;
+};
+
+// Can two fp32 steps share one k_stencil7_f4x2 pass?
+static bool f4x2_ok(const MatView& M, const ChainStep<float>& A, const ChainStep<float>& B) {
+  if (M.format != FMT_STENCIL7 || M.nx % 4 != 0 || M.nx > kX2MaxNx) return false;
+  if (B.in != A.out || (B.e.u && B.e.u != A.in)) return false;
+  for (const void* q : {(const void*)A.in, (const void*)A.out, (const void*)A.e.u, (const void*)A.e.v,
+                        (const void*)B.out, (const void*)B.e.v})
+    if (!aligned16(q)) return false;
+  return true;
+}
+
+static St7 st7_of(const MatView& M, float a, float cx) {
+  const double ar = (double)a;
+  return St7{float(ar * M.st[0] + (double)cx), float(ar * M.st[1]), float(ar * M.st[2]), float(ar * M.st[3]),
+             float(ar * M.st[4]), float(ar * M.st[5]), float(ar * M.st[6])};
+}
+
+template <class T>
+static void run_chain(const MatView& Ks, const std::vector<ChainStep<T>>& steps, const int* skip, cudaStream_t st) {
+  size_t k = 0;
+  while (k < steps.size()) {
+    if constexpr (std::is_same<T, float>::value) {
+      if (k + 1 < steps.size() && f4x2_ok(Ks, steps[k], steps[k + 1])) {
+        const ChainStep<float>& A = steps[k];
+        const ChainStep<float>& B = steps[k + 1];
+        // A's output goes to HBM only if a later step reads it before it is overwritten
+        bool need = false;
+        for (size_t q = k + 2; q < steps.size(); ++q) {
+          if (steps[q].in == A.out || steps[q].e.u == A.out) { need = true; break; }
+          if (steps[q].out == A.out) break;
+        }
+        const int gy = (Ks.ny + kX2Rows - 1) / kX2Rows;
+        const long target = 3L * num_sms();
+        int zc = (int)std::max(4L, std::min((long)Ks.nz, ((long)Ks.nz * gy + target - 1) / target));
+        dim3 blk(32 * ((Ks.nx + 127) / 128), kX2Halo, 1);
+        dim3 grid(gy, (Ks.nz + zc - 1) / zc, 1);
+        k_stencil7_f4x2<<<grid, blk, 0, st>>>(
+            Ks.nx, Ks.ny, Ks.nz, zc, st7_of(Ks, A.e.a, A.e.cx), A.e.u ? A.e.cu : 0.f, A.e.v ? A.e.cv : 0.f,
+            st7_of(Ks, B.e.a, B.e.cx), B.e.u ? B.e.cu : 0.f, B.e.v ? B.e.cv : 0.f, A.in, A.e.u, A.e.v, B.e.v,
+            need ? A.out : nullptr, B.out, skip);
+        IDRS_LAUNCH_CHECK();
+        k += 2;
+        continue;
+      }
+    }
+    spmv_ex<T>(Ks, steps[k].in, steps[k].out, steps[k].e, skip, st);
+    ++k;
+  }
+}
+
 // A p(A) v with p evaluated through the three-term recurrence of its
 // tridiagonal Jacobi matrix (Chebyshev / Neumann, matrix_module.f90:851-941)
 // instead of monomial Horner.  With r_i(t) = 1 - t p_i(t) and column i of J
@@ -852,6 +1012,7 @@ void op_chain(const MatView& Ks, const std::vector<c128>& alpha, int degree, con
 // and p(A) v = y_{d+1}.  The iterates stay of the size of A^-1 v, so the fp32
 // form keeps its accuracy where the monomial coefficients (|alpha| ~ 10^3-10^4
 // with alternating signs for a degree-8 Chebyshev polynomial) cancel.
+// fp32 stencil chains run two steps per pass (k_stencil7_f4x2).
 template <class T>
 void op_chain_recur(const MatView& Ks, const JacobiCols& J, int degree, const T* v, T* w, T* t1,
                     T* t2, T* t3, const int* skip, cudaStream_t st, T fa, T fcv, const T* fv) {
@@ -860,44 +1021,46 @@ void op_chain_recur(const MatView& Ks, const JacobiCols& J, int degree, const T*
     return;
   }
   auto C = [](c128 z) { return narrow<T>(z); };
-  // y_1 = -v/c_1 ; y_2 = (A y_1 - b_2 y_1 - v)/c_2 read from v alone
+  std::vector<ChainStep<T>> steps;
   T* buf[3] = {t1, t2, t3};
   const T* ym2 = nullptr;  // y_{i-2}
   const T* ym1 = nullptr;  // y_{i-1}
   {
+    // y_1 = -v/c_1 ; y_2 = (A y_1 - b_2 y_1 - v)/c_2 read from v alone
     c128 c1 = J.c[0], b2 = J.b[1], c2 = J.c[1];
-    c128 s1 = c128(-1.0) / c1;  // y_1 = s1 v
-    Epi<T> e;
-    e.a = C(s1 / c2);            // (A y_1)/c2
-    e.cx = C((c128(0.0) - b2 * s1 - c128(1.0)) / c2);  // (-b2 y_1 - v)/c2, y_1 and v share v
-    spmv_ex<T>(Ks, v, buf[0], e, skip, st);
-    ym2 = nullptr;
+    c128 s1 = c128(-1.0) / c1;  // y_1 = s1 v, kept implicit
+    ChainStep<T> s0{v, buf[0], Epi<T>()};
+    s0.e.a = C(s1 / c2);                                   // (A y_1)/c2
+    s0.e.cx = C((c128(0.0) - b2 * s1 - c128(1.0)) / c2);  // (-b2 y_1 - v)/c2, y_1 and v share v
+    steps.push_back(s0);
     ym1 = buf[0];
-    // y_1 itself is s1*v: keep it implicit, the next step needs y_{i-2} = y_1
   }
   int nb = 1;
   for (int i = 3; i <= degree + 1; ++i) {
     c128 ai = J.a[i - 1], bi = J.b[i - 1], ci = J.c[i - 1];
-    Epi<T> e;
-    e.a = C(c128(1.0) / ci);
-    e.cx = C(c128(0.0) - bi / ci);
-    e.cv = C(c128(-1.0) / ci);
-    e.v = v;
+    ChainStep<T> sk{ym1, buf[nb % 3], Epi<T>()};
+    sk.e.a = C(c128(1.0) / ci);
+    sk.e.cx = C(c128(0.0) - bi / ci);
+    sk.e.cv = C(c128(-1.0) / ci);
+    sk.e.v = v;
     if (i == 3) {  // y_{i-2} = y_1 = s1 v: fold into the v term
       c128 s1 = c128(-1.0) / J.c[0];
-      e.cv = C((c128(-1.0) - ai * s1) / ci);
+      sk.e.cv = C((c128(-1.0) - ai * s1) / ci);
     } else if (ai != c128(0.0)) {  // Neumann: a_i = 0, no y_{i-2} read
-      e.cu = C(c128(0.0) - ai / ci);
-      e.u = ym2;
+      sk.e.cu = C(c128(0.0) - ai / ci);
+      sk.e.u = ym2;
     }
-    T* out = buf[nb % 3];
-    spmv_ex<T>(Ks, ym1, out, e, skip, st);
+    steps.push_back(sk);
     ym2 = ym1;
-    ym1 = out;
+    ym1 = sk.out;
     ++nb;
   }
-  (void)ym2;
-  spmv<T>(Ks, ym1, w, fa, fcv, fv, skip, st);
+  ChainStep<T> fin{ym1, w, Epi<T>()};
+  fin.e.a = fa;
+  fin.e.cv = fcv;
+  fin.e.v = fv;
+  steps.push_back(fin);
+  run_chain<T>(Ks, steps, skip, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -126,6 +126,11 @@ int idrs_complex_ms_parameters(idrs_matrix A, int n_sigma, const double *sigma,
 /* operator(*): rmatvec / cmatvec, matrix_module.f90:135-167 */
 int idrs_rmatvec(idrs_matrix A, const double *v, double *w);
 int idrs_cmatvec(idrs_matrix A, const double *v, double *w);
+/* A*v evaluated in fp32, the operator of the fp32 inner solves (new, no
+ * reference counterpart): v is rounded to fp32, the polynomial is applied by
+ * its stable recurrence when A holds a Chebyshev/Neumann preconditioner, and
+ * w is returned widened to fp64. */
+int idrs_rmatvec32(idrs_matrix A, const double *v, double *w);
 /* operator(/): rprecon / cprecon, matrix_module.f90:306-400  (w = v/A) */
 int idrs_rprecon(idrs_matrix A, const double *v, double *w);
 int idrs_cprecon(idrs_matrix A, const double *v, double *w);

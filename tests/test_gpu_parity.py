@@ -298,3 +298,23 @@ def test_mixed_precision_with_chebyshev(gpu, P):
     assert r.flag == 0 and r.iterations <= 10
     assert r.relres_original <= 1.01e-8
     np.testing.assert_allclose(r.x, 1.0, atol=1e-6)
+
+
+@pytest.mark.parametrize("dims", [(12, 12, 12), (256, 3, 5), (20, 9, 33), (30, 30, 30), (260, 4, 4), (4, 1, 7)])
+@pytest.mark.parametrize("poly", ["chebyshev", "neumann"])
+def test_fp32_chain_matches_fp64(gpu, P, dims, poly):
+    """The fp32 operator of the inner solves (polynomial by its recurrence,
+    two stencil steps per pass where nx % 4 == 0 and nx <= 256, single steps
+    otherwise) against the fp64 operator: agreement to fp32 accuracy."""
+    nx, ny, nz = dims
+    coef = P.cdr_coefficients(max(nx, ny, nz))
+    K = gpu.stencil7_format(nx, ny, nz, coef)
+    A = gpu.Matrix(K, P=gpu.real_precon(1, K))
+    if poly == "chebyshev":
+        A.preconditioner(2, 8, foci=[0.05, 1.9])
+    else:
+        A.preconditioner(1, 6, center=1.0)
+    v = np.random.default_rng(nx + ny + nz).standard_normal(nx * ny * nz)
+    w64 = A * v
+    w32 = A.matvec32(v)
+    assert _rel(w32, w64) <= 2e-5
