@@ -776,12 +776,12 @@ int idrs_rmatvec32(idrs_matrix A, const double* v, double* w) {
     Staged sv(A, sizeof(double) * n);
     const double* dv = (const double*)sv.in(v);
     double* dw = (double*)sv.out(w);
-    DBuf v32(4 * n, st), w32(4 * n, st), t1(4 * n, st), t2(4 * n, st), t3(4 * n, st);
+    DBuf v32(4 * n, st), w32(4 * n, st), t1(4 * n, st), t2(4 * n, st), t3(4 * n, st), t4(4 * n, st);
     vec_convert<double, float>(n, dv, v32.as<float>(), nullptr, st);
     const MatView& M = A->view(32);
     if (A->jac.valid())
       op_chain_recur<float>(M, A->jac, A->degree, v32.as<float>(), w32.as<float>(), t1.as<float>(),
-                            t2.as<float>(), t3.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
+                            t2.as<float>(), t3.as<float>(), t4.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
     else
       op_chain<float>(M, A->alpha_p, A->degree, v32.as<float>(), w32.as<float>(), t1.as<float>(),
                       t2.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
@@ -1101,7 +1101,7 @@ int idrs_time_matvec(idrs_matrix A, int prec, int warmup, int reps, double* ms_p
     long n = A->n();
     cudaStream_t st = A->stream;
     size_t es = (A->cplx ? 2 : 1) * (prec == 64 ? 8 : 4);
-    DBuf v(es * n, st), w(es * n, st), t1(es * n, st), t2(es * n, st), t3(es * n, st);
+    DBuf v(es * n, st), w(es * n, st), t1(es * n, st), t2(es * n, st), t3(es * n, st), t4(es * n, st);
     IDRS_CUDA(cudaMemsetAsync(v.p, 0, es * n, st));
     const MatView& M = A->view(prec);
     const bool recur = (prec == 32 && A->jac.valid());
@@ -1109,13 +1109,13 @@ int idrs_time_matvec(idrs_matrix A, int prec, int warmup, int reps, double* ms_p
       if (prec == 64 && !A->cplx)
         op_chain<double>(M, A->alpha_p, A->degree, v.as<double>(), w.as<double>(), t1.as<double>(), t2.as<double>(), nullptr, st, 1.0, 0.0, nullptr);
       else if (prec == 32 && !A->cplx && recur)
-        op_chain_recur<float>(M, A->jac, A->degree, v.as<float>(), w.as<float>(), t1.as<float>(), t2.as<float>(), t3.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
+        op_chain_recur<float>(M, A->jac, A->degree, v.as<float>(), w.as<float>(), t1.as<float>(), t2.as<float>(), t3.as<float>(), t4.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
       else if (prec == 32 && !A->cplx)
         op_chain<float>(M, A->alpha_p, A->degree, v.as<float>(), w.as<float>(), t1.as<float>(), t2.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
       else if (prec == 64)
         op_chain<c128>(M, A->alpha_p, A->degree, v.as<c128>(), w.as<c128>(), t1.as<c128>(), t2.as<c128>(), nullptr, st, c128(1.0), c128(0.0), nullptr);
       else if (recur)
-        op_chain_recur<c64>(M, A->jac, A->degree, v.as<c64>(), w.as<c64>(), t1.as<c64>(), t2.as<c64>(), t3.as<c64>(), nullptr, st, c64(1.0f), c64(0.0f), nullptr);
+        op_chain_recur<c64>(M, A->jac, A->degree, v.as<c64>(), w.as<c64>(), t1.as<c64>(), t2.as<c64>(), t3.as<c64>(), t4.as<c64>(), nullptr, st, c64(1.0f), c64(0.0f), nullptr);
       else
         op_chain<c64>(M, A->alpha_p, A->degree, v.as<c64>(), w.as<c64>(), t1.as<c64>(), t2.as<c64>(), nullptr, st, c64(1.0f), c64(0.0f), nullptr);
     };

@@ -473,7 +473,7 @@ class IdrsGpu {
   cudaStream_t st;
   RedBuf rb;
   T *G = nullptr, *U = nullptr, *r = nullptr, *v = nullptr, *t = nullptr, *t1 = nullptr, *t2 = nullptr,
-    *t3 = nullptr, *PT = nullptr;
+    *t3 = nullptr, *t4 = nullptr, *PT = nullptr;
   IdrsState<W>* d_st = nullptr;
   int* h_stop = nullptr;  // pinned, 2 slots
   cudaEvent_t ev[2];

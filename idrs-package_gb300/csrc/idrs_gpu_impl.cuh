@@ -30,7 +30,10 @@ IdrsGpu<T>::IdrsGpu(Operator& A_, int prec_, int s_, int method_)
   t = dalloc<T>(n, st);
   t1 = dalloc<T>(n, st);
   t2 = dalloc<T>(n, st);
-  if (prec == 32) t3 = dalloc<T>(n, st);
+  if (prec == 32) {
+    t3 = dalloc<T>(n, st);
+    t4 = dalloc<T>(n, st);
+  }
   PT = dalloc<T>((long)rows * n, st);
   IDRS_CUDA(cudaMallocAsync((void**)&d_st, sizeof(IdrsState<W>), st));
   IDRS_CUDA(cudaMemsetAsync(d_st, 0, sizeof(IdrsState<W>), st));
@@ -43,7 +46,8 @@ IdrsGpu<T>::IdrsGpu(Operator& A_, int prec_, int s_, int method_)
 
 template <class T>
 IdrsGpu<T>::~IdrsGpu() {
-  for (void* p : {(void*)G, (void*)U, (void*)r, (void*)v, (void*)t, (void*)t1, (void*)t2, (void*)t3, (void*)PT, (void*)d_st})
+  for (void* p : {(void*)G, (void*)U, (void*)r, (void*)v, (void*)t, (void*)t1, (void*)t2, (void*)t3, (void*)t4,
+                  (void*)PT, (void*)d_st})
     if (p) cudaFreeAsync(p, st);
   if (h_stop) cudaFreeHost(h_stop);
   cudaEventDestroy(ev[0]);
@@ -55,7 +59,7 @@ void IdrsGpu<T>::matvec(const T* in, T* out, const int* skip, T fa, T fcv, const
   // fp32 evaluates the polynomial by its stable three-term recurrence; fp64
   // keeps the monomial Horner form of rpolpre (matrix_module.f90:266-284)
   if (prec == 32 && A.jac.valid())
-    op_chain_recur<T>(A.view(prec), A.jac, A.degree, in, out, t1, t2, t3, skip, st, fa, fcv, fv);
+    op_chain_recur<T>(A.view(prec), A.jac, A.degree, in, out, t1, t2, t3, t4, skip, st, fa, fcv, fv);
   else
     op_chain<T>(A.view(prec), A.alpha_p, A.degree, in, out, t1, t2, skip, st, fa, fcv, fv);
 }

@@ -958,6 +958,10 @@ struct ChainStep {
 static bool f4x2_ok(const MatView& M, const ChainStep<float>& A, const ChainStep<float>& B) {
   if (M.format != FMT_STENCIL7 || M.nx % 4 != 0 || M.nx > kX2MaxNx) return false;
   if (B.in != A.out || (B.e.u && B.e.u != A.in)) return false;
+  // B writes while A still reads: its output must not be one of A's inputs
+  if (B.out == A.in || (A.e.u && B.out == A.e.u) || (A.e.v && B.out == A.e.v) ||
+      (B.e.v && (B.out == B.e.v || A.out == B.e.v)))
+    return false;
   for (const void* q : {(const void*)A.in, (const void*)A.out, (const void*)A.e.u, (const void*)A.e.v,
                         (const void*)B.out, (const void*)B.e.v})
     if (!aligned16(q)) return false;
@@ -1015,14 +1019,15 @@ static void run_chain(const MatView& Ks, const std::vector<ChainStep<T>>& steps,
 // fp32 stencil chains run two steps per pass (k_stencil7_f4x2).
 template <class T>
 void op_chain_recur(const MatView& Ks, const JacobiCols& J, int degree, const T* v, T* w, T* t1,
-                    T* t2, T* t3, const int* skip, cudaStream_t st, T fa, T fcv, const T* fv) {
+                    T* t2, T* t3, T* t4, const int* skip, cudaStream_t st, T fa, T fcv, const T* fv) {
   if (degree == 0) {
     spmv<T>(Ks, v, w, fa, fcv, fv, skip, st);
     return;
   }
   auto C = [](c128 z) { return narrow<T>(z); };
   std::vector<ChainStep<T>> steps;
-  T* buf[3] = {t1, t2, t3};
+  T* buf[4] = {t1, t2, t3, t4};
+  const int nbuf = t4 ? 4 : 3;
   const T* ym2 = nullptr;  // y_{i-2}
   const T* ym1 = nullptr;  // y_{i-1}
   {
@@ -1038,7 +1043,7 @@ void op_chain_recur(const MatView& Ks, const JacobiCols& J, int degree, const T*
   int nb = 1;
   for (int i = 3; i <= degree + 1; ++i) {
     c128 ai = J.a[i - 1], bi = J.b[i - 1], ci = J.c[i - 1];
-    ChainStep<T> sk{ym1, buf[nb % 3], Epi<T>()};
+    ChainStep<T> sk{ym1, buf[nb % nbuf], Epi<T>()};
     sk.e.a = C(c128(1.0) / ci);
     sk.e.cx = C(c128(0.0) - bi / ci);
     sk.e.cv = C(c128(-1.0) / ci);
@@ -1427,7 +1432,7 @@ void operator_free(Operator* A) {
 #define IDRS_INST(T)                                                                              \
   template void spmv<T>(const MatView&, const T*, T*, T, T, const T*, const int*, cudaStream_t);    \
   template void spmv_ex<T>(const MatView&, const T*, T*, const Epi<T>&, const int*, cudaStream_t); \
-  template void op_chain_recur<T>(const MatView&, const JacobiCols&, int, const T*, T*, T*, T*, T*, \
+  template void op_chain_recur<T>(const MatView&, const JacobiCols&, int, const T*, T*, T*, T*, T*, T*, \
                                   const int*, cudaStream_t, T, T, const T*);                       \
   template void op_chain<T>(const MatView&, const std::vector<c128>&, int, const T*, T*, T*, T*,   \
                             const int*, cudaStream_t, T, T, const T*);                            \

@@ -177,10 +177,13 @@ template <class T>
 void spmv_ex(const MatView& M, const T* x, T* y, const Epi<T>& e, const int* skip, cudaStream_t st);
 
 // w = fa * Ks p(Ks) v + fcv * fv with p from its Jacobi three-term recurrence
-// (numerically stable; used by the fp32 inner solves).  t1..t3: scratch.
+// (numerically stable; used by the fp32 inner solves).  t1..t3: scratch; t4:
+// optional fourth scratch vector that lets every pair of fp32 stencil steps
+// run as one pass (with three, only pairs whose outputs overwrite none of
+// their inputs are fused).
 template <class T>
 void op_chain_recur(const MatView& Ks, const JacobiCols& J, int degree, const T* v, T* w, T* t1,
-                    T* t2, T* t3, const int* skip, cudaStream_t st, T fa = T(1), T fcv = T(0),
+                    T* t2, T* t3, T* t4, const int* skip, cudaStream_t st, T fa = T(1), T fcv = T(0),
                     const T* fv = nullptr);
 
 // w = Ks p(Ks) v, then the final product gets the epilogue

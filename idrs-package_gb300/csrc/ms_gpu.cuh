@@ -400,7 +400,7 @@ class MsIdrsGpu {
   cudaStream_t st;
   RedBuf rb;
   T *pool = nullptr, *Wb = nullptr, *v = nullptr, *t = nullptr, *tm = nullptr, *t1 = nullptr,
-    *t2 = nullptr, *t3 = nullptr, *PT = nullptr;
+    *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *PT = nullptr;
   MsIdrsState<W>* d_st = nullptr;
   int* h_stop = nullptr;
   cudaEvent_t ev[2];

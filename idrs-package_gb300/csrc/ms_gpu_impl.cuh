@@ -27,7 +27,10 @@ MsIdrsGpu<T>::MsIdrsGpu(Operator& A_, int prec_, int s_, int ns_, int method_)
   tm = dalloc<T>(n, st);
   t1 = dalloc<T>(n, st);
   t2 = dalloc<T>(n, st);
-  if (prec == 32) t3 = dalloc<T>(n, st);
+  if (prec == 32) {
+    t3 = dalloc<T>(n, st);
+    t4 = dalloc<T>(n, st);
+  }
   PT = dalloc<T>((long)rows * n, st);
   IDRS_CUDA(cudaMallocAsync((void**)&d_st, sizeof(MsIdrsState<W>), st));
   IDRS_CUDA(cudaMemsetAsync(d_st, 0, sizeof(MsIdrsState<W>), st));
@@ -41,7 +44,7 @@ MsIdrsGpu<T>::MsIdrsGpu(Operator& A_, int prec_, int s_, int ns_, int method_)
 template <class T>
 MsIdrsGpu<T>::~MsIdrsGpu() {
   for (void* p : {(void*)pool, (void*)Wb, (void*)v, (void*)t, (void*)tm, (void*)t1, (void*)t2, (void*)t3,
-                  (void*)PT, (void*)d_st})
+                  (void*)t4, (void*)PT, (void*)d_st})
     if (p) cudaFreeAsync(p, st);
   if (h_stop) cudaFreeHost(h_stop);
   cudaEventDestroy(ev[0]);
@@ -51,7 +54,7 @@ MsIdrsGpu<T>::~MsIdrsGpu() {
 template <class T>
 void MsIdrsGpu<T>::matvec(const T* in, T* out, const int* skip, T fa, T fcv, const T* fv) {
   if (prec == 32 && A.jac.valid())
-    op_chain_recur<T>(A.view(prec), A.jac, A.degree, in, out, t1, t2, t3, skip, st, fa, fcv, fv);
+    op_chain_recur<T>(A.view(prec), A.jac, A.degree, in, out, t1, t2, t3, t4, skip, st, fa, fcv, fv);
   else
     op_chain<T>(A.view(prec), A.alpha_p, A.degree, in, out, t1, t2, skip, st, fa, fcv, fv);
 }
