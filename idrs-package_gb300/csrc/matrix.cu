@@ -324,13 +324,15 @@ __device__ __forceinline__ void axpy4(float4& r, float a, float4 x) {
   r.x += a * x.x; r.y += a * x.y; r.z += a * x.z; r.w += a * x.w;
 }
 
-__global__ void __launch_bounds__(64 * kX2Halo) k_stencil7_f4x2(
+__global__ void __launch_bounds__(64 * kX2Halo, 2) k_stencil7_f4x2(
     int nx, int ny, int nz, int zc, St7 ca, float cua, float cva, St7 cb, float cub, float cvb,
     const float* __restrict__ xin, const float* __restrict__ u, const float* __restrict__ v,
     const float* __restrict__ vb, float* __restrict__ ya, float* __restrict__ yb,
     const int* __restrict__ skip) {
   if (skip && *skip) return;
-  __shared__ __align__(16) float sA[3][kX2Halo][kX2MaxNx];
+  // ring of four yA planes: step A writes plane z+2 while step B reads z-1..z+1,
+  // so one barrier per plane suffices
+  __shared__ __align__(16) float sA[4][kX2Halo][kX2MaxNx];
   const int tx = threadIdx.x;
   const int lane = tx & 31;
   const int ty = threadIdx.y;
@@ -344,9 +346,11 @@ __global__ void __launch_bounds__(64 * kX2Halo) k_stencil7_f4x2(
   const long plane = (long)nx * ny;
   const long roff = act ? (long)j * nx + i0 : 0;
   const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-  auto ldx = [&](int z) -> float4 { return (act && z >= 0 && z < nz) ? ld4(xin + z * plane + roff) : zero; };
-  // step A at plane zp from xm = xin(zp-1), xc = xin(zp), xp = xin(zp+1) into slot zp mod 3
-  auto stepA = [&](int zp, float4 xm, float4 xc, float4 xp) {
+  auto ld = [&](const float* a, int z) -> float4 {
+    return (a && act && z >= 0 && z < nz) ? ld4(a + z * plane + roff) : zero;
+  };
+  // step A at plane zp from xm, xc, xp = xin(zp-1 .. zp+1) and uc, vc = u(zp), v(zp)
+  auto stepA = [&](int zp, float4 xm, float4 xc, float4 xp, float4 uc, float4 vc) {
     float4 r = zero;
     if (zp >= 0 && zp < nz) {  // uniform over the block
       const long o = zp * plane + roff;
@@ -358,38 +362,41 @@ __global__ void __launch_bounds__(64 * kX2Halo) k_stencil7_f4x2(
       if (lane == 31) right = (act && i0 + 4 < nx) ? __ldg(xin + o + 4) : 0.f;
       if (act) {
         r = st7_apply(ca, xm, xc, xp, xs, xn, left, right);
-        if (u) axpy4(r, cua, ld4(u + o));
-        if (v) axpy4(r, cva, ld4(v + o));
+        axpy4(r, cua, uc);
+        axpy4(r, cva, vc);
         if (ya && interior && zp >= z0 && zp < z1) *reinterpret_cast<float4*>(ya + o) = r;
       }
     }
-    if (xok) *reinterpret_cast<float4*>(&sA[(zp + 3) % 3][ty][i0]) = r;
+    if (xok) *reinterpret_cast<float4*>(&sA[(zp + 4) & 3][ty][i0]) = r;
   };
-  float4 m = ldx(z0 - 2), c = ldx(z0 - 1), p = ldx(z0);
-  stepA(z0 - 1, m, c, p);
-  m = c; c = p; p = ldx(z0 + 1);
-  stepA(z0, m, c, p);
+  float4 m = ld(xin, z0 - 2), c = ld(xin, z0 - 1), p = ld(xin, z0);
+  stepA(z0 - 1, m, c, p, ld(u, z0 - 1), ld(v, z0 - 1));
+  m = c; c = p; p = ld(xin, z0 + 1);
+  stepA(z0, m, c, p, ld(u, z0), ld(v, z0));
+  // software pipeline: the next input plane is requested a step ahead
+  float4 pn = ld(xin, z0 + 2);
   for (int z = z0; z < z1; ++z) {
     const float4 xz = c;  // xin(z)
-    m = c; c = p; p = ldx(z + 2);
-    stepA(z + 1, m, c, p);
+    m = c; c = p; p = pn;
+    pn = ld(xin, z + 3);
+    stepA(z + 1, m, c, p, ld(u, z + 1), ld(v, z + 1));
     __syncthreads();
     if (interior) {
-      const int s0 = (z + 2) % 3, s1 = z % 3, s2 = (z + 1) % 3;  // planes z-1, z, z+1
+      const int s0 = (z + 3) & 3, s1 = z & 3, s2 = (z + 1) & 3;  // planes z-1, z, z+1
       const float4 bm = *reinterpret_cast<const float4*>(&sA[s0][ty][i0]);
       const float4 bc = *reinterpret_cast<const float4*>(&sA[s1][ty][i0]);
       const float4 bp = *reinterpret_cast<const float4*>(&sA[s2][ty][i0]);
       const float4 bs = *reinterpret_cast<const float4*>(&sA[s1][ty - 1][i0]);
       const float4 bn = *reinterpret_cast<const float4*>(&sA[s1][ty + 1][i0]);
-      const float bl = (i0 > 0) ? sA[s1][ty][i0 - 1] : 0.f;
-      const float br = (i0 + 4 < nx) ? sA[s1][ty][i0 + 4] : 0.f;
+      float bl = __shfl_up_sync(0xffffffffu, bc.w, 1);
+      float br = __shfl_down_sync(0xffffffffu, bc.x, 1);
+      if (lane == 0) bl = (i0 > 0) ? sA[s1][ty][i0 - 1] : 0.f;
+      if (lane == 31) br = (i0 + 4 < nx) ? sA[s1][ty][i0 + 4] : 0.f;
       float4 r = st7_apply(cb, bm, bc, bp, bs, bn, bl, br);
       axpy4(r, cub, xz);
-      const long o = z * plane + roff;
-      if (vb) axpy4(r, cvb, ld4(vb + o));
-      *reinterpret_cast<float4*>(yb + o) = r;
+      axpy4(r, cvb, ld(vb, z));
+      *reinterpret_cast<float4*>(yb + z * plane + roff) = r;
     }
-    __syncthreads();
   }
 }
 
@@ -954,6 +961,15 @@ struct ChainStep {
   Epi<T> e;
 };
 
+static int f4x2_resident() {
+  static const int b = [] {
+    int r = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_stencil7_f4x2, 64 * kX2Halo, 0) != cudaSuccess) r = 0;
+    return r > 0 ? r : 1;
+  }();
+  return b;
+}
+
 // Can two fp32 steps share one k_stencil7_f4x2 pass?
 static bool f4x2_ok(const MatView& M, const ChainStep<float>& A, const ChainStep<float>& B) {
   if (M.format != FMT_STENCIL7 || M.nx % 4 != 0 || M.nx > kX2MaxNx) return false;
@@ -988,9 +1004,11 @@ static void run_chain(const MatView& Ks, const std::vector<ChainStep<T>>& steps,
           if (steps[q].in == A.out || steps[q].e.u == A.out) { need = true; break; }
           if (steps[q].out == A.out) break;
         }
+        // two full waves of resident blocks (each SM holds f4x2_resident() blocks)
         const int gy = (Ks.ny + kX2Rows - 1) / kX2Rows;
-        const long target = 3L * num_sms();
-        int zc = (int)std::max(4L, std::min((long)Ks.nz, ((long)Ks.nz * gy + target - 1) / target));
+        const long target = 2L * num_sms() * f4x2_resident();
+        const long chunks = std::max(1L, std::min((long)Ks.nz, (target + gy - 1) / gy));
+        int zc = (int)std::max(4L, ((long)Ks.nz + chunks - 1) / chunks);
         dim3 blk(32 * ((Ks.nx + 127) / 128), kX2Halo, 1);
         dim3 grid(gy, (Ks.nz + zc - 1) / zc, 1);
         k_stencil7_f4x2<<<grid, blk, 0, st>>>(
