@@ -381,15 +381,19 @@ __global__ void __launch_bounds__(64 * kX2Halo, 2) k_stencil7_f4x2(
     pn = ld(xin, z + 3);
     stepA(z + 1, m, c, p, ld(u, z + 1), ld(v, z + 1));
     __syncthreads();
+    // step B; every lane runs the shuffles (lanes past the grid hold zeros)
+    const int s0 = (z + 3) & 3, s1 = z & 3, s2 = (z + 1) & 3;  // planes z-1, z, z+1
+    float4 bm = zero, bc = zero, bp = zero, bs = zero, bn = zero;
     if (interior) {
-      const int s0 = (z + 3) & 3, s1 = z & 3, s2 = (z + 1) & 3;  // planes z-1, z, z+1
-      const float4 bm = *reinterpret_cast<const float4*>(&sA[s0][ty][i0]);
-      const float4 bc = *reinterpret_cast<const float4*>(&sA[s1][ty][i0]);
-      const float4 bp = *reinterpret_cast<const float4*>(&sA[s2][ty][i0]);
-      const float4 bs = *reinterpret_cast<const float4*>(&sA[s1][ty - 1][i0]);
-      const float4 bn = *reinterpret_cast<const float4*>(&sA[s1][ty + 1][i0]);
-      float bl = __shfl_up_sync(0xffffffffu, bc.w, 1);
-      float br = __shfl_down_sync(0xffffffffu, bc.x, 1);
+      bm = *reinterpret_cast<const float4*>(&sA[s0][ty][i0]);
+      bc = *reinterpret_cast<const float4*>(&sA[s1][ty][i0]);
+      bp = *reinterpret_cast<const float4*>(&sA[s2][ty][i0]);
+      bs = *reinterpret_cast<const float4*>(&sA[s1][ty - 1][i0]);
+      bn = *reinterpret_cast<const float4*>(&sA[s1][ty + 1][i0]);
+    }
+    float bl = __shfl_up_sync(0xffffffffu, bc.w, 1);
+    float br = __shfl_down_sync(0xffffffffu, bc.x, 1);
+    if (interior) {
       if (lane == 0) bl = (i0 > 0) ? sA[s1][ty][i0 - 1] : 0.f;
       if (lane == 31) br = (i0 + 4 < nx) ? sA[s1][ty][i0 + 4] : 0.f;
       float4 r = st7_apply(cb, bm, bc, bp, bs, bn, bl, br);
