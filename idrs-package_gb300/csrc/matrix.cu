@@ -373,12 +373,9 @@ __global__ void __launch_bounds__(64 * kX2Halo, 2) k_stencil7_f4x2(
   stepA(z0 - 1, m, c, p, ld(u, z0 - 1), ld(v, z0 - 1));
   m = c; c = p; p = ld(xin, z0 + 1);
   stepA(z0, m, c, p, ld(u, z0), ld(v, z0));
-  // software pipeline: the next input plane is requested a step ahead
-  float4 pn = ld(xin, z0 + 2);
   for (int z = z0; z < z1; ++z) {
     const float4 xz = c;  // xin(z)
-    m = c; c = p; p = pn;
-    pn = ld(xin, z + 3);
+    m = c; c = p; p = ld(xin, z + 2);
     stepA(z + 1, m, c, p, ld(u, z + 1), ld(v, z + 1));
     __syncthreads();
     // step B; every lane runs the shuffles (lanes past the grid hold zeros)
