@@ -222,16 +222,18 @@ def run_ours(args, rank, world, dist):
     err_vs_fp64 = float(np.linalg.norm(x_mixed - x_fp64) / np.linalg.norm(x_fp64))
     err_exact = float(np.max(np.abs(x_mixed - 1.0)))
 
-    # roofline of the dominant kernel: the fp32 stencil step of the Chebyshev
-    # chain, evaluated by its three-term recurrence (one product = 9 launches;
-    # algorithmic bytes per product at 4 B per value: first step 8N (reads v,
-    # writes y2), second 12N (y2, v -> y3), six 16N steps (y_{i-1}, y_{i-2},
-    # v -> y_i) and the final 8N: 124N)
+    # roofline of the dominant kernel: the fp32 Chebyshev(8) chain evaluated by
+    # its three-term recurrence, two stencil steps per pass (k_stencil7_f4x2,
+    # 4 launches + 1 single step per product).  Algorithmic bytes per product
+    # at 4 B per value: pair (y2, y3) reads v, writes y2, y3: 12N; pairs
+    # (y4, y5), (y6, y7) read y_{i-1}, y_{i-2}, v and write two: 20N each; pair
+    # (y8, y9) writes y9 only: 16N; the last step reads y9, writes w: 8N -> 76N.
+    # (Nine unfused steps would need 124N.)
     A = pkg.Matrix(K, P=D)
     A.preconditioner(2, 8, foci=list(r_mixed.foci))
     ms_prod32, ms_launch32 = A.time_matvec(32, 5, 20)
     ms_prod64, ms_launch64 = A.time_matvec(64, 3, 10)
-    bytes32 = 124.0 * N
+    bytes32 = 76.0 * N
     bytes64 = 200.0 * N
     peaks = {}
     try:
@@ -243,7 +245,7 @@ def run_ours(args, rank, world, dist):
     traffic = None
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        traffic = prof.get("stencil7_fp32_horner_per_launch_bytes_scaled")
+        traffic = prof.get("stencil7_fp32_chain_per_product_bytes")
     except Exception:
         pass
 
@@ -286,11 +288,13 @@ def run_ours(args, rank, world, dist):
                  "stencil_fp64_chain_ms_per_product": ms_prod64, "stencil_fp64_ms_per_launch": ms_launch64,
                  "stencil_fp64_GBps": round(bytes64 / (ms_prod64 * 1e-3) / 1e9, 1),
                  "note": "fp64 stencil is bound by GB300's FP64 pipe, not by HBM"},
-        "roofline": {"bound": "hbm", "kernel": "k_stencil7<float> (Chebyshev recurrence step, fp32)",
+        "roofline": {"bound": "hbm", "kernel": "k_stencil7_f4x2 + k_stencil7_f4 (fp32 Chebyshev(8) recurrence product)",
                      "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                      "traffic": traffic,
-                     "algorithmic_bytes": "124 N per 9-launch product (8N + 12N + 6x16N + 8N), N = 256^3"},
+                     "algorithmic_bytes": "76 N per 5-launch product (12N + 20N + 20N + 16N + 8N), N = 256^3; "
+                                          "traffic = ncu DRAM bytes per product",
+                     "unfused_equivalent_GBps": round(124.0 * N / (ms_prod32 * 1e-3) / 1e9, 1)},
         "e2e": {"value": round(statistics.mean(t_e2e), 5), "unit": "s",
                 "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
                 "flag": r_e2e.flag, "relres_original": r_e2e.relres_original},
