@@ -213,8 +213,8 @@ def run_ours(args, rank, world, dist):
     with ClockSampler(torch.cuda.current_device()) as clk:
         t_mixed, r_mixed = timed("mixed", args.steps)
     launches = (pkg.lib().idrs_launch_count() - launches0) // max(args.steps, 1)
+    x_mixed = x_dev.cpu().numpy()  # the last timed mixed solve's x
     t_fp64, r_fp64 = timed("fp64", max(1, min(2, args.steps)))
-    x_mixed = x_dev.cpu().numpy()
     t_e2e, r_e2e = timed("mixed", args.steps, host=True)
     # accuracy of the mixed solution against the fp64 one and the exact x = 1
     solve("fp64", tols["fp64"])
