@@ -49,9 +49,11 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--profile", choices=["solve", "chain32", "chain64", "spmv_pagerank", "grad128"], default=None,
                    help="profiling driver: one mixed solve, or the fp32/fp64 Chebyshev(8) chain alone")
-    p.add_argument("--workload", choices=["cdr256", "pagerank", "multishift", "adjoint"], default="cdr256",
+    p.add_argument("--workload", choices=["cdr256", "pagerank", "multishift", "adjoint", "sequence"],
+                   default="cdr256",
                    help="cdr256: the headline line; the others measure the remaining configurations "
-                        "(PageRank 4M, complex multishift 128^3, adjoint 128^3) and print one JSON line each")
+                        "(PageRank 4M, complex multishift 128^3, adjoint 128^3, an 8 right-hand-side "
+                        "sequence with warm start and recycling at 128^3) and print one JSON line each")
     p.add_argument("--fd-samples", type=int, default=64,
                    help="adjoint workload: finite-difference samples of b and of A's nonzeros (each)")
     return p.parse_args()
@@ -651,13 +653,73 @@ def run_adjoint(args):
                                "seconds": round(fd_sec, 1)}}), flush=True)
 
 
+def run_sequence(args):
+    """A sequence of 8 right-hand sides on the 128^3 convection-diffusion
+    stencil (diagonal scaling, Ritz-estimated Chebyshev(4), IDR(4), tol 1e-8)
+    through PP_MR_IDRS: b_1 = K x_model, b_k = b_1 + 1e-3 k |b_1|/sqrt(N) xi_k
+    (xi_k seeded N(0,1)).  Each solve starts from the previous solution; the
+    variants add the recycle space U0, or (without the polynomial) 32 Ritz
+    omegas.  Timed end to end
+    (host b_all in, host x_all out); the oracle runs a bounded sample."""
+    import torch  # noqa: F401  (CUDA context for the events)
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    P = pkg.problems
+    n, nrhs = 128, 8
+    N = n ** 3
+    coef = P.cdr_coefficients(n)
+    S = pkg.stencil7_format(n, n, n, coef)
+    D = pkg.real_precon(1, S)
+    b1 = P.stencil_apply(n, n, n, coef, P.model_solution(n, n, n))
+    rng = np.random.default_rng(31)
+    B = np.empty((N, nrhs), order="F")
+    for k in range(nrhs):
+        B[:, k] = b1 + (1e-3 * k * np.linalg.norm(b1) / np.sqrt(N)) * rng.standard_normal(N)
+    kw = dict(s=4, tol=1e-8, maxit=4000, preconditioner=2, degree=4, n_ritz=16)
+    plain = dict(s=4, tol=1e-8, maxit=4000, preconditioner=0, n_ritz=32)
+    pkg.PP_MR_IDRS(S, B[:, :1], P=D, **kw)  # warm-up (library load, pools)
+    out = {}
+    for name, opts in (("cheb4+warm_start", kw), ("cheb4+warm_start+recycle", dict(kw, recycle=True)),
+                       ("scaling_only+warm_start", plain),
+                       ("scaling_only+warm_start+omega32", dict(plain, n_omega=32)),
+                       ("scaling_only+warm_start+recycle", dict(plain, recycle=True))):
+        t0 = time.perf_counter()
+        r = pkg.PP_MR_IDRS(S, B, P=D, **opts)
+        sec = time.perf_counter() - t0
+        assert list(r.flags) == [0] * nrhs
+        out[name] = {"seconds_total": round(sec, 4), "seconds_setup": round(r.seconds_setup, 4),
+                     "iterations": [int(i) for i in r.iterations],
+                     "max_relres_original": float(np.max(r.relres_original)),
+                     "recycle_iterations": r.recycle_iterations}
+    cold = []
+    t0 = time.perf_counter()
+    for k in range(nrhs):
+        cold.append(pkg.PP_IDRS(S, B[:, k], P=D, **kw).iterations)
+    out["independent_pp_idrs"] = {"seconds_total": round(time.perf_counter() - t0, 4),
+                                  "iterations": cold}
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle as O
+        O.build()
+        So = O.stencil7_format(n, n, n, coef)
+        t0 = time.perf_counter()
+        ro = O.pp_mr_idrs(So, B[:, :2], P=O.real_precon(1, So), recycle=True, **kw)
+        cpu = {"seconds": round(time.perf_counter() - t0, 2), "cores": O.get_threads(),
+               "kind": "port", "sample": "PP_MR_IDRS with recycle, first 2 right-hand sides",
+               "iterations": [int(i) for i in ro.iterations],
+               "recycle_iterations": ro.recycle_iterations}
+    print(json.dumps({"workload": "sequence_cdr128_stencil_cheb4_idr4_tol1e-8_8rhs", "N": N,
+                      "variants": out, "cpu_baseline": cpu}), flush=True)
+
+
 def main():
     args = parse()
     if args.profile:
         run_profile(args)
         return
     if args.workload != "cdr256":
-        {"pagerank": run_pagerank, "multishift": run_multishift, "adjoint": run_adjoint}[args.workload](args)
+        {"pagerank": run_pagerank, "multishift": run_multishift, "adjoint": run_adjoint,
+         "sequence": run_sequence}[args.workload](args)
         return
     rank, world, dist = dist_init(args.gpus)
     if args.impl == "reference":

@@ -106,8 +106,10 @@ _PROTOS = {
     "idrs_rinprod": (_i, [_vp, _vp, _vp, _vp]),
     "idrs_cinprod": (_i, [_vp, _vp, _vp, _vp]),
     "idrs_rinprod_noalloc": (_i, [C.c_long, _vp, _vp, _vp, _vp]),
-    "idrs_ridrs_ritz": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp]),
+    "idrs_ridrs_ritz": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp,
+                             _i, _vp, _i, _vp, _i, _i, _vp, _vp]),
     "idrs_rpp_idrs": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "idrs_rpp_mr_idrs": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 
@@ -115,7 +117,8 @@ class PPOptions(C.Structure):
     _fields_ = [("method", C.c_int), ("s", C.c_int), ("tol", C.c_double), ("maxit", C.c_int),
                 ("in_s", C.c_int), ("in_it", C.c_int), ("in_tol", C.c_double),
                 ("preconditioner", C.c_int), ("degree", C.c_int), ("n_ritz", C.c_int),
-                ("inner_precision", C.c_int), ("device_pointers", C.c_int)]
+                ("inner_precision", C.c_int), ("device_pointers", C.c_int),
+                ("n_omega", C.c_int), ("recycle", C.c_int)]
 
 
 class PPReport(C.Structure):
@@ -124,7 +127,9 @@ class PPReport(C.Structure):
                 ("relres_original", C.c_double), ("foci", C.c_double * 2), ("center", C.c_double),
                 ("seconds_setup", C.c_double), ("seconds_solve", C.c_double),
                 ("seconds_total", C.c_double), ("inner_solves", C.c_int),
-                ("inner_iterations", C.c_int), ("inner_max", C.c_int)]
+                ("inner_iterations", C.c_int), ("inner_max", C.c_int),
+                ("recycle_flag", C.c_int), ("recycle_iterations", C.c_int),
+                ("recycle_relres", C.c_double)]
 
 
 def load(path: str | None = None):
@@ -619,28 +624,56 @@ def INPROD(A: Matrix, u, v):
     return complex(out[0], out[1]) if A.cplx else float(out[0])
 
 
-def IDRS_RITZ(A: Matrix, b, s, tolerance=None, maximum_iterations=None, x0=None, H_shape=None):
-    """IDRS_RITZ (ritz_module.f90:389-556): Hessenberg output and nritz."""
+def IDRS_RITZ(A: Matrix, b, s, M: Matrix | None = None, tolerance=None, maximum_iterations=None,
+              variant=None, x0=None, n_omega=0, dimU0=0, resvec=False, H_shape=None) -> Result:
+    """x = IDRS_RITZ(A, b, s[, M, tolerance, maximum_iterations, variant, flag, relres,
+    iterations, x0, U0, omega, resvec, H]) (ritz_module.f90:389-556).
+
+    The reference's optional outputs are requested by size: n_omega (omega),
+    dimU0 (the recycle space U0, n x dimU0), H_shape (H) and resvec."""
     b = _solver_common(A, b)
     x = np.empty_like(b)
     flag, relres, iters, nritz = C.c_int(), C.c_double(), C.c_int(), C.c_int()
-    Hm = None
-    if H_shape:
-        Hm = np.zeros(H_shape, order="F")
-    _check(lib().idrs_ridrs_ritz(A.handle, _p(b), int(s), _ref_dbl(tolerance),
-                                 _ref_int(maximum_iterations), C.byref(flag), C.byref(relres),
-                                 C.byref(iters), _p(_arr(x0, False, A.n)), _p(Hm),
+    Hm = np.zeros(H_shape, order="F") if H_shape else None
+    om = np.zeros(n_omega) if n_omega else None
+    U0 = np.zeros((A.n, dimU0), order="F") if dimU0 else None
+    maxit = maximum_iterations if maximum_iterations is not None else min(2 * A.n, 1000)
+    rv = np.zeros(maxit + 1) if resvec else None
+    _check(lib().idrs_ridrs_ritz(A.handle, _p(b), int(s), M.handle if M else None,
+                                 _ref_dbl(tolerance), _ref_int(maximum_iterations),
+                                 _ref_int(variant), C.byref(flag), C.byref(relres), C.byref(iters),
+                                 _p(_arr(x0, False, A.n)), _p(U0), int(dimU0), _p(om), int(n_omega),
+                                 _p(rv), 0 if rv is None else len(rv), _p(Hm),
                                  0 if Hm is None else H_shape[0], 0 if Hm is None else H_shape[1],
                                  C.byref(nritz), _p(x)))
     r = Result(x=x, flag=flag.value, relres=relres.value, iterations=iters.value, nritz=nritz.value)
-    if Hm is not None:
-        r["H"] = Hm
+    for key, val in (("H", Hm), ("omega", om), ("U0", U0), ("resvec", rv)):
+        if val is not None:
+            r[key] = val
     return r
+
+
+def _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
+                inner_precision, dev, n_omega, recycle):
+    return PPOptions(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
+                     inner_precision, int(dev), int(n_omega), int(bool(recycle)))
+
+
+def _pp_result(rep: PPReport, **extra) -> Result:
+    return Result(flag=rep.flag, iterations=rep.iterations,
+                  ritz_iterations=rep.ritz_iterations, nritz=rep.nritz,
+                  relres=rep.relres_solver, relres_original=rep.relres_original,
+                  foci=tuple(rep.foci), center=rep.center, seconds_setup=rep.seconds_setup,
+                  seconds_solve=rep.seconds_solve, seconds_total=rep.seconds_total,
+                  inner_solves=rep.inner_solves, inner_iterations=rep.inner_iterations,
+                  inner_max=rep.inner_max, recycle_flag=rep.recycle_flag,
+                  recycle_iterations=rep.recycle_iterations, recycle_relres=rep.recycle_relres,
+                  **extra)
 
 
 def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=None, *, method=1,
             s=4, tol=1e-6, maxit=1000, in_s=1, in_it=0, in_tol=0.1, preconditioner=0, degree=0,
-            n_ritz=32, inner_precision=64, x_out=None) -> Result:
+            n_ritz=32, inner_precision=64, n_omega=0, x_out=None) -> Result:
     """x = pp_idrs(K, b[, P, center, foci]) (RPP_IDRS, pp_idrs_module.f90:118-162);
     the command-line options of initialize.inc:4-31 are keyword arguments.
 
@@ -654,16 +687,48 @@ def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=Non
     else:
         b = _arr(b, False, K.nrows)
         x = np.empty_like(b)
-    o = PPOptions(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
-                  inner_precision, int(dev))
+    o = _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
+                    inner_precision, dev, n_omega, False)
     rep = PPReport()
     f = None if foci is None else np.ascontiguousarray(foci, dtype=np.float64)
     _check(lib().idrs_rpp_idrs(K.handle, _p(b), P.handle if P else None, _ref_dbl(center), _p(f),
                                C.byref(o), C.byref(rep), _p(x)))
-    return Result(x=None if dev else x, flag=rep.flag, iterations=rep.iterations,
-                  ritz_iterations=rep.ritz_iterations, nritz=rep.nritz,
-                  relres=rep.relres_solver, relres_original=rep.relres_original,
-                  foci=tuple(rep.foci), center=rep.center, seconds_setup=rep.seconds_setup,
-                  seconds_solve=rep.seconds_solve, seconds_total=rep.seconds_total,
-                  inner_solves=rep.inner_solves, inner_iterations=rep.inner_iterations,
-                  inner_max=rep.inner_max)
+    return _pp_result(rep, x=None if dev else x)
+
+
+def PP_MR_IDRS(K: UserMatrix, b_all, P: UserMatrix | None = None, center=None, foci=None, *,
+               method=1, s=4, tol=1e-6, maxit=1000, in_s=1, in_it=0, in_tol=0.1,
+               preconditioner=0, degree=0, n_ritz=32, inner_precision=64, n_omega=0,
+               recycle=False, nrhs=None, x_out=None) -> Result:
+    """x_all = pp_idrs(K, b_all[, P, center, foci]) for a sequence of right-hand sides
+    (RPP_MR_IDRS, pp_idrs_module.f90:222-279, recycle.inc, run_mr_idrs.inc).
+
+    b_all: n x nrhs numpy array, or the int device address of a column-major
+    n x nrhs array (then nrhs and the device address x_out are required).
+    Returns x (n x nrhs, host case) and per right-hand side arrays flags,
+    iterations, relres, relres_original, seconds_solve."""
+    dev = isinstance(b_all, int)
+    n = K.nrows
+    if dev:
+        if not isinstance(x_out, int) or not nrhs:
+            raise ValueError("a device b_all needs nrhs and a device x_out")
+        x = x_out
+    else:
+        b_all = np.asfortranarray(b_all, dtype=np.float64)
+        if b_all.ndim != 2 or b_all.shape[0] != n:
+            raise ValueError("b_all must be n x nrhs")
+        nrhs = b_all.shape[1]
+        x = np.zeros((n, nrhs), order="F")
+    o = _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
+                    inner_precision, dev, n_omega, recycle)
+    reps = (PPReport * nrhs)()
+    f = None if foci is None else np.ascontiguousarray(foci, dtype=np.float64)
+    _check(lib().idrs_rpp_mr_idrs(K.handle, int(nrhs), _p(b_all), P.handle if P else None,
+                                  _ref_dbl(center), _p(f), C.byref(o), reps, _p(x)))
+    r = _pp_result(reps[nrhs - 1], x=None if dev else x)
+    r["flags"] = np.array([q.flag for q in reps])
+    r["iterations"] = np.array([q.iterations for q in reps])
+    r["relres"] = np.array([q.relres_solver for q in reps])
+    r["relres_original"] = np.array([q.relres_original for q in reps])
+    r["seconds_solve"] = np.array([q.seconds_solve for q in reps])
+    return r

@@ -10,6 +10,7 @@
 
 #include "../../include/idrs_gb300.h"
 #include "adjoint.h"
+#include "recycle.h"
 #include "idrs_gpu.cuh"
 #include "ms_gpu.cuh"
 #include "setup.h"
@@ -1321,29 +1322,65 @@ int idrs_radjoint(idrs_matrix AT, idrs_user_matrix K, const double* x, const dou
   });
 }
 
-int idrs_ridrs_ritz(idrs_matrix A, const double* b, int s, const double* tolerance,
-                    const int* maximum_iterations, int* flag, double* relres, int* iterations,
-                    const double* x0, double* H, int ldh, int nh, int* nritz, double* x) {
+int idrs_ridrs_ritz(idrs_matrix A, const double* b, int s, idrs_matrix M,
+                    const double* tolerance, const int* maximum_iterations, const int* variant,
+                    int* flag, double* relres, int* iterations, const double* x0, double* U0,
+                    int dimU0, double* omega, int n_omega, double* resvec, int resvec_len,
+                    double* H, int ldh, int nh, int* nritz, double* x) {
   return guard([&] {
     REQUIRE(A && !A->cplx && b && x, "ridrs_ritz: bad arguments");
+    REQUIRE(!M || !M->cplx, "ridrs_ritz: M must be real");
     long n = A->n();
+    if (tolerance) REQUIRE(*tolerance >= 0, "Illegal value for parameter tolerance");
     int maxit = maximum_iterations ? *maximum_iterations : (int)std::min<long>(2 * n, 1000);
     REQUIRE(maxit >= 1, "ridrs_ritz: maximum_iterations must be positive");
+    if (resvec) REQUIRE(resvec_len >= maxit + 1, "Length of vector with residual norms too small, should be maxit+1");
+    if (U0 && dimU0 > 0) {
+      REQUIRE(dimU0 <= MAXS, "ridrs_ritz: dimension of U0 larger than 16");
+    }
     std::vector<double> Hf((size_t)(maxit + 1) * maxit, 0.0);
     std::vector<double> zeros;
     const double* xs = x0;
     if (!xs && !A->device_pointers) { zeros.assign(n, 0.0); xs = zeros.data(); }
-    int conv = -1, iter = 0, one = 1;
+    int conv = -1, iter = 0, method = variant ? *variant : 1;
     double rel = 1.0;
     std::vector<double> resnrm(maxit + 1);
-    int st = run_idrs<double>(A, b, s, nullptr, tolerance, &maxit, &one, &conv, &rel, &iter, xs,
+    int st = run_idrs<double>(A, b, s, M, tolerance, &maxit, &method, &conv, &rel, &iter, xs,
                               nullptr, nullptr, 0, resnrm.data(), maxit + 1, Hf.data(), maxit + 1,
                               maxit, x);
     if (st) return st;
+    const int nr = (iter / (s + 1)) * s + iter % (s + 1);
     if (flag) *flag = conv;
     if (relres) *relres = rel;
     if (iterations) *iterations = iter;
-    if (nritz) *nritz = (iter / (s + 1)) * s + iter % (s + 1);
+    if (nritz) *nritz = nr;
+    if (resvec) std::copy(resnrm.begin(), resnrm.end(), resvec);
+    if (omega && n_omega > 0) {
+      REQUIRE(nr >= n_omega, "Too many parameters omega requested, reduce omega.");
+      ritz_omega(Hf.data(), maxit + 1, n_omega, omega);
+    }
+    if (U0 && dimU0 > 0) {
+      REQUIRE(nr >= dimU0, "Recycle space is too large, reduce dimension of U0.");
+      cudaStream_t cs = A->stream;
+      std::vector<double> vec((size_t)nr * dimU0), resval(dimU0);
+      si_power(Hf.data(), maxit + 1, nr, dimU0, 0.0, kSiPowerSeed, vec.data());
+      Staged sb(A, sizeof(double) * n), su(A, sizeof(double) * n * dimU0);
+      const double* d_b = (const double*)sb.in(b);
+      double* d_U = (double*)su.out(U0);
+      Operator* Mp = (M && M->dkind != 0) ? M : nullptr;
+      compute_u0(*A, Mp, Hf.data(), maxit + 1, nr, vec.data(), dimU0, d_b, d_U, resval.data(), cs);
+      if (Mp)
+        for (int j = 0; j < dimU0; ++j) {
+          DBuf tmp(sizeof(double) * n, cs);
+          op_precon<double>(*Mp, 64, d_U + (size_t)n * j, tmp.as<double>(), nullptr, cs);
+          IDRS_CUDA(cudaMemcpyAsync(d_U + (size_t)n * j, tmp.p, sizeof(double) * n,
+                                    cudaMemcpyDeviceToDevice, cs));
+        }
+      int dep = global_qr(n, dimU0, d_U, nullptr, A->red, cs);
+      REQUIRE(dep == 0, " V has dependent columns ");
+      su.finish(U0, d_U);
+      IDRS_CUDA(cudaStreamSynchronize(cs));
+    }
     if (H) {
       REQUIRE((long)ldh * nh <= (long)(maxit + 1) * maxit && ldh <= maxit + 1 && nh <= maxit,
               "Dimensions of Hessenberg matrix too large");
@@ -1354,6 +1391,151 @@ int idrs_ridrs_ritz(idrs_matrix A, const double* b, int s, const double* toleran
   });
 }
 
+}  // extern "C"
+
+// ------------------------------------------------------------- pp_idrs
+namespace {
+
+// One pp_idrs job: the operator built from K (and P), its device buffers and
+// what the set-up solves produced (x0, omega, U0).
+struct PPJob {
+  idrs_matrix A = nullptr;
+  long n = 0;
+  cudaStream_t cs = nullptr;
+  DBuf d_x0, d_y, t1, t2, r, res;
+  std::vector<double> omega;  // allocated when the initial solve ran
+  DBuf U0;
+  bool have_U0 = false;
+  ~PPJob() {
+    // device buffers go back on the operator's stream before it is destroyed
+    d_x0 = DBuf(); d_y = DBuf(); t1 = DBuf(); t2 = DBuf(); r = DBuf(); res = DBuf(); U0 = DBuf();
+    if (A) idrs_matrix_free(A);
+  }
+};
+
+// real_preconditioner.inc:10-34: the initial IDRS_RITZ solve (x0, H and,
+// with n_omega > 0, omega) and the polynomial preconditioner.
+int pp_setup(PPJob& J, const double* pb, const double* center, const double* foci,
+             const idrs_pp_options* opt, idrs_pp_report& rep) {
+  const int s = opt->s;
+  int preconditioner = opt->degree == 0 ? 0 : opt->preconditioner;
+  bool estimate = preconditioner != 0;
+  if (preconditioner == 1 && center) estimate = false;
+  if (preconditioner == 2 && foci) estimate = false;
+  const bool initial = estimate || opt->n_omega > 0;
+  double tol = opt->tol;
+  int st = 0;
+  std::vector<double> H;
+  int ldh = 0;
+  if (initial) {
+    int ini_iter = opt->n_ritz + opt->n_ritz / s;
+    ldh = ini_iter + 1;
+    H.assign((size_t)ldh * ini_iter, 0.0);
+    J.omega.assign(std::max(opt->n_omega, 0), 0.0);
+    int flag = -1, iter = 0, nr = 0, one = 1;
+    double rel = 1;
+    st = idrs_ridrs_ritz(J.A, pb, s, nullptr, &tol, &ini_iter, &one, &flag, &rel, &iter,
+                         J.d_x0.as<double>(), nullptr, 0,
+                         opt->n_omega > 0 ? J.omega.data() : nullptr, opt->n_omega, nullptr, 0,
+                         H.data(), ldh, ini_iter, &nr, J.d_x0.as<double>());
+    if (st) return st;
+    rep.ritz_iterations = iter;
+    rep.nritz = nr;
+  }
+  if (estimate) {
+    analyse_spectrum(H.data(), ldh, rep.nritz, rep.foci, &rep.center, nullptr);
+    st = set_preconditioner(J.A, preconditioner, opt->degree, nullptr, nullptr, H.data(), ldh, rep.nritz);
+  } else {
+    double f[2] = {0.15, 1.85}, c = 1.0;
+    if (foci) { f[0] = foci[0]; f[1] = foci[1]; }
+    if (center) c = *center;
+    rep.foci[0] = f[0]; rep.foci[1] = f[1]; rep.center = c;
+    st = set_preconditioner(J.A, preconditioner, opt->degree, f, &c, nullptr, 0, 0);
+  }
+  return st;
+}
+
+// recycle.inc: x0 = IDRS_RITZ(A, b, s, tol, maxit, variant 1) with U0 (n x s)
+int pp_recycle(PPJob& J, const double* pb, const idrs_pp_options* opt, idrs_pp_report& rep) {
+  const int s = opt->s;
+  J.U0 = DBuf(sizeof(double) * J.n * s, J.cs);
+  double tol = opt->tol;
+  int maxit = opt->maxit, one = 1;
+  int st = idrs_ridrs_ritz(J.A, pb, s, nullptr, &tol, &maxit, &one, &rep.recycle_flag,
+                           &rep.recycle_relres, &rep.recycle_iterations, nullptr,
+                           J.U0.as<double>(), s, nullptr, 0, nullptr, 0, nullptr, 0, 0, nullptr,
+                           J.d_x0.as<double>());
+  if (st) return st;
+  J.have_U0 = true;
+  return IDRS_OK;
+}
+
+// One solve of run_idrs.inc:9-60 / run_mr_idrs.inc:15-72 from x0 (then
+// x0 = y), x = scaleback(A, b, y) and the original system's relative residual.
+int pp_solve(PPJob& J, const double* pb, double* px, const idrs_pp_options* opt,
+             idrs_pp_report& rep) {
+  idrs_matrix A = J.A;
+  const long n = J.n;
+  const int s = opt->s;
+  double tol = opt->tol;
+  int maxit = opt->maxit, st = 0;
+  const double* om = J.omega.empty() ? nullptr : J.omega.data();
+  const int n_om = (int)J.omega.size();
+  if (opt->method == 0) {
+    int in_s = opt->in_s, in_it = opt->in_it, prec = opt->inner_precision ? opt->inner_precision : 64;
+    double in_tol = opt->in_tol;
+    st = idrs_rqmridr(A, pb, s, nullptr, &tol, &maxit, &rep.flag, &rep.relres_solver,
+                      &rep.iterations, &in_s, &in_tol, &in_it, J.d_x0.as<double>(), om, n_om,
+                      nullptr, 0, &prec, J.d_y.as<double>());
+    rep.inner_solves = A->last_inner_calls;
+    rep.inner_iterations = A->last_inner_total;
+    rep.inner_max = A->last_inner_max;
+  } else {
+    int variant = opt->method == 2 ? 2 : 1;
+    st = idrs_ridrs(A, pb, s, nullptr, &tol, &maxit, &variant, &rep.flag, &rep.relres_solver,
+                    &rep.iterations, J.d_x0.as<double>(),
+                    J.have_U0 ? J.U0.as<double>() : nullptr, om, n_om, nullptr, 0, nullptr, 0, 0,
+                    J.d_y.as<double>());
+  }
+  if (st) return st;
+  cudaStream_t cs = J.cs;
+  // x0 = y (the warm start of the next right-hand side); x = scaleback(A, b, y)
+  IDRS_CUDA(cudaMemcpyAsync(J.d_x0.p, J.d_y.p, 8 * n, cudaMemcpyDeviceToDevice, cs));
+  op_scaleback<double>(*A, 64, A->alpha_p, A->degree, J.d_y.as<double>(), px, J.t1.as<double>(),
+                       J.t2.as<double>(), nullptr, cs);
+  spmv<double>(A->k64, px, J.r.as<double>(), -1.0, 1.0, pb, nullptr, cs);
+  launch_fused<1, double>(n, BNorm<double>{J.r.as<double>()}, TStoreVals<double>{J.res.as<double>(), 1}, A->red, nullptr, cs);
+  launch_fused<1, double>(n, BNorm<double>{pb}, TStoreVals<double>{J.res.as<double>() + 1, 1}, A->red, nullptr, cs);
+  double h[2] = {0, 0};
+  IDRS_CUDA(cudaMemcpyAsync(h, J.res.p, 16, cudaMemcpyDeviceToHost, cs));
+  IDRS_CUDA(cudaStreamSynchronize(cs));
+  rep.relres_original = std::sqrt(h[0]) / std::sqrt(h[1]);
+  return IDRS_OK;
+}
+
+int pp_open(PPJob& J, idrs_user_matrix K, idrs_user_matrix P, const idrs_pp_options* opt) {
+  REQUIRE(opt->s >= 1, "rpp_idrs: s must be positive");
+  REQUIRE(opt->n_omega >= 0, "rpp_idrs: n_omega must not be negative");
+  int st = idrs_matrix_create(K, P, 0, nullptr, &J.A);
+  if (st) return st;
+  J.n = J.A->n();
+  J.cs = J.A->stream;
+  const long n = J.n;
+  J.d_x0 = DBuf(8 * n, J.cs);
+  J.d_y = DBuf(8 * n, J.cs);
+  J.t1 = DBuf(8 * n, J.cs);
+  J.t2 = DBuf(8 * n, J.cs);
+  J.r = DBuf(8 * n, J.cs);
+  J.res = DBuf(16, J.cs);
+  IDRS_CUDA(cudaMemsetAsync(J.d_x0.p, 0, 8 * n, J.cs));
+  J.A->device_pointers = true;
+  return IDRS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int idrs_rpp_idrs(idrs_user_matrix K, const double* b, idrs_user_matrix P, const double* center,
                   const double* foci, const idrs_pp_options* opt, idrs_pp_report* report,
                   double* x) {
@@ -1361,91 +1543,85 @@ int idrs_rpp_idrs(idrs_user_matrix K, const double* b, idrs_user_matrix P, const
     REQUIRE(K && b && opt && x, "rpp_idrs: bad arguments");
     using clk = std::chrono::steady_clock;
     auto t0 = clk::now();
-    idrs_matrix A = nullptr;
-    int st = idrs_matrix_create(K, P, 0, nullptr, &A);
+    PPJob J;
+    int st = pp_open(J, K, P, opt);
     if (st) return st;
-    std::unique_ptr<idrs_matrix_s, int (*)(idrs_matrix)> guardA(A, idrs_matrix_free);
-    long n = A->n();
-    const int s = opt->s;
-    REQUIRE(s >= 1, "rpp_idrs: s must be positive");
-    int preconditioner = opt->degree == 0 ? 0 : opt->preconditioner;
-    bool estimate = preconditioner != 0;
-    if (preconditioner == 1 && center) estimate = false;
-    if (preconditioner == 2 && foci) estimate = false;
-    cudaStream_t cs = A->stream;
+    const long n = J.n;
     const bool dev = opt->device_pointers != 0;
-    DBuf hb_buf, hx_buf, d_x0(8 * n, cs), d_y(8 * n, cs);
+    DBuf hb, hx;
     const double* pb = b;
     double* px = x;
     if (!dev) {
-      hb_buf = DBuf(8 * n, cs);
-      hx_buf = DBuf(8 * n, cs);
-      IDRS_CUDA(cudaMemcpyAsync(hb_buf.p, b, 8 * n, cudaMemcpyHostToDevice, cs));
-      pb = hb_buf.as<double>();
-      px = hx_buf.as<double>();
+      hb = DBuf(8 * n, J.cs);
+      hx = DBuf(8 * n, J.cs);
+      IDRS_CUDA(cudaMemcpyAsync(hb.p, b, 8 * n, cudaMemcpyHostToDevice, J.cs));
+      pb = hb.as<double>();
+      px = hx.as<double>();
     }
-    IDRS_CUDA(cudaMemsetAsync(d_x0.p, 0, 8 * n, cs));
-    A->device_pointers = true;
     idrs_pp_report rep{};
-    double tol = opt->tol;
-    if (estimate) {
-      int ini_iter = opt->n_ritz + opt->n_ritz / s;
-      int ldh = ini_iter + 1;
-      std::vector<double> H((size_t)ldh * ini_iter, 0.0);
-      int flag = -1, iter = 0, nr = 0;
-      double rel = 1;
-      st = idrs_ridrs_ritz(A, pb, s, &tol, &ini_iter, &flag, &rel, &iter,
-                           d_x0.as<double>(), H.data(), ldh, ini_iter, &nr, d_x0.as<double>());
-      if (st) return st;
-      rep.ritz_iterations = iter;
-      rep.nritz = nr;
-      analyse_spectrum(H.data(), ldh, nr, rep.foci, &rep.center, nullptr);
-      set_preconditioner(A, preconditioner, opt->degree, nullptr, nullptr, H.data(), ldh, nr);
-    } else {
-      double f[2] = {0.15, 1.85}, c = 1.0;
-      if (foci) { f[0] = foci[0]; f[1] = foci[1]; }
-      if (center) c = *center;
-      rep.foci[0] = f[0]; rep.foci[1] = f[1]; rep.center = c;
-      set_preconditioner(A, preconditioner, opt->degree, f, &c, nullptr, 0, 0);
-    }
-    IDRS_CUDA(cudaStreamSynchronize(cs));
-    auto t1 = clk::now();
-    int maxit = opt->maxit;
-    if (opt->method == 0) {
-      int in_s = opt->in_s, in_it = opt->in_it, prec = opt->inner_precision ? opt->inner_precision : 64;
-      double in_tol = opt->in_tol;
-      st = idrs_rqmridr(A, pb, s, nullptr, &tol, &maxit, &rep.flag, &rep.relres_solver,
-                        &rep.iterations, &in_s, &in_tol, &in_it, d_x0.as<double>(), nullptr, 0,
-                        nullptr, 0, &prec, d_y.as<double>());
-      rep.inner_solves = A->last_inner_calls;
-      rep.inner_iterations = A->last_inner_total;
-      rep.inner_max = A->last_inner_max;
-    } else {
-      int variant = opt->method == 2 ? 2 : 1;
-      st = idrs_ridrs(A, pb, s, nullptr, &tol, &maxit, &variant, &rep.flag,
-                      &rep.relres_solver, &rep.iterations, d_x0.as<double>(), nullptr, nullptr, 0,
-                      nullptr, 0, nullptr, 0, 0, d_y.as<double>());
-    }
+    st = pp_setup(J, pb, center, foci, opt, rep);
     if (st) return st;
-    // x = scaleback(A, b, y); relres on the original system (run_idrs.inc:113-120)
-    DBuf t1b(8 * n, cs), t2b(8 * n, cs), r(8 * n, cs), res(8, cs);
-    op_scaleback<double>(*A, 64, A->alpha_p, A->degree, d_y.as<double>(), px,
-                         t1b.as<double>(), t2b.as<double>(), nullptr, cs);
-    spmv<double>(A->k64, px, r.as<double>(), -1.0, 1.0, pb, nullptr, cs);
-    launch_fused<1, double>(n, BNorm<double>{r.as<double>()}, TStoreVals<double>{res.as<double>(), 1}, A->red, nullptr, cs);
-    double rr = 0, bb = 0;
-    IDRS_CUDA(cudaMemcpyAsync(&rr, res.p, 8, cudaMemcpyDeviceToHost, cs));
-    launch_fused<1, double>(n, BNorm<double>{pb}, TStoreVals<double>{res.as<double>(), 1}, A->red, nullptr, cs);
-    IDRS_CUDA(cudaStreamSynchronize(cs));
-    IDRS_CUDA(cudaMemcpyAsync(&bb, res.p, 8, cudaMemcpyDeviceToHost, cs));
-    if (!dev) IDRS_CUDA(cudaMemcpyAsync(x, px, 8 * n, cudaMemcpyDeviceToHost, cs));
-    IDRS_CUDA(cudaStreamSynchronize(cs));
-    rep.relres_original = std::sqrt(rr) / std::sqrt(bb);
+    IDRS_CUDA(cudaStreamSynchronize(J.cs));
+    auto t1 = clk::now();
+    st = pp_solve(J, pb, px, opt, rep);
+    if (st) return st;
+    if (!dev) IDRS_CUDA(cudaMemcpyAsync(x, px, 8 * n, cudaMemcpyDeviceToHost, J.cs));
+    IDRS_CUDA(cudaStreamSynchronize(J.cs));
     auto t2 = clk::now();
     rep.seconds_setup = std::chrono::duration<double>(t1 - t0).count();
     rep.seconds_solve = std::chrono::duration<double>(t2 - t1).count();
     rep.seconds_total = std::chrono::duration<double>(t2 - t0).count();
     if (report) *report = rep;
+    return IDRS_OK;
+  });
+}
+
+int idrs_rpp_mr_idrs(idrs_user_matrix K, int nrhs, const double* b_all, idrs_user_matrix P,
+                     const double* center, const double* foci, const idrs_pp_options* opt,
+                     idrs_pp_report* reports, double* x_all) {
+  return guard([&] {
+    REQUIRE(K && b_all && opt && x_all && nrhs >= 1, "rpp_mr_idrs: bad arguments");
+    using clk = std::chrono::steady_clock;
+    auto t0 = clk::now();
+    PPJob J;
+    int st = pp_open(J, K, P, opt);
+    if (st) return st;
+    const long n = J.n;
+    const bool dev = opt->device_pointers != 0;
+    // one right-hand side on the device at a time (host arrays are staged per column)
+    DBuf hb, hx;
+    if (!dev) { hb = DBuf(8 * n, J.cs); hx = DBuf(8 * n, J.cs); }
+    auto column_b = [&](int irhs) -> const double* {
+      if (dev) return b_all + (size_t)n * irhs;
+      IDRS_CUDA(cudaMemcpyAsync(hb.p, b_all + (size_t)n * irhs, 8 * n, cudaMemcpyHostToDevice, J.cs));
+      return hb.as<double>();
+    };
+    idrs_pp_report base{};
+    st = pp_setup(J, column_b(0), center, foci, opt, base);
+    if (st) return st;
+    if (opt->recycle) {
+      st = pp_recycle(J, column_b(0), opt, base);
+      if (st) return st;
+    }
+    IDRS_CUDA(cudaStreamSynchronize(J.cs));
+    auto t1 = clk::now();
+    const double setup = std::chrono::duration<double>(t1 - t0).count();
+    for (int irhs = 0; irhs < nrhs; ++irhs) {
+      auto ts = clk::now();
+      idrs_pp_report rep = base;
+      const double* pb = column_b(irhs);
+      double* px = dev ? x_all + (size_t)n * irhs : hx.as<double>();
+      st = pp_solve(J, pb, px, opt, rep);
+      if (st) return st;
+      if (!dev)
+        IDRS_CUDA(cudaMemcpyAsync(x_all + (size_t)n * irhs, px, 8 * n, cudaMemcpyDeviceToHost, J.cs));
+      IDRS_CUDA(cudaStreamSynchronize(J.cs));
+      auto te = clk::now();
+      rep.seconds_setup = setup;
+      rep.seconds_solve = std::chrono::duration<double>(te - ts).count();
+      rep.seconds_total = std::chrono::duration<double>(te - t0).count();
+      if (reports) reports[irhs] = rep;
+    }
     return IDRS_OK;
   });
 }

@@ -1,0 +1,45 @@
+// recycle.h -- the recycling outputs of IDRS_RITZ (ritz_module.f90:389-556):
+// the omega parameters from the Ritz values and the recycle space U0 (Schur
+// vectors of the Hessenberg matrix by block shift-and-invert power iteration,
+// the Krylov basis rebuilt on the device from the Hessenberg recurrence, and
+// a global modified Gram-Schmidt QR of the result).
+#pragma once
+
+#include <cstdint>
+
+#include "matrix.cuh"
+
+namespace idrs {
+
+// Seed of the SI_power start block.  The reference draws it from
+// RANDOM_NUMBER; here it is uniform01(kSiPowerSeed, i + n*j).
+constexpr uint64_t kSiPowerSeed = 2;
+
+// RSI_power (dense_la_module.f90:531-603): s Schur vectors of H(1:n,1:n)
+// (column-major, leading dimension ldh) nearest `shift`; vec is n x s.
+// Returns 0, or 1 for bad sizes.
+int si_power(const double* H, int ldh, int n, int s, double shift, uint64_t seed, double* vec);
+
+// omega(1:n_omega) = 1/Re(QR_eig(Hf(1:n_omega,1:n_omega))) (|Re| < eps -> 1),
+// ordered greedily by the largest residual-polynomial value
+// (ritz_module.f90:497-520).
+void ritz_omega(const double* Hf, int ldh, int n_omega, double* omega);
+
+// rcompute_U0 (ritz_module.f90:100-160) on the device: rebuilds v_1 = b,
+// v_{i+1} = (A v_i - sum_{l=max(1,i-s)}^{i} v_l H(l,i)) / H(i+1,i) for
+// i = 1..nritz and accumulates U(:,j) = sum_i eigvec(i,j) v_i.  With resnrm
+// (host, length ns) the columns are normalised and the Ritz residual norms
+// returned.  H (ldh >= nritz+1) and eigvec (nritz x ns) are host arrays;
+// b and U (n x ns, leading dimension n) are device arrays.  M: optional
+// preconditioner (the products are A (v / M)).
+void compute_u0(Operator& A, Operator* M, const double* H, int ldh, int nritz,
+                const double* eigvec, int ns, const double* b, double* U, double* resnrm,
+                cudaStream_t st);
+
+// global_RQR_factorization (ritz_module.f90:66-96): modified Gram-Schmidt
+// with global inner products, in place on the device matrix Q (n x s,
+// leading dimension n).  R (host, s x s) optional.  Returns 0, or the
+// 1-based index of the first dependent column.
+int global_qr(long n, int s, double* Q, double* R, RedBuf rb, cudaStream_t st);
+
+}  // namespace idrs

@@ -274,12 +274,23 @@ int idrs_cinprod(idrs_matrix A, const double *u, const double *v, double *uv);
 int idrs_rinprod_noalloc(long n, const double *u, const double *v, double *uv, void *stream);
 
 /* x = IDRS_RITZ(A, b, s[, M, tolerance, maximum_iterations, variant, flag,
- *               relres, iterations, x0, ..., H]): ritz_module.f90:389-556
- * (the Hessenberg output; recycling U0/omega outputs are not provided).
- * H(ldh, nh) receives Hf(1:ldh, 1:nh); *nritz = (iter/(s+1))*s + mod(iter,s+1). */
-int idrs_ridrs_ritz(idrs_matrix A, const double *b, int s, const double *tolerance,
-                    const int *maximum_iterations, int *flag, double *relres, int *iterations,
-                    const double *x0, double *H, int ldh, int nh, int *nritz, double *x);
+ *               relres, iterations, x0, U0, omega, resvec, H]): ritz_module.f90:389-556.
+ * Runs IDRS with the Hessenberg output Hf and returns, besides x:
+ *  - H(ldh, nh) = Hf(1:ldh, 1:nh) (NULL: not wanted);
+ *  - *nritz = (iter/(s+1))*s + mod(iter,s+1);
+ *  - omega(n_omega): 1/Re of the Ritz values of Hf(1:n_omega,1:n_omega),
+ *    ordered greedily (n_omega > nritz: IDRS_ERR_ARG, as the reference's stop);
+ *  - U0(n, dimU0), dimU0 <= 16: the recycle space, an orthonormal basis of
+ *    the Krylov combination of the dimU0 Schur vectors of Hf(1:nritz,1:nritz)
+ *    nearest 0 (SI_power, compute_U0, global QR).  The reference starts
+ *    SI_power from RANDOM_NUMBER; this library from a fixed counter-based
+ *    uniform block (seed 2).  U0 follows the pointer mode of A (host or device).
+ * resvec(resvec_len >= maxit+1) receives the residual norms. */
+int idrs_ridrs_ritz(idrs_matrix A, const double *b, int s, idrs_matrix M,
+                    const double *tolerance, const int *maximum_iterations, const int *variant,
+                    int *flag, double *relres, int *iterations, const double *x0, double *U0,
+                    int dimU0, double *omega, int n_omega, double *resvec, int resvec_len,
+                    double *H, int ldh, int nh, int *nritz, double *x);
 
 /* ---------------------------------------------------------------------- */
 /* pp_idrs: M/PP_IDRS/pp_idrs_module.f90:118-162 (RPP_IDRS) with            */
@@ -299,6 +310,8 @@ typedef struct idrs_pp_options {
   int n_ritz;          /* -ritz (default 32) */
   int inner_precision; /* 64 or 32 */
   int device_pointers; /* 1: b and x are device pointers */
+  int n_omega;         /* -omega: number of Ritz-value omegas (default 0) */
+  int recycle;         /* -recycle: 1 builds the s-dimensional recycle space U0 */
 } idrs_pp_options;
 
 typedef struct idrs_pp_report {
@@ -307,11 +320,24 @@ typedef struct idrs_pp_report {
   double foci[2], center;
   double seconds_setup, seconds_solve, seconds_total;
   int inner_solves, inner_iterations, inner_max;  /* flexible QMRIDR: inner IDR(s) statistics */
+  int recycle_flag, recycle_iterations;            /* the recycle.inc solve (recycle = 1) */
+  double recycle_relres;
 } idrs_pp_report;
 
 int idrs_rpp_idrs(idrs_user_matrix K, const double *b, idrs_user_matrix P, const double *center,
                   const double *foci, const idrs_pp_options *opt, idrs_pp_report *report,
                   double *x);
+
+/* x_all = pp_idrs(K, b_all[, P, center, foci]) for nrhs right-hand sides:
+ * RPP_MR_IDRS (pp_idrs_module.f90:222-279) with real_preconditioner.inc,
+ * recycle.inc and run_mr_idrs.inc.  The set-up solves use b_all(:,1); the
+ * systems are then solved in order, each started from the previous
+ * (preconditioned) solution, with U0 (opt->recycle, IDRS only) and omega
+ * (opt->n_omega).  b_all and x_all are n x nrhs column-major, host or (with
+ * opt->device_pointers) device arrays.  reports: nrhs entries or NULL. */
+int idrs_rpp_mr_idrs(idrs_user_matrix K, int nrhs, const double *b_all, idrs_user_matrix P,
+                     const double *center, const double *foci, const idrs_pp_options *opt,
+                     idrs_pp_report *reports, double *x_all);
 
 #ifdef __cplusplus
 }

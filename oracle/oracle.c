@@ -674,10 +674,207 @@ int or_complex_ms_parameters(or_mat *A, int n_sigma, const or_cplx *sigma, or_cp
 }
 
 /* ------------------------------------------------------------------------ */
-/* IDRS_RITZ: M/IDRS/ritz_module.f90:389-556 (H output; recycling omitted)  */
+/* Recycling helpers (real): dense_la_module.f90:84-124 (RQR_factorization, */
+/* refine = 2), :159-190 (RQR_solve), :531-603 (RSI_power); ritz_module.f90 */
+/* :66-96 (global_RQR_factorization), :100-160 (rcompute_U0) and :497-520   */
+/* (the omega ordering of RIDRS_RITZ).                                      */
+/* ------------------------------------------------------------------------ */
+/* Q(m x n), R(n x n) column-major.  Returns 0, or the 1-based column that was
+ * found dependent (Q and R are then partial, as in the reference). */
+static int or_rqr_fact(int m, int n, const double *V, int ldv, double *Q, double *R) {
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) Q[i + (size_t)m * j] = V[i + (size_t)ldv * j];
+  for (int i = 0; i < n * n; ++i) R[i] = 0;
+  for (int j = 0; j < n; ++j) {
+    double *qj = Q + (size_t)m * j;
+    for (int k = 0; k < 2; ++k)
+      for (int i = 0; i < j; ++i) {
+        const double *qi = Q + (size_t)m * i;
+        double t = 0;
+        for (int q = 0; q < m; ++q) t += qi[q] * qj[q];
+        for (int q = 0; q < m; ++q) qj[q] = qj[q] - t * qi[q];
+        R[i + n * j] = R[i + n * j] + t;
+      }
+    double nr = 0;
+    for (int q = 0; q < m; ++q) nr += qj[q] * qj[q];
+    R[j + n * j] = sqrt(nr);
+    if (R[j + n * j] > DBL_MIN) {
+      for (int q = 0; q < m; ++q) qj[q] = qj[q] / R[j + n * j];
+    } else {
+      return j + 1;
+    }
+  }
+  return 0;
+}
+
+/* X(n x s) = R^-1 Q^T B with Q(m x n), B(m x s) */
+static void or_rqr_solve(int m, int n, int s, const double *Q, const double *R, const double *B,
+                         double *X) {
+  for (int c = 0; c < s; ++c)
+    for (int i = 0; i < n; ++i) {
+      double t = 0;
+      for (int q = 0; q < m; ++q) t += Q[q + (size_t)m * i] * B[q + (size_t)m * c];
+      X[i + (size_t)n * c] = t;
+    }
+  for (int j = n - 1; j >= 0; --j)
+    for (int c = 0; c < s; ++c) {
+      X[j + (size_t)n * c] = X[j + (size_t)n * c] / R[j + n * j];
+      for (int i = 0; i < j; ++i) X[i + (size_t)n * c] = X[i + (size_t)n * c] - R[i + n * j] * X[j + (size_t)n * c];
+    }
+}
+
+/* RSI_power: s Schur vectors of H(1:n,1:n) nearest `shift` by block
+ * shift-and-invert power iteration.  The reference starts from
+ * RANDOM_NUMBER; here the start block is or_uniform(seed, i + n*j). */
+int or_rsi_power(const double *H, int ldh, int n, int s, double shift, uint64_t seed,
+                 double *vec) {
+  if (s < 1 || n < s) return OR_EARG;
+  double *A = calloc((size_t)n * n, sizeof(double)), *Q = malloc(sizeof(double) * n * n),
+         *R = malloc(sizeof(double) * n * n), *sv = malloc(sizeof(double) * n * s),
+         *Qs = malloc(sizeof(double) * n * s), *Rs = malloc(sizeof(double) * s * s);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) A[i + (size_t)n * j] = H[i + (size_t)ldh * j];
+  for (int i = 0; i < n; ++i) A[i + (size_t)n * i] = A[i + (size_t)n * i] - shift;
+  or_rqr_fact(n, n, A, n, Q, R);
+  for (long k = 0; k < (long)n * s; ++k) sv[k] = or_uniform(seed, (uint64_t)k);
+  or_rqr_fact(n, s, sv, n, Qs, Rs);
+  double trace0 = 0;
+  for (int i = 0; i < s; ++i) trace0 += Rs[i + s * i];
+  double trace_old = trace0, err = 1;
+  int iter = 0;
+  while (err > 1e-3 && iter < 1000) {
+    iter = iter + 1;
+    or_rqr_solve(n, n, s, Q, R, Qs, sv);
+    or_rqr_fact(n, s, sv, n, Qs, Rs);
+    double trace = 0;
+    for (int i = 0; i < s; ++i) trace += Rs[i + s * i];
+    err = fabs(trace - trace_old) / trace0;
+    trace_old = trace;
+  }
+  memcpy(vec, Qs, sizeof(double) * n * s);
+  free(A); free(Q); free(R); free(sv); free(Qs); free(Rs);
+  return OR_OK;
+}
+
+/* rcompute_U0: rebuild the Krylov basis v_1 = b, v_{i+1} = (A v_i -
+ * sum_{l=max(1,i-s)}^{i} v_l H(l,i)) / H(i+1,i) from the Hessenberg matrix
+ * H(ldh, >= nritz) and accumulate U0(:,j) = sum_i eigvec(i,j) v_i.  With
+ * resnrm (length ns) the columns are normalised and the Ritz residual norms
+ * returned.  M: optional preconditioner (A*(v/M)). */
+int or_rcompute_U0(const or_mat *A, const or_mat *M, int n, const double *H, int ldh, int nritz,
+                   const double *eigvec, int ns, const double *b, double *U0, double *resnrm) {
+  const int s = ns;
+  double *W = calloc((size_t)n * (s + 1), sizeof(double)), *v = malloc(sizeof(double) * n),
+         *t = malloc(sizeof(double) * n), *u = malloc(sizeof(double) * n);
+  int *ind = calloc(nritz + 1, sizeof(int));
+  for (long q = 0; q < (long)n * s; ++q) U0[q] = 0;
+  memcpy(v, b, sizeof(double) * n);
+  int k = 0;
+  for (int i = 1; i <= nritz; ++i) {
+    k = k + 1;
+    if (k > s + 1) k = 1;
+    ind[i] = k;
+    memcpy(W + (size_t)n * (k - 1), v, sizeof(double) * n);
+    for (int j = 0; j < s; ++j) {
+      double e = eigvec[(i - 1) + (size_t)nritz * j];
+      double *uj = U0 + (size_t)n * j;
+      for (int q = 0; q < n; ++q) uj[q] = uj[q] + e * v[q];
+    }
+    int low = i - s > 1 ? i - s : 1;
+    if (M) {
+      or_precon_r(M, n, v, u);
+      or_matvec_r(A, n, u, t);
+    } else {
+      or_matvec_r(A, n, v, t);
+    }
+    double hd = H[i + (size_t)ldh * (i - 1)];
+    for (int q = 0; q < n; ++q) {
+      double acc = 0;
+      for (int l = low; l <= i; ++l) acc += W[q + (size_t)n * (ind[l] - 1)] * H[(l - 1) + (size_t)ldh * (i - 1)];
+      v[q] = (t[q] - acc) / hd;
+    }
+  }
+  if (resnrm) {
+    double nv = or_norm_r(n, v);
+    for (int j = 0; j < s; ++j) {
+      double *uj = U0 + (size_t)n * j;
+      double nrm = or_norm_r(n, uj);
+      for (int q = 0; q < n; ++q) uj[q] = uj[q] / nrm;
+      resnrm[j] = nv * fabs(H[nritz + (size_t)ldh * (nritz - 1)]) *
+                  fabs(eigvec[(nritz - 1) + (size_t)nritz * j]) / nrm;
+    }
+  }
+  free(W); free(v); free(t); free(u); free(ind);
+  return OR_OK;
+}
+
+/* global_RQR_factorization: modified Gram-Schmidt with global inner products.
+ * Q(n x s) may alias V.  R(s x s) optional.  OR_EARG: dependent columns. */
+int or_rglobal_qr(int n, int s, const double *V, double *Q, double *R) {
+  if (Q != V) memcpy(Q, V, sizeof(double) * n * s);
+  double *Rl = calloc((size_t)s * s, sizeof(double));
+  int st = OR_OK;
+  for (int j = 0; j < s && st == OR_OK; ++j) {
+    double *qj = Q + (size_t)n * j;
+    for (int i = 0; i < j; ++i) {
+      const double *qi = Q + (size_t)n * i;
+      double r = 0;
+      for (int q = 0; q < n; ++q) r += qi[q] * qj[q];
+      Rl[i + s * j] = r;
+      for (int q = 0; q < n; ++q) qj[q] = qj[q] - r * qi[q];
+    }
+    Rl[j + s * j] = or_norm_r(n, qj);
+    if (Rl[j + s * j] > DBL_MIN) {
+      for (int q = 0; q < n; ++q) qj[q] = qj[q] / Rl[j + s * j];
+    } else {
+      st = OR_EARG;
+    }
+  }
+  if (R) memcpy(R, Rl, sizeof(double) * s * s);
+  free(Rl);
+  return st;
+}
+
+/* omega = 1/Re(Ritz values of Hf(1:n_omega,1:n_omega)) (|Re| < eps -> 1),
+ * ordered greedily: step i takes the omega whose Ritz value maximises |p|
+ * over positions i..n_omega, then p *= 1 - Re(ritz) omega(i). */
+int or_ritz_omega(const double *Hf, int ldh, int n_omega, double *omega) {
+  if (n_omega < 1) return OR_EARG;
+  or_cplx *rv = malloc(sizeof(or_cplx) * n_omega);
+  double *p = malloc(sizeof(double) * n_omega);
+  int converged = 0;
+  or_rqr_eig(Hf, ldh, n_omega, rv, &converged);
+  for (int i = 0; i < n_omega; ++i) {
+    double w = creal(rv[i]);
+    if (fabs(w) < DBL_EPSILON) w = 1.;
+    omega[i] = 1. / w;
+    p[i] = 1.;
+  }
+  for (int i = 0; i < n_omega; ++i) {
+    int mp = i;
+    for (int k = i + 1; k < n_omega; ++k)
+      if (fabs(p[k]) > fabs(p[mp])) mp = k;
+    double mo = omega[mp];
+    omega[mp] = omega[i];
+    omega[i] = mo;
+    for (int k = 0; k < n_omega; ++k) p[k] = p[k] * (1. - creal(rv[k]) * omega[i]);
+  }
+  free(rv); free(p);
+  return OR_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* IDRS_RITZ: M/IDRS/ritz_module.f90:389-556 with its H, omega and U0       */
+/* outputs (U0: SI_power Schur vectors of Hf, compute_U0, global QR).       */
 /* ------------------------------------------------------------------------ */
 int or_idrs_ritz_r(const or_mat *A, int n, const double *b, int s, const or_opts *o, double *x,
                    int *nritz) {
+  return or_idrs_ritz_rx(A, n, b, s, o, x, nritz, NULL, 0, NULL, 0, 0);
+}
+
+int or_idrs_ritz_rx(const or_mat *A, int n, const double *b, int s, const or_opts *o, double *x,
+                    int *nritz, double *omega, int n_omega, double *U0, int dimU0,
+                    uint64_t si_seed) {
   double tol = (o && o->tolerance) ? *o->tolerance : (double)1e-6f;
   if (tol < 0) return OR_EARG;
   int maxit = (2 * n < 1000) ? 2 * n : 1000;
@@ -697,7 +894,8 @@ int or_idrs_ritz_r(const or_mat *A, int n, const double *b, int s, const or_opts
   io.PT = o ? o->PT : NULL; io.p_seed = o ? o->p_seed : 0;
   int st = or_idrs_r(A, n, b, s, &io, x);
   if (st != OR_OK) { free(Hf); free(resnrm); free(xs); return st; }
-  if (nritz) *nritz = (iter / (s + 1)) * s + iter % (s + 1);
+  const int nr = (iter / (s + 1)) * s + iter % (s + 1);
+  if (nritz) *nritz = nr;
   if (o && o->flag) *o->flag = conv;
   if (o && o->relres) *o->relres = relnrm;
   if (o && o->iterations) *o->iterations = iter;
@@ -708,8 +906,29 @@ int or_idrs_ritz_r(const or_mat *A, int n, const double *b, int s, const or_opts
     for (int j = 0; j < o->H_cols; ++j)
       for (int i = 0; i < o->H_rows; ++i) H[i + (size_t)o->H_rows * j] = Hf[i + (size_t)(maxit + 1) * j];
   }
+  if (omega && n_omega > 0) {
+    if (nr < n_omega) st = OR_EARG;  /* "Too many parameters omega requested" */
+    else or_ritz_omega(Hf, maxit + 1, n_omega, omega);
+  }
+  if (st == OR_OK && U0 && dimU0 > 0) {
+    if (nr < dimU0) st = OR_EARG;    /* "Recycle space is too large" */
+    else {
+      double *vec = malloc(sizeof(double) * nr * dimU0), *U = malloc(sizeof(double) * n * dimU0),
+             *resval = malloc(sizeof(double) * dimU0);
+      or_rsi_power(Hf, maxit + 1, nr, dimU0, 0.0, si_seed ? si_seed : 2, vec);
+      const or_mat *M = o ? o->M1 : NULL;
+      or_rcompute_U0(A, M, n, Hf, maxit + 1, nr, vec, dimU0, b, U, resval);
+      if (M)
+        for (int j = 0; j < dimU0; ++j) {
+          or_precon_r(M, n, U + (size_t)n * j, U0);
+          memcpy(U + (size_t)n * j, U0, sizeof(double) * n);
+        }
+      st = or_rglobal_qr(n, dimU0, U, U0, NULL);
+      free(vec); free(U); free(resval);
+    }
+  }
   free(Hf); free(resnrm); free(xs);
-  return OR_OK;
+  return st;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -724,68 +943,141 @@ static double or_wtime(void) {
 #endif
 }
 
-int or_pp_idrs_r(const or_umat *K, const or_umat *P, int n, const double *b, or_pp_args *a,
-                 double *x) {
-  double t0 = or_wtime();
-  or_mat *A;
-  or_matrix_create(K, P, NULL, 0, &A);
-  double *x0 = calloc(n, sizeof(double)), *y = malloc(sizeof(double) * n),
-         *t = malloc(sizeof(double) * n);
+/* real_preconditioner.inc:10-34: the initial IDRS_RITZ solve (which also
+ * yields x0 and, with n_omega > 0, the omega parameters) and the polynomial
+ * preconditioner.  *omega is allocated when the initial solve ran. */
+static int or_pp_setup_r(or_mat *A, int n, const double *b, or_pp_args *a, double *x0,
+                         double **omega) {
   int preconditioner = a->degree == 0 ? 0 : a->preconditioner;
   int estimate = 1;
   if (preconditioner == 0) estimate = 0;
   if (preconditioner == 1 && a->center) estimate = 0;
   if (preconditioner == 2 && a->foci) estimate = 0;
+  int initial = estimate || a->n_omega > 0;
   a->ritz_iterations = 0; a->nritz_used = 0;
+  *omega = NULL;
   int st = OR_OK;
-  if (estimate) {
+  double *H = NULL;
+  int ldh = 0;
+  if (initial) {
     int ini_iter = a->n_ritz + a->n_ritz / a->s;
-    int ldh = ini_iter + 1;
-    double *H = calloc((size_t)ldh * ini_iter, sizeof(double));
+    ldh = ini_iter + 1;
+    H = calloc((size_t)ldh * ini_iter, sizeof(double));
+    *omega = calloc(a->n_omega > 0 ? a->n_omega : 1, sizeof(double));
     int flag = -1, iter = 0, one = 1, nritz = 0; double relres = 1;
     or_opts o; memset(&o, 0, sizeof o);
     o.tolerance = &a->tol; o.maximum_iterations = &ini_iter; o.variant = &one;
     o.flag = &flag; o.relres = &relres; o.iterations = &iter;
     o.H = H; o.H_rows = ldh; o.H_cols = ini_iter; o.p_seed = a->p_seed;
-    st = or_idrs_ritz_r(A, n, b, a->s, &o, x0, &nritz);
+    st = or_idrs_ritz_rx(A, n, b, a->s, &o, x0, &nritz, *omega, a->n_omega, NULL, 0, 0);
     a->ritz_iterations = iter;
     a->nritz_used = (iter / (a->s + 1)) * a->s + iter % (a->s + 1);
-    if (st == OR_OK) {
+    for (int i = 0; i < a->n_omega && i < 64; ++i) a->omega_used[i] = (*omega)[i];
+  }
+  if (st == OR_OK) {
+    if (estimate) {
       or_ranalyse_spectrum(H, ldh, a->nritz_used, a->foci_used, &a->center_used, NULL);
       st = or_real_preconditioner(A, preconditioner, a->degree, NULL, NULL, H, ldh, a->nritz_used);
+    } else {
+      double f[2] = {0.15, 1.85}, c = 1.;
+      if (a->foci) { f[0] = a->foci[0]; f[1] = a->foci[1]; }
+      if (a->center) c = *a->center;
+      a->foci_used[0] = f[0]; a->foci_used[1] = f[1]; a->center_used = c;
+      st = or_real_preconditioner(A, preconditioner, a->degree, f, &c, NULL, 0, 0);
     }
-    free(H);
+  }
+  if (st == OR_OK)
+    for (int i = 0; i <= A->degree && i < 64; ++i) a->alpha_p[i] = A->ralpha_p ? A->ralpha_p[i] : 1.;
+  free(H);
+  return st;
+}
+
+/* One solve of run_idrs.inc:9-60 / run_mr_idrs.inc:15-72: y from the
+ * selected method with x0, U0 and omega, x = scaleback(A, b, y) and the
+ * relative residual of the original system. */
+static int or_pp_solve_r(const or_mat *A, const or_umat *K, int n, const double *b,
+                         const or_pp_args *a, const double *x0, const double *U0,
+                         const double *omega, double *y, double *x, int *flag, int *iter,
+                         double *relres, double *relres_original) {
+  or_opts o; memset(&o, 0, sizeof o);
+  double tol = a->tol; int maxit = a->maxit, in_s = a->in_s, in_it = a->in_it;
+  double in_tol = a->in_tol;
+  o.tolerance = &tol; o.maximum_iterations = &maxit; o.x0 = x0; o.p_seed = a->p_seed;
+  o.flag = flag; o.relres = relres; o.iterations = iter;
+  if (omega && a->n_omega > 0) { o.omega = omega; o.n_omega = a->n_omega; }
+  int variant = a->method == 2 ? 2 : 1, st;
+  if (a->method == 0) {
+    o.inner_s = &in_s; o.inner_tolerance = &in_tol; o.inner_iterations = &in_it;
+    st = or_qmridr_r(A, n, b, a->s, &o, y);
   } else {
-    double f[2] = {0.15, 1.85}, c = 1.;
-    if (a->foci) { f[0] = a->foci[0]; f[1] = a->foci[1]; }
-    if (a->center) c = *a->center;
-    a->foci_used[0] = f[0]; a->foci_used[1] = f[1]; a->center_used = c;
-    st = or_real_preconditioner(A, preconditioner, a->degree, f, &c, NULL, 0, 0);
+    o.variant = &variant;
+    o.U0 = U0;
+    st = or_idrs_r(A, n, b, a->s, &o, y);
+  }
+  if (st != OR_OK) return st;
+  double *t = malloc(sizeof(double) * n);
+  or_scaleback_r(A, n, b, y, x);
+  or_user_mv_r(K, x, t);
+  for (int i = 0; i < n; ++i) t[i] = b[i] - t[i];
+  *relres_original = or_norm_r(n, t) / or_norm_r(n, b);
+  free(t);
+  return OR_OK;
+}
+
+int or_pp_idrs_r(const or_umat *K, const or_umat *P, int n, const double *b, or_pp_args *a,
+                 double *x) {
+  double t0 = or_wtime();
+  or_mat *A;
+  or_matrix_create(K, P, NULL, 0, &A);
+  double *x0 = calloc(n, sizeof(double)), *y = malloc(sizeof(double) * n), *omega = NULL;
+  int st = or_pp_setup_r(A, n, b, a, x0, &omega);
+  double t1 = or_wtime();
+  a->seconds_setup = t1 - t0;
+  if (st == OR_OK)
+    st = or_pp_solve_r(A, K, n, b, a, x0, NULL, omega, y, x, &a->flag, &a->iterations,
+                       &a->relres_solver, &a->relres_original);
+  a->seconds_solve = or_wtime() - t1;
+  free(x0); free(y); free(omega);
+  or_matrix_free(A);
+  return st;
+}
+
+int or_pp_mr_idrs_r(const or_umat *K, const or_umat *P, int n, int nrhs, const double *b_all,
+                    or_pp_args *a, double *x_all) {
+  if (nrhs < 1) return OR_EARG;
+  double t0 = or_wtime();
+  or_mat *A;
+  or_matrix_create(K, P, NULL, 0, &A);
+  double *x0 = calloc(n, sizeof(double)), *y = malloc(sizeof(double) * n), *omega = NULL,
+         *U0 = NULL;
+  int st = or_pp_setup_r(A, n, b_all, a, x0, &omega);
+  a->recycle_flag = 0; a->recycle_iterations = 0; a->recycle_relres = 0;
+  if (st == OR_OK && a->recycle) {  /* recycle.inc */
+    U0 = malloc(sizeof(double) * n * a->s);
+    int one = 1, nritz = 0, maxit = a->maxit;
+    double tol = a->tol;
+    or_opts o; memset(&o, 0, sizeof o);
+    o.tolerance = &tol; o.maximum_iterations = &maxit; o.variant = &one;
+    o.flag = &a->recycle_flag; o.relres = &a->recycle_relres; o.iterations = &a->recycle_iterations;
+    o.p_seed = a->p_seed;
+    st = or_idrs_ritz_rx(A, n, b_all, a->s, &o, x0, &nritz, NULL, 0, U0, a->s, a->si_seed);
   }
   double t1 = or_wtime();
   a->seconds_setup = t1 - t0;
-  if (st == OR_OK) {
-    for (int i = 0; i <= A->degree && i < 64; ++i) a->alpha_p[i] = A->ralpha_p ? A->ralpha_p[i] : 1.;
-    or_opts o; memset(&o, 0, sizeof o);
-    o.tolerance = &a->tol; o.maximum_iterations = &a->maxit; o.x0 = x0; o.p_seed = a->p_seed;
-    o.flag = &a->flag; o.relres = &a->relres_solver; o.iterations = &a->iterations;
-    int variant = a->method == 2 ? 2 : 1;
-    if (a->method == 0) {
-      o.inner_s = &a->in_s; o.inner_tolerance = &a->in_tol; o.inner_iterations = &a->in_it;
-      st = or_qmridr_r(A, n, b, a->s, &o, y);
-    } else {
-      o.variant = &variant;
-      st = or_idrs_r(A, n, b, a->s, &o, y);
-    }
-  }
-  if (st == OR_OK) {
-    or_scaleback_r(A, n, b, y, x);
-    or_user_mv_r(K, x, t);
-    for (int i = 0; i < n; ++i) t[i] = b[i] - t[i];
-    a->relres_original = or_norm_r(n, t) / or_norm_r(n, b);
+  for (int irhs = 0; irhs < nrhs && st == OR_OK; ++irhs) {
+    const double *b = b_all + (size_t)n * irhs;
+    int flag = -1, iter = 0; double rel = 1, relo = 1;
+    st = or_pp_solve_r(A, K, n, b, a, x0, U0, omega, y, x_all + (size_t)n * irhs, &flag, &iter,
+                       &rel, &relo);
+    memcpy(x0, y, sizeof(double) * n);  /* warm start: the preconditioned solution */
+    if (a->flags) a->flags[irhs] = flag;
+    if (a->iters) a->iters[irhs] = iter;
+    if (a->relres_solver_all) a->relres_solver_all[irhs] = rel;
+    if (a->relres_original_all) a->relres_original_all[irhs] = relo;
+    a->flag = flag; a->iterations = iter; a->relres_solver = rel; a->relres_original = relo;
   }
   a->seconds_solve = or_wtime() - t1;
-  free(x0); free(y); free(t);
+  free(x0); free(y); free(omega); free(U0);
   or_matrix_free(A);
   return st;
 }

@@ -163,9 +163,21 @@ int or_msqmridr_r(const or_mat *A, int n, const double *b, int n_sigma, const do
 int or_msqmridr_c(const or_mat *A, int n, const or_cplx *b, int n_sigma, const or_cplx *sigma,
                   int s, const or_opts *o, or_cplx *x);
 
-/* ---- ritz_module (H output only; recycling is out of scope) ---- */
+/* ---- ritz_module ----
+ * or_idrs_ritz_rx: IDRS_RITZ with the H output (o->H), omega(n_omega) and
+ * the recycle space U0(n x dimU0) (NULL / 0: not requested).  si_seed seeds
+ * the start block of SI_power (0: seed 2). */
 int or_idrs_ritz_r(const or_mat *A, int n, const double *b, int s, const or_opts *o,
                    double *x, int *nritz);
+int or_idrs_ritz_rx(const or_mat *A, int n, const double *b, int s, const or_opts *o,
+                    double *x, int *nritz, double *omega, int n_omega, double *U0, int dimU0,
+                    uint64_t si_seed);
+int or_rsi_power(const double *H, int ldh, int n, int s, double shift, uint64_t seed,
+                 double *vec);
+int or_rcompute_U0(const or_mat *A, const or_mat *M, int n, const double *H, int ldh, int nritz,
+                   const double *eigvec, int ns, const double *b, double *U0, double *resnrm);
+int or_rglobal_qr(int n, int s, const double *V, double *Q, double *R);
+int or_ritz_omega(const double *Hf, int ldh, int n_omega, double *omega);
 
 /* ---- pp_idrs pipeline (real, single right-hand side) ----
  * method: 1 idrs, 2 bicgstab, 0 qmridr.  preconditioner: 0 none, 1 neumann,
@@ -181,9 +193,22 @@ typedef struct or_pp_args {
   double foci_used[2], center_used;
   double alpha_p[64];
   double seconds_setup, seconds_solve; /* wall clock of the set-up and the solve */
+  /* -omega and -recycle (initialize.inc:162-163) */
+  int n_omega, recycle;
+  uint64_t si_seed;
+  double omega_used[64];
+  int recycle_flag, recycle_iterations;
+  double recycle_relres;
+  /* per right-hand side outputs of or_pp_mr_idrs_r (arrays of nrhs; may be NULL) */
+  int *flags, *iters;
+  double *relres_solver_all, *relres_original_all;
 } or_pp_args;
 int or_pp_idrs_r(const or_umat *K, const or_umat *P, int n, const double *b, or_pp_args *a,
                  double *x);
+/* PP_MR_IDRS (real): pp_idrs_module.f90:222-279 with real_preconditioner.inc,
+ * recycle.inc and run_mr_idrs.inc.  b_all, x_all: n x nrhs column-major. */
+int or_pp_mr_idrs_r(const or_umat *K, const or_umat *P, int n, int nrhs, const double *b_all,
+                    or_pp_args *a, double *x_all);
 
 /* ---- adjoint (new; no counterpart in the reference) ----
  * grad = -lambda_i * x_j over the CRS pattern of K. */

@@ -63,6 +63,13 @@ class PPArgs(C.Structure):
         ("foci_used", C.c_double * 2), ("center_used", C.c_double),
         ("alpha_p", C.c_double * 64),
         ("seconds_setup", C.c_double), ("seconds_solve", C.c_double),
+        ("n_omega", C.c_int), ("recycle", C.c_int),
+        ("si_seed", C.c_uint64),
+        ("omega_used", C.c_double * 64),
+        ("recycle_flag", C.c_int), ("recycle_iterations", C.c_int),
+        ("recycle_relres", C.c_double),
+        ("flags", c_int_p), ("iters", c_int_p),
+        ("relres_solver_all", c_dbl_p), ("relres_original_all", c_dbl_p),
     ]
 
 
@@ -494,9 +501,8 @@ def analyse_spectrum(H):
     return f, c.value, sh.value
 
 
-def pp_idrs(K: UserMatrix, b, *, P: UserMatrix | None = None, method=1, s=4, tol=1e-6, maxit=1000,
-            in_s=4, in_tol=0.1, in_it=0, preconditioner=0, degree=0, n_ritz=32, foci=None,
-            center=None, p_seed=1):
+def _pp_args(method, s, tol, maxit, in_s, in_tol, in_it, preconditioner, degree, n_ritz, foci,
+             center, p_seed, n_omega=0, recycle=False, si_seed=0):
     a = PPArgs()
     a.method, a.s, a.maxit, a.in_s, a.in_it = method, s, maxit, in_s, in_it
     a.preconditioner, a.degree, a.n_ritz = preconditioner, degree, n_ritz
@@ -507,16 +513,102 @@ def pp_idrs(K: UserMatrix, b, *, P: UserMatrix | None = None, method=1, s=4, tol
     if center is not None:
         c = C.c_double(center); keep.append(c); a.center = C.pointer(c)
     a.p_seed = p_seed
+    a.n_omega, a.recycle, a.si_seed = int(n_omega), int(bool(recycle)), int(si_seed)
+    return a, keep
+
+
+def _pp_common(a, degree):
+    return dict(ritz_iterations=a.ritz_iterations, nritz=a.nritz_used,
+                foci=tuple(a.foci_used), center=a.center_used,
+                alpha_p=np.array(a.alpha_p[: degree + 1]),
+                omega=np.array(a.omega_used[: a.n_omega]),
+                seconds_setup=a.seconds_setup, seconds_solve=a.seconds_solve)
+
+
+def pp_idrs(K: UserMatrix, b, *, P: UserMatrix | None = None, method=1, s=4, tol=1e-6, maxit=1000,
+            in_s=4, in_tol=0.1, in_it=0, preconditioner=0, degree=0, n_ritz=32, foci=None,
+            center=None, p_seed=1, n_omega=0):
+    a, keep = _pp_args(method, s, tol, maxit, in_s, in_tol, in_it, preconditioner, degree, n_ritz,
+                       foci, center, p_seed, n_omega)
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.empty_like(b)
     st = lib().or_pp_idrs_r(K.ptr, P.ptr if P else None, len(b), _p(b), C.byref(a), _p(x))
     if st:
         raise ValueError(f"or_pp_idrs status {st}")
-    return Result(x=x, flag=a.flag, iterations=a.iterations, ritz_iterations=a.ritz_iterations,
-                  nritz=a.nritz_used, relres=a.relres_solver, relres_original=a.relres_original,
-                  foci=tuple(a.foci_used), center=a.center_used,
-                  alpha_p=np.array(a.alpha_p[: degree + 1]),
-                  seconds_setup=a.seconds_setup, seconds_solve=a.seconds_solve)
+    return Result(x=x, flag=a.flag, iterations=a.iterations, relres=a.relres_solver,
+                  relres_original=a.relres_original, **_pp_common(a, degree))
+
+
+def pp_mr_idrs(K: UserMatrix, b_all, *, P: UserMatrix | None = None, method=1, s=4, tol=1e-6,
+               maxit=1000, in_s=4, in_tol=0.1, in_it=0, preconditioner=0, degree=0, n_ritz=32,
+               foci=None, center=None, p_seed=1, n_omega=0, recycle=False, si_seed=0):
+    """PP_MR_IDRS (pp_idrs_module.f90:222-279): b_all is n x nrhs."""
+    a, keep = _pp_args(method, s, tol, maxit, in_s, in_tol, in_it, preconditioner, degree, n_ritz,
+                       foci, center, p_seed, n_omega, recycle, si_seed)
+    b_all = np.asfortranarray(b_all, dtype=np.float64)
+    n, nrhs = b_all.shape
+    x_all = np.zeros((n, nrhs), order="F")
+    flags, iters = np.zeros(nrhs, np.int32), np.zeros(nrhs, np.int32)
+    rel, relo = np.zeros(nrhs), np.zeros(nrhs)
+    a.flags, a.iters = flags.ctypes.data_as(c_int_p), iters.ctypes.data_as(c_int_p)
+    a.relres_solver_all, a.relres_original_all = rel.ctypes.data_as(c_dbl_p), relo.ctypes.data_as(c_dbl_p)
+    st = lib().or_pp_mr_idrs_r(K.ptr, P.ptr if P else None, n, nrhs, _p(b_all), C.byref(a), _p(x_all))
+    if st:
+        raise ValueError(f"or_pp_mr_idrs status {st}")
+    return Result(x=x_all, flags=flags, iterations=iters, relres=rel, relres_original=relo,
+                  recycle_flag=a.recycle_flag, recycle_iterations=a.recycle_iterations,
+                  recycle_relres=a.recycle_relres, **_pp_common(a, degree))
+
+
+def idrs_ritz(A: Matrix, b, s, *, n_omega=0, dimU0=0, si_seed=0, H_shape=None, **kw):
+    """IDRS_RITZ (ritz_module.f90:389-556) with its H, omega and U0 outputs."""
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    o, keep, outs = _opts(len(b), np.float64, H_shape=H_shape, **kw)
+    x = np.empty_like(b)
+    nritz = C.c_int(0)
+    om = np.zeros(max(n_omega, 1))
+    U0 = np.zeros((len(b), max(dimU0, 1)), order="F")
+    st = lib().or_idrs_ritz_rx(A.ptr, len(b), _p(b), int(s), C.byref(o), _p(x), C.byref(nritz),
+                               _p(om) if n_omega else None, int(n_omega),
+                               _p(U0) if dimU0 else None, int(dimU0), C.c_uint64(si_seed))
+    if st:
+        raise ValueError(f"or_idrs_ritz status {st}")
+    r = _result(x, outs)
+    r["nritz"] = nritz.value
+    if n_omega:
+        r["omega"] = om
+    if dimU0:
+        r["U0"] = U0
+    return r
+
+
+def si_power(H, s, shift=0.0, seed=2):
+    """RSI_power (dense_la_module.f90:531-603); H is n x n."""
+    H = np.asfortranarray(H, dtype=np.float64)
+    n = H.shape[1]
+    vec = np.zeros((n, s), order="F")
+    st = lib().or_rsi_power(_p(H), H.shape[0], n, int(s), C.c_double(shift), C.c_uint64(seed), _p(vec))
+    if st:
+        raise ValueError(f"or_rsi_power status {st}")
+    return vec
+
+
+def global_qr(V):
+    V = np.asfortranarray(V, dtype=np.float64)
+    n, s = V.shape
+    Q = np.zeros((n, s), order="F")
+    R = np.zeros((s, s), order="F")
+    st = lib().or_rglobal_qr(n, s, _p(V), _p(Q), _p(R))
+    if st:
+        raise ValueError("V has dependent columns")
+    return Q, R
+
+
+def ritz_omega(H, n_omega):
+    H = np.asfortranarray(H, dtype=np.float64)
+    om = np.zeros(n_omega)
+    lib().or_ritz_omega(_p(H), H.shape[0], int(n_omega), _p(om))
+    return om
 
 
 def crs_transpose(K: UserMatrix) -> UserMatrix:

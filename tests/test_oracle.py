@@ -204,3 +204,113 @@ def test_adjoint_oracle(oracle, P):
         e[k] = eps
         fd = central(np.linalg.solve(D, e), np.linalg.solve(D, -e))
         assert abs(fd - lam[k]) <= 1e-5 * abs(lam[k])
+
+
+# --------------------------------------------------------------------------
+# recycling: IDRS_RITZ's omega and U0 outputs, PP_MR_IDRS
+# --------------------------------------------------------------------------
+def _mgs(V, refine):
+    """Modified Gram-Schmidt QR (refine sweeps per column), numpy."""
+    Q = np.array(V, dtype=float, copy=True)
+    R = np.zeros((V.shape[1], V.shape[1]))
+    for j in range(V.shape[1]):
+        for _ in range(refine):
+            for i in range(j):
+                t = Q[:, i] @ Q[:, j]
+                Q[:, j] -= t * Q[:, i]
+                R[i, j] += t
+        R[j, j] = np.linalg.norm(Q[:, j])
+        Q[:, j] /= R[j, j]
+    return Q, R
+
+
+def _ritz_problem(oracle, P, n=10, s=4, seed=0):
+    coef = P.cdr_coefficients(n)
+    rp, ci, vals = P.stencil_to_crs(n, n, n, coef)
+    K = oracle.crs_format(n ** 3, n ** 3, rp, ci, vals)
+    b = np.random.default_rng(seed).standard_normal(n ** 3)
+    return K, oracle.Matrix(K), b
+
+
+def test_si_power_matches_numpy(oracle, P):
+    """RSI_power (dense_la_module.f90:531-603) restated in numpy from the same
+    counter-based start block: block inverse iteration with MGS(refine 2)
+    re-orthonormalisation until the summed column lengths change by <= 1e-3
+    of the start block's."""
+    K, A, b = _ritz_problem(oracle, P)
+    s = 4
+    r = oracle.idrs(A, b, s, tolerance=1e-8, maximum_iterations=200, H_shape=(201, 200))
+    nr = (r.iterations // (s + 1)) * s + r.iterations % (s + 1)
+    Hn = r.H[:nr, :nr]
+    Q, R = _mgs(Hn, 2)
+    X = np.array([oracle.uniform(2, k) for k in range(nr * s)]).reshape(s, nr).T
+    Qs, Rs = _mgs(X, 2)
+    tr0 = told = np.trace(Rs)
+    for _ in range(1000):
+        Qs, Rs = _mgs(np.linalg.solve(np.triu(R), Q.T @ Qs), 2)
+        err = abs(np.trace(Rs) - told) / tr0
+        told = np.trace(Rs)
+        if err <= 1e-3:
+            break
+    np.testing.assert_allclose(oracle.si_power(Hn, s), Qs, rtol=0, atol=1e-10)
+
+
+def test_ritz_omega_and_u0_match_numpy(oracle, P):
+    """IDRS_RITZ's omega ordering (ritz_module.f90:497-520) and the recycle
+    space (compute_U0 :100-160 + global QR :66-96) restated in numpy."""
+    K, A, b = _ritz_problem(oracle, P)
+    s, n_om = 4, 6
+    r = oracle.idrs_ritz(A, b, s, tolerance=1e-8, n_omega=n_om, dimU0=s)
+    h = oracle.idrs(A, b, s, tolerance=1e-8, H_shape=(1001, 1000))
+    assert r.iterations == h.iterations and r.flag == 0
+    nr = r.nritz
+    H = h.H
+    # omega: Ritz values of H(1:n_omega,1:n_omega) in QR_eig's order, greedy |p|
+    rv, _ = oracle.qr_eig(H[:n_om, :n_om])
+    om = 1.0 / np.where(np.abs(rv.real) < np.finfo(float).eps, 1.0, rv.real)
+    p = np.ones(n_om)
+    for i in range(n_om):
+        m = i + int(np.argmax(np.abs(p[i:])))
+        om[i], om[m] = om[m], om[i]
+        p *= 1.0 - rv.real * om[i]
+    np.testing.assert_allclose(r.omega, om, rtol=1e-12)
+    # U0: Krylov basis rebuilt from the Hessenberg recurrence, then MGS
+    vec = oracle.si_power(H[:nr, :nr], s)
+    V = [b.copy()]
+    U = np.zeros((len(b), s))
+    for i in range(nr):
+        U += np.outer(V[i], vec[i])
+        low = max(0, i - s)
+        acc = sum(V[l] * H[l, i] for l in range(low, i + 1))
+        V.append((A.matvec(V[i]) - acc) / H[i + 1, i])
+    U /= np.linalg.norm(U, axis=0)
+    Q, _ = _mgs(U, 1)
+    np.testing.assert_allclose(r.U0, Q, rtol=0, atol=1e-9)
+    assert np.abs(r.U0.T @ r.U0 - np.eye(s)).max() < 1e-12
+    with pytest.raises(ValueError):  # more omegas than Ritz values
+        oracle.idrs_ritz(A, b, s, tolerance=1e-8, maximum_iterations=3, n_omega=6)
+
+
+def test_pp_mr_idrs_oracle(oracle, P):
+    """PP_MR_IDRS: every right-hand side meets the tolerance on the original
+    system; the warm start makes a repeated right-hand side free, and the
+    recycle solve already solves b_all(:,1)."""
+    n = 10
+    coef = P.cdr_coefficients(n)
+    S = oracle.stencil7_format(n, n, n, coef)
+    D = oracle.real_precon(1, S)
+    rng = np.random.default_rng(1)
+    B = rng.standard_normal((n ** 3, 3))
+    B = np.column_stack([B, B[:, 1]])  # rhs 4 repeats rhs 2
+    r = oracle.pp_mr_idrs(S, B, P=D, s=4, tol=1e-8, preconditioner=2, degree=4, n_ritz=12,
+                          n_omega=3)
+    assert list(r.flags) == [0, 0, 0, 0]
+    assert np.all(r.relres_original < 1e-7)
+    for j in range(B.shape[1]):
+        res = B[:, j] - S.mv(r.x[:, j])
+        assert np.linalg.norm(res) <= 1e-7 * np.linalg.norm(B[:, j])
+    rr = oracle.pp_mr_idrs(S, B[:, :2], P=D, s=4, tol=1e-8, recycle=True)
+    assert rr.recycle_flag == 0 and rr.recycle_iterations > 0
+    assert rr.iterations[0] == 0 and rr.flags[1] == 0
+    same = oracle.pp_mr_idrs(S, np.column_stack([B[:, 0], B[:, 0]]), s=4, tol=1e-8)
+    assert same.iterations[1] <= 1
