@@ -62,6 +62,7 @@ _PROTOS = {
     "idrs_cuser_mv": (_i, [_vp, _vp, _vp]),
     "idrs_user_matrix_free": (_i, [_vp]),
     "idrs_matrix_create": (_i, [_vp, _vp, _i, _vp, _vp]),
+    "idrs_matrix_create_ext": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _i, _vp]),
     "idrs_matrix_free": (_i, [_vp]),
     "idrs_matrix_set_stream": (_i, [_vp, _vp]),
     "idrs_matrix_set_pointer_mode": (_i, [_vp, _i]),
@@ -320,17 +321,24 @@ def complex_diagonal(K: UserMatrix):
 # matrix_module
 # ---------------------------------------------------------------------------
 class Matrix:
-    """type(matrix) (M/PP_MATRIX/matrix_module.f90:38-81): K, the diagonal
-    preconditioner P, the seed shift and the polynomial preconditioner."""
+    """type(matrix) (M/PP_MATRIX/matrix_module.f90:38-81): K, the mass and
+    damping matrices M and C, the diagonal preconditioner P, the seed shift
+    and the polynomial preconditioner.  With multishift and C the operator
+    is the 2n x 2n block system (vectors of length 2n)."""
 
     __array_ufunc__ = None  # `v / A` must reach __rtruediv__ with the whole vector
 
-    def __init__(self, K: UserMatrix, P: UserMatrix | None = None, seed=None, complex=False):
-        self.K, self.P, self.cplx, self.n = K, P, bool(complex), K.nrows
+    def __init__(self, K: UserMatrix, P: UserMatrix | None = None, seed=None, complex=False,
+                 M: UserMatrix | None = None, C_: UserMatrix | None = None, multishift=False):
+        self.K, self.P, self.cplx = K, P, bool(complex)
+        block = bool(multishift) and C_ is not None
+        self.n = 2 * K.nrows if block else K.nrows
         sd = None if seed is None else np.array([np.real(seed), np.imag(seed)], dtype=np.float64)
         h = C.c_void_p()
-        _check(lib().idrs_matrix_create(K.handle, P.handle if P else None, int(self.cplx), _p(sd),
-                                        C.byref(h)))
+        _check(lib().idrs_matrix_create_ext(K.handle, M.handle if M else None,
+                                            C_.handle if C_ else None, P.handle if P else None,
+                                            int(self.cplx), _p(sd), int(bool(multishift)),
+                                            C.byref(h)))
         self.handle = h.value
         self.device_pointers = False
 

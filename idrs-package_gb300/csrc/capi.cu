@@ -1025,6 +1025,202 @@ int idrs_matrix_create(idrs_user_matrix K, idrs_user_matrix P, int is_complex, c
   });
 }
 
+}  // extern "C"
+
+// ------------------------------------------------- mass / damping systems
+namespace {
+
+// One CRS term of an assembled system row: coef * M(row, :) at column offset.
+struct SysTerm {
+  const int* rp = nullptr; const int* ci = nullptr; const void* val = nullptr;
+  bool vcplx = false; c128 coef; int col_off = 0;
+};
+
+// Output row r of the assembled matrix.  Rows r < nn concatenate the terms'
+// rows r (and an optional diagonal entry diag_top at (r, r)); rows nn + i of
+// the block system hold 1 at (nn+i, i) and, with a seed, -seed at (nn+i, nn+i).
+template <class V>
+__global__ void k_sys_fill(int nn, int nrows, const int* __restrict__ rp_out, int* ci_out,
+                           V* val_out, SysTerm t0, SysTerm t1, SysTerm t2, int nterms,
+                           bool has_diag_top, c128 diag_top, bool block, c128 low_diag) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
+    int o = rp_out[r];
+    if (r < nn) {
+      const SysTerm ts[3] = {t0, t1, t2};
+      for (int q = 0; q < nterms; ++q) {
+        const SysTerm& t = ts[q];
+        for (int k = t.rp[r]; k < t.rp[r + 1]; ++k, ++o) {
+          ci_out[o] = t.ci[k] + t.col_off;
+          c128 v = t.vcplx ? ((const c128*)t.val)[k] : c128(((const double*)t.val)[k], 0.0);
+          val_out[o] = narrow<V>(t.coef * v);
+        }
+      }
+      if (has_diag_top) { ci_out[o] = r; val_out[o] = narrow<V>(diag_top); }
+    } else if (block) {
+      const int i = r - nn;
+      ci_out[o] = i;
+      val_out[o] = narrow<V>(c128(1.0, 0.0));
+      if (low_diag.x != 0.0 || low_diag.y != 0.0) { ci_out[o + 1] = r; val_out[o + 1] = narrow<V>(low_diag); }
+    }
+  }
+}
+
+// D = [P; 1] for the block system (rprecon scales the first half only)
+__global__ void k_block_diag(long nn, const void* pd, bool pcplx, bool uniform, c128 pu, bool ocplx,
+                             void* out) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < 2 * nn; i += gridDim.x * (long)blockDim.x) {
+    c128 v(1.0, 0.0);
+    if (i < nn) v = uniform ? pu : (pcplx ? ((const c128*)pd)[i] : c128(((const double*)pd)[i], 0.0));
+    if (ocplx) ((c128*)out)[i] = v;
+    else ((double*)out)[i] = v.x;
+  }
+}
+
+std::vector<int> host_row_ptr(const UserMatrix& M) {
+  std::vector<int> rp(M.nrows + 1);
+  IDRS_CUDA(cudaMemcpy(rp.data(), M.row_ptr, sizeof(int) * (M.nrows + 1), cudaMemcpyDeviceToHost));
+  return rp;
+}
+
+// The system matrix of real_mv / complex_mv (matrix_module.f90:170-264)
+// assembled once as one CRS matrix, so that each product is a single SpMV:
+//   standard: K + seed C + seed^2 M | K + seed C + seed^2 I | K - seed M
+//   block (multishift with C), 2nn x 2nn:
+//     [ -C - seed M   -K      ]   (without M: -seed I in the (1,1) block)
+//     [  I            -seed I ]
+idrs_user_matrix assemble_system(const UserMatrix& K, const UserMatrix* Mm, const UserMatrix* Cm,
+                                 c128 seed, bool block) {
+  const int nn = K.nrows;
+  const bool seeded = seed.x != 0.0 || seed.y != 0.0;
+  auto term = [&](const UserMatrix& M, c128 coef, int off) {
+    SysTerm t;
+    t.rp = M.row_ptr; t.ci = M.col_ind; t.val = M.val; t.vcplx = M.vals == 2; t.coef = coef; t.col_off = off;
+    srcs.push_back(&M);
+    return t;
+  };
+  std::vector<SysTerm> terms;
+  std::vector<const UserMatrix*> srcs;
+  bool has_diag_top = false;
+  c128 diag_top(0.0, 0.0), low_diag(0.0, 0.0);
+  const c128 one(1.0, 0.0), mone(-1.0, 0.0);
+  if (block) {
+    terms.push_back(term(*Cm, mone, 0));
+    terms.push_back(term(K, mone, nn));
+    if (seeded) {
+      if (Mm) terms.push_back(term(*Mm, c128(-seed.x, -seed.y), 0));
+      else { has_diag_top = true; diag_top = c128(-seed.x, -seed.y); }
+      low_diag = c128(-seed.x, -seed.y);
+    }
+  } else {
+    terms.push_back(term(K, one, 0));
+    if (Cm) {
+      terms.push_back(term(*Cm, seed, 0));
+      if (Mm) terms.push_back(term(*Mm, seed * seed, 0));
+      else { has_diag_top = true; diag_top = seed * seed; }
+    } else if (Mm) {
+      terms.push_back(term(*Mm, c128(-seed.x, -seed.y), 0));
+    }
+  }
+  std::vector<std::vector<int>> rps;
+  for (const UserMatrix* src : srcs) rps.push_back(host_row_ptr(*src));
+  const int nrows = block ? 2 * nn : nn;
+  std::vector<int> rp(nrows + 1, 0);
+  for (int r = 0; r < nrows; ++r) {
+    long len = 0;
+    if (r < nn) {
+      for (auto& h : rps) len += h[r + 1] - h[r];
+      if (has_diag_top) len += 1;
+    } else {
+      len = 1 + ((low_diag.x != 0.0 || low_diag.y != 0.0) ? 1 : 0);
+    }
+    REQUIRE((long)rp[r] + len <= INT32_MAX, "system matrix: more than 2^31 nonzeros");
+    rp[r + 1] = rp[r] + (int)len;
+  }
+  const long nnz = rp[nrows];
+  bool cplx = seed.y != 0.0 || K.vals == 2 || (Mm && Mm->vals == 2) || (Cm && Cm->vals == 2);
+  auto* S = new idrs_user_matrix_s();
+  S->format = FMT_CRS;
+  S->nrows = S->ncols = nrows;
+  S->nnz = nnz;
+  S->vals = cplx ? 2 : 1;
+  S->row_ptr = (int*)upload(rp.data(), sizeof(int) * (nrows + 1));
+  IDRS_CUDA(cudaMalloc((void**)&S->col_ind, sizeof(int) * std::max<long>(nnz, 1)));
+  IDRS_CUDA(cudaMalloc(&S->val, (cplx ? 16 : 8) * std::max<long>(nnz, 1)));
+  SysTerm t[3];
+  for (size_t q = 0; q < terms.size(); ++q) t[q] = terms[q];
+  const int grid = std::max(1, std::min((nrows + 255) / 256, num_sms() * 8));
+  if (cplx)
+    k_sys_fill<c128><<<grid, 256>>>(nn, nrows, S->row_ptr, S->col_ind, (c128*)S->val, t[0], t[1], t[2],
+                                    (int)terms.size(), has_diag_top, diag_top, block, low_diag);
+  else
+    k_sys_fill<double><<<grid, 256>>>(nn, nrows, S->row_ptr, S->col_ind, (double*)S->val, t[0], t[1], t[2],
+                                      (int)terms.size(), has_diag_top, diag_top, block, low_diag);
+  IDRS_LAUNCH_CHECK();
+  IDRS_CUDA(cudaDeviceSynchronize());
+  S->group = crs_group(nnz, nrows);
+  build_row_plan(*S, rp.data());
+  return S;
+}
+
+idrs_user_matrix block_diagonal(const UserMatrix& P, long nn) {
+  auto* D = new idrs_user_matrix_s();
+  D->format = P.format;
+  D->which_precon = 1;
+  D->nrows = D->ncols = (int)(2 * nn);
+  const bool ocplx = P.diag_cplx || (P.diag_uniform && P.diag_u.y != 0.0);
+  D->diag_cplx = ocplx;
+  IDRS_CUDA(cudaMalloc(&D->diag, (ocplx ? 16 : 8) * (size_t)(2 * nn)));
+  k_block_diag<<<stream_grid(2 * nn), kThreads>>>(nn, P.diag, P.diag_cplx, P.diag_uniform, P.diag_u, ocplx, D->diag);
+  IDRS_LAUNCH_CHECK();
+  IDRS_CUDA(cudaDeviceSynchronize());
+  return D;
+}
+
+}  // namespace
+
+extern "C" {
+
+int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix Mm, idrs_user_matrix Cm,
+                           idrs_user_matrix P, int is_complex, const double* seed, int multishift,
+                           idrs_matrix* A) {
+  return guard([&] {
+    REQUIRE(K && A, "matrix_create: bad arguments");
+    if (!Mm && !Cm) return idrs_matrix_create(K, P, is_complex, seed, A);
+    REQUIRE(K->nrows == K->ncols, "matrix_create: K must be square");
+    for (const UserMatrix* X : {(const UserMatrix*)Mm, (const UserMatrix*)Cm}) {
+      if (!X) continue;
+      REQUIRE(X->nrows == K->nrows && X->ncols == K->ncols, "matrix_create: M and C must match K");
+      if (X->format != FMT_CRS)
+        throw unsupported_error("matrix_create: mass and damping matrices must be CRS");
+    }
+    if (K->format != FMT_CRS)
+      throw unsupported_error("matrix_create: with mass or damping matrices K must be CRS");
+    REQUIRE(!P || P->nrows == K->nrows, "matrix_create: P size mismatch");
+    REQUIRE(!P || P->which_precon == 1, "matrix_create: only a diagonal P is supported here");
+    init_runtime();
+    const bool cplx = is_complex != 0;
+    c128 sd(0.0, 0.0);
+    if (seed) sd = cplx ? c128(seed[0], seed[1]) : c128(seed[0], 0.0);
+    const bool block = multishift && Cm;
+    const bool seeded = sd.x != 0.0 || sd.y != 0.0;
+    idrs_user_matrix S = nullptr, D = nullptr;
+    if (block || seeded) S = assemble_system(*K, Mm, Cm, sd, block);
+    if (block && P) D = block_diagonal(*P, K->nrows);
+    // an assembled matrix already holds the seed: build without it, then
+    // record it for the parameters derived from it (foci, centre, shifts)
+    int st = idrs_matrix_create(S ? S : K, D ? D : P, is_complex, S ? nullptr : seed, A);
+    // the operator holds its own references
+    if (S) user_matrix_release(S);
+    if (D) user_matrix_release(D);
+    if (st) return st;
+    if (S) {
+      (*A)->seed = sd;
+      (*A)->seed_folded = true;
+    }
+    return IDRS_OK;
+  });
+}
+
 int idrs_matrix_free(idrs_matrix A) {
   return guard([&] {
     if (A) {

@@ -1322,13 +1322,15 @@ int build_operator(Operator* A) {
       IDRS_LAUNCH_CHECK();
     }
   }
-  bool seeded = (A->seed.x != 0.0 || A->seed.y != 0.0);
   if (!A->cplx && A->seed.y != 0.0) { set_error("complex seed on a real problem"); return 1; }
+  // a seed already folded into an assembled system matrix is not applied again
+  const c128 es = A->seed_folded ? c128(0.0, 0.0) : A->seed;
+  bool seeded = (es.x != 0.0 || es.y != 0.0);
   if (K.format == FMT_STENCIL7) {
     if (A->dkind == 2) { set_error("stencil operator: only a constant diagonal scaling is supported"); return 5; }
-    if (A->seed.y != 0.0 || A->dinv_u.y != 0.0) { set_error("stencil operator: complex seed/scaling unsupported"); return 5; }
+    if (es.y != 0.0 || A->dinv_u.y != 0.0) { set_error("stencil operator: complex seed/scaling unsupported"); return 5; }
     double du = A->dinv_u.x;
-    A->ks64.st[0] = (K.st[0] - A->seed.x) * du;
+    A->ks64.st[0] = (K.st[0] - es.x) * du;
     for (int i = 1; i < 7; ++i) A->ks64.st[i] = K.st[i] * du;
     return 0;
   }
@@ -1336,7 +1338,7 @@ int build_operator(Operator* A) {
   // scaled copy of the values
   long cnt = value_count(K);
   bool dvec_cplx = (A->dkind == 2 && A->dinv_cplx) || (A->dkind == 1 && A->dinv_u.y != 0.0);
-  bool out_cplx = (K.vals == 2) || dvec_cplx || A->seed.y != 0.0;
+  bool out_cplx = (K.vals == 2) || dvec_cplx || es.y != 0.0;
   // uniform scaling is applied through a temporary constant vector for simplicity
   void* dtmp = nullptr;
   const void* dptr = A->dinv64;
@@ -1370,11 +1372,11 @@ int build_operator(Operator* A) {
       IDRS_LAUNCH_CHECK();
       kv = (const c128*)kval_tmp;
     }
-    if (dptr && !dcplx) scale_values<c128, double>(K, kv, (const double*)dptr, A->seed, (c128*)A->ks_val64, st, d_missing);
-    else scale_values<c128, c128>(K, kv, (const c128*)dptr, A->seed, (c128*)A->ks_val64, st, d_missing);
+    if (dptr && !dcplx) scale_values<c128, double>(K, kv, (const double*)dptr, es, (c128*)A->ks_val64, st, d_missing);
+    else scale_values<c128, c128>(K, kv, (const c128*)dptr, es, (c128*)A->ks_val64, st, d_missing);
   } else {
     IDRS_CUDA(cudaMallocAsync(&A->ks_val64, 8 * std::max<long>(cnt, 1), st));
-    scale_values<double, double>(K, kval, (const double*)dptr, A->seed.x, (double*)A->ks_val64, st, d_missing);
+    scale_values<double, double>(K, kval, (const double*)dptr, es.x, (double*)A->ks_val64, st, d_missing);
   }
   int missing = 0;
   IDRS_CUDA(cudaMemcpyAsync(&missing, d_missing, sizeof(int), cudaMemcpyDeviceToHost, st));

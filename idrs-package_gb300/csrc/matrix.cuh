@@ -124,6 +124,7 @@ struct Operator {
   UserMatrix* P = nullptr;  // diagonal preconditioner or null
   bool cplx = false;        // vectors complex?
   c128 seed;                // rseed / cseed
+  bool seed_folded = false;  // the seed is part of an assembled system matrix K
   int preconditioner = 0, degree = 0;
   std::vector<c128> alpha_p;  // 0..degree
   JacobiCols jac;             // tridiagonal Jacobi matrix of the polynomial (Chebyshev/Neumann)

@@ -98,6 +98,17 @@ int idrs_user_matrix_free(idrs_user_matrix K);
  * is_complex selects the real (r*) or complex (c*) specifics; seed = {re[, im]}. */
 int idrs_matrix_create(idrs_user_matrix K, idrs_user_matrix P, int is_complex,
                        const double *seed, idrs_matrix *A);
+/* The same with mass M and damping C (real_matrix.inc:9-43; NULL = absent)
+ * and the multishift flag.  real_mv/complex_mv (matrix_module.f90:170-264):
+ *   seed 0: K;  C and M: K + seed C + seed^2 M;  C: K + seed C + seed^2 I;
+ *   M: K - seed M;  multishift with C: the 2n x 2n block system
+ *   [-C - seed M, -K; I, -seed I] (without M: -seed I in the (1,1) block),
+ *   whose vectors have length 2n and whose diagonal scaling is [P; 1].
+ * The combination is assembled once into one CRS matrix (K, M, C must be
+ * CRS; others: IDRS_ERR_UNSUPPORTED), so each product is one SpMV. */
+int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix M, idrs_user_matrix C,
+                           idrs_user_matrix P, int is_complex, const double *seed, int multishift,
+                           idrs_matrix *A);
 int idrs_matrix_free(idrs_matrix A);
 int idrs_matrix_set_stream(idrs_matrix A, void *cuda_stream);
 int idrs_matrix_set_pointer_mode(idrs_matrix A, int mode);

@@ -314,6 +314,18 @@ int or_complex_precon(int which_precon, const or_umat *K, const double *shift, o
 /* ------------------------------------------------------------------------ */
 /* type(matrix): M/PP_MATRIX/matrix_module.f90:38-81                        */
 /* ------------------------------------------------------------------------ */
+int or_matrix_create_ext(const or_umat *K, const or_umat *M, const or_umat *C,
+                         const or_umat *P, const double *seed, int cplx, int multishift,
+                         or_mat **out) {
+  int st = or_matrix_create(K, P, seed, cplx, out);
+  if (st != OR_OK) return st;
+  (*out)->M = M; (*out)->C = C;
+  (*out)->mass_matrix = M != NULL;
+  (*out)->damping_matrix = C != NULL;
+  (*out)->block_system = multishift && C != NULL;
+  return OR_OK;
+}
+
 int or_matrix_create(const or_umat *K, const or_umat *P, const double *seed, int cplx, or_mat **out) {
   if (!K || !out) return OR_EARG;
   or_mat *A = calloc(1, sizeof(or_mat));

@@ -58,6 +58,8 @@ typedef struct or_umat {
 
 typedef struct or_mat {
   const or_umat *K, *P;        /* P: user preconditioner (diagonal) or NULL */
+  const or_umat *M, *C;        /* mass and damping matrices or NULL */
+  int mass_matrix, damping_matrix, block_system;
   double rseed; or_cplx cseed;
   int preconditioner, degree;
   double *ralpha_p; or_cplx *calpha_p;   /* 0..degree */
@@ -111,6 +113,11 @@ void or_user_precon_c(const or_umat *A, const or_cplx *v, or_cplx *w);
 /* ---- matrix_module ---- */
 int or_matrix_create(const or_umat *K, const or_umat *P, const double *seed, int cplx,
                      or_mat **out);
+/* type(matrix) with mass M and damping C (real_matrix.inc:9-43): the 2x2
+ * block system when multishift and C are both present (vectors of 2n). */
+int or_matrix_create_ext(const or_umat *K, const or_umat *M, const or_umat *C,
+                         const or_umat *P, const double *seed, int cplx, int multishift,
+                         or_mat **out);
 void or_matrix_free(or_mat *A);
 int or_real_preconditioner(or_mat *A, int preconditioner, int degree, const double *foci,
                            const double *center, const double *H, int ldh, int nh);

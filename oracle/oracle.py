@@ -226,13 +226,19 @@ def real_diagonal(K: UserMatrix):
 # type(matrix)
 # --------------------------------------------------------------------------
 class Matrix:
-    def __init__(self, K: UserMatrix, P: UserMatrix | None = None, seed=None, cplx=False):
-        self.K, self.P, self.cplx, self.n = K, P, cplx, K.n
+    def __init__(self, K: UserMatrix, P: UserMatrix | None = None, seed=None, cplx=False,
+                 M: UserMatrix | None = None, C_: UserMatrix | None = None, multishift=False):
+        self.K, self.P, self.cplx = K, P, cplx
+        self.M, self.C = M, C_  # keep the user matrices alive
+        block = bool(multishift) and C_ is not None
+        self.n = 2 * K.n if block else K.n
         sd = None
         if seed is not None:
             sd = np.array([np.real(seed), np.imag(seed)], dtype=np.float64)
         out = C.c_void_p()
-        st = lib().or_matrix_create(K.ptr, P.ptr if P else None, _p(sd), int(cplx), C.byref(out))
+        st = lib().or_matrix_create_ext(K.ptr, M.ptr if M else None, C_.ptr if C_ else None,
+                                        P.ptr if P else None, _p(sd), int(cplx), int(bool(multishift)),
+                                        C.byref(out))
         if st:
             raise ValueError(f"or_matrix_create status {st}")
         self.ptr = out

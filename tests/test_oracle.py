@@ -314,3 +314,48 @@ def test_pp_mr_idrs_oracle(oracle, P):
     assert rr.iterations[0] == 0 and rr.flags[1] == 0
     same = oracle.pp_mr_idrs(S, np.column_stack([B[:, 0], B[:, 0]]), s=4, tol=1e-8)
     assert same.iterations[1] <= 1
+
+
+@pytest.mark.parametrize("useM,useC,ms,seed", [
+    (True, True, False, 3.0), (False, True, False, -2.0), (True, False, False, 5.0),
+    (False, False, False, 1.5), (True, True, False, 0.0), (True, True, True, 4.0),
+    (False, True, True, 4.0), (True, True, True, 0.0), (False, True, True, 0.0)])
+def test_system_operator_oracle_matches_dense(oracle, P, useM, useC, ms, seed):
+    """real_mv (matrix_module.f90:218-264) with mass/damping matrices and the
+    2x2 block system, against dense numpy matrices (with diagonal scaling)."""
+    n = 4
+    N = n ** 3
+    rp, ci, kv = P.stencil_to_crs(n, n, n, P.cdr_coefficients(n))
+    rows = np.repeat(np.arange(N), np.diff(rp))
+    Kd = np.zeros((N, N)); Kd[rows, ci - 1] = kv
+    rng = np.random.default_rng(3)
+    Md = np.diag(rng.uniform(1, 2, N)) + 0.1 * np.diag(rng.uniform(0, 1, N - 1), 1)
+    Cd = 0.05 * Kd + 0.01 * np.diag(rng.uniform(0, 1, N - 1), -1)
+
+    def crs(D):
+        r, c = np.nonzero(D)
+        rp_ = np.concatenate([[1], 1 + np.cumsum(np.bincount(r, minlength=N))]).astype(np.int32)
+        return oracle.crs_format(N, N, rp_, (c + 1).astype(np.int32), D[r, c])
+    K, M, Cm = crs(Kd), crs(Md), crs(Cd)
+    Pd = oracle.real_precon(1, K)
+    A = oracle.Matrix(K, P=Pd, M=M if useM else None, C_=Cm if useC else None, seed=seed,
+                      multishift=ms)
+    dinv = 1.0 / np.diag(Kd)
+    I = np.eye(N)
+    if ms and useC:
+        top = -Cd - (seed * Md if (useM and seed) else seed * I)
+        S = np.block([[top, -Kd], [I, -seed * I]])
+        dv = np.concatenate([dinv, np.ones(N)])
+    else:
+        if seed == 0:
+            S = Kd
+        elif useC:
+            S = Kd + seed * Cd + seed ** 2 * (Md if useM else I)
+        elif useM:
+            S = Kd - seed * Md
+        else:
+            S = Kd - seed * I
+        dv = dinv
+    v = rng.standard_normal(A.n)
+    np.testing.assert_allclose(A.matvec(v), S @ (dv * v), rtol=1e-12, atol=1e-10)
+    np.testing.assert_allclose(A.precon(v), dv * v, rtol=1e-15)
