@@ -1092,6 +1092,7 @@ idrs_user_matrix assemble_system(const UserMatrix& K, const UserMatrix* Mm, cons
                                  c128 seed, bool block) {
   const int nn = K.nrows;
   const bool seeded = seed.x != 0.0 || seed.y != 0.0;
+  std::vector<const UserMatrix*> srcs;  // the matrix of each term
   auto term = [&](const UserMatrix& M, c128 coef, int off) {
     SysTerm t;
     t.rp = M.row_ptr; t.ci = M.col_ind; t.val = M.val; t.vcplx = M.vals == 2; t.coef = coef; t.col_off = off;
@@ -1099,7 +1100,6 @@ idrs_user_matrix assemble_system(const UserMatrix& K, const UserMatrix* Mm, cons
     return t;
   };
   std::vector<SysTerm> terms;
-  std::vector<const UserMatrix*> srcs;
   bool has_diag_top = false;
   c128 diag_top(0.0, 0.0), low_diag(0.0, 0.0);
   const c128 one(1.0, 0.0), mone(-1.0, 0.0);
