@@ -658,8 +658,9 @@ def run_sequence(args):
     stencil (diagonal scaling, Ritz-estimated Chebyshev(4), IDR(4), tol 1e-8)
     through PP_MR_IDRS: b_1 = K x_model, b_k = b_1 + 1e-3 k |b_1|/sqrt(N) xi_k
     (xi_k seeded N(0,1)).  Each solve starts from the previous solution; the
-    variants add the recycle space U0, or (without the polynomial) 32 Ritz
-    omegas.  Timed end to end
+    variants add the recycle space U0 and drop the polynomial (Ritz omegas
+    are left out: the reference's cyclic omega polynomial diverges on this
+    operator, 128 omegas included, as the oracle shows).  Timed end to end
     (host b_all in, host x_all out); the oracle runs a bounded sample."""
     import torch  # noqa: F401  (CUDA context for the events)
     import __graft_entry__ as g
@@ -676,18 +677,17 @@ def run_sequence(args):
     for k in range(nrhs):
         B[:, k] = b1 + (1e-3 * k * np.linalg.norm(b1) / np.sqrt(N)) * rng.standard_normal(N)
     kw = dict(s=4, tol=1e-8, maxit=4000, preconditioner=2, degree=4, n_ritz=16)
-    plain = dict(s=4, tol=1e-8, maxit=4000, preconditioner=0, n_ritz=32)
+    plain = dict(s=4, tol=1e-8, maxit=4000, preconditioner=0)
     pkg.PP_MR_IDRS(S, B[:, :1], P=D, **kw)  # warm-up (library load, pools)
     out = {}
     for name, opts in (("cheb4+warm_start", kw), ("cheb4+warm_start+recycle", dict(kw, recycle=True)),
                        ("scaling_only+warm_start", plain),
-                       ("scaling_only+warm_start+omega32", dict(plain, n_omega=32)),
                        ("scaling_only+warm_start+recycle", dict(plain, recycle=True))):
         t0 = time.perf_counter()
         r = pkg.PP_MR_IDRS(S, B, P=D, **opts)
         sec = time.perf_counter() - t0
-        assert list(r.flags) == [0] * nrhs
-        out[name] = {"seconds_total": round(sec, 4), "seconds_setup": round(r.seconds_setup, 4),
+        out[name] = {"flags": [int(f) for f in r.flags],
+                     "seconds_total": round(sec, 4), "seconds_setup": round(r.seconds_setup, 4),
                      "iterations": [int(i) for i in r.iterations],
                      "max_relres_original": float(np.max(r.relres_original)),
                      "recycle_iterations": r.recycle_iterations}
