@@ -53,6 +53,8 @@ _PROTOS = {
     "idrs_coo_format": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "idrs_cds_format": (_i, [_i, _i, _i, _vp, _vp, _vp]),
     "idrs_dense_format": (_i, [_i, _i, _vp, _vp, _vp]),
+    "idrs_mm_matrix": (_i, [C.c_char_p, C.c_char_p, _vp]),
+    "idrs_mm_read": (_i, [C.c_char_p, C.c_char_p, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "idrs_stencil7_format": (_i, [_i, _i, _i, _vp, _vp]),
     "idrs_real_precon": (_i, [_i, _vp, _vp, _vp]),
     "idrs_complex_precon": (_i, [_i, _vp, _vp, _vp]),
@@ -280,6 +282,50 @@ def dense_format(rmat=None, imat=None, cmat=None) -> UserMatrix:
     h = C.c_void_p()
     _check(lib().idrs_dense_format(mat.shape[0], mat.shape[1], _p(rv), _p(cv), C.byref(h)))
     return UserMatrix(h.value, mat.shape[0], mat.shape[1], cv is not None)
+
+
+def mm_read(mm_file, which_format=None) -> Result:
+    """The conversion of mm_matrix (E/MATRIX_MARKET/mm_module.f90:48-154) into
+    host arrays: rep ('coordinate'/'array'), field, nrows, ncols, nnz and
+    row_ptr/col_ind ('crs'), indx/jndx ('coo', the default) and vals
+    (array, column order, nrows x ncols).  Indices are 1-based."""
+    f = os.fsencode(mm_file)
+    w = None if which_format is None else which_format.encode()
+    rep, field, nr, nc, nnz = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_long()
+    _check(lib().idrs_mm_read(f, w, C.byref(rep), C.byref(field), C.byref(nr), C.byref(nc),
+                              C.byref(nnz), None, None, None))
+    cplx = field.value == 1
+    crs = which_format is not None and which_format.lower() == "crs"
+    n = nnz.value
+    vals = np.zeros(n * (2 if cplx else 1))
+    r = Result(rep="coordinate" if rep.value == 0 else "array",
+               field=("real", "complex", "integer", "pattern")[field.value],
+               nrows=nr.value, ncols=nc.value, nnz=n)
+    if rep.value == 1:
+        _check(lib().idrs_mm_read(f, w, None, None, None, None, None, None, None, _p(vals)))
+        v = vals.view(np.complex128) if cplx else vals
+        r["vals"] = v.reshape((nr.value, nc.value), order="F")
+        return r
+    ptr = np.zeros(nr.value + 1 if crs else n, np.int32)
+    ind = np.zeros(n, np.int32)
+    _check(lib().idrs_mm_read(f, w, None, None, None, None, None, _p(ptr), _p(ind), _p(vals)))
+    v = vals.view(np.complex128) if cplx else vals
+    if crs:
+        r.update(row_ptr=ptr, col_ind=ind, vals=v)
+    else:
+        r.update(indx=ptr, jndx=ind, vals=v)
+    return r
+
+
+def mm_matrix(mm_file, which_format=None) -> UserMatrix:
+    """A = mm_matrix(mm_file[, which_format]) (mm_module.f90:48-154): a COO
+    (default) or CRS user_matrix for coordinate files, dense for arrays."""
+    info = mm_read(mm_file, which_format)  # sizes and kind (host parse)
+    h = C.c_void_p()
+    w = None if which_format is None else which_format.encode()
+    _check(lib().idrs_mm_matrix(os.fsencode(mm_file), w, C.byref(h)))
+    return UserMatrix(h.value, info.nrows, info.ncols, info.field == "complex",
+                      nnz=info.nnz if info.rep == "coordinate" else None)
 
 
 def stencil7_format(nx, ny, nz, coef) -> UserMatrix:

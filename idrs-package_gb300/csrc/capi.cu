@@ -1088,6 +1088,8 @@ std::vector<int> host_row_ptr(const UserMatrix& M) {
 //   block (multishift with C), 2nn x 2nn:
 //     [ -C - seed M   -K      ]   (without M: -seed I in the (1,1) block)
 //     [  I            -seed I ]
+// K, M, C: CRS or COO (COO is stored row-sorted with row pointers, so both
+// are read the same way); the result is CRS.
 idrs_user_matrix assemble_system(const UserMatrix& K, const UserMatrix* Mm, const UserMatrix* Cm,
                                  c128 seed, bool block) {
   const int nn = K.nrows;
@@ -1190,11 +1192,11 @@ int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix Mm, idrs_user_ma
     for (const UserMatrix* X : {(const UserMatrix*)Mm, (const UserMatrix*)Cm}) {
       if (!X) continue;
       REQUIRE(X->nrows == K->nrows && X->ncols == K->ncols, "matrix_create: M and C must match K");
-      if (X->format != FMT_CRS)
-        throw unsupported_error("matrix_create: mass and damping matrices must be CRS");
+      if (X->format != FMT_CRS && X->format != FMT_COO)
+        throw unsupported_error("matrix_create: mass and damping matrices must be CRS or COO");
     }
-    if (K->format != FMT_CRS)
-      throw unsupported_error("matrix_create: with mass or damping matrices K must be CRS");
+    if (K->format != FMT_CRS && K->format != FMT_COO)
+      throw unsupported_error("matrix_create: with mass or damping matrices K must be CRS or COO");
     REQUIRE(!P || P->nrows == K->nrows, "matrix_create: P size mismatch");
     REQUIRE(!P || P->which_precon == 1, "matrix_create: only a diagonal P is supported here");
     init_runtime();

@@ -91,6 +91,25 @@ int idrs_cuser_mv(idrs_user_matrix K, const double *v, double *w);
 int idrs_user_matrix_free(idrs_user_matrix K);
 
 /* ---------------------------------------------------------------------- */
+/* Matrix Market input: E/MATRIX_MARKET/mm_module.f90:48-154 (mm_matrix)  */
+/* ---------------------------------------------------------------------- */
+/* A = mm_matrix(mm_file[, which_format]): coordinate files become a COO
+ * (which_format NULL or "coo", the reference's default) or CRS ("crs")
+ * user_matrix, array files a dense one.  Symmetric, skew-symmetric and
+ * Hermitian files are expanded; complex entries pass through single
+ * precision and integer entries become reals, as in the reference. */
+int idrs_mm_matrix(const char *mm_file, const char *which_format, idrs_user_matrix *A);
+/* The same conversion into host arrays (no GPU needed).  Call once with
+ * ptr = ind = vals = NULL for the sizes, then with arrays of those sizes.
+ * rep: 0 coordinate, 1 array; field: 0 real, 1 complex, 2 integer, 3 pattern.
+ * coordinate "crs": ptr = row_ptr (nrows+1), ind = col_ind (nnz), 1-based;
+ * coordinate "coo": ptr = indx (nnz), ind = jndx (nnz), 1-based;
+ * array: nnz = nrows*ncols values in column order (ptr, ind unused);
+ * vals: nnz reals, or 2*nnz interleaved re/im for complex. */
+int idrs_mm_read(const char *mm_file, const char *which_format, int *rep, int *field, int *nrows,
+                 int *ncols, long *nnz, int *ptr, int *ind, double *vals);
+
+/* ---------------------------------------------------------------------- */
 /* matrix_module                                                          */
 /* ---------------------------------------------------------------------- */
 
@@ -105,7 +124,7 @@ int idrs_matrix_create(idrs_user_matrix K, idrs_user_matrix P, int is_complex,
  *   [-C - seed M, -K; I, -seed I] (without M: -seed I in the (1,1) block),
  *   whose vectors have length 2n and whose diagonal scaling is [P; 1].
  * The combination is assembled once into one CRS matrix (K, M, C must be
- * CRS; others: IDRS_ERR_UNSUPPORTED), so each product is one SpMV. */
+ * CRS or COO; others: IDRS_ERR_UNSUPPORTED), so each product is one SpMV. */
 int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix M, idrs_user_matrix C,
                            idrs_user_matrix P, int is_complex, const double *seed, int multishift,
                            idrs_matrix *A);

@@ -208,6 +208,15 @@ def stencil7_format(nx, ny, nz, coef) -> UserMatrix:
     return UserMatrix(out, nx * ny * nz, keep=(c,))
 
 
+def complex_precon(which, K: UserMatrix, shift=None) -> UserMatrix:
+    out = C.c_void_p()
+    sh = None if shift is None else np.array([np.real(shift), np.imag(shift)])
+    st = lib().or_complex_precon(int(which), K.ptr, _p(sh), C.byref(out))
+    if st:
+        raise ValueError(f"or_complex_precon status {st}")
+    return UserMatrix(out, K.n)
+
+
 def real_precon(which, K: UserMatrix, shift=None) -> UserMatrix:
     out = C.c_void_p()
     st = lib().or_real_precon(int(which), K.ptr, _dp(shift), C.byref(out))
