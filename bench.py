@@ -699,7 +699,8 @@ def run_sequence(args):
                                   "iterations": cold}
     cpu = None
     if not args.no_cpu_baseline:
-        import oracle as O
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O  # CPU restatement (the baseline)
         O.build()
         So = O.stencil7_format(n, n, n, coef)
         t0 = time.perf_counter()

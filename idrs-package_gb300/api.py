@@ -58,6 +58,8 @@ _PROTOS = {
     "idrs_stencil7_format": (_i, [_i, _i, _i, _vp, _vp]),
     "idrs_real_precon": (_i, [_i, _vp, _vp, _vp]),
     "idrs_complex_precon": (_i, [_i, _vp, _vp, _vp]),
+    "idrs_real_precon_ext": (_i, [_i, _vp, _vp, _vp, _vp, _vp]),
+    "idrs_complex_precon_ext": (_i, [_i, _vp, _vp, _vp, _vp, _vp]),
     "idrs_real_diagonal": (_i, [_vp, _vp]),
     "idrs_complex_diagonal": (_i, [_vp, _vp]),
     "idrs_ruser_mv": (_i, [_vp, _vp, _vp]),
@@ -337,17 +339,23 @@ def stencil7_format(nx, ny, nz, coef) -> UserMatrix:
     return UserMatrix(h.value, n, n, False)
 
 
-def real_precon(which_precon, K: UserMatrix, shift=None) -> UserMatrix:
-    """REAL_PRECON (user_module.f90:1327-1463): 0 none, 1 diagonal scaling."""
+def real_precon(which_precon, K: UserMatrix, shift=None, M: UserMatrix | None = None,
+                C_: UserMatrix | None = None) -> UserMatrix:
+    """REAL_PRECON(which_precon, K[, M, C, shift]) (user_module.f90:1327-1463):
+    0 none, 1 diagonal scaling (of K + shift C + shift^2 M with a shift)."""
     h = C.c_void_p()
-    _check(lib().idrs_real_precon(int(which_precon), K.handle, _ref_dbl(shift), C.byref(h)))
+    _check(lib().idrs_real_precon_ext(int(which_precon), K.handle, M.handle if M else None,
+                                      C_.handle if C_ else None, _ref_dbl(shift), C.byref(h)))
     return UserMatrix(h.value, K.nrows, K.ncols, False)
 
 
-def complex_precon(which_precon, K: UserMatrix, shift=None) -> UserMatrix:
+def complex_precon(which_precon, K: UserMatrix, shift=None, M: UserMatrix | None = None,
+                   C_: UserMatrix | None = None) -> UserMatrix:
+    """COMPLEX_PRECON(which_precon, K[, M, C, shift]) (user_module.f90:1465-1602)."""
     h = C.c_void_p()
     sh = None if shift is None else np.array([np.real(shift), np.imag(shift)])
-    _check(lib().idrs_complex_precon(int(which_precon), K.handle, _p(sh), C.byref(h)))
+    _check(lib().idrs_complex_precon_ext(int(which_precon), K.handle, M.handle if M else None,
+                                         C_.handle if C_ else None, _p(sh), C.byref(h)))
     return UserMatrix(h.value, K.nrows, K.ncols, True)
 
 

@@ -580,7 +580,64 @@ struct BDotc {
   __device__ void operator()(long i, Shared&, A (&acc)[ND]) const { acc_add(acc[0], conj_(u[i]) * v[i]); }
 };
 
-static int precon_common(int which, idrs_user_matrix K, c128 shift, bool want_cplx, idrs_user_matrix* P) {
+// D = dK + a dC + b dM + c   (each diagonal with zeros replaced by 1)
+template <class V>
+__global__ void k_diag_combine(int n, V* D, const V* dC, const V* dM, V a, V b, V c) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x) {
+    V d = D[i];
+    if (dC) d = d + a * dC[i];
+    if (dM) d = d + b * dM[i];
+    D[i] = d + c;
+  }
+}
+template <class V>
+__global__ void k_fill(long n, V* D, V v) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x) D[i] = v;
+}
+
+// REAL_PRECON / COMPLEX_PRECON diagonal with mass and damping matrices
+// (user_module.f90:1352-1381): diag(K) + shift diag(C) + shift^2 diag(M);
+// C only: diag(K) + shift diag(C) + shift^2; M only: diag(K) - shift diag(M).
+static void* diagonal_with_mc(const UserMatrix& K, const UserMatrix* Mm, const UserMatrix* Cm,
+                              bool want_cplx, c128 shift, bool* is_cplx) {
+  const int n = K.nrows;
+  bool cplx = want_cplx || shift.y != 0.0 || K.vals == 2 || (Mm && Mm->vals == 2) || (Cm && Cm->vals == 2);
+  *is_cplx = cplx;
+  auto diag_of = [&](const UserMatrix& X) -> void* {
+    bool c = false;
+    if (X.format == FMT_STENCIL7) {
+      void* d = nullptr;
+      IDRS_CUDA(cudaMalloc(&d, (cplx ? 16 : 8) * (size_t)std::max(n, 1)));
+      double v = X.st[0] == 0.0 ? 1.0 : X.st[0];
+      if (cplx) k_fill<c128><<<stream_grid(n), kThreads>>>(n, (c128*)d, c128(v, 0.0));
+      else k_fill<double><<<stream_grid(n), kThreads>>>(n, (double*)d, v);
+      IDRS_LAUNCH_CHECK();
+      return d;
+    }
+    return make_diagonal(X, cplx, c128(0.0), &c);
+  };
+  void* D = diag_of(K);
+  void* dC = Cm ? diag_of(*Cm) : nullptr;
+  void* dM = Mm ? diag_of(*Mm) : nullptr;
+  c128 a(0.0), b(0.0), c(0.0);
+  if (Mm && Cm) { a = shift; b = shift * shift; }
+  else if (Cm) { a = shift; c = shift * shift; }
+  else if (Mm) { b = c128(-shift.x, -shift.y); }
+  else { c = c128(-shift.x, -shift.y); }
+  if (cplx)
+    k_diag_combine<c128><<<stream_grid(n), kThreads>>>(n, (c128*)D, (const c128*)dC, (const c128*)dM, a, b, c);
+  else
+    k_diag_combine<double><<<stream_grid(n), kThreads>>>(n, (double*)D, (const double*)dC, (const double*)dM,
+                                                         a.x, b.x, c.x);
+  IDRS_LAUNCH_CHECK();
+  IDRS_CUDA(cudaDeviceSynchronize());
+  if (dC) cudaFree(dC);
+  if (dM) cudaFree(dM);
+  return D;
+}
+
+static int precon_common(int which, idrs_user_matrix K, c128 shift, bool want_cplx, idrs_user_matrix* P,
+                         idrs_user_matrix Mm = nullptr, idrs_user_matrix Cm = nullptr) {
   REQUIRE(K && P, "real_precon: bad arguments");
   if (which != 0 && which != 1) throw unsupported_error("precon: only which_precon 0 and 1 (diagonal scaling) are supported");
   auto* M = new idrs_user_matrix_s();
@@ -588,7 +645,13 @@ static int precon_common(int which, idrs_user_matrix K, c128 shift, bool want_cp
   M->which_precon = which;
   M->nrows = K->nrows;
   M->ncols = K->ncols;
-  if (which == 1) {
+  if (which == 1 && (Mm || Cm)) {
+    for (const UserMatrix* X : {(const UserMatrix*)Mm, (const UserMatrix*)Cm})
+      REQUIRE(!X || (X->nrows == K->nrows && X->ncols == K->ncols), "precon: M and C must match K");
+    bool cplx = false;
+    M->diag = diagonal_with_mc(*K, Mm, Cm, want_cplx, shift, &cplx);
+    M->diag_cplx = cplx;
+  } else if (which == 1) {
     if (K->format == FMT_STENCIL7) {
       M->diag_uniform = true;
       c128 d(K->st[0], 0.0);
@@ -983,6 +1046,21 @@ int idrs_complex_precon(int which_precon, idrs_user_matrix K, const double* shif
   return guard([&] {
     c128 sh = shift ? c128(shift[0], shift[1]) : c128(0.0);
     return precon_common(which_precon, K, sh, true, P);
+  });
+}
+int idrs_real_precon_ext(int which_precon, idrs_user_matrix K, idrs_user_matrix M,
+                         idrs_user_matrix C, const double* shift, idrs_user_matrix* P) {
+  return guard([&] {
+    // without a shift the reference takes diag(K) alone
+    if (!shift) return precon_common(which_precon, K, c128(0.0), false, P);
+    return precon_common(which_precon, K, c128(*shift, 0.0), false, P, M, C);
+  });
+}
+int idrs_complex_precon_ext(int which_precon, idrs_user_matrix K, idrs_user_matrix M,
+                            idrs_user_matrix C, const double* shift, idrs_user_matrix* P) {
+  return guard([&] {
+    if (!shift) return precon_common(which_precon, K, c128(0.0), true, P);
+    return precon_common(which_precon, K, c128(shift[0], shift[1]), true, P, M, C);
   });
 }
 

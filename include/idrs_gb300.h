@@ -82,6 +82,13 @@ int idrs_real_precon(int which_precon, idrs_user_matrix K, const double *shift,
 /* COMPLEX_PRECON: user_module.f90:1465-1603 (shift = {re, im}) */
 int idrs_complex_precon(int which_precon, idrs_user_matrix K, const double *shift,
                         idrs_user_matrix *P);
+/* The same with mass M and damping C (NULL = absent), user_module.f90:1327-1381
+ * and :1465-1520: with a shift the diagonal of K + shift C + shift^2 M (C only:
+ * + shift^2; M only: K - shift M), each matrix's diagonal with zeros -> 1. */
+int idrs_real_precon_ext(int which_precon, idrs_user_matrix K, idrs_user_matrix M,
+                         idrs_user_matrix C, const double *shift, idrs_user_matrix *P);
+int idrs_complex_precon_ext(int which_precon, idrs_user_matrix K, idrs_user_matrix M,
+                            idrs_user_matrix C, const double *shift, idrs_user_matrix *P);
 /* real_diagonal(K) / complex_diagonal(K): user_module.f90:960-1047, 1049-1136 */
 int idrs_real_diagonal(idrs_user_matrix K, double *D);
 int idrs_complex_diagonal(idrs_user_matrix K, double *D);

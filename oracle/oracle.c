@@ -280,35 +280,75 @@ int or_complex_diagonal(const or_umat *A, or_cplx *D) {
 
 /* REAL_PRECON: user_module.f90:1327-1381, which_precon = 1 (diagonal
  * scaling, optionally shifted: D(K) - shift).  Dense/band LU are out of scope. */
-int or_real_precon(int which_precon, const or_umat *K, const double *shift, or_umat **out) {
+/* REAL_PRECON / COMPLEX_PRECON, which_precon 0/1: user_module.f90:1327-1381 and
+ * :1465-1520.  The diagonal of K, or with a shift that of K + shift C +
+ * shift^2 M (C only: + shift^2; M only: K - shift M; neither: K - shift), each
+ * matrix's diagonal taken with its zeros replaced by 1 (real_diagonal). */
+int or_real_precon_ext(int which_precon, const or_umat *K, const or_umat *M, const or_umat *C,
+                       const double *shift, or_umat **out) {
   if (!K || !out) return OR_EARG;
   or_umat *P = umat_new(0, K->nrows, K->ncols);
   P->which_precon = which_precon;
+  int n = K->nrows;
   if (which_precon == 1) {
     P->format = OR_CDS; P->half_band = 0; P->vals = 1;
-    P->rband = malloc(sizeof(double) * (K->nrows > 0 ? K->nrows : 1));
-    or_real_diagonal(K, P->rband);
-    if (shift) for (int i = 0; i < K->nrows; ++i) P->rband[i] -= *shift;
+    P->rband = malloc(sizeof(double) * (n > 0 ? n : 1));
+    double *D = P->rband;
+    or_real_diagonal(K, D);
+    if (shift) {
+      double sh = *shift;
+      double *dc = malloc(sizeof(double) * (n > 0 ? n : 1)), *dm = malloc(sizeof(double) * (n > 0 ? n : 1));
+      if (C) or_real_diagonal(C, dc);
+      if (M) or_real_diagonal(M, dm);
+      for (int i = 0; i < n; ++i) {
+        if (M && C) D[i] = D[i] + sh * dc[i] + (sh * sh) * dm[i];
+        else if (C) D[i] = (D[i] + sh * dc[i]) + sh * sh;
+        else if (M) D[i] = D[i] - sh * dm[i];
+        else D[i] = D[i] - sh;
+      }
+      free(dc); free(dm);
+    }
   } else if (which_precon != 0) {
     or_umat_free(P); return OR_EUNSUP;
   }
   *out = P;
   return OR_OK;
 }
-int or_complex_precon(int which_precon, const or_umat *K, const double *shift, or_umat **out) {
+int or_complex_precon_ext(int which_precon, const or_umat *K, const or_umat *M, const or_umat *C,
+                          const double *shift, or_umat **out) {
   if (!K || !out) return OR_EARG;
   or_umat *P = umat_new(0, K->nrows, K->ncols);
   P->which_precon = which_precon;
+  int n = K->nrows;
   if (which_precon == 1) {
     P->format = OR_CDS; P->half_band = 0; P->vals = 2;
-    P->cband = malloc(sizeof(or_cplx) * (K->nrows > 0 ? K->nrows : 1));
-    or_complex_diagonal(K, P->cband);
-    if (shift) for (int i = 0; i < K->nrows; ++i) P->cband[i] -= shift[0] + I * shift[1];
+    P->cband = malloc(sizeof(or_cplx) * (n > 0 ? n : 1));
+    or_cplx *D = P->cband;
+    or_complex_diagonal(K, D);
+    if (shift) {
+      or_cplx sh = shift[0] + I * shift[1];
+      or_cplx *dc = malloc(sizeof(or_cplx) * (n > 0 ? n : 1)), *dm = malloc(sizeof(or_cplx) * (n > 0 ? n : 1));
+      if (C) or_complex_diagonal(C, dc);
+      if (M) or_complex_diagonal(M, dm);
+      for (int i = 0; i < n; ++i) {
+        if (M && C) D[i] = D[i] + sh * dc[i] + (sh * sh) * dm[i];
+        else if (C) D[i] = (D[i] + sh * dc[i]) + sh * sh;
+        else if (M) D[i] = D[i] - sh * dm[i];
+        else D[i] = D[i] - sh;
+      }
+      free(dc); free(dm);
+    }
   } else if (which_precon != 0) {
     or_umat_free(P); return OR_EUNSUP;
   }
   *out = P;
   return OR_OK;
+}
+int or_real_precon(int which_precon, const or_umat *K, const double *shift, or_umat **out) {
+  return or_real_precon_ext(which_precon, K, NULL, NULL, shift, out);
+}
+int or_complex_precon(int which_precon, const or_umat *K, const double *shift, or_umat **out) {
+  return or_complex_precon_ext(which_precon, K, NULL, NULL, shift, out);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -102,6 +102,10 @@ int or_dense_format(int nrows, int ncols, const double *rmat, const double *cmat
 int or_stencil7_format(int nx, int ny, int nz, const double coef[7], or_umat **out);
 int or_real_precon(int which_precon, const or_umat *K, const double *shift, or_umat **out);
 int or_complex_precon(int which_precon, const or_umat *K, const double *shift, or_umat **out);
+int or_real_precon_ext(int which_precon, const or_umat *K, const or_umat *M, const or_umat *C,
+                       const double *shift, or_umat **out);
+int or_complex_precon_ext(int which_precon, const or_umat *K, const or_umat *M, const or_umat *C,
+                          const double *shift, or_umat **out);
 int or_real_diagonal(const or_umat *K, double *D);
 int or_complex_diagonal(const or_umat *K, or_cplx *D);
 void or_umat_free(or_umat *A);

@@ -208,18 +208,22 @@ def stencil7_format(nx, ny, nz, coef) -> UserMatrix:
     return UserMatrix(out, nx * ny * nz, keep=(c,))
 
 
-def complex_precon(which, K: UserMatrix, shift=None) -> UserMatrix:
+def complex_precon(which, K: UserMatrix, shift=None, M: UserMatrix | None = None,
+                   C_: UserMatrix | None = None) -> UserMatrix:
     out = C.c_void_p()
     sh = None if shift is None else np.array([np.real(shift), np.imag(shift)])
-    st = lib().or_complex_precon(int(which), K.ptr, _p(sh), C.byref(out))
+    st = lib().or_complex_precon_ext(int(which), K.ptr, M.ptr if M else None,
+                                     C_.ptr if C_ else None, _p(sh), C.byref(out))
     if st:
         raise ValueError(f"or_complex_precon status {st}")
     return UserMatrix(out, K.n)
 
 
-def real_precon(which, K: UserMatrix, shift=None) -> UserMatrix:
+def real_precon(which, K: UserMatrix, shift=None, M: UserMatrix | None = None,
+                C_: UserMatrix | None = None) -> UserMatrix:
     out = C.c_void_p()
-    st = lib().or_real_precon(int(which), K.ptr, _dp(shift), C.byref(out))
+    st = lib().or_real_precon_ext(int(which), K.ptr, M.ptr if M else None, C_.ptr if C_ else None,
+                                  _dp(shift), C.byref(out))
     if st:
         raise ValueError(f"or_real_precon status {st}")
     return UserMatrix(out, K.n)

@@ -118,3 +118,22 @@ def test_system_rejects_unsupported_formats(gpu, P):
     Mc = gpu.crs_format(n ** 3, n ** 3, rp, ci, rval=kv)
     with pytest.raises(gpu.IDRSError):
         gpu.Matrix(S, M=Mc, seed=1.0)
+
+
+@pytest.mark.parametrize("useM,useC", [(True, True), (False, True), (True, False), (False, False)])
+@pytest.mark.parametrize("shift", [None, 2.5, 1.0 - 0.5j])
+def test_diagonal_precon_with_mass_and_damping(gpu, oracle, P, useM, useC, shift):
+    """REAL_PRECON / COMPLEX_PRECON(1, K, M, C, shift): v / A with A = the
+    identity operator scaled by that diagonal, against the oracle."""
+    N, G, O = _system(gpu, oracle, P, n=6)
+    cplx = isinstance(shift, complex)
+    kg = dict(M=G["M"] if useM else None, C_=G["C"] if useC else None, shift=shift)
+    ko = dict(M=O["M"] if useM else None, C_=O["C"] if useC else None, shift=shift)
+    if cplx:
+        Pg, Po = gpu.complex_precon(1, G["K"], **kg), oracle.complex_precon(1, O["K"], **ko)
+    else:
+        Pg, Po = gpu.real_precon(1, G["K"], **kg), oracle.real_precon(1, O["K"], **ko)
+    A = gpu.Matrix(G["K"], P=Pg, complex=cplx)
+    Ao = oracle.Matrix(O["K"], P=Po, cplx=cplx)
+    v = np.random.default_rng(8).standard_normal(N) * (1 + 0.5j if cplx else 1)
+    np.testing.assert_allclose(v / A, Ao.precon(v), rtol=1e-15, atol=0)

@@ -359,3 +359,39 @@ def test_system_operator_oracle_matches_dense(oracle, P, useM, useC, ms, seed):
     v = rng.standard_normal(A.n)
     np.testing.assert_allclose(A.matvec(v), S @ (dv * v), rtol=1e-12, atol=1e-10)
     np.testing.assert_allclose(A.precon(v), dv * v, rtol=1e-15)
+
+
+@pytest.mark.parametrize("useM,useC", [(True, True), (False, True), (True, False), (False, False)])
+@pytest.mark.parametrize("shift", [None, 2.5, 1.0 - 0.5j])
+def test_precon_with_mass_and_damping_oracle(oracle, P, useM, useC, shift):
+    """REAL_PRECON / COMPLEX_PRECON(1, K, M, C, shift) (user_module.f90:1352-1381):
+    each matrix's diagonal with zeros -> 1, combined by the shift."""
+    n = 4
+    N = n ** 3
+    rp, ci, kv = P.stencil_to_crs(n, n, n, P.cdr_coefficients(n))
+    K = oracle.crs_format(N, N, rp, ci, kv)
+    dm = np.where(np.arange(N) % 3 == 0, 0.0, 1.5)    # zeros become 1
+    dc = np.where(np.arange(N) % 4 == 0, 0.3, 0.0)
+    ii = np.arange(1, N + 2, dtype=np.int32)
+    M = oracle.crs_format(N, N, ii, ii[:-1], dm)
+    C = oracle.crs_format(N, N, ii, ii[:-1], dc)
+    cplx = isinstance(shift, complex)
+    fn = oracle.complex_precon if cplx else oracle.real_precon
+    Pm = fn(1, K, shift=shift, M=M if useM else None, C_=C if useC else None)
+    fix = lambda d: np.where(d == 0, 1.0, d)
+    dK = fix(np.array([kv[p] for i in range(N) for p in range(rp[i] - 1, rp[i + 1] - 1)
+                       if ci[p] - 1 == i]))
+    s = 0.0 if shift is None else shift
+    if shift is None:
+        D = dK
+    elif useM and useC:
+        D = dK + s * fix(dc) + s ** 2 * fix(dm)
+    elif useC:
+        D = dK + s * fix(dc) + s ** 2
+    elif useM:
+        D = dK - s * fix(dm)
+    else:
+        D = dK - s
+    A = oracle.Matrix(K, P=Pm, cplx=cplx)
+    v = np.random.default_rng(1).standard_normal(N) + (0.5j if cplx else 0)
+    np.testing.assert_allclose(A.precon(v), v / D, rtol=1e-15)
