@@ -67,6 +67,9 @@ _PROTOS = {
     "idrs_user_matrix_free": (_i, [_vp]),
     "idrs_matrix_create": (_i, [_vp, _vp, _i, _vp, _vp]),
     "idrs_matrix_create_ext": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _i, _vp]),
+    "idrs_make_deflation": (_i, [_vp, _vp, _i]),
+    "idrs_rpmul": (_i, [_vp, _vp, _vp]),
+    "idrs_cpmul": (_i, [_vp, _vp, _vp]),
     "idrs_matrix_free": (_i, [_vp]),
     "idrs_matrix_set_stream": (_i, [_vp, _vp]),
     "idrs_matrix_set_pointer_mode": (_i, [_vp, _i]),
@@ -452,6 +455,25 @@ class Matrix:
         fn = lib().idrs_complex_ms_parameters if self.cplx else lib().idrs_real_ms_parameters
         _check(fn(self.handle, len(sigma), _p(sigma), _p(sp)))
         return sp
+
+    def make_deflation(self, V):
+        """make_deflation(A, V) (matrix_module.f90:1284-1346): V is n x k (k <= 16);
+        None or k = 0 removes the deflation."""
+        if V is None:
+            _check(lib().idrs_make_deflation(self.handle, None, 0))
+            return
+        V = np.asfortranarray(V, dtype=self.dtype)
+        if V.ndim != 2 or V.shape[0] != self.n:
+            raise ValueError("V must be n x k")
+        _check(lib().idrs_make_deflation(self.handle, _p(V), V.shape[1]))
+
+    def pmul(self, v):
+        """w = Pmul(A, v) (matrix_module.f90:1348-1418)."""
+        v = _arr(v, self.cplx, self.n)
+        w = np.empty_like(v)
+        fn = lib().idrs_cpmul if self.cplx else lib().idrs_rpmul
+        _check(fn(self.handle, _p(v), _p(w)))
+        return w
 
     def matvec32(self, v):
         """A*v evaluated in fp32 (the operator of the fp32 inner solves), widened to fp64."""

@@ -706,8 +706,10 @@ static int ms_parameters(idrs_matrix A, int n_sigma, const double* sigma, double
   int d = A->degree;
   A->n_sigma = n_sigma;
   A->alpha_s.assign((size_t)(d + 1) * n_sigma, c128(0.0));
+  A->sigma_s.assign(n_sigma, c128(0.0));
   for (int i = 0; i < n_sigma; ++i) {
     cd ss = (cplx ? cd(sigma[2 * i], sigma[2 * i + 1]) : cd(sigma[i], 0.0)) - cd(A->seed.x, A->seed.y);
+    A->sigma_s[i] = c128(ss.real(), ss.imag());
     cd sp;
     if (d > 0) {
       std::vector<cd> as(d + 1);
@@ -752,33 +754,40 @@ static int precon_t(idrs_matrix A, const double* v, double* w) {
 }
 
 template <class T>
-static int scaleback_t(idrs_matrix A, const double* y, double* x) {
+static int scaleback_t(idrs_matrix A, const double* b, const double* y, double* x) {
   REQUIRE(A && y && x, "scaleback: bad arguments");
+  REQUIRE(b || !A->defl, "scaleback: a deflated operator needs b");
   long n = A->n();
   Staged sv(A, sizeof(T) * n);
   const T* dy = (const T*)sv.in(y);
+  const T* db = (const T*)sv.in(b);
   T* dx = (T*)sv.out(x);
   DBuf t1(sizeof(T) * n, A->stream), t2(sizeof(T) * n, A->stream);
-  op_scaleback<T>(*A, 64, A->alpha_p, A->degree, dy, dx, t1.as<T>(), t2.as<T>(), nullptr, A->stream);
+  op_scaleback<T>(*A, 64, A->alpha_p, A->degree, dy, dx, t1.as<T>(), t2.as<T>(), nullptr, A->stream, db);
   sv.finish(x, dx);
   IDRS_CUDA(cudaStreamSynchronize(A->stream));
   return IDRS_OK;
 }
 
 template <class T>
-static int ms_scaleback_t(idrs_matrix A, int n_sigma, const double* y, double* x) {
+static int ms_scaleback_t(idrs_matrix A, int n_sigma, const double* b, const double* y, double* x) {
   REQUIRE(A && y && x && n_sigma >= 1, "ms_scaleback: bad arguments");
   REQUIRE(A->degree == 0 || A->n_sigma == n_sigma, "ms_scaleback: call ms_parameters with these shifts first");
+  REQUIRE(!A->defl || (b && (int)A->sigma_s.size() == n_sigma),
+          "ms_scaleback: a deflated operator needs b and ms_parameters with these shifts");
   long n = A->n();
-  Staged sv(A, sizeof(T) * n * n_sigma);
+  Staged sv(A, sizeof(T) * n * n_sigma), sb(A, sizeof(T) * n);
   const T* dy = (const T*)sv.in(y);
+  const T* db = (const T*)sb.in(b);
   T* dx = (T*)sv.out(x);
   DBuf t1(sizeof(T) * n, A->stream), t2(sizeof(T) * n, A->stream);
   int d = A->degree;
   for (int i = 0; i < n_sigma; ++i) {
     std::vector<c128> al(A->alpha_s.begin() + (size_t)(d + 1) * i, A->alpha_s.begin() + (size_t)(d + 1) * (i + 1));
     if (d == 0) al.assign(1, c128(1.0));
-    op_scaleback<T>(*A, 64, al, d, dy + n * i, dx + n * i, t1.as<T>(), t2.as<T>(), nullptr, A->stream);
+    const c128 ss = A->defl ? A->sigma_s[i] : c128(0.0);
+    op_scaleback<T>(*A, 64, al, d, dy + n * i, dx + n * i, t1.as<T>(), t2.as<T>(), nullptr, A->stream,
+                    db, ss);
   }
   sv.finish(x, dx);
   IDRS_CUDA(cudaStreamSynchronize(A->stream));
@@ -869,25 +878,23 @@ int idrs_cprecon(idrs_matrix A, const double* v, double* w) {
 }
 
 int idrs_rscaleback(idrs_matrix A, const double* b, const double* y, double* x) {
-  (void)b;
-  return guard([&] { REQUIRE(A && !A->cplx, "rscaleback: real handle required"); return scaleback_t<double>(A, y, x); });
+  return guard([&] { REQUIRE(A && !A->cplx, "rscaleback: real handle required"); return scaleback_t<double>(A, b, y, x); });
 }
 
 int idrs_cscaleback(idrs_matrix A, const double* b, const double* y, double* x) {
-  (void)b;
-  return guard([&] { REQUIRE(A && A->cplx, "cscaleback: complex handle required"); return scaleback_t<c128>(A, y, x); });
+  return guard([&] { REQUIRE(A && A->cplx, "cscaleback: complex handle required"); return scaleback_t<c128>(A, b, y, x); });
 }
 
 int idrs_ms_rscaleback(idrs_matrix A, int n_sigma, const double* sigma, const double* b,
                        const double* y, double* x) {
-  (void)sigma; (void)b;
-  return guard([&] { REQUIRE(A && !A->cplx, "ms_rscaleback: real handle required"); return ms_scaleback_t<double>(A, n_sigma, y, x); });
+  (void)sigma;
+  return guard([&] { REQUIRE(A && !A->cplx, "ms_rscaleback: real handle required"); return ms_scaleback_t<double>(A, n_sigma, b, y, x); });
 }
 
 int idrs_ms_cscaleback(idrs_matrix A, int n_sigma, const double* sigma, const double* b,
                        const double* y, double* x) {
-  (void)sigma; (void)b;
-  return guard([&] { REQUIRE(A && A->cplx, "ms_cscaleback: complex handle required"); return ms_scaleback_t<c128>(A, n_sigma, y, x); });
+  (void)sigma;
+  return guard([&] { REQUIRE(A && A->cplx, "ms_cscaleback: complex handle required"); return ms_scaleback_t<c128>(A, n_sigma, b, y, x); });
 }
 
 int idrs_rnorm(idrs_matrix A, const double* w, double* norm) { return guard([&] { return norm_t<double>(A, w, nullptr, norm, false); }); }
@@ -1265,7 +1272,11 @@ int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix Mm, idrs_user_ma
                            idrs_matrix* A) {
   return guard([&] {
     REQUIRE(K && A, "matrix_create: bad arguments");
-    if (!Mm && !Cm) return idrs_matrix_create(K, P, is_complex, seed, A);
+    if (!Mm && !Cm) {
+      int st = idrs_matrix_create(K, P, is_complex, seed, A);
+      if (!st) (*A)->multishift = multishift != 0;
+      return st;
+    }
     REQUIRE(K->nrows == K->ncols, "matrix_create: K must be square");
     for (const UserMatrix* X : {(const UserMatrix*)Mm, (const UserMatrix*)Cm}) {
       if (!X) continue;
@@ -1297,8 +1308,48 @@ int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix Mm, idrs_user_ma
       (*A)->seed = sd;
       (*A)->seed_folded = true;
     }
+    (*A)->multishift = multishift != 0;
     return IDRS_OK;
   });
+}
+
+int idrs_make_deflation(idrs_matrix A, const double* V, int k) {
+  return guard([&] {
+    REQUIRE(A && k >= 0 && (k == 0 || V), "make_deflation: bad arguments");
+    REQUIRE(k <= MAXS, "make_deflation: at most 16 deflation vectors");
+    const long n = A->n();
+    Staged sv(A, (A->cplx ? 16 : 8) * (size_t)n * std::max(k, 1));
+    const void* dV = k ? sv.in(V) : nullptr;
+    deflation_make(*A, dV, k);
+    return IDRS_OK;
+  });
+}
+
+}  // extern "C"
+
+template <class T>
+static int pmul_t(idrs_matrix A, const double* v, double* w) {
+  REQUIRE(A && v && w, "pmul: bad arguments");
+  const long n = A->n();
+  Staged sv(A, sizeof(T) * n);
+  const T* dv = (const T*)sv.in(v);
+  T* dw = (T*)sv.out(w);
+  if (A->defl && A->defl->k > 0)
+    deflation_pmul<T>(*A->defl, dv, dw, T(1.0), T(0.0), nullptr, nullptr, A->stream);
+  else
+    vec_copy<T>(n, dv, dw, nullptr, A->stream);
+  sv.finish(w, dw);
+  IDRS_CUDA(cudaStreamSynchronize(A->stream));
+  return IDRS_OK;
+}
+
+extern "C" {
+
+int idrs_rpmul(idrs_matrix A, const double* v, double* w) {
+  return guard([&] { REQUIRE(A && !A->cplx, "rpmul: real handle required"); return pmul_t<double>(A, v, w); });
+}
+int idrs_cpmul(idrs_matrix A, const double* v, double* w) {
+  return guard([&] { REQUIRE(A && A->cplx, "cpmul: complex handle required"); return pmul_t<c128>(A, v, w); });
 }
 
 int idrs_matrix_free(idrs_matrix A) {
@@ -1778,7 +1829,7 @@ int pp_solve(PPJob& J, const double* pb, double* px, const idrs_pp_options* opt,
   // x0 = y (the warm start of the next right-hand side); x = scaleback(A, b, y)
   IDRS_CUDA(cudaMemcpyAsync(J.d_x0.p, J.d_y.p, 8 * n, cudaMemcpyDeviceToDevice, cs));
   op_scaleback<double>(*A, 64, A->alpha_p, A->degree, J.d_y.as<double>(), px, J.t1.as<double>(),
-                       J.t2.as<double>(), nullptr, cs);
+                       J.t2.as<double>(), nullptr, cs, pb);
   spmv<double>(A->k64, px, J.r.as<double>(), -1.0, 1.0, pb, nullptr, cs);
   launch_fused<1, double>(n, BNorm<double>{J.r.as<double>()}, TStoreVals<double>{J.res.as<double>(), 1}, A->red, nullptr, cs);
   launch_fused<1, double>(n, BNorm<double>{pb}, TStoreVals<double>{J.res.as<double>() + 1, 1}, A->red, nullptr, cs);

@@ -936,11 +936,27 @@ void spmv(const MatView& M, const T* x, T* y, T a, T cv, const T* v, const int* 
 // ---------------------------------------------------------------------------
 template <class T> static inline T narrow_c(c128 v) { return narrow<T>(v); }
 
+// The last product of a chain: w = fa * Pmul(Ks u) + fcv * fv (Pmul only with
+// a deflated fp64 operator).
+template <class T>
+static void chain_last(const MatView& Ks, const T* u, T* w, T fa, T fcv, const T* fv, const int* skip,
+                       cudaStream_t st) {
+  if constexpr (sizeof(typename traits<T>::real) == 8) {
+    if (Ks.defl && Ks.defl->k > 0) {
+      T* tmp = (T*)Ks.defl->tmp;
+      spmv<T>(Ks, u, tmp, T(1), T(0), nullptr, skip, st);
+      deflation_pmul<T>(*Ks.defl, tmp, w, fa, fcv, fv, skip, st);
+      return;
+    }
+  }
+  spmv<T>(Ks, u, w, fa, fcv, fv, skip, st);
+}
+
 template <class T>
 void op_chain(const MatView& Ks, const std::vector<c128>& alpha, int degree, const T* v, T* w,
               T* t1, T* t2, const int* skip, cudaStream_t st, T fa, T fcv, const T* fv) {
   if (degree == 0) {
-    spmv<T>(Ks, v, w, fa, fcv, fv, skip, st);
+    chain_last<T>(Ks, v, w, fa, fcv, fv, skip, st);
     return;
   }
   // u_{d-1} = Ks (alpha_d v) + alpha_{d-1} v
@@ -951,7 +967,7 @@ void op_chain(const MatView& Ks, const std::vector<c128>& alpha, int degree, con
     spmv<T>(Ks, cur, nxt, T(1), narrow_c<T>(alpha[k]), v, skip, st);
     std::swap(cur, nxt);
   }
-  spmv<T>(Ks, cur, w, fa, fcv, fv, skip, st);
+  chain_last<T>(Ks, cur, w, fa, fcv, fv, skip, st);
 }
 
 // One step of a polynomial chain: out = Epi(Ks in).
@@ -1164,9 +1180,29 @@ void op_precon(Operator& A, int prec, const T* v, T* w, const int* skip, cudaStr
 
 template <class T>
 void op_scaleback(Operator& A, int prec, const std::vector<c128>& alpha, int degree, const T* y,
-                  T* x, T* t1, T* t2, const int* skip, cudaStream_t st) {
+                  T* x, T* t1, T* t2, const int* skip, cudaStream_t st, const T* b, c128 sigma_s) {
   const MatView& Ks = A.view(prec);
   long n = A.n();
+  if constexpr (sizeof(typename traits<T>::real) == 8) {
+    if (A.defl && A.defl->k > 0) {
+      if (!b) throw std::runtime_error("scaleback: a deflated operator needs the right-hand side b");
+      // p = polpre(y) (no scaling yet), q = add_deflation(b, p), x = q / A
+      const T* cur = y;
+      T* bufs[2] = {t1, t2};
+      int nb = 0;
+      for (int k = degree - 1; k >= 0; --k) {
+        T a = (k == degree - 1) ? narrow<T>(alpha[degree]) : T(1);
+        T* dst = bufs[nb];
+        nb ^= 1;
+        spmv<T>(Ks, cur, dst, a, narrow<T>(alpha[k]), y, skip, st);
+        cur = dst;
+      }
+      T* q = bufs[nb];
+      deflation_add<T>(A, sigma_s, b, cur, q, skip, st);
+      op_precon<T>(A, prec, q, x, skip, st);
+      return;
+    }
+  }
   if (degree == 0) {
     op_precon<T>(A, prec, y, x, skip, st);
     return;
@@ -1400,7 +1436,12 @@ __global__ void k_narrow(long n, const Tin* a, Tout* b) {
 }
 
 const MatView& Operator::view(int prec) {
-  if (prec != 32) return ks64;
+  if (prec != 32) {
+    ks64.defl = defl;
+    return ks64;
+  }
+  if (defl && defl->k > 0)
+    throw std::runtime_error("deflation is not available in the fp32 operator (inner_precision 32)");
   if (ks32.format != FMT_NONE) return ks32;
   ks32 = ks64;
   cudaStream_t st = stream;
@@ -1440,6 +1481,7 @@ void operator_free(Operator* A) {
   if (A->lb_carry) cudaFreeAsync(A->lb_carry, st);
   for (auto& p : A->shadows) cudaFreeAsync(p.second, st);
   A->shadows.clear();
+  if (A->defl) { deflation_free(A->defl); A->defl = nullptr; }
   free_redbuf(A->red, st);
   cudaStreamSynchronize(st);
   if (A->own_stream) cudaStreamDestroy(st);
@@ -1458,7 +1500,7 @@ void operator_free(Operator* A) {
   template void op_chain<T>(const MatView&, const std::vector<c128>&, int, const T*, T*, T*, T*,   \
                             const int*, cudaStream_t, T, T, const T*);                            \
   template void op_scaleback<T>(Operator&, int, const std::vector<c128>&, int, const T*, T*, T*,  \
-                                T*, const int*, cudaStream_t);                                     \
+                                T*, const int*, cudaStream_t, const T*, c128);                     \
   template void op_precon<T>(Operator&, int, const T*, T*, const int*, cudaStream_t);             \
   template void vec_copy<T>(long, const T*, T*, const int*, cudaStream_t);                        \
   template void vec_scale_vec<T>(long, const void*, bool, const T*, T*, const int*, cudaStream_t);

@@ -25,6 +25,8 @@ enum Format { FMT_NONE = 0, FMT_DENSE = 1, FMT_CRS = 2, FMT_COO = 3, FMT_CDS = 4
 
 // Read-only view of one matrix in one precision (values double/c128 for
 // prec 64, float/c64 for prec 32; `vcplx` tells whether values are complex).
+struct Deflation;
+
 struct MatView {
   int format = FMT_NONE;
   int nrows = 0, ncols = 0;
@@ -52,6 +54,27 @@ struct MatView {
   int n_empty = 0;
   const int* empty_rows = nullptr;
   void* carry = nullptr;
+  // deflation projector applied after the last product of a polynomial chain
+  // (rmatvec = Pmul(real_mv(polpre v))); set on the fp64 view only
+  const Deflation* defl = nullptr;
+};
+
+// Deflation of type(matrix) (matrix_module.f90:1284-1623): V (n x k), AV =
+// real_mv(A, V) and E = V^H A V, all on the device (wide type).  Pmul is
+// I - AV E^-1 V^H, or I - V V^H for a multishift operator.
+struct Deflation {
+  int k = 0;
+  bool multishift = false;
+  bool cplx = false;
+  long n = 0;
+  void* V = nullptr;
+  void* AV = nullptr;
+  void* E = nullptr;     // k x k with leading dimension 16 (the device solver's layout)
+  void* coef = nullptr;  // 2 x 16 coefficient slots written by the reduction tails
+  void* tmp = nullptr;   // n-vector scratch of the chain's last product
+  void* tmp2 = nullptr;  // n-vector scratch of add_deflation
+  RedBuf rb{nullptr, nullptr};
+  cudaStream_t st = nullptr;
 };
 
 constexpr int kCooWarpNnz = 256;   // entries per warp of the segmented reduction (8 per lane)
@@ -159,6 +182,12 @@ struct Operator {
   // statistics of the last flexible (QMRIDR) solve with inner iterations
   int last_inner_calls = 0, last_inner_total = 0, last_inner_max = 0;
 
+  // multishift operator (deflation projector I - V V^H; block system with C)
+  bool multishift = false;
+  Deflation* defl = nullptr;
+  // shifts relative to the seed of the last ms_parameters call (sigma_s)
+  std::vector<c128> sigma_s;
+
   int n() const { return K->nrows; }
   const MatView& view(int prec);
 };
@@ -195,10 +224,26 @@ void op_chain(const MatView& Ks, const std::vector<c128>& alpha, int degree, con
               T* t1, T* t2, const int* skip, cudaStream_t st, T fa = T(1), T fcv = T(0),
               const T* fv = nullptr);
 
-// x = D^-1 p(Ks) y   (scaleback of matrix_module.f90:831-849 without deflation)
+// x = D^-1 p(Ks) y   (scaleback of matrix_module.f90:724-849); with a
+// deflated operator and b, add_deflation (shift sigma_s) comes before D^-1
 template <class T>
 void op_scaleback(Operator& A, int prec, const std::vector<c128>& alpha, int degree,
-                  const T* y, T* x, T* t1, T* t2, const int* skip, cudaStream_t st);
+                  const T* y, T* x, T* t1, T* t2, const int* skip, cudaStream_t st,
+                  const T* b = nullptr, c128 sigma_s = c128(0.0, 0.0));
+
+// Deflation (deflation.cu).  deflation_make: V (device, n x k, the
+// operator's wide type) -> A.defl; k = 0 removes it.  deflation_pmul:
+// out = fa * Pmul(w) + fcv * fv.  deflation_add: add_deflation with the
+// shift sigma_s (0 for a single system): x = V Hs^-1 V^H b +
+// (y - V Hs^-1 V^H (Ks y - sigma_s y)), Hs = E - sigma_s I.
+void deflation_make(Operator& A, const void* V, int k);
+void deflation_free(Deflation* D);
+template <class T>
+void deflation_pmul(const Deflation& D, const T* w, T* out, T fa, T fcv, const T* fv,
+                    const int* skip, cudaStream_t st);
+template <class T>
+void deflation_add(Operator& A, c128 sigma_s, const T* b, const T* y, T* x, const int* skip,
+                   cudaStream_t st);
 
 // w = D^-1 v  (operator / of matrix_module.f90:306-352 for a standard system)
 template <class T>

@@ -171,6 +171,19 @@ int idrs_rmatvec32(idrs_matrix A, const double *v, double *w);
 /* operator(/): rprecon / cprecon, matrix_module.f90:306-400  (w = v/A) */
 int idrs_rprecon(idrs_matrix A, const double *v, double *w);
 int idrs_cprecon(idrs_matrix A, const double *v, double *w);
+/* make_deflation(A, V): matrix_module.f90:1284-1346.  V(n, k), k <= 16,
+ * column-major (complex: interleaved), host or device per the pointer mode;
+ * stores V, A V = real_mv(A, V) and V^H A V; k = 0 removes the deflation.
+ * From then on A*v is Pmul(real_mv(polpre(v))) (matrix_module.f90:152-167)
+ * and scaleback adds the deflated components (add_deflation, :1420-1623).
+ * Pmul is I - AV (V^H A V)^-1 V^H, or I - V V^H for a multishift operator
+ * (idrs_matrix_create_ext with multishift = 1).  The reference's real branch
+ * subtracts V t instead of AV t (matrix_module.f90:1415); this library uses
+ * AV for both kinds.  Not available with fp32 inner solves. */
+int idrs_make_deflation(idrs_matrix A, const double *V, int k);
+/* w = Pmul(A, v): matrix_module.f90:1348-1418 */
+int idrs_rpmul(idrs_matrix A, const double *v, double *w);
+int idrs_cpmul(idrs_matrix A, const double *v, double *w);
 /* scaleback(A, b, y): matrix_module.f90:811-849 */
 int idrs_rscaleback(idrs_matrix A, const double *b, const double *y, double *x);
 int idrs_cscaleback(idrs_matrix A, const double *b, const double *y, double *x);

@@ -363,6 +363,7 @@ int or_matrix_create_ext(const or_umat *K, const or_umat *M, const or_umat *C,
   (*out)->mass_matrix = M != NULL;
   (*out)->damping_matrix = C != NULL;
   (*out)->block_system = multishift && C != NULL;
+  (*out)->multishift = multishift != 0;
   return OR_OK;
 }
 
@@ -380,6 +381,7 @@ int or_matrix_create(const or_umat *K, const or_umat *P, const double *seed, int
 void or_matrix_free(or_mat *A) {
   if (!A) return;
   free(A->ralpha_p); free(A->calpha_p); free(A->ralpha_s); free(A->calpha_s);
+  free(A->sigma_s); free(A->defl_V); free(A->defl_AV); free(A->defl_E);
   free(A);
 }
 
@@ -696,8 +698,10 @@ int or_complex_preconditioner(or_mat *A, int preconditioner, int degree, const o
 int or_real_ms_parameters(or_mat *A, int n_sigma, const double *sigma, double *sigma_p) {
   int d = A->degree;
   free(A->ralpha_s); A->ralpha_s = NULL; A->n_sigma = n_sigma;
+  free(A->sigma_s); A->sigma_s = calloc(n_sigma > 0 ? n_sigma : 1, sizeof(double));
   for (int i = 0; i < n_sigma; ++i) {
     double ss = sigma[i] - A->rseed;
+    ((double *)A->sigma_s)[i] = ss;
     if (d > 0) {
       if (!A->ralpha_s) A->ralpha_s = calloc((size_t)(d + 1) * n_sigma, sizeof(double));
       double *as = A->ralpha_s + (size_t)(d + 1) * i;
@@ -712,8 +716,10 @@ int or_real_ms_parameters(or_mat *A, int n_sigma, const double *sigma, double *s
 int or_complex_ms_parameters(or_mat *A, int n_sigma, const or_cplx *sigma, or_cplx *sigma_p) {
   int d = A->degree;
   free(A->calpha_s); A->calpha_s = NULL; A->n_sigma = n_sigma;
+  free(A->sigma_s); A->sigma_s = calloc(n_sigma > 0 ? n_sigma : 1, sizeof(or_cplx));
   for (int i = 0; i < n_sigma; ++i) {
     or_cplx ss = sigma[i] - A->cseed;
+    ((or_cplx *)A->sigma_s)[i] = ss;
     if (d > 0) {
       if (!A->calpha_s) A->calpha_s = calloc((size_t)(d + 1) * n_sigma, sizeof(or_cplx));
       or_cplx *as = A->calpha_s + (size_t)(d + 1) * i;

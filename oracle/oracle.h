@@ -64,6 +64,10 @@ typedef struct or_mat {
   int preconditioner, degree;
   double *ralpha_p; or_cplx *calpha_p;   /* 0..degree */
   int n_sigma; double *ralpha_s; or_cplx *calpha_s; /* (degree+1) x n_sigma */
+  void *sigma_s;               /* n_sigma shifts relative to the seed (ms_parameters) */
+  int multishift;              /* deflation projector I - V V^H */
+  int n_deflation;             /* deflation: V, AV (n x k), V^H A V (k x k) */
+  void *defl_V, *defl_AV, *defl_E;
 } or_mat;
 
 /* Optional arguments of the solvers: a NULL pointer means "not present". */
@@ -137,6 +141,16 @@ void or_scaleback_r(const or_mat *A, int n, const double *b, const double *y, do
 void or_scaleback_c(const or_mat *A, int n, const or_cplx *b, const or_cplx *y, or_cplx *x);
 void or_ms_scaleback_r(const or_mat *A, int n, int n_sigma, const double *y, double *x);
 void or_ms_scaleback_c(const or_mat *A, int n, int n_sigma, const or_cplx *y, or_cplx *x);
+/* ms_scaleback with the right-hand side b (needed by a deflated operator) */
+void or_ms_scaleback_b_r(const or_mat *A, int n, int n_sigma, const double *b, const double *y, double *x);
+void or_ms_scaleback_b_c(const or_mat *A, int n, int n_sigma, const or_cplx *b, const or_cplx *y, or_cplx *x);
+/* make_deflation (matrix_module.f90:1284-1346), Pmul (:1348-1418) and
+ * add_deflation (:1420-1623).  The real projector uses AV like the complex
+ * one (the reference's real branch subtracts V t instead). */
+int or_make_deflation_r(or_mat *A, int n, const double *V, int k);
+int or_make_deflation_c(or_mat *A, int n, const or_cplx *V, int k);
+void or_pmul_r(const or_mat *A, int n, const double *v, double *w);
+void or_pmul_c(const or_mat *A, int n, const or_cplx *v, or_cplx *w);
 int or_rneumann(int degree, double center, double *alpha);
 int or_rchebyshev(int degree, const double foci[2], double *alpha);
 int or_rcompute_alpha(int degree, const double *H, int ldh, int nh, double *alpha);

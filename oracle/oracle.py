@@ -307,12 +307,30 @@ class Matrix:
         fn(self.ptr, len(y), _p(b), _p(y), _p(x))
         return x
 
-    def ms_scaleback(self, Y):
-        Y = np.asfortranarray(Y, dtype=np.complex128 if self.cplx else np.float64)
+    def ms_scaleback(self, Y, b=None):
+        dt = np.complex128 if self.cplx else np.float64
+        Y = np.asfortranarray(Y, dtype=dt)
         X = np.empty_like(Y, order="F")
-        fn = lib().or_ms_scaleback_c if self.cplx else lib().or_ms_scaleback_r
-        fn(self.ptr, Y.shape[0], Y.shape[1], _p(Y), _p(X))
+        bb = None if b is None else np.ascontiguousarray(b, dtype=dt)
+        fn = lib().or_ms_scaleback_b_c if self.cplx else lib().or_ms_scaleback_b_r
+        fn(self.ptr, Y.shape[0], Y.shape[1], _p(bb), _p(Y), _p(X))
         return X
+
+    def make_deflation(self, V):
+        """make_deflation(A, V) (matrix_module.f90:1284-1346); V is n x k."""
+        V = np.asfortranarray(V, dtype=np.complex128 if self.cplx else np.float64)
+        self._V = V
+        fn = lib().or_make_deflation_c if self.cplx else lib().or_make_deflation_r
+        st = fn(self.ptr, V.shape[0], _p(V), V.shape[1])
+        if st:
+            raise ValueError(f"or_make_deflation status {st}")
+
+    def pmul(self, v):
+        v = np.ascontiguousarray(v, dtype=np.complex128 if self.cplx else np.float64)
+        w = np.empty_like(v)
+        fn = lib().or_pmul_c if self.cplx else lib().or_pmul_r
+        fn(self.ptr, len(v), _p(v), _p(w))
+        return w
 
 
 # --------------------------------------------------------------------------

@@ -395,3 +395,47 @@ def test_precon_with_mass_and_damping_oracle(oracle, P, useM, useC, shift):
     A = oracle.Matrix(K, P=Pm, cplx=cplx)
     v = np.random.default_rng(1).standard_normal(N) + (0.5j if cplx else 0)
     np.testing.assert_allclose(A.precon(v), v / D, rtol=1e-15)
+
+
+def _scaled_cdr(oracle, P, n=6):
+    N = n ** 3
+    rp, ci, kv = P.stencil_to_crs(n, n, n, P.cdr_coefficients(n))
+    rows = np.repeat(np.arange(N), np.diff(rp))
+    D = np.zeros((N, N))
+    D[rows, ci - 1] = kv
+    K = oracle.crs_format(N, N, rp, ci, kv)
+    return N, K, D, D / np.diag(D)[None, :]   # As = K D^-1
+
+
+def test_deflation_oracle(oracle, P):
+    """make_deflation / Pmul / add_deflation (matrix_module.f90:1284-1623)
+    against dense numpy; a deflated solve recovers the solution of A x = b;
+    the multishift projector I - V V^H with V spanning an invariant subspace
+    gives every shifted system's solution."""
+    N, K, D, As = _scaled_cdr(oracle, P)
+    rng = np.random.default_rng(0)
+    V = rng.standard_normal((N, 3))
+    A = oracle.Matrix(K, P=oracle.real_precon(1, K))
+    A.make_deflation(V)
+    w = rng.standard_normal(N)
+    AV = As @ V
+    np.testing.assert_allclose(A.pmul(w), w - AV @ np.linalg.solve(V.T @ AV, V.T @ w), atol=1e-12)
+    b = rng.standard_normal(N)
+    r = oracle.idrs(A, A.pmul(b), 4, tolerance=1e-11, maximum_iterations=2000)
+    x = A.scaleback(b, r.x)
+    assert r.flag == 0 and np.linalg.norm(b - D @ x) <= 1e-9 * np.linalg.norm(b)
+    # complex, multishift: I - V V^H, V an orthonormal basis of an invariant subspace of As
+    ev, EV = np.linalg.eig(As)
+    Vi, _ = np.linalg.qr(EV[:, np.argsort(np.abs(ev))[:2]])
+    Ac = oracle.Matrix(K, P=oracle.complex_precon(1, K), cplx=True, multishift=True)
+    Ac.make_deflation(Vi)
+    wc = w + 1j * rng.standard_normal(N)
+    np.testing.assert_allclose(Ac.pmul(wc), wc - Vi @ (Vi.conj().T @ wc), atol=1e-12)
+    bc = b + 1j * rng.standard_normal(N)
+    sig = np.array([0.1, 0.3 + 0.1j])
+    o = oracle.msidrs(Ac, Ac.pmul(bc), Ac.ms_parameters(sig), 4, tolerance=1e-11,
+                      maximum_iterations=3000)
+    X = Ac.ms_scaleback(o.x, bc)
+    Dm = np.diag(np.diag(D))
+    for k, s in enumerate(sig):  # (K D^-1 - s) y = b  <=>  (K - s D) x = b
+        assert np.linalg.norm(bc - (D - s * Dm) @ X[:, k]) <= 1e-9 * np.linalg.norm(bc)
