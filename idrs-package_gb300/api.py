@@ -66,7 +66,7 @@ _PROTOS = {
     "idrs_cuser_mv": (_i, [_vp, _vp, _vp]),
     "idrs_user_matrix_free": (_i, [_vp]),
     "idrs_matrix_create": (_i, [_vp, _vp, _i, _vp, _vp]),
-    "idrs_matrix_create_ext": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _i, _vp]),
+    "idrs_matrix_create_ext": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp, _i, _vp]),
     "idrs_make_deflation": (_i, [_vp, _vp, _i]),
     "idrs_rpmul": (_i, [_vp, _vp, _vp]),
     "idrs_cpmul": (_i, [_vp, _vp, _vp]),
@@ -345,7 +345,8 @@ def stencil7_format(nx, ny, nz, coef) -> UserMatrix:
 def real_precon(which_precon, K: UserMatrix, shift=None, M: UserMatrix | None = None,
                 C_: UserMatrix | None = None) -> UserMatrix:
     """REAL_PRECON(which_precon, K[, M, C, shift]) (user_module.f90:1327-1463):
-    0 none, 1 diagonal scaling (of K + shift C + shift^2 M with a shift)."""
+    0 none, 1 diagonal scaling, 2 dense LU, 3 band LU (of K + shift C +
+    shift^2 M with a shift)."""
     h = C.c_void_p()
     _check(lib().idrs_real_precon_ext(int(which_precon), K.handle, M.handle if M else None,
                                       C_.handle if C_ else None, _ref_dbl(shift), C.byref(h)))
@@ -386,15 +387,17 @@ class Matrix:
     __array_ufunc__ = None  # `v / A` must reach __rtruediv__ with the whole vector
 
     def __init__(self, K: UserMatrix, P: UserMatrix | None = None, seed=None, complex=False,
-                 M: UserMatrix | None = None, C_: UserMatrix | None = None, multishift=False):
+                 M: UserMatrix | None = None, C_: UserMatrix | None = None, multishift=False,
+                 shift=None):
         self.K, self.P, self.cplx = K, P, bool(complex)
         block = bool(multishift) and C_ is not None
         self.n = 2 * K.nrows if block else K.nrows
         sd = None if seed is None else np.array([np.real(seed), np.imag(seed)], dtype=np.float64)
+        sh = None if shift is None else np.array([np.real(shift), np.imag(shift)], dtype=np.float64)
         h = C.c_void_p()
         _check(lib().idrs_matrix_create_ext(K.handle, M.handle if M else None,
                                             C_.handle if C_ else None, P.handle if P else None,
-                                            int(self.cplx), _p(sd), int(bool(multishift)),
+                                            int(self.cplx), _p(sd), _p(sh), int(bool(multishift)),
                                             C.byref(h)))
         self.handle = h.value
         self.device_pointers = False

@@ -16,7 +16,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libidrs_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 SOURCES = ["matrix.cu", "solvers_real.cu", "solvers_cplx.cu", "solvers_ms_real.cu", "solvers_ms_cplx.cu",
-           "adjoint.cu", "recycle.cu", "deflation.cu", "capi.cu", "setup.cpp", "mm.cpp", "noalloc.cu"]
+           "adjoint.cu", "recycle.cu", "deflation.cu", "lu.cu", "capi.cu", "setup.cpp", "mm.cpp", "noalloc.cu"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
               "-Xcompiler", "-fPIC", "-I", INCLUDE]
 

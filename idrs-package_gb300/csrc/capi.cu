@@ -637,14 +637,32 @@ static void* diagonal_with_mc(const UserMatrix& K, const UserMatrix* Mm, const U
 }
 
 static int precon_common(int which, idrs_user_matrix K, c128 shift, bool want_cplx, idrs_user_matrix* P,
-                         idrs_user_matrix Mm = nullptr, idrs_user_matrix Cm = nullptr) {
+                         idrs_user_matrix Mm = nullptr, idrs_user_matrix Cm = nullptr,
+                         bool has_shift = false) {
   REQUIRE(K && P, "real_precon: bad arguments");
-  if (which != 0 && which != 1) throw unsupported_error("precon: only which_precon 0 and 1 (diagonal scaling) are supported");
+  if (which < 0 || which > 3) throw unsupported_error("precon: which_precon must be 0..3");
+  for (const UserMatrix* X : {(const UserMatrix*)Mm, (const UserMatrix*)Cm})
+    REQUIRE(!X || (X->nrows == K->nrows && X->ncols == K->ncols), "precon: M and C must match K");
   auto* M = new idrs_user_matrix_s();
   M->format = FMT_CDS;
   M->which_precon = which;
   M->nrows = K->nrows;
   M->ncols = K->ncols;
+  if (which == 2 || which == 3) {
+    // shift-and-invert: dense (2) or band (3) LU of the shifted matrix
+    bool cplx = want_cplx || shift.y != 0.0 || K->vals == 2 || (Mm && Mm->vals == 2) || (Cm && Cm->vals == 2);
+    try {
+      lu_build(*K, has_shift ? Mm : nullptr, has_shift ? Cm : nullptr, has_shift, shift, which, cplx, *M);
+    } catch (const cuda_error&) {
+      delete M;
+      throw;
+    } catch (const std::exception& e) {
+      delete M;
+      throw arg_error(e.what());
+    }
+    *P = M;
+    return IDRS_OK;
+  }
   if (which == 1 && (Mm || Cm)) {
     for (const UserMatrix* X : {(const UserMatrix*)Mm, (const UserMatrix*)Cm})
       REQUIRE(!X || (X->nrows == K->nrows && X->ncols == K->ncols), "precon: M and C must match K");
@@ -707,8 +725,16 @@ static int ms_parameters(idrs_matrix A, int n_sigma, const double* sigma, double
   A->n_sigma = n_sigma;
   A->alpha_s.assign((size_t)(d + 1) * n_sigma, c128(0.0));
   A->sigma_s.assign(n_sigma, c128(0.0));
+  const cd seed(A->seed.x, A->seed.y), shift(A->shift.x, A->shift.y);
+  auto sig = [&](int i) { return cplx ? cd(sigma[2 * i], sigma[2 * i + 1]) : cd(sigma[i], 0.0); };
+  if (A->shift_invert) {
+    REQUIRE(shift != seed, "Preconditioner shift should not be equal to seed, choose preconditioner shift and seed differently");
+    for (int i = 0; i < n_sigma; ++i)
+      REQUIRE(shift != sig(i), "Preconditioner shift should not be equal to one of the shifts, choose different preconditioner shift");
+  }
   for (int i = 0; i < n_sigma; ++i) {
-    cd ss = (cplx ? cd(sigma[2 * i], sigma[2 * i + 1]) : cd(sigma[i], 0.0)) - cd(A->seed.x, A->seed.y);
+    // shift-and-invert: (sigma - seed)/(sigma - shift) (matrix_module.f90:445-455)
+    cd ss = A->shift_invert ? (sig(i) - seed) / (sig(i) - shift) : sig(i) - seed;
     A->sigma_s[i] = c128(ss.real(), ss.imag());
     cd sp;
     if (d > 0) {
@@ -770,7 +796,8 @@ static int scaleback_t(idrs_matrix A, const double* b, const double* y, double* 
 }
 
 template <class T>
-static int ms_scaleback_t(idrs_matrix A, int n_sigma, const double* b, const double* y, double* x) {
+static int ms_scaleback_t(idrs_matrix A, int n_sigma, const double* sigma, const double* b,
+                          const double* y, double* x) {
   REQUIRE(A && y && x && n_sigma >= 1, "ms_scaleback: bad arguments");
   REQUIRE(A->degree == 0 || A->n_sigma == n_sigma, "ms_scaleback: call ms_parameters with these shifts first");
   REQUIRE(!A->defl || (b && (int)A->sigma_s.size() == n_sigma),
@@ -786,8 +813,15 @@ static int ms_scaleback_t(idrs_matrix A, int n_sigma, const double* b, const dou
     std::vector<c128> al(A->alpha_s.begin() + (size_t)(d + 1) * i, A->alpha_s.begin() + (size_t)(d + 1) * (i + 1));
     if (d == 0) al.assign(1, c128(1.0));
     const c128 ss = A->defl ? A->sigma_s[i] : c128(0.0);
+    c128 factor(1.0, 0.0);
+    if (A->shift_invert) {  // (seed - shift)/(sigma - shift), matrix_module.f90:755-761
+      REQUIRE(sigma, "ms_scaleback: shift-and-invert needs the shifts");
+      const cd sg = traits<T>::is_cplx ? cd(sigma[2 * i], sigma[2 * i + 1]) : cd(sigma[i], 0.0);
+      const cd f = (cd(A->seed.x, A->seed.y) - cd(A->shift.x, A->shift.y)) / (sg - cd(A->shift.x, A->shift.y));
+      factor = c128(f.real(), f.imag());
+    }
     op_scaleback<T>(*A, 64, al, d, dy + n * i, dx + n * i, t1.as<T>(), t2.as<T>(), nullptr, A->stream,
-                    db, ss);
+                    db, ss, factor);
   }
   sv.finish(x, dx);
   IDRS_CUDA(cudaStreamSynchronize(A->stream));
@@ -887,14 +921,12 @@ int idrs_cscaleback(idrs_matrix A, const double* b, const double* y, double* x) 
 
 int idrs_ms_rscaleback(idrs_matrix A, int n_sigma, const double* sigma, const double* b,
                        const double* y, double* x) {
-  (void)sigma;
-  return guard([&] { REQUIRE(A && !A->cplx, "ms_rscaleback: real handle required"); return ms_scaleback_t<double>(A, n_sigma, b, y, x); });
+  return guard([&] { REQUIRE(A && !A->cplx, "ms_rscaleback: real handle required"); return ms_scaleback_t<double>(A, n_sigma, sigma, b, y, x); });
 }
 
 int idrs_ms_cscaleback(idrs_matrix A, int n_sigma, const double* sigma, const double* b,
                        const double* y, double* x) {
-  (void)sigma;
-  return guard([&] { REQUIRE(A && A->cplx, "ms_cscaleback: complex handle required"); return ms_scaleback_t<c128>(A, n_sigma, b, y, x); });
+  return guard([&] { REQUIRE(A && A->cplx, "ms_cscaleback: complex handle required"); return ms_scaleback_t<c128>(A, n_sigma, sigma, b, y, x); });
 }
 
 int idrs_rnorm(idrs_matrix A, const double* w, double* norm) { return guard([&] { return norm_t<double>(A, w, nullptr, norm, false); }); }
@@ -1047,27 +1079,30 @@ int idrs_stencil7_format(int nx, int ny, int nz, const double* coef, idrs_user_m
 }
 
 int idrs_real_precon(int which_precon, idrs_user_matrix K, const double* shift, idrs_user_matrix* P) {
-  return guard([&] { return precon_common(which_precon, K, c128(shift ? *shift : 0.0, 0.0), false, P); });
+  return guard([&] {
+    return precon_common(which_precon, K, c128(shift ? *shift : 0.0, 0.0), false, P, nullptr, nullptr,
+                         shift != nullptr);
+  });
 }
 int idrs_complex_precon(int which_precon, idrs_user_matrix K, const double* shift, idrs_user_matrix* P) {
   return guard([&] {
     c128 sh = shift ? c128(shift[0], shift[1]) : c128(0.0);
-    return precon_common(which_precon, K, sh, true, P);
+    return precon_common(which_precon, K, sh, true, P, nullptr, nullptr, shift != nullptr);
   });
 }
 int idrs_real_precon_ext(int which_precon, idrs_user_matrix K, idrs_user_matrix M,
                          idrs_user_matrix C, const double* shift, idrs_user_matrix* P) {
   return guard([&] {
-    // without a shift the reference takes diag(K) alone
+    // without a shift the reference takes K alone
     if (!shift) return precon_common(which_precon, K, c128(0.0), false, P);
-    return precon_common(which_precon, K, c128(*shift, 0.0), false, P, M, C);
+    return precon_common(which_precon, K, c128(*shift, 0.0), false, P, M, C, true);
   });
 }
 int idrs_complex_precon_ext(int which_precon, idrs_user_matrix K, idrs_user_matrix M,
                             idrs_user_matrix C, const double* shift, idrs_user_matrix* P) {
   return guard([&] {
     if (!shift) return precon_common(which_precon, K, c128(0.0), true, P);
-    return precon_common(which_precon, K, c128(shift[0], shift[1]), true, P, M, C);
+    return precon_common(which_precon, K, c128(shift[0], shift[1]), true, P, M, C, true);
   });
 }
 
@@ -1265,18 +1300,28 @@ idrs_user_matrix block_diagonal(const UserMatrix& P, long nn) {
 
 }  // namespace
 
+inline bool block_of(int multishift, const UserMatrix* Cm) { return multishift && Cm; }
+
 extern "C" {
 
 int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix Mm, idrs_user_matrix Cm,
-                           idrs_user_matrix P, int is_complex, const double* seed, int multishift,
-                           idrs_matrix* A) {
+                           idrs_user_matrix P, int is_complex, const double* seed,
+                           const double* shift, int multishift, idrs_matrix* A) {
   return guard([&] {
     REQUIRE(K && A, "matrix_create: bad arguments");
-    if (!Mm && !Cm) {
-      int st = idrs_matrix_create(K, P, is_complex, seed, A);
-      if (!st) (*A)->multishift = multishift != 0;
-      return st;
-    }
+    const bool si = P && shift;
+    if (si && multishift && Cm)
+      throw unsupported_error("matrix_create: shift-and-invert of the block system is not supported");
+    auto finish = [&](int st) {
+      if (st) return st;
+      (*A)->multishift = multishift != 0;
+      if (si) {
+        (*A)->shift_invert = true;
+        (*A)->shift = is_complex ? c128(shift[0], shift[1]) : c128(shift[0], 0.0);
+      }
+      return IDRS_OK;
+    };
+    if (!Mm && !Cm) return finish(idrs_matrix_create(K, P, is_complex, seed, A));
     REQUIRE(K->nrows == K->ncols, "matrix_create: K must be square");
     for (const UserMatrix* X : {(const UserMatrix*)Mm, (const UserMatrix*)Cm}) {
       if (!X) continue;
@@ -1287,7 +1332,8 @@ int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix Mm, idrs_user_ma
     if (K->format != FMT_CRS && K->format != FMT_COO)
       throw unsupported_error("matrix_create: with mass or damping matrices K must be CRS or COO");
     REQUIRE(!P || P->nrows == K->nrows, "matrix_create: P size mismatch");
-    REQUIRE(!P || P->which_precon == 1, "matrix_create: only a diagonal P is supported here");
+    REQUIRE(!P || P->which_precon <= 1 || !block_of(multishift, Cm),
+            "matrix_create: the block system takes a diagonal P");
     init_runtime();
     const bool cplx = is_complex != 0;
     c128 sd(0.0, 0.0);
@@ -1308,8 +1354,7 @@ int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix Mm, idrs_user_ma
       (*A)->seed = sd;
       (*A)->seed_folded = true;
     }
-    (*A)->multishift = multishift != 0;
-    return IDRS_OK;
+    return finish(IDRS_OK);
   });
 }
 

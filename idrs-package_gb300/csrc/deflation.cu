@@ -115,7 +115,7 @@ void make_typed(Operator& A, Deflation& D, const T* V) {
   MatView Ks = A.view(64);
   Ks.defl = nullptr;
   for (int j = 0; j < k; ++j)
-    spmv<T>(Ks, (const T*)D.V + (size_t)n * j, (T*)D.AV + (size_t)n * j, T(1), T(0), nullptr, nullptr, st);
+    ks_mv<T>(Ks, (const T*)D.V + (size_t)n * j, (T*)D.AV + (size_t)n * j, T(1), T(0), nullptr, nullptr, st);
   IDRS_CUDA(cudaMemsetAsync(D.E, 0, sizeof(T) * MAXS * MAXS, st));
   for (int j = 0; j < k; ++j)
     launch_fused_nd<T>(k, n, BDefDots<T>{(const T*)D.V, n, (const T*)D.AV + (size_t)n * j, k},
@@ -183,7 +183,7 @@ void deflation_add(Operator& A, c128 sigma_s, const T* b, const T* y, T* x, cons
   MatView Ks = A.view(64);
   Ks.defl = nullptr;
   T* ay = (T*)D.tmp2;
-  spmv<T>(Ks, y, ay, T(1), T(0) - ss, y, skip, st);
+  ks_mv<T>(Ks, y, ay, T(1), T(0) - ss, y, skip, st);
   dots_then<T>(D, ay, TDefSolve<T>{(const T*)D.E, t2, D.k, true, ss}, skip, st);
   k_defl_add<T><<<stream_grid(D.n), kThreads, 0, st>>>(D.n, (const T*)D.V, D.k, t1, t2, y, x, skip);
   IDRS_LAUNCH_CHECK();

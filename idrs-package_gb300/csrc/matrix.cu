@@ -936,6 +936,18 @@ void spmv(const MatView& M, const T* x, T* y, T a, T cv, const T* v, const int* 
 // ---------------------------------------------------------------------------
 template <class T> static inline T narrow_c(c128 v) { return narrow<T>(v); }
 
+template <class T>
+void ks_mv(const MatView& Ks, const T* x, T* y, T a, T cv, const T* v, const int* skip,
+           cudaStream_t st) {
+  if constexpr (sizeof(typename traits<T>::real) == 8) {
+    if (Ks.lu) {
+      lu_solve<T>(*Ks.lu, x, (T*)Ks.lu_tmp, skip, st);
+      x = (const T*)Ks.lu_tmp;
+    }
+  }
+  spmv<T>(Ks, x, y, a, cv, v, skip, st);
+}
+
 // The last product of a chain: w = fa * Pmul(Ks u) + fcv * fv (Pmul only with
 // a deflated fp64 operator).
 template <class T>
@@ -944,12 +956,12 @@ static void chain_last(const MatView& Ks, const T* u, T* w, T fa, T fcv, const T
   if constexpr (sizeof(typename traits<T>::real) == 8) {
     if (Ks.defl && Ks.defl->k > 0) {
       T* tmp = (T*)Ks.defl->tmp;
-      spmv<T>(Ks, u, tmp, T(1), T(0), nullptr, skip, st);
+      ks_mv<T>(Ks, u, tmp, T(1), T(0), nullptr, skip, st);
       deflation_pmul<T>(*Ks.defl, tmp, w, fa, fcv, fv, skip, st);
       return;
     }
   }
-  spmv<T>(Ks, u, w, fa, fcv, fv, skip, st);
+  ks_mv<T>(Ks, u, w, fa, fcv, fv, skip, st);
 }
 
 template <class T>
@@ -960,11 +972,11 @@ void op_chain(const MatView& Ks, const std::vector<c128>& alpha, int degree, con
     return;
   }
   // u_{d-1} = Ks (alpha_d v) + alpha_{d-1} v
-  spmv<T>(Ks, v, t1, narrow_c<T>(alpha[degree]), narrow_c<T>(alpha[degree - 1]), v, skip, st);
+  ks_mv<T>(Ks, v, t1, narrow_c<T>(alpha[degree]), narrow_c<T>(alpha[degree - 1]), v, skip, st);
   T* cur = t1;
   T* nxt = t2;
   for (int k = degree - 2; k >= 0; --k) {
-    spmv<T>(Ks, cur, nxt, T(1), narrow_c<T>(alpha[k]), v, skip, st);
+    ks_mv<T>(Ks, cur, nxt, T(1), narrow_c<T>(alpha[k]), v, skip, st);
     std::swap(cur, nxt);
   }
   chain_last<T>(Ks, cur, w, fa, fcv, fv, skip, st);
@@ -1167,6 +1179,12 @@ void vec_scale_vec(long n, const void* d, bool dcplx, const T* a, T* b, const in
 template <class T>
 void op_precon(Operator& A, int prec, const T* v, T* w, const int* skip, cudaStream_t st) {
   long n = A.n();
+  if constexpr (sizeof(typename traits<T>::real) == 8) {
+    if (A.P && (A.P->which_precon == 2 || A.P->which_precon == 3)) {
+      lu_solve<T>(*A.P, v, w, skip, st);
+      return;
+    }
+  }
   if (A.dkind == 0) {
     vec_copy<T>(n, v, w, skip, st);
   } else if (A.dkind == 1) {
@@ -1180,13 +1198,16 @@ void op_precon(Operator& A, int prec, const T* v, T* w, const int* skip, cudaStr
 
 template <class T>
 void op_scaleback(Operator& A, int prec, const std::vector<c128>& alpha, int degree, const T* y,
-                  T* x, T* t1, T* t2, const int* skip, cudaStream_t st, const T* b, c128 sigma_s) {
+                  T* x, T* t1, T* t2, const int* skip, cudaStream_t st, const T* b, c128 sigma_s,
+                  c128 factor) {
   const MatView& Ks = A.view(prec);
   long n = A.n();
   if constexpr (sizeof(typename traits<T>::real) == 8) {
-    if (A.defl && A.defl->k > 0) {
-      if (!b) throw std::runtime_error("scaleback: a deflated operator needs the right-hand side b");
-      // p = polpre(y) (no scaling yet), q = add_deflation(b, p), x = q / A
+    const bool defl = A.defl && A.defl->k > 0;
+    const bool lu = A.P && (A.P->which_precon == 2 || A.P->which_precon == 3);
+    if (defl || lu || factor.x != 1.0 || factor.y != 0.0) {
+      if (defl && !b) throw std::runtime_error("scaleback: a deflated operator needs the right-hand side b");
+      // p = polpre(y) with real_mv; add_deflation; the shift-and-invert factor; x = p / A
       const T* cur = y;
       T* bufs[2] = {t1, t2};
       int nb = 0;
@@ -1194,12 +1215,22 @@ void op_scaleback(Operator& A, int prec, const std::vector<c128>& alpha, int deg
         T a = (k == degree - 1) ? narrow<T>(alpha[degree]) : T(1);
         T* dst = bufs[nb];
         nb ^= 1;
-        spmv<T>(Ks, cur, dst, a, narrow<T>(alpha[k]), y, skip, st);
+        ks_mv<T>(Ks, cur, dst, a, narrow<T>(alpha[k]), y, skip, st);
         cur = dst;
       }
-      T* q = bufs[nb];
-      deflation_add<T>(A, sigma_s, b, cur, q, skip, st);
-      op_precon<T>(A, prec, q, x, skip, st);
+      if (defl) {
+        T* q = bufs[nb];
+        nb ^= 1;
+        deflation_add<T>(A, sigma_s, b, cur, q, skip, st);
+        cur = q;
+      }
+      if (factor.x != 1.0 || factor.y != 0.0) {
+        T* q = bufs[nb];
+        k_scale_uniform<T><<<stream_grid(n), kThreads, 0, st>>>(n, narrow<T>(factor), cur, q, skip);
+        IDRS_LAUNCH_CHECK();
+        cur = q;
+      }
+      op_precon<T>(A, prec, cur, x, skip, st);
       return;
     }
   }
@@ -1337,6 +1368,11 @@ int build_operator(Operator* A) {
   A->k64.carry = A->lb_carry;
   A->ks64 = A->k64;
   A->ks32 = MatView();
+  if (A->P && (A->P->which_precon == 2 || A->P->which_precon == 3)) {
+    if (A->P->nrows != (int)n) { set_error("shift-and-invert preconditioner size mismatch"); return 1; }
+    if (A->P->vals == 2 && !A->cplx) { set_error("complex LU preconditioner on a real problem"); return 1; }
+    if (!A->lu_tmp) IDRS_CUDA(cudaMallocAsync(&A->lu_tmp, (A->cplx ? 16 : 8) * std::max<long>(n, 1), st));
+  }
   A->dkind = 0;
   A->dinv_u = c128(1.0, 0.0);
   A->dinv_cplx = false;
@@ -1436,12 +1472,16 @@ __global__ void k_narrow(long n, const Tin* a, Tout* b) {
 }
 
 const MatView& Operator::view(int prec) {
+  const bool lu = P && (P->which_precon == 2 || P->which_precon == 3);
   if (prec != 32) {
     ks64.defl = defl;
+    ks64.lu = lu ? P : nullptr;
+    ks64.lu_tmp = lu_tmp;
     return ks64;
   }
   if (defl && defl->k > 0)
     throw std::runtime_error("deflation is not available in the fp32 operator (inner_precision 32)");
+  if (lu) throw std::runtime_error("shift-and-invert is not available in the fp32 operator (inner_precision 32)");
   if (ks32.format != FMT_NONE) return ks32;
   ks32 = ks64;
   cudaStream_t st = stream;
@@ -1482,6 +1522,7 @@ void operator_free(Operator* A) {
   for (auto& p : A->shadows) cudaFreeAsync(p.second, st);
   A->shadows.clear();
   if (A->defl) { deflation_free(A->defl); A->defl = nullptr; }
+  if (A->lu_tmp) { cudaFreeAsync(A->lu_tmp, st); A->lu_tmp = nullptr; }
   free_redbuf(A->red, st);
   cudaStreamSynchronize(st);
   if (A->own_stream) cudaStreamDestroy(st);
@@ -1500,7 +1541,8 @@ void operator_free(Operator* A) {
   template void op_chain<T>(const MatView&, const std::vector<c128>&, int, const T*, T*, T*, T*,   \
                             const int*, cudaStream_t, T, T, const T*);                            \
   template void op_scaleback<T>(Operator&, int, const std::vector<c128>&, int, const T*, T*, T*,  \
-                                T*, const int*, cudaStream_t, const T*, c128);                     \
+                                T*, const int*, cudaStream_t, const T*, c128, c128);               \
+  template void ks_mv<T>(const MatView&, const T*, T*, T, T, const T*, const int*, cudaStream_t); \
   template void op_precon<T>(Operator&, int, const T*, T*, const int*, cudaStream_t);             \
   template void vec_copy<T>(long, const T*, T*, const int*, cudaStream_t);                        \
   template void vec_scale_vec<T>(long, const void*, bool, const T*, T*, const int*, cudaStream_t);

@@ -57,6 +57,10 @@ struct MatView {
   // deflation projector applied after the last product of a polynomial chain
   // (rmatvec = Pmul(real_mv(polpre v))); set on the fp64 view only
   const Deflation* defl = nullptr;
+  // shift-and-invert preconditioner: every product is Ks (P^-1 v), the
+  // triangular solves of P's LU factor into lu_tmp first (fp64 view only)
+  const struct UserMatrix* lu = nullptr;
+  void* lu_tmp = nullptr;
 };
 
 // Deflation of type(matrix) (matrix_module.f90:1284-1623): V (n x k), AV =
@@ -184,6 +188,11 @@ struct Operator {
 
   // multishift operator (deflation projector I - V V^H; block system with C)
   bool multishift = false;
+  // shift-and-invert: P is the LU factor of the matrix at `shift`
+  // (which_precon 2 dense, 3 band); lu_tmp is the solves' scratch vector
+  bool shift_invert = false;
+  c128 shift;
+  void* lu_tmp = nullptr;
   Deflation* defl = nullptr;
   // shifts relative to the seed of the last ms_parameters call (sigma_s)
   std::vector<c128> sigma_s;
@@ -229,7 +238,22 @@ void op_chain(const MatView& Ks, const std::vector<c128>& alpha, int degree, con
 template <class T>
 void op_scaleback(Operator& A, int prec, const std::vector<c128>& alpha, int degree,
                   const T* y, T* x, T* t1, T* t2, const int* skip, cudaStream_t st,
-                  const T* b = nullptr, c128 sigma_s = c128(0.0, 0.0));
+                  const T* b = nullptr, c128 sigma_s = c128(0.0, 0.0),
+                  c128 factor = c128(1.0, 0.0));
+
+// Shift-and-invert LU factors (lu.cu).  lu_build: P = the dense (which 2) or
+// band (which 3) LU factor, without pivoting, of K + shift C + shift^2 M (C
+// only: + shift^2 I; M only: K - shift M; no shift: K); throws on a zero
+// pivot.  lu_solve: x = P^-1 b (x may equal b).
+void lu_build(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, bool has_shift,
+              c128 shift, int which, bool cplx, UserMatrix& P);
+template <class T>
+void lu_solve(const UserMatrix& P, const T* b, T* x, const int* skip, cudaStream_t st);
+// y = a * Ks (P^-1 x) + cv * v: real_mv of matrix_module.f90:218-264 on a
+// view (the LU solve only with a shift-and-invert preconditioner)
+template <class T>
+void ks_mv(const MatView& Ks, const T* x, T* y, T a, T cv, const T* v, const int* skip,
+           cudaStream_t st);
 
 // Deflation (deflation.cu).  deflation_make: V (device, n x k, the
 // operator's wide type) -> A.defl; k = 0 removes it.  deflation_pmul:

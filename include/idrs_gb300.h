@@ -82,9 +82,13 @@ int idrs_real_precon(int which_precon, idrs_user_matrix K, const double *shift,
 /* COMPLEX_PRECON: user_module.f90:1465-1603 (shift = {re, im}) */
 int idrs_complex_precon(int which_precon, idrs_user_matrix K, const double *shift,
                         idrs_user_matrix *P);
-/* The same with mass M and damping C (NULL = absent), user_module.f90:1327-1381
- * and :1465-1520: with a shift the diagonal of K + shift C + shift^2 M (C only:
- * + shift^2; M only: K - shift M), each matrix's diagonal with zeros -> 1. */
+/* The same with mass M and damping C (NULL = absent), user_module.f90:1327-1602.
+ * which_precon 1: with a shift the diagonal of K + shift C + shift^2 M (C only:
+ * + shift^2; M only: K - shift M), each matrix's diagonal with zeros -> 1.
+ * which_precon 2 / 3: the dense / band LU factor (no pivoting, as the
+ * reference; a zero pivot is IDRS_ERR_ARG) of that shifted matrix, factored
+ * on the device; K, M, C must be CRS or COO.  v/P is then two triangular
+ * solves on the device. */
 int idrs_real_precon_ext(int which_precon, idrs_user_matrix K, idrs_user_matrix M,
                          idrs_user_matrix C, const double *shift, idrs_user_matrix *P);
 int idrs_complex_precon_ext(int which_precon, idrs_user_matrix K, idrs_user_matrix M,
@@ -131,10 +135,15 @@ int idrs_matrix_create(idrs_user_matrix K, idrs_user_matrix P, int is_complex,
  *   [-C - seed M, -K; I, -seed I] (without M: -seed I in the (1,1) block),
  *   whose vectors have length 2n and whose diagonal scaling is [P; 1].
  * The combination is assembled once into one CRS matrix (K, M, C must be
- * CRS or COO; others: IDRS_ERR_UNSUPPORTED), so each product is one SpMV. */
+ * CRS or COO; others: IDRS_ERR_UNSUPPORTED), so each product is one SpMV.
+ * With a shift-and-invert P (which_precon 2/3) and `shift` (NULL = absent),
+ * A%shift_invert holds (real_matrix.inc:23-29): every product is
+ * K' (P^-1 v), ms_parameters uses (sigma - seed)/(sigma - shift) and the
+ * multishift scaleback the factor (seed - shift)/(sigma - shift).  The block
+ * system's shift-and-invert form is not supported (IDRS_ERR_UNSUPPORTED). */
 int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix M, idrs_user_matrix C,
-                           idrs_user_matrix P, int is_complex, const double *seed, int multishift,
-                           idrs_matrix *A);
+                           idrs_user_matrix P, int is_complex, const double *seed,
+                           const double *shift, int multishift, idrs_matrix *A);
 int idrs_matrix_free(idrs_matrix A);
 int idrs_matrix_set_stream(idrs_matrix A, void *cuda_stream);
 int idrs_matrix_set_pointer_mode(idrs_matrix A, int mode);

@@ -280,6 +280,171 @@ int or_complex_diagonal(const or_umat *A, or_cplx *D) {
 
 /* REAL_PRECON: user_module.f90:1327-1381, which_precon = 1 (diagonal
  * scaling, optionally shifted: D(K) - shift).  Dense/band LU are out of scope. */
+/* ------------------------------------------------------------------------ */
+/* Shift-and-invert preconditioners, which_precon 2 (dense LU) and 3 (band  */
+/* LU): user_module.f90:1383-1463, :1520-1602, real_dense :1163-1235,      */
+/* get_band :1833-1872, real_band :1981-2066, LU_decomp :1604-1701,         */
+/* band_LU_decomp :2068-2179.  Values are combined in complex arithmetic    */
+/* and stored by kind.                                                      */
+/* ------------------------------------------------------------------------ */
+static or_cplx umat_val(const or_umat *A, long k) {
+  if (A->vals == 2) return A->cval[k];
+  if (A->vals == 1) return A->rval[k];
+  return 1.;
+}
+
+/* real_dense / complex_dense: dense (all), CRS, COO; other formats give zeros */
+static void to_dense(const or_umat *A, or_cplx *D) {
+  long n = A->nrows;
+  for (long i = 0; i < n * (long)A->ncols; ++i) D[i] = 0;
+  if (A->format == OR_DENSE) {
+    for (long i = 0; i < n * (long)A->ncols; ++i) D[i] = A->cmat ? A->cmat[i] : (A->rmat ? A->rmat[i] : 0.);
+  } else if (A->format == OR_CRS) {
+    for (long i = 0; i < n; ++i)
+      for (int k = A->row_ptr[i]; k < A->row_ptr[i + 1]; ++k) D[i + n * A->col_ind[k]] += umat_val(A, k);
+  } else if (A->format == OR_COO) {
+    for (long k = 0; k < A->nnz; ++k) D[A->indx[k] + n * A->jndx[k]] += umat_val(A, k);
+  }
+}
+
+/* get_band */
+static int band_of(const or_umat *A) {
+  int hb = 0;
+  if (A->format == OR_DENSE) return A->ncols;
+  if (A->format == OR_CRS) {
+    for (int i = 0; i < A->nrows; ++i)
+      for (int k = A->row_ptr[i]; k < A->row_ptr[i + 1]; ++k) {
+        int d = abs(A->col_ind[k] - i);
+        if (d > hb) hb = d;
+      }
+  } else if (A->format == OR_COO) {
+    for (long k = 0; k < A->nnz; ++k) {
+      int d = abs(A->jndx[k] - A->indx[k]);
+      if (d > hb) hb = d;
+    }
+  } else if (A->format == OR_CDS) {
+    hb = A->half_band;
+  }
+  return hb;
+}
+
+/* real_band / complex_band: B(n, -hb:hb) from CRS, COO, CDS; dense gives zeros */
+static void to_band(const or_umat *A, int hb, or_cplx *B) {
+  long n = A->nrows, w = 2L * hb + 1;
+  for (long i = 0; i < n * w; ++i) B[i] = 0;
+  if (A->format == OR_CRS) {
+    for (long i = 0; i < n; ++i)
+      for (int k = A->row_ptr[i]; k < A->row_ptr[i + 1]; ++k)
+        B[i + n * ((long)(A->col_ind[k] - i) + hb)] += umat_val(A, k);
+  } else if (A->format == OR_COO) {
+    for (long k = 0; k < A->nnz; ++k)
+      B[A->indx[k] + n * ((long)(A->jndx[k] - A->indx[k]) + hb)] += umat_val(A, k);
+  } else if (A->format == OR_CDS) {
+    int h = A->half_band;
+    for (long d = -h; d <= h; ++d)
+      for (long i = 0; i < n; ++i) {
+        or_cplx v = A->cband ? A->cband[i + n * (d + h)] : (A->rband ? A->rband[i + n * (d + h)] : 1.);
+        B[i + n * (d + hb)] = v;
+      }
+  }
+}
+
+/* the shifted matrix K + shift C + shift^2 M (C only: + shift^2 I; M only:
+ * K - shift M; neither: K - shift I), element by element like the reference */
+static void combine(long cnt, or_cplx *S, const or_cplx *Cd, const or_cplx *Md, int hasC, int hasM,
+                    or_cplx sh) {
+  for (long i = 0; i < cnt; ++i) {
+    if (hasM && hasC) S[i] = S[i] + sh * Cd[i] + (sh * sh) * Md[i];
+    else if (hasC) S[i] = S[i] + sh * Cd[i];
+    else if (hasM) S[i] = S[i] - sh * Md[i];
+  }
+}
+
+/* LU_decomp without pivoting; returns OR_EARG on a zero pivot */
+static int lu_decomp_dense(long n, or_cplx *LU) {
+  for (long k = 0; k < n; ++k) {
+    or_cplx p = LU[k + n * k];
+    if (p == 0) return OR_EARG;  /* 'Pivot equal to zero in LU decomposition' */
+    for (long i = k + 1; i < n; ++i) {
+      if (LU[i + n * k] == 0) continue;
+      LU[i + n * k] = LU[i + n * k] / p;
+      or_cplx l = LU[i + n * k];
+      for (long j = k + 1; j < n; ++j) LU[i + n * j] = LU[i + n * j] - l * LU[k + n * j];
+    }
+  }
+  return OR_OK;
+}
+
+/* band_LU_decomp without pivoting on B(n, -hb:hb) */
+static int lu_decomp_band(long n, int hb, or_cplx *B) {
+#define BB(i, d) B[(i) + n * ((long)(d) + hb)]
+  for (long k = 0; k < n - 1; ++k) {
+    or_cplx p = BB(k, 0);
+    if (p == 0) return OR_EARG;
+    long last = k + hb < n - 1 ? k + hb : n - 1;
+    for (long i = k + 1; i <= last; ++i) {
+      long dia = k - i;
+      BB(i, dia) = BB(i, dia) / p;
+      or_cplx l = BB(i, dia);
+      for (long j = 1; j <= hb; ++j) BB(i, dia + j) = BB(i, dia + j) - l * BB(k, j);
+    }
+  }
+#undef BB
+  return OR_OK;
+}
+
+static int lu_precon(int which, const or_umat *K, const or_umat *M, const or_umat *C,
+                     const double *shift, int cplx, or_umat *P) {
+  long n = K->nrows;
+  or_cplx sh = 0;
+  if (shift) sh = cplx ? shift[0] + I * shift[1] : shift[0];
+  int st = OR_OK;
+  if (which == 2) {
+    long cnt = n * n;
+    or_cplx *S = malloc(sizeof(or_cplx) * (cnt ? cnt : 1)), *Cd = NULL, *Md = NULL;
+    to_dense(K, S);
+    if (shift) {
+      if (C) { Cd = malloc(sizeof(or_cplx) * (cnt ? cnt : 1)); to_dense(C, Cd); }
+      if (M) { Md = malloc(sizeof(or_cplx) * (cnt ? cnt : 1)); to_dense(M, Md); }
+      combine(cnt, S, Cd, Md, C != NULL, M != NULL, sh);
+      if (C && !M) for (long i = 0; i < n; ++i) S[i + n * i] += sh * sh;
+      if (!C && !M) for (long i = 0; i < n; ++i) S[i + n * i] -= sh;
+    }
+    st = lu_decomp_dense(n, S);
+    P->format = OR_DENSE;
+    if (cplx) { P->vals = 2; P->cmat = S; S = NULL; }
+    else {
+      P->vals = 1; P->rmat = malloc(sizeof(double) * (cnt ? cnt : 1));
+      for (long i = 0; i < cnt; ++i) P->rmat[i] = creal(S[i]);
+    }
+    free(S); free(Cd); free(Md);
+  } else {
+    int hb = band_of(K);
+    if (shift && C && band_of(C) > hb) hb = band_of(C);
+    if (shift && M && band_of(M) > hb) hb = band_of(M);
+    long cnt = n * (2L * hb + 1);
+    or_cplx *S = malloc(sizeof(or_cplx) * (cnt ? cnt : 1)), *Cd = NULL, *Md = NULL;
+    to_band(K, hb, S);
+    if (shift) {
+      if (C) { Cd = malloc(sizeof(or_cplx) * (cnt ? cnt : 1)); to_band(C, hb, Cd); }
+      if (M) { Md = malloc(sizeof(or_cplx) * (cnt ? cnt : 1)); to_band(M, hb, Md); }
+      combine(cnt, S, Cd, Md, C != NULL, M != NULL, sh);
+      if (C && !M) for (long i = 0; i < n; ++i) S[i + n * hb] += sh * sh;
+      if (!C && !M) for (long i = 0; i < n; ++i) S[i + n * hb] -= sh;
+    }
+    st = lu_decomp_band(n, hb, S);
+    P->format = OR_CDS;
+    P->half_band = hb;
+    if (cplx) { P->vals = 2; P->cband = S; S = NULL; }
+    else {
+      P->vals = 1; P->rband = malloc(sizeof(double) * (cnt ? cnt : 1));
+      for (long i = 0; i < cnt; ++i) P->rband[i] = creal(S[i]);
+    }
+    free(S); free(Cd); free(Md);
+  }
+  return st;
+}
+
 /* REAL_PRECON / COMPLEX_PRECON, which_precon 0/1: user_module.f90:1327-1381 and
  * :1465-1520.  The diagonal of K, or with a shift that of K + shift C +
  * shift^2 M (C only: + shift^2; M only: K - shift M; neither: K - shift), each
@@ -308,6 +473,9 @@ int or_real_precon_ext(int which_precon, const or_umat *K, const or_umat *M, con
       }
       free(dc); free(dm);
     }
+  } else if (which_precon == 2 || which_precon == 3) {
+    int st = lu_precon(which_precon, K, M, C, shift, 0, P);
+    if (st != OR_OK) { or_umat_free(P); return st; }
   } else if (which_precon != 0) {
     or_umat_free(P); return OR_EUNSUP;
   }
@@ -338,6 +506,9 @@ int or_complex_precon_ext(int which_precon, const or_umat *K, const or_umat *M, 
       }
       free(dc); free(dm);
     }
+  } else if (which_precon == 2 || which_precon == 3) {
+    int st = lu_precon(which_precon, K, M, C, shift, 1, P);
+    if (st != OR_OK) { or_umat_free(P); return st; }
   } else if (which_precon != 0) {
     or_umat_free(P); return OR_EUNSUP;
   }
@@ -355,10 +526,16 @@ int or_complex_precon(int which_precon, const or_umat *K, const double *shift, o
 /* type(matrix): M/PP_MATRIX/matrix_module.f90:38-81                        */
 /* ------------------------------------------------------------------------ */
 int or_matrix_create_ext(const or_umat *K, const or_umat *M, const or_umat *C,
-                         const or_umat *P, const double *seed, int cplx, int multishift,
-                         or_mat **out) {
+                         const or_umat *P, const double *seed, const double *shift, int cplx,
+                         int multishift, or_mat **out) {
+  if (P && shift && multishift && C) return OR_EUNSUP;
   int st = or_matrix_create(K, P, seed, cplx, out);
   if (st != OR_OK) return st;
+  if (P && shift) {
+    (*out)->shift_invert = 1;
+    if (cplx) (*out)->cshift = shift[0] + I * shift[1];
+    else (*out)->rshift = shift[0];
+  }
   (*out)->M = M; (*out)->C = C;
   (*out)->mass_matrix = M != NULL;
   (*out)->damping_matrix = C != NULL;
@@ -381,7 +558,7 @@ int or_matrix_create(const or_umat *K, const or_umat *P, const double *seed, int
 void or_matrix_free(or_mat *A) {
   if (!A) return;
   free(A->ralpha_p); free(A->calpha_p); free(A->ralpha_s); free(A->calpha_s);
-  free(A->sigma_s); free(A->defl_V); free(A->defl_AV); free(A->defl_E);
+  free(A->sigma_s); free(A->sigma); free(A->defl_V); free(A->defl_AV); free(A->defl_E);
   free(A);
 }
 
@@ -699,8 +876,14 @@ int or_real_ms_parameters(or_mat *A, int n_sigma, const double *sigma, double *s
   int d = A->degree;
   free(A->ralpha_s); A->ralpha_s = NULL; A->n_sigma = n_sigma;
   free(A->sigma_s); A->sigma_s = calloc(n_sigma > 0 ? n_sigma : 1, sizeof(double));
+  free(A->sigma); A->sigma = calloc(n_sigma > 0 ? n_sigma : 1, sizeof(double));
+  memcpy(A->sigma, sigma, sizeof(double) * n_sigma);
+  if (A->shift_invert) {
+    if (A->rshift == A->rseed) return OR_EARG;
+    for (int i = 0; i < n_sigma; ++i) if (A->rshift == sigma[i]) return OR_EARG;
+  }
   for (int i = 0; i < n_sigma; ++i) {
-    double ss = sigma[i] - A->rseed;
+    double ss = A->shift_invert ? (sigma[i] - A->rseed) / (sigma[i] - A->rshift) : sigma[i] - A->rseed;
     ((double *)A->sigma_s)[i] = ss;
     if (d > 0) {
       if (!A->ralpha_s) A->ralpha_s = calloc((size_t)(d + 1) * n_sigma, sizeof(double));
@@ -717,8 +900,14 @@ int or_complex_ms_parameters(or_mat *A, int n_sigma, const or_cplx *sigma, or_cp
   int d = A->degree;
   free(A->calpha_s); A->calpha_s = NULL; A->n_sigma = n_sigma;
   free(A->sigma_s); A->sigma_s = calloc(n_sigma > 0 ? n_sigma : 1, sizeof(or_cplx));
+  free(A->sigma); A->sigma = calloc(n_sigma > 0 ? n_sigma : 1, sizeof(or_cplx));
+  memcpy(A->sigma, sigma, sizeof(or_cplx) * n_sigma);
+  if (A->shift_invert) {
+    if (A->cshift == A->cseed) return OR_EARG;
+    for (int i = 0; i < n_sigma; ++i) if (A->cshift == sigma[i]) return OR_EARG;
+  }
   for (int i = 0; i < n_sigma; ++i) {
-    or_cplx ss = sigma[i] - A->cseed;
+    or_cplx ss = A->shift_invert ? (sigma[i] - A->cseed) / (sigma[i] - A->cshift) : sigma[i] - A->cseed;
     ((or_cplx *)A->sigma_s)[i] = ss;
     if (d > 0) {
       if (!A->calpha_s) A->calpha_s = calloc((size_t)(d + 1) * n_sigma, sizeof(or_cplx));

@@ -65,7 +65,10 @@ typedef struct or_mat {
   double *ralpha_p; or_cplx *calpha_p;   /* 0..degree */
   int n_sigma; double *ralpha_s; or_cplx *calpha_s; /* (degree+1) x n_sigma */
   void *sigma_s;               /* n_sigma shifts relative to the seed (ms_parameters) */
+  void *sigma;                 /* the shifts of the last ms_parameters call */
   int multishift;              /* deflation projector I - V V^H */
+  int shift_invert;            /* P is the LU of the matrix at `shift` */
+  double rshift; or_cplx cshift;
   int n_deflation;             /* deflation: V, AV (n x k), V^H A V (k x k) */
   void *defl_V, *defl_AV, *defl_E;
 } or_mat;
@@ -122,10 +125,12 @@ void or_user_precon_c(const or_umat *A, const or_cplx *v, or_cplx *w);
 int or_matrix_create(const or_umat *K, const or_umat *P, const double *seed, int cplx,
                      or_mat **out);
 /* type(matrix) with mass M and damping C (real_matrix.inc:9-43): the 2x2
- * block system when multishift and C are both present (vectors of 2n). */
+ * block system when multishift and C are both present (vectors of 2n); with
+ * P and shift, P is a shift-and-invert preconditioner (the block system's
+ * shift-and-invert form is not restated: OR_EUNSUP). */
 int or_matrix_create_ext(const or_umat *K, const or_umat *M, const or_umat *C,
-                         const or_umat *P, const double *seed, int cplx, int multishift,
-                         or_mat **out);
+                         const or_umat *P, const double *seed, const double *shift, int cplx,
+                         int multishift, or_mat **out);
 void or_matrix_free(or_mat *A);
 int or_real_preconditioner(or_mat *A, int preconditioner, int degree, const double *foci,
                            const double *center, const double *H, int ldh, int nh);

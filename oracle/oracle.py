@@ -240,7 +240,8 @@ def real_diagonal(K: UserMatrix):
 # --------------------------------------------------------------------------
 class Matrix:
     def __init__(self, K: UserMatrix, P: UserMatrix | None = None, seed=None, cplx=False,
-                 M: UserMatrix | None = None, C_: UserMatrix | None = None, multishift=False):
+                 M: UserMatrix | None = None, C_: UserMatrix | None = None, multishift=False,
+                 shift=None):
         self.K, self.P, self.cplx = K, P, cplx
         self.M, self.C = M, C_  # keep the user matrices alive
         block = bool(multishift) and C_ is not None
@@ -248,10 +249,13 @@ class Matrix:
         sd = None
         if seed is not None:
             sd = np.array([np.real(seed), np.imag(seed)], dtype=np.float64)
+        sh = None
+        if shift is not None:
+            sh = np.array([np.real(shift), np.imag(shift)], dtype=np.float64)
         out = C.c_void_p()
         st = lib().or_matrix_create_ext(K.ptr, M.ptr if M else None, C_.ptr if C_ else None,
-                                        P.ptr if P else None, _p(sd), int(cplx), int(bool(multishift)),
-                                        C.byref(out))
+                                        P.ptr if P else None, _p(sd), _p(sh), int(cplx),
+                                        int(bool(multishift)), C.byref(out))
         if st:
             raise ValueError(f"or_matrix_create status {st}")
         self.ptr = out

@@ -439,3 +439,60 @@ def test_deflation_oracle(oracle, P):
     Dm = np.diag(np.diag(D))
     for k, s in enumerate(sig):  # (K D^-1 - s) y = b  <=>  (K - s D) x = b
         assert np.linalg.norm(bc - (D - s * Dm) @ X[:, k]) <= 1e-9 * np.linalg.norm(bc)
+
+
+def _mass_and_damping(oracle, N, rng):
+    """a tridiagonal mass matrix and a diagonal damping matrix, CRS, plus dense copies"""
+    Md = np.diag(rng.uniform(1.0, 2.0, N)) + np.diag(np.full(N - 1, 0.1), 1) + np.diag(np.full(N - 1, 0.1), -1)
+    Cd = np.diag(rng.uniform(0.0, 0.5, N))
+
+    def crs(Dm):
+        r, c = np.nonzero(Dm)
+        rp = np.concatenate([[1], 1 + np.cumsum(np.bincount(r, minlength=N))]).astype(np.int32)
+        return oracle.crs_format(N, N, rp, (c + 1).astype(np.int32), Dm[r, c])
+    return crs(Md), Md, crs(Cd), Cd
+
+
+@pytest.mark.parametrize("which", [2, 3])
+@pytest.mark.parametrize("form", ["none", "K", "M", "C", "MC"])
+def test_lu_preconditioners_oracle(oracle, P, which, form):
+    """REAL_PRECON(2 dense LU / 3 band LU, K[, M, C, shift]) (user_module.f90:1383-1463):
+    v / P solves with the shifted matrix."""
+    N, K, D, _ = _scaled_cdr(oracle, P, n=4)
+    rng = np.random.default_rng(4)
+    M, Md, C, Cd = _mass_and_damping(oracle, N, rng)
+    sh = 2.5
+    kw, S = {}, D.copy()
+    if form == "K":
+        kw, S = dict(shift=sh), D - sh * np.eye(N)
+    elif form == "M":
+        kw, S = dict(shift=sh, M=M), D - sh * Md
+    elif form == "C":
+        kw, S = dict(shift=sh, C_=C), D + sh * Cd + sh ** 2 * np.eye(N)
+    elif form == "MC":
+        kw, S = dict(shift=sh, M=M, C_=C), D + sh * Cd + sh ** 2 * Md
+    Pm = oracle.real_precon(which, K, **kw)
+    A = oracle.Matrix(K, P=Pm)
+    v = rng.standard_normal(N)
+    np.testing.assert_allclose(A.precon(v), np.linalg.solve(S, v), rtol=1e-10, atol=1e-13)
+
+
+def test_shift_and_invert_multishift_oracle(oracle, P):
+    """Multishift with a band-LU shift-and-invert preconditioner at `shift`
+    (matrix_module.f90:402-483, :724-766): the shifted systems
+    (K - sigma M) x = b all come out of one MSIDRS run."""
+    N, K, D, _ = _scaled_cdr(oracle, P, n=5)
+    rng = np.random.default_rng(6)
+    M, Md, _, _ = _mass_and_damping(oracle, N, rng)
+    seed, shift = 0.0, -60.0
+    Pm = oracle.complex_precon(3, K, shift=shift, M=M)
+    A = oracle.Matrix(K, P=Pm, M=M, seed=seed, shift=shift, cplx=True, multishift=True)
+    sig = np.array([10.0, 20.0 + 5j, -5.0])
+    sp = A.ms_parameters(sig)
+    np.testing.assert_allclose(sp, (sig - seed) / (sig - shift), rtol=1e-15)
+    b = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    o = oracle.msidrs(A, b, sp, 4, tolerance=1e-11, maximum_iterations=2000)
+    assert o.flag == 0
+    X = A.ms_scaleback(o.x, b)
+    for k, s in enumerate(sig):
+        assert np.linalg.norm(b - (D - s * Md) @ X[:, k]) <= 1e-9 * np.linalg.norm(b)
