@@ -1179,10 +1179,12 @@ void vec_scale_vec(long n, const void* d, bool dcplx, const T* a, T* b, const in
 template <class T>
 void op_precon(Operator& A, int prec, const T* v, T* w, const int* skip, cudaStream_t st) {
   long n = A.n();
-  if constexpr (sizeof(typename traits<T>::real) == 8) {
-    if (A.P && (A.P->which_precon == 2 || A.P->which_precon == 3)) {
+  if (A.P && (A.P->which_precon == 2 || A.P->which_precon == 3)) {
+    if constexpr (sizeof(typename traits<T>::real) == 8) {
       lu_solve<T>(*A.P, v, w, skip, st);
       return;
+    } else {
+      throw std::runtime_error("shift-and-invert is not available in fp32 (inner_precision 32)");
     }
   }
   if (A.dkind == 0) {
