@@ -9,7 +9,8 @@ Python identifier).
 from . import build as build_recipe  # noqa: F401
 from . import problems  # noqa: F401
 from .api import (  # noqa: F401
-    ADJOINT, IDRS, IDRS_RITZ, INPROD, MSIDRS, MSQMRIDR, NORM, PP_IDRS, PP_MR_IDRS, QMRIDR, IDRSError,
+    ADJOINT, IDRS, IDRS_RITZ, INPROD, MSIDRS, MSQMRIDR, NORM, PP_IDRS, PP_MR_IDRS, PP_MS_IDRS, QMRIDR,
+    IDRSError,
     Matrix,
     POINTER_DEVICE, crs_transpose, sparse_outer_grad, mm_matrix, mm_read,
     POINTER_HOST, Result, UserMatrix, cds_format, complex_diagonal, complex_precon, coo_format,

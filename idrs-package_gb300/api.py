@@ -118,6 +118,12 @@ _PROTOS = {
                              _i, _vp, _i, _vp, _i, _i, _vp, _vp]),
     "idrs_rpp_idrs": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "idrs_rpp_mr_idrs": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "idrs_rpp_idrs_ext": (_i, [_vp] * 9),
+    "idrs_cpp_idrs": (_i, [_vp] * 9),
+    "idrs_rpp_mr_idrs_ext": (_i, [_vp, _i] + [_vp] * 8),
+    "idrs_cpp_mr_idrs": (_i, [_vp, _i] + [_vp] * 8),
+    "idrs_rpp_ms_idrs": (_i, [_vp, _vp, _i] + [_vp] * 9),
+    "idrs_cpp_ms_idrs": (_i, [_vp, _vp, _i] + [_vp] * 9),
 }
 
 
@@ -137,7 +143,14 @@ class PPReport(C.Structure):
                 ("seconds_total", C.c_double), ("inner_solves", C.c_int),
                 ("inner_iterations", C.c_int), ("inner_max", C.c_int),
                 ("recycle_flag", C.c_int), ("recycle_iterations", C.c_int),
-                ("recycle_relres", C.c_double)]
+                ("recycle_relres", C.c_double), ("foci_imag", C.c_double * 2),
+                ("center_imag", C.c_double)]
+
+
+class PPInputs(C.Structure):
+    """idrs_pp_inputs: M, C, seed, shift, V of pp_idrs (pointers; NULL = absent)."""
+    _fields_ = [("M", C.c_void_p), ("C", C.c_void_p), ("seed", C.c_void_p),
+                ("shift", C.c_void_p), ("V", C.c_void_p), ("n_deflation", C.c_int)]
 
 
 def load(path: str | None = None):
@@ -747,10 +760,13 @@ def _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degr
 
 
 def _pp_result(rep: PPReport, **extra) -> Result:
+    foci = tuple(complex(rep.foci[q], rep.foci_imag[q]) if rep.foci_imag[q] else rep.foci[q]
+                 for q in range(2))
+    center = complex(rep.center, rep.center_imag) if rep.center_imag else rep.center
     return Result(flag=rep.flag, iterations=rep.iterations,
                   ritz_iterations=rep.ritz_iterations, nritz=rep.nritz,
                   relres=rep.relres_solver, relres_original=rep.relres_original,
-                  foci=tuple(rep.foci), center=rep.center, seconds_setup=rep.seconds_setup,
+                  foci=foci, center=center, seconds_setup=rep.seconds_setup,
                   seconds_solve=rep.seconds_solve, seconds_total=rep.seconds_total,
                   inner_solves=rep.inner_solves, inner_iterations=rep.inner_iterations,
                   inner_max=rep.inner_max, recycle_flag=rep.recycle_flag,
@@ -758,37 +774,81 @@ def _pp_result(rep: PPReport, **extra) -> Result:
                   **extra)
 
 
+def _pp_kind(K, b, M, C_, seed, shift, complex_):
+    if complex_ is not None:
+        return bool(complex_)
+    return bool(K.cplx or (M is not None and M.cplx) or (C_ is not None and C_.cplx)
+                or np.iscomplexobj(b) or np.iscomplexobj(seed) or np.iscomplexobj(shift))
+
+
+def _pp_inputs(cplx, M, C_, seed, shift, V, keep):
+    """idrs_pp_inputs (or None when every optional input is absent)."""
+    if M is None and C_ is None and seed is None and shift is None and V is None:
+        return None
+    inp = PPInputs()
+    inp.M = M.handle if M else None
+    inp.C = C_.handle if C_ else None
+    for name, v in (("seed", seed), ("shift", shift)):
+        if v is not None:
+            a = np.array([np.real(v), np.imag(v)], dtype=np.float64)
+            keep.append(a)
+            setattr(inp, name, a.ctypes.data)
+    if V is not None:
+        Va = np.asfortranarray(V, dtype=np.complex128 if cplx else np.float64)
+        keep.append(Va)
+        inp.V = Va.ctypes.data
+        inp.n_deflation = Va.shape[1]
+    keep.append(inp)
+    return C.byref(inp)
+
+
+def _pp_cf(cplx, center, foci):
+    """center / foci in the pipeline's kind (complex: re/im pairs)."""
+    dt = np.complex128 if cplx else np.float64
+    c = None if center is None else np.asarray([center], dtype=dt)
+    f = None if foci is None else np.ascontiguousarray(foci, dtype=dt)
+    return c, f
+
+
 def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=None, *, method=1,
             s=4, tol=1e-6, maxit=1000, in_s=1, in_it=0, in_tol=0.1, preconditioner=0, degree=0,
-            n_ritz=32, inner_precision=64, n_omega=0, x_out=None) -> Result:
-    """x = pp_idrs(K, b[, P, center, foci]) (RPP_IDRS, pp_idrs_module.f90:118-162);
-    the command-line options of initialize.inc:4-31 are keyword arguments.
+            n_ritz=32, inner_precision=64, n_omega=0, M=None, C_=None, seed=None, shift=None,
+            V=None, complex=None, x_out=None) -> Result:
+    """x = pp_idrs(K, b[, M, C, P, center, foci, seed, shift, V]) (RPP_IDRS / CPP_IDRS,
+    pp_idrs_module.f90:64-162); the command-line options of initialize.inc:4-31
+    are keyword arguments.
 
     b may be a numpy array (host) or an int device address; with a device b,
     x_out must be the device address of the solution vector."""
     dev = isinstance(b, int)
+    cplx = _pp_kind(K, None if dev else b, M, C_, seed, shift, complex)
     if dev:
         if not isinstance(x_out, int):
             raise ValueError("a device b needs a device x_out")
         x = x_out
     else:
-        b = _arr(b, False, K.nrows)
+        b = _arr(b, cplx, K.nrows)
         x = np.empty_like(b)
     o = _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
                     inner_precision, dev, n_omega, False)
     rep = PPReport()
-    f = None if foci is None else np.ascontiguousarray(foci, dtype=np.float64)
-    _check(lib().idrs_rpp_idrs(K.handle, _p(b), P.handle if P else None, _ref_dbl(center), _p(f),
-                               C.byref(o), C.byref(rep), _p(x)))
+    keep = []
+    c, f = _pp_cf(cplx, center, foci)
+    inp = _pp_inputs(cplx, M, C_, seed, shift, V, keep)
+    fn = lib().idrs_cpp_idrs if cplx else lib().idrs_rpp_idrs_ext
+    _check(fn(K.handle, _p(b), P.handle if P else None, _p(c), _p(f), inp, C.byref(o), C.byref(rep),
+              _p(x)))
     return _pp_result(rep, x=None if dev else x)
 
 
 def PP_MR_IDRS(K: UserMatrix, b_all, P: UserMatrix | None = None, center=None, foci=None, *,
                method=1, s=4, tol=1e-6, maxit=1000, in_s=1, in_it=0, in_tol=0.1,
                preconditioner=0, degree=0, n_ritz=32, inner_precision=64, n_omega=0,
-               recycle=False, nrhs=None, x_out=None) -> Result:
-    """x_all = pp_idrs(K, b_all[, P, center, foci]) for a sequence of right-hand sides
-    (RPP_MR_IDRS, pp_idrs_module.f90:222-279, recycle.inc, run_mr_idrs.inc).
+               recycle=False, M=None, C_=None, seed=None, shift=None, V=None, complex=None,
+               nrhs=None, x_out=None) -> Result:
+    """x_all = pp_idrs(K, b_all[, M, C, P, center, foci, seed, shift, V]) for a sequence
+    of right-hand sides (RPP_MR_IDRS / CPP_MR_IDRS, pp_idrs_module.f90:164-279,
+    recycle.inc, run_mr_idrs.inc).
 
     b_all: n x nrhs numpy array, or the int device address of a column-major
     n x nrhs array (then nrhs and the device address x_out are required).
@@ -796,22 +856,27 @@ def PP_MR_IDRS(K: UserMatrix, b_all, P: UserMatrix | None = None, center=None, f
     iterations, relres, relres_original, seconds_solve."""
     dev = isinstance(b_all, int)
     n = K.nrows
+    cplx = _pp_kind(K, None if dev else b_all, M, C_, seed, shift, complex)
+    dt = np.complex128 if cplx else np.float64
     if dev:
         if not isinstance(x_out, int) or not nrhs:
             raise ValueError("a device b_all needs nrhs and a device x_out")
         x = x_out
     else:
-        b_all = np.asfortranarray(b_all, dtype=np.float64)
+        b_all = np.asfortranarray(b_all, dtype=dt)
         if b_all.ndim != 2 or b_all.shape[0] != n:
             raise ValueError("b_all must be n x nrhs")
         nrhs = b_all.shape[1]
-        x = np.zeros((n, nrhs), order="F")
+        x = np.zeros((n, nrhs), dtype=dt, order="F")
     o = _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
                     inner_precision, dev, n_omega, recycle)
     reps = (PPReport * nrhs)()
-    f = None if foci is None else np.ascontiguousarray(foci, dtype=np.float64)
-    _check(lib().idrs_rpp_mr_idrs(K.handle, int(nrhs), _p(b_all), P.handle if P else None,
-                                  _ref_dbl(center), _p(f), C.byref(o), reps, _p(x)))
+    keep = []
+    c, f = _pp_cf(cplx, center, foci)
+    inp = _pp_inputs(cplx, M, C_, seed, shift, V, keep)
+    fn = lib().idrs_cpp_mr_idrs if cplx else lib().idrs_rpp_mr_idrs_ext
+    _check(fn(K.handle, int(nrhs), _p(b_all), P.handle if P else None, _p(c), _p(f), inp,
+              C.byref(o), reps, _p(x)))
     r = _pp_result(reps[nrhs - 1], x=None if dev else x)
     r["flags"] = np.array([q.flag for q in reps])
     r["iterations"] = np.array([q.iterations for q in reps])
@@ -819,3 +884,30 @@ def PP_MR_IDRS(K: UserMatrix, b_all, P: UserMatrix | None = None, center=None, f
     r["relres_original"] = np.array([q.relres_original for q in reps])
     r["seconds_solve"] = np.array([q.seconds_solve for q in reps])
     return r
+
+
+def PP_MS_IDRS(K: UserMatrix, rhs, sigma, P: UserMatrix | None = None, center=None, foci=None, *,
+               method=1, s=4, tol=1e-6, maxit=1000, in_s=1, in_it=0, in_tol=0.1,
+               preconditioner=0, degree=0, n_ritz=32, inner_precision=64, n_omega=0, M=None,
+               C_=None, seed=None, shift=None, V=None, complex=None) -> Result:
+    """x(n, n_sigma) = pp_idrs(K, rhs, sigma[, M, C, P, center, foci, seed, shift, V])
+    (RPP_MS_IDRS / CPP_MS_IDRS with run_ms_idrs.inc).  With C the block system
+    is solved and x is the second half of each solution.  relres_sigma: the
+    true residual of every shifted system."""
+    cplx = _pp_kind(K, rhs, M, C_, seed, shift, complex) or np.iscomplexobj(sigma)
+    dt = np.complex128 if cplx else np.float64
+    rhs = _arr(rhs, cplx, K.nrows)
+    sig = np.ascontiguousarray(sigma, dtype=dt)
+    ns = len(sig)
+    x = np.zeros((K.nrows, ns), dtype=dt, order="F")
+    rel = np.zeros(ns)
+    o = _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
+                    inner_precision, False, n_omega, False)
+    rep = PPReport()
+    keep = []
+    c, f = _pp_cf(cplx, center, foci)
+    inp = _pp_inputs(cplx, M, C_, seed, shift, V, keep)
+    fn = lib().idrs_cpp_ms_idrs if cplx else lib().idrs_rpp_ms_idrs
+    _check(fn(K.handle, _p(rhs), ns, _p(sig), P.handle if P else None, _p(c), _p(f), inp,
+              C.byref(o), C.byref(rep), _p(rel), _p(x)))
+    return _pp_result(rep, x=x, relres_sigma=rel)

@@ -1768,14 +1768,20 @@ int idrs_ridrs_ritz(idrs_matrix A, const double* b, int s, idrs_matrix M,
 // ------------------------------------------------------------- pp_idrs
 namespace {
 
-// One pp_idrs job: the operator built from K (and P), its device buffers and
-// what the set-up solves produced (x0, omega, U0).
+using clk = std::chrono::steady_clock;
+
+// One pp_idrs job (pp_idrs_module.f90): the operator built from K (M, C, P,
+// seed, shift, V), its device buffers and what the set-up solves produced
+// (x0, omega, U0).  T: double (RPP_*) or c128 (CPP_*).
+template <class T>
 struct PPJob {
   idrs_matrix A = nullptr;
-  long n = 0;
+  long n = 0;          // vector length (2 nn for the block system)
+  long nn = 0;         // rows of K
+  bool block = false;  // multishift with C: the 2 x 2 block system
   cudaStream_t cs = nullptr;
   DBuf d_x0, d_y, t1, t2, r, res;
-  std::vector<double> omega;  // allocated when the initial solve ran
+  std::vector<T> omega;  // allocated when the initial solve ran
   DBuf U0;
   bool have_U0 = false;
   ~PPJob() {
@@ -1785,122 +1791,226 @@ struct PPJob {
   }
 };
 
-// real_preconditioner.inc:10-34: the initial IDRS_RITZ solve (x0, H and,
-// with n_omega > 0, omega) and the polynomial preconditioner.
-int pp_setup(PPJob& J, const double* pb, const double* center, const double* foci,
+template <class T> constexpr bool kCplx = traits<T>::is_cplx;
+
+// stores the real part of a reduction result (|w|^2 of a real or complex w)
+__device__ inline double re_of(double v) { return v; }
+__device__ inline double re_of(c128 v) { return v.x; }
+template <class W> struct TStoreRe {
+  double* out;
+  __device__ void operator()(const W* v) const { *out = re_of(v[0]); }
+};
+
+// y = y + a x
+template <class T>
+__global__ void k_axpy(long n, T a, const T* __restrict__ x, T* y) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x)
+    y[i] = y[i] + a * x[i];
+}
+template <class T>
+void axpy(long n, T a, const T* x, T* y, cudaStream_t st) {
+  k_axpy<T><<<stream_grid(n), kThreads, 0, st>>>(n, a, x, y);
+  IDRS_LAUNCH_CHECK();
+}
+
+// real_matrix.inc / complex_matrix.inc (+ make_deflation when V is given)
+template <class T>
+int pp_open(PPJob<T>& J, idrs_user_matrix K, idrs_user_matrix P, const idrs_pp_inputs* in,
+            bool multishift, const idrs_pp_options* opt) {
+  REQUIRE(K, "pp_idrs: K is required");
+  REQUIRE(opt->s >= 1, "rpp_idrs: s must be positive");
+  REQUIRE(opt->n_omega >= 0, "rpp_idrs: n_omega must not be negative");
+  idrs_user_matrix M = in ? in->M : nullptr, C = in ? in->C : nullptr;
+  int st = idrs_matrix_create_ext(K, M, C, P, kCplx<T> ? 1 : 0, in ? in->seed : nullptr,
+                                  in ? in->shift : nullptr, multishift ? 1 : 0, &J.A);
+  if (st) return st;
+  J.n = J.A->n();
+  J.nn = K->nrows;
+  J.block = multishift && C;
+  J.cs = J.A->stream;
+  const size_t vb = sizeof(T) * J.n;
+  J.d_x0 = DBuf(vb, J.cs);
+  J.d_y = DBuf(vb, J.cs);
+  J.t1 = DBuf(vb, J.cs);
+  J.t2 = DBuf(vb, J.cs);
+  J.r = DBuf(vb, J.cs);
+  J.res = DBuf(16, J.cs);
+  IDRS_CUDA(cudaMemsetAsync(J.d_x0.p, 0, vb, J.cs));
+  if (in && in->V && in->n_deflation > 0) {  // host V (n x k)
+    st = idrs_make_deflation(J.A, in->V, in->n_deflation);
+    if (st) return st;
+  }
+  J.A->device_pointers = true;
+  return IDRS_OK;
+}
+
+// IDRS_RITZ for the set-up solves: real -> idrs_ridrs_ritz; complex -> IDRS
+// with the Hessenberg output and the complex omega ordering.
+template <class T>
+int pp_ritz(PPJob<T>& J, const T* pb, int s, double tol, int maxit, T* x, double* H, int ldh,
+            int nh, int n_omega, T* omega, double* U0, int dimU0, int* flag, double* relres,
+            int* iter, int* nritz) {
+  int one = 1;
+  if constexpr (!kCplx<T>) {
+    return idrs_ridrs_ritz(J.A, pb, s, nullptr, &tol, &maxit, &one, flag, relres, iter, nullptr,
+                           U0, dimU0, n_omega > 0 ? omega : nullptr, n_omega, nullptr, 0, H, ldh, nh,
+                           nritz, x);
+  } else {
+    REQUIRE(dimU0 == 0, "pp_idrs: the complex recycle space is not supported");
+    std::vector<double> Hf((size_t)2 * (maxit + 1) * maxit, 0.0), resnrm(maxit + 1);
+    int st = run_idrs<c128>(J.A, (const double*)pb, s, nullptr, &tol, &maxit, &one, flag, relres, iter,
+                            nullptr, nullptr, nullptr, 0, resnrm.data(), maxit + 1, Hf.data(), maxit + 1,
+                            maxit, (double*)x);
+    if (st) return st;
+    const int nr = (*iter / (s + 1)) * s + *iter % (s + 1);
+    *nritz = nr;
+    if (omega && n_omega > 0) {
+      REQUIRE(nr >= n_omega, "Too many parameters omega requested, reduce omega.");
+      ritz_omega((const std::complex<double>*)Hf.data(), maxit + 1, n_omega, (std::complex<double>*)omega);
+    }
+    if (H)
+      for (int j = 0; j < nh; ++j)
+        for (int i = 0; i < ldh; ++i) {
+          H[2 * (i + (size_t)ldh * j)] = Hf[2 * (i + (size_t)(maxit + 1) * j)];
+          H[2 * (i + (size_t)ldh * j) + 1] = Hf[2 * (i + (size_t)(maxit + 1) * j) + 1];
+        }
+    return IDRS_OK;
+  }
+}
+
+// real_preconditioner.inc / complex_preconditioner.inc: the initial
+// IDRS_RITZ solve (x0, H and, with n_omega > 0, omega) and the polynomial
+// preconditioner.  center / foci: 1 / 2 values of the kind of T.
+template <class T>
+int pp_setup(PPJob<T>& J, const T* pb, const double* center, const double* foci,
              const idrs_pp_options* opt, idrs_pp_report& rep) {
   const int s = opt->s;
+  constexpr int vw = kCplx<T> ? 2 : 1;
   int preconditioner = opt->degree == 0 ? 0 : opt->preconditioner;
   bool estimate = preconditioner != 0;
   if (preconditioner == 1 && center) estimate = false;
   if (preconditioner == 2 && foci) estimate = false;
   const bool initial = estimate || opt->n_omega > 0;
-  double tol = opt->tol;
-  int st = 0;
   std::vector<double> H;
   int ldh = 0;
   if (initial) {
     int ini_iter = opt->n_ritz + opt->n_ritz / s;
     ldh = ini_iter + 1;
-    H.assign((size_t)ldh * ini_iter, 0.0);
-    J.omega.assign(std::max(opt->n_omega, 0), 0.0);
-    int flag = -1, iter = 0, nr = 0, one = 1;
+    H.assign((size_t)vw * ldh * ini_iter, 0.0);
+    J.omega.assign(std::max(opt->n_omega, 0), T(0.0));
+    int flag = -1, iter = 0, nr = 0;
     double rel = 1;
-    st = idrs_ridrs_ritz(J.A, pb, s, nullptr, &tol, &ini_iter, &one, &flag, &rel, &iter,
-                         J.d_x0.as<double>(), nullptr, 0,
-                         opt->n_omega > 0 ? J.omega.data() : nullptr, opt->n_omega, nullptr, 0,
-                         H.data(), ldh, ini_iter, &nr, J.d_x0.as<double>());
+    int st = pp_ritz<T>(J, pb, s, opt->tol, ini_iter, J.d_x0.template as<T>(), H.data(), ldh, ini_iter,
+                        opt->n_omega, J.omega.data(), nullptr, 0, &flag, &rel, &iter, &nr);
     if (st) return st;
     rep.ritz_iterations = iter;
     rep.nritz = nr;
   }
   if (estimate) {
-    analyse_spectrum(H.data(), ldh, rep.nritz, rep.foci, &rep.center, nullptr);
-    st = set_preconditioner(J.A, preconditioner, opt->degree, nullptr, nullptr, H.data(), ldh, rep.nritz);
-  } else {
-    double f[2] = {0.15, 1.85}, c = 1.0;
-    if (foci) { f[0] = foci[0]; f[1] = foci[1]; }
-    if (center) c = *center;
-    rep.foci[0] = f[0]; rep.foci[1] = f[1]; rep.center = c;
-    st = set_preconditioner(J.A, preconditioner, opt->degree, f, &c, nullptr, 0, 0);
+    if constexpr (kCplx<T>) {
+      std::vector<std::complex<double>> Hc((size_t)ldh * std::max(rep.nritz, 1));
+      for (size_t q = 0; q < Hc.size() && 2 * q + 1 < H.size(); ++q) Hc[q] = {H[2 * q], H[2 * q + 1]};
+      std::complex<double> f[2], c;
+      analyse_spectrum(Hc.data(), ldh, rep.nritz, f, &c, nullptr);
+      rep.foci[0] = f[0].real(); rep.foci[1] = f[1].real(); rep.center = c.real();
+      rep.foci_imag[0] = f[0].imag(); rep.foci_imag[1] = f[1].imag(); rep.center_imag = c.imag();
+    } else {
+      analyse_spectrum(H.data(), ldh, rep.nritz, rep.foci, &rep.center, nullptr);
+    }
+    return set_preconditioner(J.A, preconditioner, opt->degree, nullptr, nullptr, H.data(), ldh, rep.nritz);
   }
-  return st;
+  double f[4] = {0.15, 0.0, 1.85, 0.0}, c[2] = {1.0, 0.0};
+  if (kCplx<T>) {
+    if (foci) for (int q = 0; q < 4; ++q) f[q] = foci[q];
+    if (center) { c[0] = center[0]; c[1] = center[1]; }
+    rep.foci[0] = f[0]; rep.foci[1] = f[2]; rep.center = c[0];
+    rep.foci_imag[0] = f[1]; rep.foci_imag[1] = f[3]; rep.center_imag = c[1];
+  } else {
+    f[1] = 1.85;
+    if (foci) { f[0] = foci[0]; f[1] = foci[1]; }
+    if (center) c[0] = *center;
+    rep.foci[0] = f[0]; rep.foci[1] = f[1]; rep.center = c[0];
+  }
+  return set_preconditioner(J.A, preconditioner, opt->degree, f, c, nullptr, 0, 0);
 }
 
 // recycle.inc: x0 = IDRS_RITZ(A, b, s, tol, maxit, variant 1) with U0 (n x s)
-int pp_recycle(PPJob& J, const double* pb, const idrs_pp_options* opt, idrs_pp_report& rep) {
+template <class T>
+int pp_recycle(PPJob<T>& J, const T* pb, const idrs_pp_options* opt, idrs_pp_report& rep) {
+  REQUIRE(!kCplx<T>, "pp_idrs: the complex recycle space is not supported");
   const int s = opt->s;
-  J.U0 = DBuf(sizeof(double) * J.n * s, J.cs);
-  double tol = opt->tol;
-  int maxit = opt->maxit, one = 1;
-  int st = idrs_ridrs_ritz(J.A, pb, s, nullptr, &tol, &maxit, &one, &rep.recycle_flag,
-                           &rep.recycle_relres, &rep.recycle_iterations, nullptr,
-                           J.U0.as<double>(), s, nullptr, 0, nullptr, 0, nullptr, 0, 0, nullptr,
-                           J.d_x0.as<double>());
+  J.U0 = DBuf(sizeof(T) * J.n * s, J.cs);
+  int nr = 0;
+  int st = pp_ritz<T>(J, pb, s, opt->tol, opt->maxit, J.d_x0.template as<T>(), nullptr, 0, 0, 0, nullptr,
+                      J.U0.template as<double>(), s, &rep.recycle_flag, &rep.recycle_relres,
+                      &rep.recycle_iterations, &nr);
   if (st) return st;
   J.have_U0 = true;
   return IDRS_OK;
 }
 
+// |b - S x| / |b| with S the unscaled system matrix at the seed (the
+// assembled K + seed C + seed^2 M, or K - seed M, ...), run_idrs.inc:44-59
+template <class T>
+double true_relres(PPJob<T>& J, const T* pb, const T* px) {
+  using W = typename traits<T>::wide;
+  cudaStream_t cs = J.cs;
+  idrs_matrix A = J.A;
+  spmv<T>(A->k64, px, J.r.template as<T>(), T(-1.0), T(1.0), pb, nullptr, cs);
+  if (!A->seed_folded && (A->seed.x != 0.0 || A->seed.y != 0.0)) {
+    // K x - seed x with an unassembled seed
+    axpy<T>(J.n, narrow<T>(A->seed), px, J.r.template as<T>(), cs);
+  }
+  launch_fused<1, T>(J.n, BNorm<T>{J.r.template as<T>()}, TStoreRe<typename traits<T>::wide>{J.res.template as<double>()}, A->red, nullptr, cs);
+  launch_fused<1, T>(J.n, BNorm<T>{pb}, TStoreRe<typename traits<T>::wide>{J.res.template as<double>() + 1}, A->red, nullptr, cs);
+  double h[2] = {0, 0};
+  IDRS_CUDA(cudaMemcpyAsync(h, J.res.p, 16, cudaMemcpyDeviceToHost, cs));
+  IDRS_CUDA(cudaStreamSynchronize(cs));
+  (void)sizeof(W);
+  return std::sqrt(h[0]) / std::sqrt(h[1]);
+}
+
 // One solve of run_idrs.inc:9-60 / run_mr_idrs.inc:15-72 from x0 (then
 // x0 = y), x = scaleback(A, b, y) and the original system's relative residual.
-int pp_solve(PPJob& J, const double* pb, double* px, const idrs_pp_options* opt,
-             idrs_pp_report& rep) {
+template <class T>
+int pp_solve(PPJob<T>& J, const T* pb, T* px, const idrs_pp_options* opt, idrs_pp_report& rep) {
   idrs_matrix A = J.A;
   const long n = J.n;
   const int s = opt->s;
   double tol = opt->tol;
   int maxit = opt->maxit, st = 0;
-  const double* om = J.omega.empty() ? nullptr : J.omega.data();
+  const double* om = J.omega.empty() ? nullptr : (const double*)J.omega.data();
   const int n_om = (int)J.omega.size();
+  // Pmul(A, b): the deflated right-hand side
+  const T* rb = pb;
+  if (A->defl && A->defl->k > 0) {
+    deflation_pmul<T>(*A->defl, pb, J.t1.template as<T>(), T(1.0), T(0.0), nullptr, nullptr, J.cs);
+    rb = J.t1.template as<T>();
+  }
   if (opt->method == 0) {
     int in_s = opt->in_s, in_it = opt->in_it, prec = opt->inner_precision ? opt->inner_precision : 64;
     double in_tol = opt->in_tol;
-    st = idrs_rqmridr(A, pb, s, nullptr, &tol, &maxit, &rep.flag, &rep.relres_solver,
-                      &rep.iterations, &in_s, &in_tol, &in_it, J.d_x0.as<double>(), om, n_om,
-                      nullptr, 0, &prec, J.d_y.as<double>());
+    st = run_qmridr<T, typename std::conditional<kCplx<T>, c64, float>::type>(
+        A, (const double*)rb, s, nullptr, &tol, &maxit, &rep.flag, &rep.relres_solver, &rep.iterations,
+        &in_s, &in_tol, &in_it, (const double*)J.d_x0.template as<T>(), om, n_om, nullptr, 0, &prec,
+        (double*)J.d_y.template as<T>());
     rep.inner_solves = A->last_inner_calls;
     rep.inner_iterations = A->last_inner_total;
     rep.inner_max = A->last_inner_max;
   } else {
     int variant = opt->method == 2 ? 2 : 1;
-    st = idrs_ridrs(A, pb, s, nullptr, &tol, &maxit, &variant, &rep.flag, &rep.relres_solver,
-                    &rep.iterations, J.d_x0.as<double>(),
-                    J.have_U0 ? J.U0.as<double>() : nullptr, om, n_om, nullptr, 0, nullptr, 0, 0,
-                    J.d_y.as<double>());
+    st = run_idrs<T>(A, (const double*)rb, s, nullptr, &tol, &maxit, &variant, &rep.flag,
+                     &rep.relres_solver, &rep.iterations, (const double*)J.d_x0.template as<T>(),
+                     J.have_U0 ? J.U0.template as<double>() : nullptr, om, n_om, nullptr, 0, nullptr, 0, 0,
+                     (double*)J.d_y.template as<T>());
   }
   if (st) return st;
   cudaStream_t cs = J.cs;
   // x0 = y (the warm start of the next right-hand side); x = scaleback(A, b, y)
-  IDRS_CUDA(cudaMemcpyAsync(J.d_x0.p, J.d_y.p, 8 * n, cudaMemcpyDeviceToDevice, cs));
-  op_scaleback<double>(*A, 64, A->alpha_p, A->degree, J.d_y.as<double>(), px, J.t1.as<double>(),
-                       J.t2.as<double>(), nullptr, cs, pb);
-  spmv<double>(A->k64, px, J.r.as<double>(), -1.0, 1.0, pb, nullptr, cs);
-  launch_fused<1, double>(n, BNorm<double>{J.r.as<double>()}, TStoreVals<double>{J.res.as<double>(), 1}, A->red, nullptr, cs);
-  launch_fused<1, double>(n, BNorm<double>{pb}, TStoreVals<double>{J.res.as<double>() + 1, 1}, A->red, nullptr, cs);
-  double h[2] = {0, 0};
-  IDRS_CUDA(cudaMemcpyAsync(h, J.res.p, 16, cudaMemcpyDeviceToHost, cs));
-  IDRS_CUDA(cudaStreamSynchronize(cs));
-  rep.relres_original = std::sqrt(h[0]) / std::sqrt(h[1]);
-  return IDRS_OK;
-}
-
-int pp_open(PPJob& J, idrs_user_matrix K, idrs_user_matrix P, const idrs_pp_options* opt) {
-  REQUIRE(opt->s >= 1, "rpp_idrs: s must be positive");
-  REQUIRE(opt->n_omega >= 0, "rpp_idrs: n_omega must not be negative");
-  int st = idrs_matrix_create(K, P, 0, nullptr, &J.A);
-  if (st) return st;
-  J.n = J.A->n();
-  J.cs = J.A->stream;
-  const long n = J.n;
-  J.d_x0 = DBuf(8 * n, J.cs);
-  J.d_y = DBuf(8 * n, J.cs);
-  J.t1 = DBuf(8 * n, J.cs);
-  J.t2 = DBuf(8 * n, J.cs);
-  J.r = DBuf(8 * n, J.cs);
-  J.res = DBuf(16, J.cs);
-  IDRS_CUDA(cudaMemsetAsync(J.d_x0.p, 0, 8 * n, J.cs));
-  J.A->device_pointers = true;
+  IDRS_CUDA(cudaMemcpyAsync(J.d_x0.p, J.d_y.p, sizeof(T) * n, cudaMemcpyDeviceToDevice, cs));
+  op_scaleback<T>(*A, 64, A->alpha_p, A->degree, J.d_y.template as<T>(), px, J.t1.template as<T>(), J.t2.template as<T>(), nullptr,
+                  cs, pb);
+  rep.relres_original = true_relres<T>(J, pb, px);
   return IDRS_OK;
 }
 
@@ -1911,90 +2021,262 @@ extern "C" {
 int idrs_rpp_idrs(idrs_user_matrix K, const double* b, idrs_user_matrix P, const double* center,
                   const double* foci, const idrs_pp_options* opt, idrs_pp_report* report,
                   double* x) {
-  return guard([&] {
-    REQUIRE(K && b && opt && x, "rpp_idrs: bad arguments");
-    using clk = std::chrono::steady_clock;
-    auto t0 = clk::now();
-    PPJob J;
-    int st = pp_open(J, K, P, opt);
-    if (st) return st;
-    const long n = J.n;
-    const bool dev = opt->device_pointers != 0;
-    DBuf hb, hx;
-    const double* pb = b;
-    double* px = x;
-    if (!dev) {
-      hb = DBuf(8 * n, J.cs);
-      hx = DBuf(8 * n, J.cs);
-      IDRS_CUDA(cudaMemcpyAsync(hb.p, b, 8 * n, cudaMemcpyHostToDevice, J.cs));
-      pb = hb.as<double>();
-      px = hx.as<double>();
-    }
-    idrs_pp_report rep{};
-    st = pp_setup(J, pb, center, foci, opt, rep);
-    if (st) return st;
-    IDRS_CUDA(cudaStreamSynchronize(J.cs));
-    auto t1 = clk::now();
-    st = pp_solve(J, pb, px, opt, rep);
-    if (st) return st;
-    if (!dev) IDRS_CUDA(cudaMemcpyAsync(x, px, 8 * n, cudaMemcpyDeviceToHost, J.cs));
-    IDRS_CUDA(cudaStreamSynchronize(J.cs));
-    auto t2 = clk::now();
-    rep.seconds_setup = std::chrono::duration<double>(t1 - t0).count();
-    rep.seconds_solve = std::chrono::duration<double>(t2 - t1).count();
-    rep.seconds_total = std::chrono::duration<double>(t2 - t0).count();
-    if (report) *report = rep;
-    return IDRS_OK;
-  });
+  return idrs_rpp_idrs_ext(K, b, P, center, foci, nullptr, opt, report, x);
 }
 
 int idrs_rpp_mr_idrs(idrs_user_matrix K, int nrhs, const double* b_all, idrs_user_matrix P,
                      const double* center, const double* foci, const idrs_pp_options* opt,
                      idrs_pp_report* reports, double* x_all) {
-  return guard([&] {
-    REQUIRE(K && b_all && opt && x_all && nrhs >= 1, "rpp_mr_idrs: bad arguments");
-    using clk = std::chrono::steady_clock;
-    auto t0 = clk::now();
-    PPJob J;
-    int st = pp_open(J, K, P, opt);
+  return idrs_rpp_mr_idrs_ext(K, nrhs, b_all, P, center, foci, nullptr, opt, reports, x_all);
+}
+
+}  // extern "C"
+
+namespace {
+
+template <class T>
+int pp_idrs_t(idrs_user_matrix K, const double* b, idrs_user_matrix P, const double* center,
+              const double* foci, const idrs_pp_inputs* in, const idrs_pp_options* opt,
+              idrs_pp_report* report, double* x) {
+  REQUIRE(K && b && opt && x, "pp_idrs: bad arguments");
+  auto t0 = clk::now();
+  PPJob<T> J;
+  int st = pp_open<T>(J, K, P, in, false, opt);
+  if (st) return st;
+  const long n = J.n;
+  const bool dev = opt->device_pointers != 0;
+  DBuf hb, hx;
+  const T* pb = (const T*)b;
+  T* px = (T*)x;
+  if (!dev) {
+    hb = DBuf(sizeof(T) * n, J.cs);
+    hx = DBuf(sizeof(T) * n, J.cs);
+    IDRS_CUDA(cudaMemcpyAsync(hb.p, b, sizeof(T) * n, cudaMemcpyHostToDevice, J.cs));
+    pb = hb.template as<T>();
+    px = hx.template as<T>();
+  }
+  idrs_pp_report rep{};
+  st = pp_setup<T>(J, pb, center, foci, opt, rep);
+  if (st) return st;
+  IDRS_CUDA(cudaStreamSynchronize(J.cs));
+  auto t1 = clk::now();
+  st = pp_solve<T>(J, pb, px, opt, rep);
+  if (st) return st;
+  if (!dev) IDRS_CUDA(cudaMemcpyAsync(x, px, sizeof(T) * n, cudaMemcpyDeviceToHost, J.cs));
+  IDRS_CUDA(cudaStreamSynchronize(J.cs));
+  auto t2 = clk::now();
+  rep.seconds_setup = std::chrono::duration<double>(t1 - t0).count();
+  rep.seconds_solve = std::chrono::duration<double>(t2 - t1).count();
+  rep.seconds_total = std::chrono::duration<double>(t2 - t0).count();
+  if (report) *report = rep;
+  return IDRS_OK;
+}
+
+template <class T>
+int pp_mr_idrs_t(idrs_user_matrix K, int nrhs, const double* b_all, idrs_user_matrix P,
+                 const double* center, const double* foci, const idrs_pp_inputs* in,
+                 const idrs_pp_options* opt, idrs_pp_report* reports, double* x_all) {
+  REQUIRE(K && b_all && opt && x_all && nrhs >= 1, "pp_mr_idrs: bad arguments");
+  auto t0 = clk::now();
+  PPJob<T> J;
+  int st = pp_open<T>(J, K, P, in, false, opt);
+  if (st) return st;
+  const long n = J.n;
+  const bool dev = opt->device_pointers != 0;
+  // one right-hand side on the device at a time (host arrays are staged per column)
+  DBuf hb, hx;
+  if (!dev) { hb = DBuf(sizeof(T) * n, J.cs); hx = DBuf(sizeof(T) * n, J.cs); }
+  const T* B = (const T*)b_all;
+  T* X = (T*)x_all;
+  auto column_b = [&](int irhs) -> const T* {
+    if (dev) return B + (size_t)n * irhs;
+    IDRS_CUDA(cudaMemcpyAsync(hb.p, B + (size_t)n * irhs, sizeof(T) * n, cudaMemcpyHostToDevice, J.cs));
+    return hb.template as<T>();
+  };
+  idrs_pp_report base{};
+  st = pp_setup<T>(J, column_b(0), center, foci, opt, base);
+  if (st) return st;
+  if (opt->recycle) {
+    st = pp_recycle<T>(J, column_b(0), opt, base);
     if (st) return st;
-    const long n = J.n;
-    const bool dev = opt->device_pointers != 0;
-    // one right-hand side on the device at a time (host arrays are staged per column)
-    DBuf hb, hx;
-    if (!dev) { hb = DBuf(8 * n, J.cs); hx = DBuf(8 * n, J.cs); }
-    auto column_b = [&](int irhs) -> const double* {
-      if (dev) return b_all + (size_t)n * irhs;
-      IDRS_CUDA(cudaMemcpyAsync(hb.p, b_all + (size_t)n * irhs, 8 * n, cudaMemcpyHostToDevice, J.cs));
-      return hb.as<double>();
-    };
-    idrs_pp_report base{};
-    st = pp_setup(J, column_b(0), center, foci, opt, base);
+  }
+  IDRS_CUDA(cudaStreamSynchronize(J.cs));
+  auto t1 = clk::now();
+  const double setup = std::chrono::duration<double>(t1 - t0).count();
+  for (int irhs = 0; irhs < nrhs; ++irhs) {
+    auto ts = clk::now();
+    idrs_pp_report rep = base;
+    const T* pb = column_b(irhs);
+    T* px = dev ? X + (size_t)n * irhs : hx.template as<T>();
+    st = pp_solve<T>(J, pb, px, opt, rep);
     if (st) return st;
-    if (opt->recycle) {
-      st = pp_recycle(J, column_b(0), opt, base);
-      if (st) return st;
-    }
+    if (!dev)
+      IDRS_CUDA(cudaMemcpyAsync(X + (size_t)n * irhs, px, sizeof(T) * n, cudaMemcpyDeviceToHost, J.cs));
     IDRS_CUDA(cudaStreamSynchronize(J.cs));
-    auto t1 = clk::now();
-    const double setup = std::chrono::duration<double>(t1 - t0).count();
-    for (int irhs = 0; irhs < nrhs; ++irhs) {
-      auto ts = clk::now();
-      idrs_pp_report rep = base;
-      const double* pb = column_b(irhs);
-      double* px = dev ? x_all + (size_t)n * irhs : hx.as<double>();
-      st = pp_solve(J, pb, px, opt, rep);
-      if (st) return st;
-      if (!dev)
-        IDRS_CUDA(cudaMemcpyAsync(x_all + (size_t)n * irhs, px, 8 * n, cudaMemcpyDeviceToHost, J.cs));
-      IDRS_CUDA(cudaStreamSynchronize(J.cs));
-      auto te = clk::now();
-      rep.seconds_setup = setup;
-      rep.seconds_solve = std::chrono::duration<double>(te - ts).count();
-      rep.seconds_total = std::chrono::duration<double>(te - t0).count();
-      if (reports) reports[irhs] = rep;
-    }
-    return IDRS_OK;
+    auto te = clk::now();
+    rep.seconds_setup = setup;
+    rep.seconds_solve = std::chrono::duration<double>(te - ts).count();
+    rep.seconds_total = std::chrono::duration<double>(te - t0).count();
+    if (reports) reports[irhs] = rep;
+  }
+  return IDRS_OK;
+}
+
+// r = rhs - K s - sigma C s - sigma^2 M s (and the other forms of
+// run_ms_idrs.inc:35-58), |r| / |rhs|, on the device with the user matrices
+template <class T>
+double ms_true_relres(PPJob<T>& J, idrs_user_matrix K, const idrs_pp_inputs* in, c128 sigma,
+                      const T* rhs, const T* sol, T* r, T* u) {
+  cudaStream_t cs = J.cs;
+  const long nn = J.nn;
+  const T sg = narrow<T>(sigma);
+  const T zero = T(0.0);
+  idrs_user_matrix M = in ? in->M : nullptr, C = in ? in->C : nullptr;
+  spmv<T>(K->view64(), sol, r, T(-1.0), T(1.0), rhs, nullptr, cs);  // r = rhs - K s
+  if (M && C) {
+    spmv<T>(C->view64(), sol, u, T(1.0), zero, nullptr, nullptr, cs);
+    axpy<T>(nn, zero - sg, u, r, cs);
+    spmv<T>(M->view64(), sol, u, T(1.0), zero, nullptr, nullptr, cs);
+    axpy<T>(nn, zero - sg * sg, u, r, cs);
+  } else if (C) {
+    spmv<T>(C->view64(), sol, u, T(1.0), zero, nullptr, nullptr, cs);
+    axpy<T>(nn, zero - sg, u, r, cs);
+    axpy<T>(nn, zero - sg * sg, sol, r, cs);
+  } else if (M) {
+    spmv<T>(M->view64(), sol, u, T(1.0), zero, nullptr, nullptr, cs);
+    axpy<T>(nn, sg, u, r, cs);
+  } else {
+    axpy<T>(nn, sg, sol, r, cs);
+  }
+  launch_fused<1, T>(nn, BNorm<T>{r}, TStoreRe<typename traits<T>::wide>{J.res.template as<double>()}, J.A->red, nullptr, cs);
+  launch_fused<1, T>(nn, BNorm<T>{rhs}, TStoreRe<typename traits<T>::wide>{J.res.template as<double>() + 1}, J.A->red, nullptr, cs);
+  double h[2] = {0, 0};
+  IDRS_CUDA(cudaMemcpyAsync(h, J.res.p, 16, cudaMemcpyDeviceToHost, cs));
+  IDRS_CUDA(cudaStreamSynchronize(cs));
+  return std::sqrt(h[0]) / std::sqrt(h[1]);
+}
+
+// RPP_MS_IDRS / CPP_MS_IDRS (pp_idrs_module.f90:281-...): b = [-rhs; 0] for
+// the block system, set-up, ms_parameters, MSIDRS or MSQMRIDR, scaleback,
+// the solution (second half for the block system), true residuals
+// (run_ms_idrs.inc).
+template <class T>
+int pp_ms_idrs_t(idrs_user_matrix K, const double* rhs, int n_sigma, const double* sigma,
+                 idrs_user_matrix P, const double* center, const double* foci,
+                 const idrs_pp_inputs* in, const idrs_pp_options* opt, idrs_pp_report* report,
+                 double* relres_sigma, double* x) {
+  REQUIRE(K && rhs && sigma && opt && x && n_sigma >= 1, "pp_ms_idrs: bad arguments");
+  REQUIRE(!opt->device_pointers, "pp_ms_idrs: host arrays only");
+  auto t0 = clk::now();
+  PPJob<T> J;
+  int st = pp_open<T>(J, K, P, in, true, opt);
+  if (st) return st;
+  const long n = J.n, nn = J.nn;
+  cudaStream_t cs = J.cs;
+  DBuf db(sizeof(T) * n, cs), drhs(sizeof(T) * nn, cs), dY(sizeof(T) * n * n_sigma, cs),
+      dX(sizeof(T) * n * n_sigma, cs), du(sizeof(T) * nn, cs);
+  IDRS_CUDA(cudaMemcpyAsync(drhs.p, rhs, sizeof(T) * nn, cudaMemcpyHostToDevice, cs));
+  if (J.block) {  // b(1:nn) = -rhs, b(nn+1:) = 0
+    IDRS_CUDA(cudaMemsetAsync(db.p, 0, sizeof(T) * n, cs));
+    axpy<T>(nn, T(-1.0), drhs.template as<T>(), db.template as<T>(), cs);
+  } else {
+    IDRS_CUDA(cudaMemcpyAsync(db.p, drhs.p, sizeof(T) * nn, cudaMemcpyDeviceToDevice, cs));
+  }
+  idrs_pp_report rep{};
+  st = pp_setup<T>(J, db.template as<T>(), center, foci, opt, rep);
+  if (st) return st;
+  IDRS_CUDA(cudaStreamSynchronize(cs));
+  auto t1 = clk::now();
+  constexpr int vw = kCplx<T> ? 2 : 1;
+  std::vector<double> sp((size_t)vw * n_sigma);
+  st = ms_parameters(J.A, n_sigma, sigma, sp.data(), kCplx<T>);
+  if (st) return st;
+  const T* rb = db.template as<T>();
+  if (J.A->defl && J.A->defl->k > 0) {
+    deflation_pmul<T>(*J.A->defl, db.template as<T>(), J.t1.template as<T>(), T(1.0), T(0.0), nullptr, nullptr, cs);
+    rb = J.t1.template as<T>();
+  }
+  double tol = opt->tol;
+  int maxit = opt->maxit;
+  std::vector<double> rel(n_sigma, 1.0);
+  const double* om = J.omega.empty() ? nullptr : (const double*)J.omega.data();
+  const int n_om = (int)J.omega.size();
+  if (opt->method == 0) {
+    int in_s = opt->in_s, in_it = opt->in_it, prec = opt->inner_precision ? opt->inner_precision : 64;
+    double in_tol = opt->in_tol;
+    st = run_msqmridr<T, typename std::conditional<kCplx<T>, c64, float>::type>(
+        J.A, (const double*)rb, n_sigma, sp.data(), opt->s, nullptr, &tol, &maxit, &rep.flag,
+        rel.data(), &rep.iterations, &in_s, &in_tol, &in_it, om, n_om, nullptr, 0, &prec,
+        (double*)dY.template as<T>());
+  } else {
+    int variant = opt->method == 2 ? 2 : 1;
+    st = run_msidrs<T>(J.A, (const double*)rb, n_sigma, sp.data(), opt->s, nullptr, &tol, &maxit,
+                       &variant, &rep.flag, rel.data(), &rep.iterations, om, n_om, nullptr, 0, nullptr,
+                       (double*)dY.template as<T>());
+  }
+  if (st) return st;
+  rep.relres_solver = *std::max_element(rel.begin(), rel.end());
+  // scaleback(A, sigma, b, x)
+  st = ms_scaleback_t<T>(J.A, n_sigma, sigma, (const double*)db.template as<T>(), (const double*)dY.template as<T>(),
+                         (double*)dX.template as<T>());
+  if (st) return st;
+  double worst = 0;
+  for (int k = 0; k < n_sigma; ++k) {
+    const T* sol = dX.template as<T>() + (size_t)n * k + (J.block ? nn : 0);
+    const c128 sg = kCplx<T> ? c128(sigma[2 * k], sigma[2 * k + 1]) : c128(sigma[k], 0.0);
+    const double rr = ms_true_relres<T>(J, K, in, sg, drhs.template as<T>(), sol, J.r.template as<T>(), du.template as<T>());
+    if (relres_sigma) relres_sigma[k] = rr;
+    worst = std::max(worst, rr);
+    IDRS_CUDA(cudaMemcpyAsync((T*)x + (size_t)nn * k, sol, sizeof(T) * nn, cudaMemcpyDeviceToHost, cs));
+  }
+  IDRS_CUDA(cudaStreamSynchronize(cs));
+  rep.relres_original = worst;
+  auto t2 = clk::now();
+  rep.seconds_setup = std::chrono::duration<double>(t1 - t0).count();
+  rep.seconds_solve = std::chrono::duration<double>(t2 - t1).count();
+  rep.seconds_total = std::chrono::duration<double>(t2 - t0).count();
+  if (report) *report = rep;
+  return IDRS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int idrs_rpp_idrs_ext(idrs_user_matrix K, const double* b, idrs_user_matrix P, const double* center,
+                      const double* foci, const idrs_pp_inputs* in, const idrs_pp_options* opt,
+                      idrs_pp_report* report, double* x) {
+  return guard([&] { return pp_idrs_t<double>(K, b, P, center, foci, in, opt, report, x); });
+}
+int idrs_cpp_idrs(idrs_user_matrix K, const double* b, idrs_user_matrix P, const double* center,
+                  const double* foci, const idrs_pp_inputs* in, const idrs_pp_options* opt,
+                  idrs_pp_report* report, double* x) {
+  return guard([&] { return pp_idrs_t<c128>(K, b, P, center, foci, in, opt, report, x); });
+}
+int idrs_rpp_mr_idrs_ext(idrs_user_matrix K, int nrhs, const double* b_all, idrs_user_matrix P,
+                         const double* center, const double* foci, const idrs_pp_inputs* in,
+                         const idrs_pp_options* opt, idrs_pp_report* reports, double* x_all) {
+  return guard([&] { return pp_mr_idrs_t<double>(K, nrhs, b_all, P, center, foci, in, opt, reports, x_all); });
+}
+int idrs_cpp_mr_idrs(idrs_user_matrix K, int nrhs, const double* b_all, idrs_user_matrix P,
+                     const double* center, const double* foci, const idrs_pp_inputs* in,
+                     const idrs_pp_options* opt, idrs_pp_report* reports, double* x_all) {
+  return guard([&] { return pp_mr_idrs_t<c128>(K, nrhs, b_all, P, center, foci, in, opt, reports, x_all); });
+}
+int idrs_rpp_ms_idrs(idrs_user_matrix K, const double* rhs, int n_sigma, const double* sigma,
+                     idrs_user_matrix P, const double* center, const double* foci,
+                     const idrs_pp_inputs* in, const idrs_pp_options* opt, idrs_pp_report* report,
+                     double* relres, double* x) {
+  return guard([&] {
+    return pp_ms_idrs_t<double>(K, rhs, n_sigma, sigma, P, center, foci, in, opt, report, relres, x);
+  });
+}
+int idrs_cpp_ms_idrs(idrs_user_matrix K, const double* rhs, int n_sigma, const double* sigma,
+                     idrs_user_matrix P, const double* center, const double* foci,
+                     const idrs_pp_inputs* in, const idrs_pp_options* opt, idrs_pp_report* report,
+                     double* relres, double* x) {
+  return guard([&] {
+    return pp_ms_idrs_t<c128>(K, rhs, n_sigma, sigma, P, center, foci, in, opt, report, relres, x);
   });
 }
 

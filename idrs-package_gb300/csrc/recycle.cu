@@ -115,6 +115,25 @@ void ritz_omega(const double* Hf, int ldh, int n_omega, double* omega) {
   }
 }
 
+void ritz_omega(const std::complex<double>* Hf, int ldh, int n_omega, std::complex<double>* omega) {
+  using cd = std::complex<double>;
+  std::vector<cd> rv(n_omega), p(n_omega, cd(1.0, 0.0));
+  int converged = 0;
+  qr_eig(Hf, ldh, n_omega, rv.data(), &converged);
+  for (int i = 0; i < n_omega; ++i) {
+    cd w = rv[i];
+    if (std::abs(w) < DBL_EPSILON) w = cd(1.0, 0.0);
+    omega[i] = cd(1.0, 0.0) / w;
+  }
+  for (int i = 0; i < n_omega; ++i) {
+    int mp = i;
+    for (int k = i + 1; k < n_omega; ++k)
+      if (std::abs(p[k]) > std::abs(p[mp])) mp = k;
+    std::swap(omega[mp], omega[i]);
+    for (int k = 0; k < n_omega; ++k) p[k] = p[k] * (cd(1.0, 0.0) - rv[k] * omega[i]);
+  }
+}
+
 // ----------------------------------------------------------------- device
 namespace {
 

@@ -5,6 +5,7 @@
 // a global modified Gram-Schmidt QR of the result).
 #pragma once
 
+#include <complex>
 #include <cstdint>
 
 #include "matrix.cuh"
@@ -24,6 +25,9 @@ int si_power(const double* H, int ldh, int n, int s, double shift, uint64_t seed
 // ordered greedily by the largest residual-polynomial value
 // (ritz_module.f90:497-520).
 void ritz_omega(const double* Hf, int ldh, int n_omega, double* omega);
+// complex version (CIDRS_RITZ, ritz_module.f90:335-358): omega = 1/ritz
+// (|ritz| < eps -> 1), p *= 1 - ritz omega(i)
+void ritz_omega(const std::complex<double>* Hf, int ldh, int n_omega, std::complex<double>* omega);
 
 // rcompute_U0 (ritz_module.f90:100-160) on the device: rebuilds v_1 = b,
 // v_{i+1} = (A v_i - sum_{l=max(1,i-s)}^{i} v_l H(l,i)) / H(i+1,i) for

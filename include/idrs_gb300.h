@@ -381,11 +381,34 @@ typedef struct idrs_pp_report {
   int inner_solves, inner_iterations, inner_max;  /* flexible QMRIDR: inner IDR(s) statistics */
   int recycle_flag, recycle_iterations;            /* the recycle.inc solve (recycle = 1) */
   double recycle_relres;
+  double foci_imag[2], center_imag;                 /* complex pipelines: imaginary parts */
 } idrs_pp_report;
+
+/* The optional inputs of pp_idrs beyond P, center and foci
+ * (pp_idrs_module.f90: M, C, seed, shift, V); NULL = all absent.  seed and
+ * shift have the kind of the pipeline (complex: {re, im}); V is n x
+ * n_deflation (host, complex interleaved).  With P and shift, P is a
+ * shift-and-invert preconditioner (which_precon 2 or 3). */
+typedef struct idrs_pp_inputs {
+  idrs_user_matrix M, C;
+  const double *seed, *shift;
+  const double *V;
+  int n_deflation;
+} idrs_pp_inputs;
 
 int idrs_rpp_idrs(idrs_user_matrix K, const double *b, idrs_user_matrix P, const double *center,
                   const double *foci, const idrs_pp_options *opt, idrs_pp_report *report,
                   double *x);
+
+/* pp_idrs with every optional input: RPP_IDRS / CPP_IDRS (pp_idrs_module.f90:
+ * 64-162; complex: center 2 and foci 4 doubles, b and x interleaved).  The
+ * complex pipelines compute the Ritz omegas; the recycle space is real only. */
+int idrs_rpp_idrs_ext(idrs_user_matrix K, const double *b, idrs_user_matrix P, const double *center,
+                      const double *foci, const idrs_pp_inputs *in, const idrs_pp_options *opt,
+                      idrs_pp_report *report, double *x);
+int idrs_cpp_idrs(idrs_user_matrix K, const double *b, idrs_user_matrix P, const double *center,
+                  const double *foci, const idrs_pp_inputs *in, const idrs_pp_options *opt,
+                  idrs_pp_report *report, double *x);
 
 /* x_all = pp_idrs(K, b_all[, P, center, foci]) for nrhs right-hand sides:
  * RPP_MR_IDRS (pp_idrs_module.f90:222-279) with real_preconditioner.inc,
@@ -397,6 +420,29 @@ int idrs_rpp_idrs(idrs_user_matrix K, const double *b, idrs_user_matrix P, const
 int idrs_rpp_mr_idrs(idrs_user_matrix K, int nrhs, const double *b_all, idrs_user_matrix P,
                      const double *center, const double *foci, const idrs_pp_options *opt,
                      idrs_pp_report *reports, double *x_all);
+/* the same with every optional input (RPP_MR_IDRS / CPP_MR_IDRS,
+ * pp_idrs_module.f90:164-279) */
+int idrs_rpp_mr_idrs_ext(idrs_user_matrix K, int nrhs, const double *b_all, idrs_user_matrix P,
+                         const double *center, const double *foci, const idrs_pp_inputs *in,
+                         const idrs_pp_options *opt, idrs_pp_report *reports, double *x_all);
+int idrs_cpp_mr_idrs(idrs_user_matrix K, int nrhs, const double *b_all, idrs_user_matrix P,
+                     const double *center, const double *foci, const idrs_pp_inputs *in,
+                     const idrs_pp_options *opt, idrs_pp_report *reports, double *x_all);
+
+/* x(n, n_sigma) = pp_idrs(K, rhs, sigma[, M, C, P, center, foci, seed, shift,
+ * V]): RPP_MS_IDRS / CPP_MS_IDRS with run_ms_idrs.inc.  With C the operator is
+ * the 2n x 2n block system, b = [-rhs; 0] and x the second half of each
+ * solution.  method 1/2 runs MSIDRS, 0 MSQMRIDR.  relres(n_sigma): the true
+ * residuals |rhs - K x - sigma C x - sigma^2 M x| / |rhs| (and the other
+ * forms); report->relres_original is their maximum.  Host arrays only. */
+int idrs_rpp_ms_idrs(idrs_user_matrix K, const double *rhs, int n_sigma, const double *sigma,
+                     idrs_user_matrix P, const double *center, const double *foci,
+                     const idrs_pp_inputs *in, const idrs_pp_options *opt, idrs_pp_report *report,
+                     double *relres, double *x);
+int idrs_cpp_ms_idrs(idrs_user_matrix K, const double *rhs, int n_sigma, const double *sigma,
+                     idrs_user_matrix P, const double *center, const double *foci,
+                     const idrs_pp_inputs *in, const idrs_pp_options *opt, idrs_pp_report *report,
+                     double *relres, double *x);
 
 #ifdef __cplusplus
 }
