@@ -1836,12 +1836,18 @@ int pp_open(PPJob<T>& J, idrs_user_matrix K, idrs_user_matrix P, const idrs_pp_i
   J.r = DBuf(vb, J.cs);
   J.res = DBuf(16, J.cs);
   IDRS_CUDA(cudaMemsetAsync(J.d_x0.p, 0, vb, J.cs));
-  if (in && in->V && in->n_deflation > 0) {  // host V (n x k)
-    st = idrs_make_deflation(J.A, in->V, in->n_deflation);
-    if (st) return st;
-  }
   J.A->device_pointers = true;
   return IDRS_OK;
+}
+
+// `if (present(V)) call make_deflation(A, V)` with a host V (n x k)
+template <class T>
+int pp_deflate(PPJob<T>& J, const idrs_pp_inputs* in) {
+  if (!in || !in->V || in->n_deflation <= 0) return IDRS_OK;
+  J.A->device_pointers = false;
+  int st = idrs_make_deflation(J.A, in->V, in->n_deflation);
+  J.A->device_pointers = true;
+  return st;
 }
 
 // IDRS_RITZ for the set-up solves: real -> idrs_ridrs_ritz; complex -> IDRS
@@ -2058,6 +2064,8 @@ int pp_idrs_t(idrs_user_matrix K, const double* b, idrs_user_matrix P, const dou
   idrs_pp_report rep{};
   st = pp_setup<T>(J, pb, center, foci, opt, rep);
   if (st) return st;
+  st = pp_deflate<T>(J, in);  // after the preconditioner (pp_idrs_module.f90:108-111, :154-157)
+  if (st) return st;
   IDRS_CUDA(cudaStreamSynchronize(J.cs));
   auto t1 = clk::now();
   st = pp_solve<T>(J, pb, px, opt, rep);
@@ -2094,8 +2102,18 @@ int pp_mr_idrs_t(idrs_user_matrix K, int nrhs, const double* b_all, idrs_user_ma
     return hb.template as<T>();
   };
   idrs_pp_report base{};
+  // RPP_MR_IDRS deflates before the preconditioner set-up, CPP_MR_IDRS after
+  // it (pp_idrs_module.f90:260-266 and :204-207)
+  if (!kCplx<T>) {
+    st = pp_deflate<T>(J, in);
+    if (st) return st;
+  }
   st = pp_setup<T>(J, column_b(0), center, foci, opt, base);
   if (st) return st;
+  if (kCplx<T>) {
+    st = pp_deflate<T>(J, in);
+    if (st) return st;
+  }
   if (opt->recycle) {
     st = pp_recycle<T>(J, column_b(0), opt, base);
     if (st) return st;
@@ -2184,6 +2202,8 @@ int pp_ms_idrs_t(idrs_user_matrix K, const double* rhs, int n_sigma, const doubl
   }
   idrs_pp_report rep{};
   st = pp_setup<T>(J, db.template as<T>(), center, foci, opt, rep);
+  if (st) return st;
+  st = pp_deflate<T>(J, in);
   if (st) return st;
   IDRS_CUDA(cudaStreamSynchronize(cs));
   auto t1 = clk::now();

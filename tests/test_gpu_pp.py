@@ -101,7 +101,7 @@ def test_rpp_ms_idrs_shifted_laplacian(gpu, oracle):
     np.testing.assert_allclose(g.x, A.ms_scaleback(o.x, b), rtol=0, atol=1e-8 * np.abs(g.x).max())
 
 
-def test_rpp_idrs_with_deflation(gpu, oracle, gpu_problems=None):
+def test_rpp_idrs_with_deflation(gpu, oracle):
     """RPP_IDRS(K, b, P, V): Pmul(b), the deflated solve, add_deflation."""
     n, K, M, C, b = _helmholtz(gpu, oracle, m=16)
     rng = np.random.default_rng(3)
@@ -118,13 +118,12 @@ def test_rpp_idrs_with_deflation(gpu, oracle, gpu_problems=None):
 
 
 def test_cpp_mr_idrs_sequence(gpu, oracle):
-    """CPP_MR_IDRS: complex sequence with warm starts and Ritz omegas."""
+    """CPP_MR_IDRS: a complex sequence with warm starts."""
     n, K, M, C, b = _helmholtz(gpu, oracle, m=12)
     rng = np.random.default_rng(4)
     B = rng.standard_normal((n, 3)) + 1j * rng.standard_normal((n, 3))
     seed = 1.0j
-    g = gpu.PP_MR_IDRS(K[0], B, M=M[0], C_=C[0], seed=seed, s=4, tol=1e-8, maxit=3000, n_omega=16,
-                       n_ritz=32)
+    g = gpu.PP_MR_IDRS(K[0], B, M=M[0], C_=C[0], seed=seed, s=4, tol=1e-8, maxit=3000)
     assert list(g.flags) == [0, 0, 0] and np.all(g.relres_original < 2e-8)
     A = oracle.Matrix(K[1], M=M[1], C_=C[1], seed=seed, cplx=True)
     D = A
