@@ -124,6 +124,8 @@ _PROTOS = {
     "idrs_cpp_mr_idrs": (_i, [_vp, _i] + [_vp] * 8),
     "idrs_rpp_ms_idrs": (_i, [_vp, _vp, _i] + [_vp] * 9),
     "idrs_cpp_ms_idrs": (_i, [_vp, _vp, _i] + [_vp] * 9),
+    "idrs_rpp_ms_mr_idrs": (_i, [_vp, _i, _vp, _i] + [_vp] * 9),
+    "idrs_cpp_ms_mr_idrs": (_i, [_vp, _i, _vp, _i] + [_vp] * 9),
 }
 
 
@@ -893,21 +895,36 @@ def PP_MS_IDRS(K: UserMatrix, rhs, sigma, P: UserMatrix | None = None, center=No
     """x(n, n_sigma) = pp_idrs(K, rhs, sigma[, M, C, P, center, foci, seed, shift, V])
     (RPP_MS_IDRS / CPP_MS_IDRS with run_ms_idrs.inc).  With C the block system
     is solved and x is the second half of each solution.  relres_sigma: the
-    true residual of every shifted system."""
+    true residual of every shifted system.  A 2-D rhs (n x nrhs) runs the
+    sequence form RPP_MS_MR_IDRS / CPP_MS_MR_IDRS: x is n x n_sigma x nrhs,
+    relres_sigma n_sigma x nrhs, flags and iterations per right-hand side."""
     cplx = _pp_kind(K, rhs, M, C_, seed, shift, complex) or np.iscomplexobj(sigma)
     dt = np.complex128 if cplx else np.float64
-    rhs = _arr(rhs, cplx, K.nrows)
+    seq = np.ndim(rhs) == 2
+    rhs = np.asfortranarray(rhs, dtype=dt) if seq else _arr(rhs, cplx, K.nrows)
+    if rhs.shape[0] != K.nrows:
+        raise ValueError("rhs must have K.nrows rows")
+    nrhs = rhs.shape[1] if seq else 1
     sig = np.ascontiguousarray(sigma, dtype=dt)
     ns = len(sig)
-    x = np.zeros((K.nrows, ns), dtype=dt, order="F")
-    rel = np.zeros(ns)
+    x = np.zeros((K.nrows, ns, nrhs), dtype=dt, order="F")
+    rel = np.zeros((ns, nrhs), order="F")
     o = _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
                     inner_precision, False, n_omega, False)
-    rep = PPReport()
     keep = []
     c, f = _pp_cf(cplx, center, foci)
     inp = _pp_inputs(cplx, M, C_, seed, shift, V, keep)
+    if seq:
+        reps = (PPReport * nrhs)()
+        fn = lib().idrs_cpp_ms_mr_idrs if cplx else lib().idrs_rpp_ms_mr_idrs
+        _check(fn(K.handle, int(nrhs), _p(rhs), ns, _p(sig), P.handle if P else None, _p(c), _p(f),
+                  inp, C.byref(o), reps, _p(rel), _p(x)))
+        r = _pp_result(reps[nrhs - 1], x=x, relres_sigma=rel)
+        r["flags"] = np.array([q.flag for q in reps])
+        r["iterations"] = np.array([q.iterations for q in reps])
+        return r
+    rep = PPReport()
     fn = lib().idrs_cpp_ms_idrs if cplx else lib().idrs_rpp_ms_idrs
     _check(fn(K.handle, _p(rhs), ns, _p(sig), P.handle if P else None, _p(c), _p(f), inp,
               C.byref(o), C.byref(rep), _p(rel), _p(x)))
-    return _pp_result(rep, x=x, relres_sigma=rel)
+    return _pp_result(rep, x=x[:, :, 0], relres_sigma=rel[:, 0])

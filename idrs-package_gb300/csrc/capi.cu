@@ -2174,16 +2174,18 @@ double ms_true_relres(PPJob<T>& J, idrs_user_matrix K, const idrs_pp_inputs* in,
   return std::sqrt(h[0]) / std::sqrt(h[1]);
 }
 
-// RPP_MS_IDRS / CPP_MS_IDRS (pp_idrs_module.f90:281-...): b = [-rhs; 0] for
-// the block system, set-up, ms_parameters, MSIDRS or MSQMRIDR, scaleback,
-// the solution (second half for the block system), true residuals
-// (run_ms_idrs.inc).
+// RPP_MS_IDRS / CPP_MS_IDRS (pp_idrs_module.f90:281-409, run_ms_idrs.inc) and
+// RPP_MS_MR_IDRS / CPP_MS_MR_IDRS (:411-..., run_ms_mr_idrs.inc): b = [-rhs; 0]
+// for the block system, set-up on the first right-hand side, ms_parameters,
+// then per right-hand side MSIDRS or MSQMRIDR on Pmul(b), scaleback, the
+// solution (second half for the block system) and the true residuals.  The
+// sequence form scales back with the deflated b, as run_ms_mr_idrs.inc does.
 template <class T>
-int pp_ms_idrs_t(idrs_user_matrix K, const double* rhs, int n_sigma, const double* sigma,
-                 idrs_user_matrix P, const double* center, const double* foci,
-                 const idrs_pp_inputs* in, const idrs_pp_options* opt, idrs_pp_report* report,
-                 double* relres_sigma, double* x) {
-  REQUIRE(K && rhs && sigma && opt && x && n_sigma >= 1, "pp_ms_idrs: bad arguments");
+int pp_ms_t(idrs_user_matrix K, int nrhs, const double* rhs_all, int n_sigma, const double* sigma,
+            idrs_user_matrix P, const double* center, const double* foci, const idrs_pp_inputs* in,
+            const idrs_pp_options* opt, idrs_pp_report* reports, double* relres_sigma, double* x,
+            bool sequence) {
+  REQUIRE(K && rhs_all && sigma && opt && x && n_sigma >= 1 && nrhs >= 1, "pp_ms_idrs: bad arguments");
   REQUIRE(!opt->device_pointers, "pp_ms_idrs: host arrays only");
   auto t0 = clk::now();
   PPJob<T> J;
@@ -2193,69 +2195,81 @@ int pp_ms_idrs_t(idrs_user_matrix K, const double* rhs, int n_sigma, const doubl
   cudaStream_t cs = J.cs;
   DBuf db(sizeof(T) * n, cs), drhs(sizeof(T) * nn, cs), dY(sizeof(T) * n * n_sigma, cs),
       dX(sizeof(T) * n * n_sigma, cs), du(sizeof(T) * nn, cs);
-  IDRS_CUDA(cudaMemcpyAsync(drhs.p, rhs, sizeof(T) * nn, cudaMemcpyHostToDevice, cs));
-  if (J.block) {  // b(1:nn) = -rhs, b(nn+1:) = 0
-    IDRS_CUDA(cudaMemsetAsync(db.p, 0, sizeof(T) * n, cs));
-    axpy<T>(nn, T(-1.0), drhs.template as<T>(), db.template as<T>(), cs);
-  } else {
-    IDRS_CUDA(cudaMemcpyAsync(db.p, drhs.p, sizeof(T) * nn, cudaMemcpyDeviceToDevice, cs));
-  }
-  idrs_pp_report rep{};
-  st = pp_setup<T>(J, db.template as<T>(), center, foci, opt, rep);
+  auto load_rhs = [&](int irhs) {  // b = rhs, or [-rhs; 0] for the block system
+    IDRS_CUDA(cudaMemcpyAsync(drhs.p, (const T*)rhs_all + (size_t)nn * irhs, sizeof(T) * nn,
+                              cudaMemcpyHostToDevice, cs));
+    if (J.block) {
+      IDRS_CUDA(cudaMemsetAsync(db.p, 0, sizeof(T) * n, cs));
+      axpy<T>(nn, T(-1.0), drhs.template as<T>(), db.template as<T>(), cs);
+    } else {
+      IDRS_CUDA(cudaMemcpyAsync(db.p, drhs.p, sizeof(T) * nn, cudaMemcpyDeviceToDevice, cs));
+    }
+  };
+  load_rhs(0);
+  idrs_pp_report base{};
+  st = pp_setup<T>(J, db.template as<T>(), center, foci, opt, base);
   if (st) return st;
   st = pp_deflate<T>(J, in);
   if (st) return st;
   IDRS_CUDA(cudaStreamSynchronize(cs));
   auto t1 = clk::now();
+  const double setup = std::chrono::duration<double>(t1 - t0).count();
   constexpr int vw = kCplx<T> ? 2 : 1;
   std::vector<double> sp((size_t)vw * n_sigma);
   st = ms_parameters(J.A, n_sigma, sigma, sp.data(), kCplx<T>);
   if (st) return st;
-  const T* rb = db.template as<T>();
-  if (J.A->defl && J.A->defl->k > 0) {
-    deflation_pmul<T>(*J.A->defl, db.template as<T>(), J.t1.template as<T>(), T(1.0), T(0.0), nullptr, nullptr, cs);
-    rb = J.t1.template as<T>();
-  }
-  double tol = opt->tol;
-  int maxit = opt->maxit;
-  std::vector<double> rel(n_sigma, 1.0);
   const double* om = J.omega.empty() ? nullptr : (const double*)J.omega.data();
   const int n_om = (int)J.omega.size();
-  if (opt->method == 0) {
-    int in_s = opt->in_s, in_it = opt->in_it, prec = opt->inner_precision ? opt->inner_precision : 64;
-    double in_tol = opt->in_tol;
-    st = run_msqmridr<T, typename std::conditional<kCplx<T>, c64, float>::type>(
-        J.A, (const double*)rb, n_sigma, sp.data(), opt->s, nullptr, &tol, &maxit, &rep.flag,
-        rel.data(), &rep.iterations, &in_s, &in_tol, &in_it, om, n_om, nullptr, 0, &prec,
-        (double*)dY.template as<T>());
-  } else {
-    int variant = opt->method == 2 ? 2 : 1;
-    st = run_msidrs<T>(J.A, (const double*)rb, n_sigma, sp.data(), opt->s, nullptr, &tol, &maxit,
-                       &variant, &rep.flag, rel.data(), &rep.iterations, om, n_om, nullptr, 0, nullptr,
-                       (double*)dY.template as<T>());
+  for (int irhs = 0; irhs < nrhs; ++irhs) {
+    auto ts = clk::now();
+    idrs_pp_report rep = base;
+    if (irhs > 0) load_rhs(irhs);
+    const T* rb = db.template as<T>();
+    if (J.A->defl && J.A->defl->k > 0) {
+      deflation_pmul<T>(*J.A->defl, db.template as<T>(), J.t1.template as<T>(), T(1.0), T(0.0),
+                        nullptr, nullptr, cs);
+      rb = J.t1.template as<T>();
+    }
+    double tol = opt->tol;
+    int maxit = opt->maxit;
+    std::vector<double> rel(n_sigma, 1.0);
+    if (opt->method == 0) {
+      int in_s = opt->in_s, in_it = opt->in_it, prec = opt->inner_precision ? opt->inner_precision : 64;
+      double in_tol = opt->in_tol;
+      st = run_msqmridr<T, typename std::conditional<kCplx<T>, c64, float>::type>(
+          J.A, (const double*)rb, n_sigma, sp.data(), opt->s, nullptr, &tol, &maxit, &rep.flag,
+          rel.data(), &rep.iterations, &in_s, &in_tol, &in_it, om, n_om, nullptr, 0, &prec,
+          (double*)dY.template as<T>());
+    } else {
+      int variant = opt->method == 2 ? 2 : 1;
+      st = run_msidrs<T>(J.A, (const double*)rb, n_sigma, sp.data(), opt->s, nullptr, &tol, &maxit,
+                         &variant, &rep.flag, rel.data(), &rep.iterations, om, n_om, nullptr, 0,
+                         nullptr, (double*)dY.template as<T>());
+    }
+    if (st) return st;
+    rep.relres_solver = *std::max_element(rel.begin(), rel.end());
+    st = ms_scaleback_t<T>(J.A, n_sigma, sigma, (const double*)(sequence ? rb : db.template as<T>()),
+                           (const double*)dY.template as<T>(), (double*)dX.template as<T>());
+    if (st) return st;
+    double worst = 0;
+    for (int k = 0; k < n_sigma; ++k) {
+      const T* sol = dX.template as<T>() + (size_t)n * k + (J.block ? nn : 0);
+      const c128 sg = kCplx<T> ? c128(sigma[2 * k], sigma[2 * k + 1]) : c128(sigma[k], 0.0);
+      const double rr = ms_true_relres<T>(J, K, in, sg, drhs.template as<T>(), sol,
+                                          J.r.template as<T>(), du.template as<T>());
+      if (relres_sigma) relres_sigma[k + (size_t)n_sigma * irhs] = rr;
+      worst = std::max(worst, rr);
+      IDRS_CUDA(cudaMemcpyAsync((T*)x + (size_t)nn * (k + (size_t)n_sigma * irhs), sol, sizeof(T) * nn,
+                                cudaMemcpyDeviceToHost, cs));
+    }
+    IDRS_CUDA(cudaStreamSynchronize(cs));
+    rep.relres_original = worst;
+    auto te = clk::now();
+    rep.seconds_setup = setup;
+    rep.seconds_solve = std::chrono::duration<double>(te - ts).count();
+    rep.seconds_total = std::chrono::duration<double>(te - t0).count();
+    if (reports) reports[irhs] = rep;
   }
-  if (st) return st;
-  rep.relres_solver = *std::max_element(rel.begin(), rel.end());
-  // scaleback(A, sigma, b, x)
-  st = ms_scaleback_t<T>(J.A, n_sigma, sigma, (const double*)db.template as<T>(), (const double*)dY.template as<T>(),
-                         (double*)dX.template as<T>());
-  if (st) return st;
-  double worst = 0;
-  for (int k = 0; k < n_sigma; ++k) {
-    const T* sol = dX.template as<T>() + (size_t)n * k + (J.block ? nn : 0);
-    const c128 sg = kCplx<T> ? c128(sigma[2 * k], sigma[2 * k + 1]) : c128(sigma[k], 0.0);
-    const double rr = ms_true_relres<T>(J, K, in, sg, drhs.template as<T>(), sol, J.r.template as<T>(), du.template as<T>());
-    if (relres_sigma) relres_sigma[k] = rr;
-    worst = std::max(worst, rr);
-    IDRS_CUDA(cudaMemcpyAsync((T*)x + (size_t)nn * k, sol, sizeof(T) * nn, cudaMemcpyDeviceToHost, cs));
-  }
-  IDRS_CUDA(cudaStreamSynchronize(cs));
-  rep.relres_original = worst;
-  auto t2 = clk::now();
-  rep.seconds_setup = std::chrono::duration<double>(t1 - t0).count();
-  rep.seconds_solve = std::chrono::duration<double>(t2 - t1).count();
-  rep.seconds_total = std::chrono::duration<double>(t2 - t0).count();
-  if (report) *report = rep;
   return IDRS_OK;
 }
 
@@ -2288,7 +2302,7 @@ int idrs_rpp_ms_idrs(idrs_user_matrix K, const double* rhs, int n_sigma, const d
                      const idrs_pp_inputs* in, const idrs_pp_options* opt, idrs_pp_report* report,
                      double* relres, double* x) {
   return guard([&] {
-    return pp_ms_idrs_t<double>(K, rhs, n_sigma, sigma, P, center, foci, in, opt, report, relres, x);
+    return pp_ms_t<double>(K, 1, rhs, n_sigma, sigma, P, center, foci, in, opt, report, relres, x, false);
   });
 }
 int idrs_cpp_ms_idrs(idrs_user_matrix K, const double* rhs, int n_sigma, const double* sigma,
@@ -2296,7 +2310,23 @@ int idrs_cpp_ms_idrs(idrs_user_matrix K, const double* rhs, int n_sigma, const d
                      const idrs_pp_inputs* in, const idrs_pp_options* opt, idrs_pp_report* report,
                      double* relres, double* x) {
   return guard([&] {
-    return pp_ms_idrs_t<c128>(K, rhs, n_sigma, sigma, P, center, foci, in, opt, report, relres, x);
+    return pp_ms_t<c128>(K, 1, rhs, n_sigma, sigma, P, center, foci, in, opt, report, relres, x, false);
+  });
+}
+int idrs_rpp_ms_mr_idrs(idrs_user_matrix K, int nrhs, const double* rhs, int n_sigma,
+                        const double* sigma, idrs_user_matrix P, const double* center,
+                        const double* foci, const idrs_pp_inputs* in, const idrs_pp_options* opt,
+                        idrs_pp_report* reports, double* relres, double* x) {
+  return guard([&] {
+    return pp_ms_t<double>(K, nrhs, rhs, n_sigma, sigma, P, center, foci, in, opt, reports, relres, x, true);
+  });
+}
+int idrs_cpp_ms_mr_idrs(idrs_user_matrix K, int nrhs, const double* rhs, int n_sigma,
+                        const double* sigma, idrs_user_matrix P, const double* center,
+                        const double* foci, const idrs_pp_inputs* in, const idrs_pp_options* opt,
+                        idrs_pp_report* reports, double* relres, double* x) {
+  return guard([&] {
+    return pp_ms_t<c128>(K, nrhs, rhs, n_sigma, sigma, P, center, foci, in, opt, reports, relres, x, true);
   });
 }
 

@@ -443,6 +443,18 @@ int idrs_cpp_ms_idrs(idrs_user_matrix K, const double *rhs, int n_sigma, const d
                      idrs_user_matrix P, const double *center, const double *foci,
                      const idrs_pp_inputs *in, const idrs_pp_options *opt, idrs_pp_report *report,
                      double *relres, double *x);
+/* x(n, n_sigma, nrhs) = pp_idrs(K, rhs(n, nrhs), sigma[, ...]): RPP_MS_MR_IDRS /
+ * CPP_MS_MR_IDRS with run_ms_mr_idrs.inc: one set-up (on rhs(:,1)) and one
+ * ms_parameters, then one multishift solve per right-hand side.
+ * reports(nrhs), relres(n_sigma, nrhs). */
+int idrs_rpp_ms_mr_idrs(idrs_user_matrix K, int nrhs, const double *rhs, int n_sigma,
+                        const double *sigma, idrs_user_matrix P, const double *center,
+                        const double *foci, const idrs_pp_inputs *in, const idrs_pp_options *opt,
+                        idrs_pp_report *reports, double *relres, double *x);
+int idrs_cpp_ms_mr_idrs(idrs_user_matrix K, int nrhs, const double *rhs, int n_sigma,
+                        const double *sigma, idrs_user_matrix P, const double *center,
+                        const double *foci, const idrs_pp_inputs *in, const idrs_pp_options *opt,
+                        idrs_pp_report *reports, double *relres, double *x);
 
 #ifdef __cplusplus
 }
