@@ -1310,8 +1310,6 @@ int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix Mm, idrs_user_ma
   return guard([&] {
     REQUIRE(K && A, "matrix_create: bad arguments");
     const bool si = P && shift;
-    if (si && multishift && Cm)
-      throw unsupported_error("matrix_create: shift-and-invert of the block system is not supported");
     auto finish = [&](int st) {
       if (st) return st;
       (*A)->multishift = multishift != 0;
@@ -1332,8 +1330,9 @@ int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix Mm, idrs_user_ma
     if (K->format != FMT_CRS && K->format != FMT_COO)
       throw unsupported_error("matrix_create: with mass or damping matrices K must be CRS or COO");
     REQUIRE(!P || P->nrows == K->nrows, "matrix_create: P size mismatch");
-    REQUIRE(!P || P->which_precon <= 1 || !block_of(multishift, Cm),
-            "matrix_create: the block system takes a diagonal P");
+    const bool block_si = block_of(multishift, Cm) && P && (P->which_precon == 2 || P->which_precon == 3);
+    REQUIRE(!P || P->which_precon <= 1 || !block_of(multishift, Cm) || shift,
+            "matrix_create: an LU preconditioner of the block system needs the shift");
     init_runtime();
     const bool cplx = is_complex != 0;
     c128 sd(0.0, 0.0);
@@ -1342,14 +1341,28 @@ int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix Mm, idrs_user_ma
     const bool seeded = sd.x != 0.0 || sd.y != 0.0;
     idrs_user_matrix S = nullptr, D = nullptr;
     if (block || seeded) S = assemble_system(*K, Mm, Cm, sd, block);
-    if (block && P) D = block_diagonal(*P, K->nrows);
+    if (block && P && !block_si) D = block_diagonal(*P, K->nrows);
     // an assembled matrix already holds the seed: build without it, then
     // record it for the parameters derived from it (foci, centre, shifts)
-    int st = idrs_matrix_create(S ? S : K, D ? D : P, is_complex, S ? nullptr : seed, A);
+    int st = idrs_matrix_create(S ? S : K, block_si ? nullptr : (D ? D : P), is_complex,
+                                S ? nullptr : seed, A);
     // the operator holds its own references
     if (S) user_matrix_release(S);
     if (D) user_matrix_release(D);
     if (st) return st;
+    if (block_si) {
+      // rprecon's block form (matrix_module.f90:318-345): P (n x n), C, M and
+      // the shift; the products apply it before the assembled block matrix
+      REQUIRE(P->nrows == K->nrows, "matrix_create: P must have the size of K");
+      Operator* op = *A;
+      op->P = P; P->refcount++;
+      op->si_C = Cm; Cm->refcount++;
+      if (Mm) { op->si_M = Mm; Mm->refcount++; }
+      const size_t es = op->cplx ? 16 : 8;
+      IDRS_CUDA(cudaMallocAsync(&op->lu_tmp, es * 2 * K->nrows, op->stream));
+      IDRS_CUDA(cudaMallocAsync(&op->si_tmp, es * 2 * K->nrows, op->stream));
+      IDRS_CUDA(cudaStreamSynchronize(op->stream));
+    }
     if (S) {
       (*A)->seed = sd;
       (*A)->seed_folded = true;

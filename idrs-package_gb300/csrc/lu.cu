@@ -241,6 +241,46 @@ void lu_solve(const UserMatrix& P, const T* b, T* x, const int* skip, cudaStream
   IDRS_LAUNCH_CHECK();
 }
 
+namespace {
+// y = y + a x
+template <class T>
+__global__ void k_si_axpy(long n, T a, const T* __restrict__ x, T* y) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x)
+    y[i] = y[i] + a * x[i];
+}
+// w1 = v2 - s t2, w2 = -t2
+template <class T>
+__global__ void k_si_finish(long nn, T s, const T* __restrict__ v, const T* __restrict__ t2, T* w,
+                            const int* __restrict__ skip) {
+  if (skip && *(volatile const int*)skip) return;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nn; i += gridDim.x * (long)blockDim.x) {
+    const T t = t2[i];
+    w[i] = v[nn + i] - s * t;
+    w[nn + i] = T(0.0) - t;
+  }
+}
+}  // namespace
+
+template <class T>
+void block_si_precon(const MatView& V, long nn, const T* v, T* w, const int* skip, cudaStream_t st) {
+  T* a = (T*)V.si_tmp;
+  T* b = a + nn;
+  const T sh = narrow<T>(V.si_shift);
+  spmv<T>(V.si_C->view64(), v + nn, a, T(1.0), T(1.0), v, skip, st);  // a = v1 + C v2
+  if (V.si_M) {
+    spmv<T>(V.si_M->view64(), v + nn, b, T(1.0), T(0.0), nullptr, skip, st);
+    k_si_axpy<T><<<stream_grid(nn), kThreads, 0, st>>>(nn, sh, b, a);
+  } else {
+    k_si_axpy<T><<<stream_grid(nn), kThreads, 0, st>>>(nn, sh, v + nn, a);
+  }
+  IDRS_LAUNCH_CHECK();
+  lu_solve<T>(*V.lu, a, b, skip, st);
+  k_si_finish<T><<<stream_grid(nn), kThreads, 0, st>>>(nn, sh, v, b, w, skip);
+  IDRS_LAUNCH_CHECK();
+}
+
+template void block_si_precon<double>(const MatView&, long, const double*, double*, const int*, cudaStream_t);
+template void block_si_precon<c128>(const MatView&, long, const c128*, c128*, const int*, cudaStream_t);
 template void lu_solve<double>(const UserMatrix&, const double*, double*, const int*, cudaStream_t);
 template void lu_solve<c128>(const UserMatrix&, const c128*, c128*, const int*, cudaStream_t);
 

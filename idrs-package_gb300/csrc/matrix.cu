@@ -940,7 +940,10 @@ template <class T>
 void ks_mv(const MatView& Ks, const T* x, T* y, T a, T cv, const T* v, const int* skip,
            cudaStream_t st) {
   if constexpr (sizeof(typename traits<T>::real) == 8) {
-    if (Ks.lu) {
+    if (Ks.lu && Ks.si_C) {
+      block_si_precon<T>(Ks, Ks.nrows / 2, x, (T*)Ks.lu_tmp, skip, st);
+      x = (const T*)Ks.lu_tmp;
+    } else if (Ks.lu) {
       lu_solve<T>(*Ks.lu, x, (T*)Ks.lu_tmp, skip, st);
       x = (const T*)Ks.lu_tmp;
     }
@@ -1181,7 +1184,8 @@ void op_precon(Operator& A, int prec, const T* v, T* w, const int* skip, cudaStr
   long n = A.n();
   if (A.P && (A.P->which_precon == 2 || A.P->which_precon == 3)) {
     if constexpr (sizeof(typename traits<T>::real) == 8) {
-      lu_solve<T>(*A.P, v, w, skip, st);
+      if (A.si_C) block_si_precon<T>(A.view(64), n / 2, v, w, skip, st);
+      else lu_solve<T>(*A.P, v, w, skip, st);
       return;
     } else {
       throw std::runtime_error("shift-and-invert is not available in fp32 (inner_precision 32)");
@@ -1479,6 +1483,10 @@ const MatView& Operator::view(int prec) {
     ks64.defl = defl;
     ks64.lu = lu ? P : nullptr;
     ks64.lu_tmp = lu_tmp;
+    ks64.si_C = si_C;
+    ks64.si_M = si_M;
+    ks64.si_shift = shift;
+    ks64.si_tmp = si_tmp;
     return ks64;
   }
   if (defl && defl->k > 0)
@@ -1525,6 +1533,9 @@ void operator_free(Operator* A) {
   A->shadows.clear();
   if (A->defl) { deflation_free(A->defl); A->defl = nullptr; }
   if (A->lu_tmp) { cudaFreeAsync(A->lu_tmp, st); A->lu_tmp = nullptr; }
+  if (A->si_tmp) { cudaFreeAsync(A->si_tmp, st); A->si_tmp = nullptr; }
+  if (A->si_C) { user_matrix_release(A->si_C); A->si_C = nullptr; }
+  if (A->si_M) { user_matrix_release(A->si_M); A->si_M = nullptr; }
   free_redbuf(A->red, st);
   cudaStreamSynchronize(st);
   if (A->own_stream) cudaStreamDestroy(st);

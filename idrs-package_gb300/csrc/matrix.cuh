@@ -61,6 +61,12 @@ struct MatView {
   // triangular solves of P's LU factor into lu_tmp first (fp64 view only)
   const struct UserMatrix* lu = nullptr;
   void* lu_tmp = nullptr;
+  // the block system's shift-and-invert form (rprecon, matrix_module.f90:
+  // 318-345) needs C, M (n/2 x n/2), the shift and a 2 x n/2 scratch
+  const struct UserMatrix* si_C = nullptr;
+  const struct UserMatrix* si_M = nullptr;
+  c128 si_shift;
+  void* si_tmp = nullptr;
 };
 
 // Deflation of type(matrix) (matrix_module.f90:1284-1623): V (n x k), AV =
@@ -193,6 +199,10 @@ struct Operator {
   bool shift_invert = false;
   c128 shift;
   void* lu_tmp = nullptr;
+  // block system with shift-and-invert: C and M of the block form (held)
+  UserMatrix* si_C = nullptr;
+  UserMatrix* si_M = nullptr;
+  void* si_tmp = nullptr;
   Deflation* defl = nullptr;
   // shifts relative to the seed of the last ms_parameters call (sigma_s)
   std::vector<c128> sigma_s;
@@ -249,6 +259,11 @@ void lu_build(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, boo
               c128 shift, int which, bool cplx, UserMatrix& P);
 template <class T>
 void lu_solve(const UserMatrix& P, const T* b, T* x, const int* skip, cudaStream_t st);
+// w = v / A for the block system with a shift-and-invert P (n = 2 nn):
+// t1 = v2, t2 = P^-1 (v1 + C v2 + shift M v2) (M absent: + shift v2),
+// w1 = t1 - shift t2, w2 = -t2.  tmp: 2 nn scratch; w must not alias v.
+template <class T>
+void block_si_precon(const MatView& V, long nn, const T* v, T* w, const int* skip, cudaStream_t st);
 // y = a * Ks (P^-1 x) + cv * v: real_mv of matrix_module.f90:218-264 on a
 // view (the LU solve only with a shift-and-invert preconditioner)
 template <class T>

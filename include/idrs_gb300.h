@@ -139,8 +139,9 @@ int idrs_matrix_create(idrs_user_matrix K, idrs_user_matrix P, int is_complex,
  * With a shift-and-invert P (which_precon 2/3) and `shift` (NULL = absent),
  * A%shift_invert holds (real_matrix.inc:23-29): every product is
  * K' (P^-1 v), ms_parameters uses (sigma - seed)/(sigma - shift) and the
- * multishift scaleback the factor (seed - shift)/(sigma - shift).  The block
- * system's shift-and-invert form is not supported (IDRS_ERR_UNSUPPORTED). */
+ * multishift scaleback the factor (seed - shift)/(sigma - shift).  For the
+ * block system P is the LU of K + shift C + shift^2 M (n x n) and v/A is
+ * rprecon's block form (matrix_module.f90:318-345). */
 int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix M, idrs_user_matrix C,
                            idrs_user_matrix P, int is_complex, const double *seed,
                            const double *shift, int multishift, idrs_matrix *A);

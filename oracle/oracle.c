@@ -528,7 +528,6 @@ int or_complex_precon(int which_precon, const or_umat *K, const double *shift, o
 int or_matrix_create_ext(const or_umat *K, const or_umat *M, const or_umat *C,
                          const or_umat *P, const double *seed, const double *shift, int cplx,
                          int multishift, or_mat **out) {
-  if (P && shift && multishift && C) return OR_EUNSUP;
   int st = or_matrix_create(K, P, seed, cplx, out);
   if (st != OR_OK) return st;
   if (P && shift) {

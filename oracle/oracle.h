@@ -126,8 +126,8 @@ int or_matrix_create(const or_umat *K, const or_umat *P, const double *seed, int
                      or_mat **out);
 /* type(matrix) with mass M and damping C (real_matrix.inc:9-43): the 2x2
  * block system when multishift and C are both present (vectors of 2n); with
- * P and shift, P is a shift-and-invert preconditioner (the block system's
- * shift-and-invert form is not restated: OR_EUNSUP). */
+ * P and shift, P is a shift-and-invert preconditioner (the LU of
+ * K + shift C + shift^2 M; for the block system rprecon's block form). */
 int or_matrix_create_ext(const or_umat *K, const or_umat *M, const or_umat *C,
                          const or_umat *P, const double *seed, const double *shift, int cplx,
                          int multishift, or_mat **out);

@@ -101,3 +101,31 @@ def test_zero_pivot_is_an_error(gpu):
     for which in (2, 3):
         with pytest.raises(gpu.IDRSError):
             gpu.real_precon(which, K)
+
+
+def test_block_shift_and_invert_matches_oracle(gpu, oracle, P):
+    """Damped multishift problem on the 2 x 2 block system with rprecon's
+    shift-and-invert block form (matrix_module.f90:318-345): GPU and oracle
+    agree and every (K + sigma C + sigma^2 M) x = rhs is solved."""
+    N, D, Md, Cd, K, M, C, rng = _mats(gpu, oracle, P, 4, seed=8)
+    tau = 3.0 + 2.0j
+    sig = np.array([1.0 + 1.0j, 2.0 + 0.5j, 4.0 + 1.0j])
+    A = gpu.Matrix(K[0], P=gpu.complex_precon(3, K[0], shift=tau, M=M[0], C_=C[0]), M=M[0], C_=C[0],
+                   seed=sig[-1], shift=tau, complex=True, multishift=True)
+    Ao = oracle.Matrix(K[1], P=oracle.complex_precon(3, K[1], shift=tau, M=M[1], C_=C[1]), M=M[1],
+                       C_=C[1], seed=sig[-1], shift=tau, cplx=True, multishift=True)
+    assert A.n == Ao.n == 2 * N
+    v = rng.standard_normal(2 * N) + 1j * rng.standard_normal(2 * N)
+    np.testing.assert_allclose(v / A, Ao.precon(v), rtol=1e-11, atol=1e-14)
+    np.testing.assert_allclose(A * v, Ao.matvec(v), rtol=1e-11, atol=1e-11)
+    rhs = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    b = np.concatenate([-rhs, np.zeros(N)])
+    sp, spo = A.ms_parameters(sig), Ao.ms_parameters(sig)
+    g = gpu.MSIDRS(A, b, sp, 4, tolerance=1e-11, maximum_iterations=3000)
+    o = oracle.msidrs(Ao, b, spo, 4, tolerance=1e-11, maximum_iterations=3000)
+    assert g.flag == o.flag == 0 and abs(g.iterations - o.iterations) <= 2
+    X = A.ms_scaleback(sig, b, g.x)[N:, :]
+    np.testing.assert_allclose(X, Ao.ms_scaleback(o.x, b)[N:, :], rtol=0, atol=1e-8 * np.abs(X).max())
+    for k, s in enumerate(sig):
+        S = D + s * Cd + s ** 2 * Md
+        assert np.linalg.norm(rhs - S @ X[:, k]) <= 1e-8 * np.linalg.norm(rhs)

@@ -496,3 +496,26 @@ def test_shift_and_invert_multishift_oracle(oracle, P):
     X = A.ms_scaleback(o.x, b)
     for k, s in enumerate(sig):
         assert np.linalg.norm(b - (D - s * Md) @ X[:, k]) <= 1e-9 * np.linalg.norm(b)
+
+
+def test_block_shift_and_invert_oracle(oracle, P):
+    """The damped multishift problem (K + sigma C + sigma^2 M) x = rhs on the
+    2 x 2 block system with rprecon's shift-and-invert block form
+    (matrix_module.f90:318-345): every frequency from one MSIDRS run."""
+    N, K, D, _ = _scaled_cdr(oracle, P, n=4)
+    rng = np.random.default_rng(8)
+    M, Md, C, Cd = _mass_and_damping(oracle, N, rng)
+    tau = 3.0 + 2.0j
+    Pm = oracle.complex_precon(3, K, shift=tau, M=M, C_=C)
+    sig = np.array([1.0 + 1.0j, 2.0 + 0.5j, 4.0 + 1.0j])
+    seed = sig[-1]
+    A = oracle.Matrix(K, P=Pm, M=M, C_=C, seed=seed, shift=tau, cplx=True, multishift=True)
+    rhs = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    b = np.concatenate([-rhs, np.zeros(N)])
+    sp = A.ms_parameters(sig)
+    o = oracle.msidrs(A, b, sp, 4, tolerance=1e-11, maximum_iterations=3000)
+    assert o.flag == 0
+    X = A.ms_scaleback(o.x, b)[N:, :]
+    for k, s in enumerate(sig):
+        S = D + s * Cd + s ** 2 * Md
+        assert np.linalg.norm(rhs - S @ X[:, k]) <= 1e-8 * np.linalg.norm(rhs)
