@@ -117,6 +117,8 @@ _PROTOS = {
     "idrs_ridrs_ritz": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp,
                              _i, _vp, _i, _vp, _i, _i, _vp, _vp]),
     "idrs_rpp_idrs": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "idrs_cidrs_ritz": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp,
+                             _i, _vp, _i, _vp, _i, _i, _vp, _vp]),
     "idrs_rpp_mr_idrs": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "idrs_rpp_idrs_ext": (_i, [_vp] * 9),
     "idrs_cpp_idrs": (_i, [_vp] * 9),
@@ -735,19 +737,21 @@ def IDRS_RITZ(A: Matrix, b, s, M: Matrix | None = None, tolerance=None, maximum_
     dimU0 (the recycle space U0, n x dimU0), H_shape (H) and resvec."""
     b = _solver_common(A, b)
     x = np.empty_like(b)
+    dt = A.dtype
     flag, relres, iters, nritz = C.c_int(), C.c_double(), C.c_int(), C.c_int()
-    Hm = np.zeros(H_shape, order="F") if H_shape else None
-    om = np.zeros(n_omega) if n_omega else None
-    U0 = np.zeros((A.n, dimU0), order="F") if dimU0 else None
+    Hm = np.zeros(H_shape, dtype=dt, order="F") if H_shape else None
+    om = np.zeros(n_omega, dtype=dt) if n_omega else None
+    U0 = np.zeros((A.n, dimU0), dtype=dt, order="F") if dimU0 else None
     maxit = maximum_iterations if maximum_iterations is not None else min(2 * A.n, 1000)
     rv = np.zeros(maxit + 1) if resvec else None
-    _check(lib().idrs_ridrs_ritz(A.handle, _p(b), int(s), M.handle if M else None,
-                                 _ref_dbl(tolerance), _ref_int(maximum_iterations),
-                                 _ref_int(variant), C.byref(flag), C.byref(relres), C.byref(iters),
-                                 _p(_arr(x0, False, A.n)), _p(U0), int(dimU0), _p(om), int(n_omega),
-                                 _p(rv), 0 if rv is None else len(rv), _p(Hm),
-                                 0 if Hm is None else H_shape[0], 0 if Hm is None else H_shape[1],
-                                 C.byref(nritz), _p(x)))
+    fn = lib().idrs_cidrs_ritz if A.cplx else lib().idrs_ridrs_ritz
+    _check(fn(A.handle, _p(b), int(s), M.handle if M else None,
+              _ref_dbl(tolerance), _ref_int(maximum_iterations),
+              _ref_int(variant), C.byref(flag), C.byref(relres), C.byref(iters),
+              _p(_arr(x0, A.cplx, A.n)), _p(U0), int(dimU0), _p(om), int(n_omega),
+              _p(rv), 0 if rv is None else len(rv), _p(Hm),
+              0 if Hm is None else H_shape[0], 0 if Hm is None else H_shape[1],
+              C.byref(nritz), _p(x)))
     r = Result(x=x, flag=flag.value, relres=relres.value, iterations=iters.value, nritz=nritz.value)
     for key, val in (("H", Hm), ("omega", om), ("U0", U0), ("resvec", rv)):
         if val is not None:

@@ -1707,72 +1707,112 @@ int idrs_radjoint(idrs_matrix AT, idrs_user_matrix K, const double* x, const dou
   });
 }
 
+}  // extern "C"
+
+// RIDRS_RITZ / CIDRS_RITZ (ritz_module.f90:268-556): IDRS with the
+// Hessenberg output, then omega and the recycle space.  T: double or c128;
+// H, omega, U0 have the kind of T (complex interleaved).
+template <class T>
+static int ritz_t(idrs_matrix A, const double* b, int s, idrs_matrix M, const double* tolerance,
+                  const int* maximum_iterations, const int* variant, int* flag, double* relres,
+                  int* iterations, const double* x0, double* U0, int dimU0, double* omega,
+                  int n_omega, double* resvec, int resvec_len, double* H, int ldh, int nh,
+                  int* nritz, double* x) {
+  constexpr bool cplx = traits<T>::is_cplx;
+  constexpr int vw = cplx ? 2 : 1;
+  REQUIRE(A && A->cplx == cplx && b && x, "idrs_ritz: bad arguments");
+  REQUIRE(!M || M->cplx == cplx, "idrs_ritz: M must have the kind of A");
+  long n = A->n();
+  if (tolerance) REQUIRE(*tolerance >= 0, "Illegal value for parameter tolerance");
+  int maxit = maximum_iterations ? *maximum_iterations : (int)std::min<long>(2 * n, 1000);
+  REQUIRE(maxit >= 1, "idrs_ritz: maximum_iterations must be positive");
+  if (resvec) REQUIRE(resvec_len >= maxit + 1, "Length of vector with residual norms too small, should be maxit+1");
+  if (U0 && dimU0 > 0) REQUIRE(dimU0 <= MAXS, "idrs_ritz: dimension of U0 larger than 16");
+  std::vector<double> Hf((size_t)vw * (maxit + 1) * maxit, 0.0);
+  std::vector<double> zeros;
+  const double* xs = x0;
+  if (!xs && !A->device_pointers) { zeros.assign((size_t)vw * n, 0.0); xs = zeros.data(); }
+  int conv = -1, iter = 0, method = variant ? *variant : 1;
+  double rel = 1.0;
+  std::vector<double> resnrm(maxit + 1);
+  int st = run_idrs<T>(A, b, s, M, tolerance, &maxit, &method, &conv, &rel, &iter, xs, nullptr,
+                       nullptr, 0, resnrm.data(), maxit + 1, Hf.data(), maxit + 1, maxit, x);
+  if (st) return st;
+  const int nr = (iter / (s + 1)) * s + iter % (s + 1);
+  if (flag) *flag = conv;
+  if (relres) *relres = rel;
+  if (iterations) *iterations = iter;
+  if (nritz) *nritz = nr;
+  if (resvec) std::copy(resnrm.begin(), resnrm.end(), resvec);
+  const T* Ht = (const T*)Hf.data();
+  if (omega && n_omega > 0) {
+    REQUIRE(nr >= n_omega, "Too many parameters omega requested, reduce omega.");
+    if constexpr (cplx) ritz_omega((const cd*)Hf.data(), maxit + 1, n_omega, (cd*)omega);
+    else ritz_omega(Hf.data(), maxit + 1, n_omega, omega);
+  }
+  if (U0 && dimU0 > 0) {
+    REQUIRE(nr >= dimU0, "Recycle space is too large, reduce dimension of U0.");
+    cudaStream_t cs = A->stream;
+    std::vector<T> vec((size_t)nr * dimU0);
+    std::vector<double> resval(dimU0);
+    if constexpr (cplx) {
+      // the first dimU0 Schur vectors of QR_eig (ritz_module.f90:367-368)
+      std::vector<cd> Vs((size_t)nr * nr), ev(nr);
+      int conv_eig = 0;
+      qr_eig((const cd*)Hf.data(), maxit + 1, nr, ev.data(), &conv_eig, Vs.data());
+      for (int j = 0; j < dimU0; ++j)
+        for (int i = 0; i < nr; ++i) vec[i + (size_t)nr * j] = c128(Vs[i + (size_t)nr * j].real(), Vs[i + (size_t)nr * j].imag());
+    } else {
+      si_power(Hf.data(), maxit + 1, nr, dimU0, 0.0, kSiPowerSeed, (double*)vec.data());
+    }
+    Staged sb(A, sizeof(T) * n), su(A, sizeof(T) * n * dimU0);
+    const T* d_b = (const T*)sb.in(b);
+    T* d_U = (T*)su.out(U0);
+    Operator* Mp = (M && M->dkind != 0) ? M : nullptr;
+    compute_u0<T>(*A, Mp, Ht, maxit + 1, nr, vec.data(), dimU0, d_b, d_U, resval.data(), cs);
+    if (Mp)
+      for (int j = 0; j < dimU0; ++j) {
+        DBuf tmp(sizeof(T) * n, cs);
+        op_precon<T>(*Mp, 64, d_U + (size_t)n * j, tmp.as<T>(), nullptr, cs);
+        IDRS_CUDA(cudaMemcpyAsync(d_U + (size_t)n * j, tmp.p, sizeof(T) * n, cudaMemcpyDeviceToDevice, cs));
+      }
+    int dep = global_qr<T>(n, dimU0, d_U, nullptr, A->red, cs);
+    REQUIRE(dep == 0, " V has dependent columns ");
+    su.finish(U0, d_U);
+    IDRS_CUDA(cudaStreamSynchronize(cs));
+  }
+  if (H) {
+    REQUIRE((long)ldh * nh <= (long)(maxit + 1) * maxit && ldh <= maxit + 1 && nh <= maxit,
+            "Dimensions of Hessenberg matrix too large");
+    for (int j = 0; j < nh; ++j)
+      for (int i = 0; i < ldh; ++i)
+        for (int c = 0; c < vw; ++c)
+          H[vw * (i + (size_t)ldh * j) + c] = Hf[vw * (i + (size_t)(maxit + 1) * j) + c];
+  }
+  return IDRS_OK;
+}
+
+extern "C" {
+
 int idrs_ridrs_ritz(idrs_matrix A, const double* b, int s, idrs_matrix M,
                     const double* tolerance, const int* maximum_iterations, const int* variant,
                     int* flag, double* relres, int* iterations, const double* x0, double* U0,
                     int dimU0, double* omega, int n_omega, double* resvec, int resvec_len,
                     double* H, int ldh, int nh, int* nritz, double* x) {
   return guard([&] {
-    REQUIRE(A && !A->cplx && b && x, "ridrs_ritz: bad arguments");
-    REQUIRE(!M || !M->cplx, "ridrs_ritz: M must be real");
-    long n = A->n();
-    if (tolerance) REQUIRE(*tolerance >= 0, "Illegal value for parameter tolerance");
-    int maxit = maximum_iterations ? *maximum_iterations : (int)std::min<long>(2 * n, 1000);
-    REQUIRE(maxit >= 1, "ridrs_ritz: maximum_iterations must be positive");
-    if (resvec) REQUIRE(resvec_len >= maxit + 1, "Length of vector with residual norms too small, should be maxit+1");
-    if (U0 && dimU0 > 0) {
-      REQUIRE(dimU0 <= MAXS, "ridrs_ritz: dimension of U0 larger than 16");
-    }
-    std::vector<double> Hf((size_t)(maxit + 1) * maxit, 0.0);
-    std::vector<double> zeros;
-    const double* xs = x0;
-    if (!xs && !A->device_pointers) { zeros.assign(n, 0.0); xs = zeros.data(); }
-    int conv = -1, iter = 0, method = variant ? *variant : 1;
-    double rel = 1.0;
-    std::vector<double> resnrm(maxit + 1);
-    int st = run_idrs<double>(A, b, s, M, tolerance, &maxit, &method, &conv, &rel, &iter, xs,
-                              nullptr, nullptr, 0, resnrm.data(), maxit + 1, Hf.data(), maxit + 1,
-                              maxit, x);
-    if (st) return st;
-    const int nr = (iter / (s + 1)) * s + iter % (s + 1);
-    if (flag) *flag = conv;
-    if (relres) *relres = rel;
-    if (iterations) *iterations = iter;
-    if (nritz) *nritz = nr;
-    if (resvec) std::copy(resnrm.begin(), resnrm.end(), resvec);
-    if (omega && n_omega > 0) {
-      REQUIRE(nr >= n_omega, "Too many parameters omega requested, reduce omega.");
-      ritz_omega(Hf.data(), maxit + 1, n_omega, omega);
-    }
-    if (U0 && dimU0 > 0) {
-      REQUIRE(nr >= dimU0, "Recycle space is too large, reduce dimension of U0.");
-      cudaStream_t cs = A->stream;
-      std::vector<double> vec((size_t)nr * dimU0), resval(dimU0);
-      si_power(Hf.data(), maxit + 1, nr, dimU0, 0.0, kSiPowerSeed, vec.data());
-      Staged sb(A, sizeof(double) * n), su(A, sizeof(double) * n * dimU0);
-      const double* d_b = (const double*)sb.in(b);
-      double* d_U = (double*)su.out(U0);
-      Operator* Mp = (M && M->dkind != 0) ? M : nullptr;
-      compute_u0(*A, Mp, Hf.data(), maxit + 1, nr, vec.data(), dimU0, d_b, d_U, resval.data(), cs);
-      if (Mp)
-        for (int j = 0; j < dimU0; ++j) {
-          DBuf tmp(sizeof(double) * n, cs);
-          op_precon<double>(*Mp, 64, d_U + (size_t)n * j, tmp.as<double>(), nullptr, cs);
-          IDRS_CUDA(cudaMemcpyAsync(d_U + (size_t)n * j, tmp.p, sizeof(double) * n,
-                                    cudaMemcpyDeviceToDevice, cs));
-        }
-      int dep = global_qr(n, dimU0, d_U, nullptr, A->red, cs);
-      REQUIRE(dep == 0, " V has dependent columns ");
-      su.finish(U0, d_U);
-      IDRS_CUDA(cudaStreamSynchronize(cs));
-    }
-    if (H) {
-      REQUIRE((long)ldh * nh <= (long)(maxit + 1) * maxit && ldh <= maxit + 1 && nh <= maxit,
-              "Dimensions of Hessenberg matrix too large");
-      for (int j = 0; j < nh; ++j)
-        for (int i = 0; i < ldh; ++i) H[i + (size_t)ldh * j] = Hf[i + (size_t)(maxit + 1) * j];
-    }
-    return IDRS_OK;
+    return ritz_t<double>(A, b, s, M, tolerance, maximum_iterations, variant, flag, relres, iterations,
+                          x0, U0, dimU0, omega, n_omega, resvec, resvec_len, H, ldh, nh, nritz, x);
+  });
+}
+
+int idrs_cidrs_ritz(idrs_matrix A, const double* b, int s, idrs_matrix M,
+                    const double* tolerance, const int* maximum_iterations, const int* variant,
+                    int* flag, double* relres, int* iterations, const double* x0, double* U0,
+                    int dimU0, double* omega, int n_omega, double* resvec, int resvec_len,
+                    double* H, int ldh, int nh, int* nritz, double* x) {
+  return guard([&] {
+    return ritz_t<c128>(A, b, s, M, tolerance, maximum_iterations, variant, flag, relres, iterations,
+                        x0, U0, dimU0, omega, n_omega, resvec, resvec_len, H, ldh, nh, nritz, x);
   });
 }
 
@@ -1870,31 +1910,10 @@ int pp_ritz(PPJob<T>& J, const T* pb, int s, double tol, int maxit, T* x, double
             int nh, int n_omega, T* omega, double* U0, int dimU0, int* flag, double* relres,
             int* iter, int* nritz) {
   int one = 1;
-  if constexpr (!kCplx<T>) {
-    return idrs_ridrs_ritz(J.A, pb, s, nullptr, &tol, &maxit, &one, flag, relres, iter, nullptr,
-                           U0, dimU0, n_omega > 0 ? omega : nullptr, n_omega, nullptr, 0, H, ldh, nh,
-                           nritz, x);
-  } else {
-    REQUIRE(dimU0 == 0, "pp_idrs: the complex recycle space is not supported");
-    std::vector<double> Hf((size_t)2 * (maxit + 1) * maxit, 0.0), resnrm(maxit + 1);
-    int st = run_idrs<c128>(J.A, (const double*)pb, s, nullptr, &tol, &maxit, &one, flag, relres, iter,
-                            nullptr, nullptr, nullptr, 0, resnrm.data(), maxit + 1, Hf.data(), maxit + 1,
-                            maxit, (double*)x);
-    if (st) return st;
-    const int nr = (*iter / (s + 1)) * s + *iter % (s + 1);
-    *nritz = nr;
-    if (omega && n_omega > 0) {
-      REQUIRE(nr >= n_omega, "Too many parameters omega requested, reduce omega.");
-      ritz_omega((const std::complex<double>*)Hf.data(), maxit + 1, n_omega, (std::complex<double>*)omega);
-    }
-    if (H)
-      for (int j = 0; j < nh; ++j)
-        for (int i = 0; i < ldh; ++i) {
-          H[2 * (i + (size_t)ldh * j)] = Hf[2 * (i + (size_t)(maxit + 1) * j)];
-          H[2 * (i + (size_t)ldh * j) + 1] = Hf[2 * (i + (size_t)(maxit + 1) * j) + 1];
-        }
-    return IDRS_OK;
-  }
+  auto fn = kCplx<T> ? idrs_cidrs_ritz : idrs_ridrs_ritz;
+  return fn(J.A, (const double*)pb, s, nullptr, &tol, &maxit, &one, flag, relres, iter, nullptr, U0,
+            dimU0, n_omega > 0 ? (double*)omega : nullptr, n_omega, nullptr, 0, H, ldh, nh, nritz,
+            (double*)x);
 }
 
 // real_preconditioner.inc / complex_preconditioner.inc: the initial
@@ -1956,12 +1975,11 @@ int pp_setup(PPJob<T>& J, const T* pb, const double* center, const double* foci,
 // recycle.inc: x0 = IDRS_RITZ(A, b, s, tol, maxit, variant 1) with U0 (n x s)
 template <class T>
 int pp_recycle(PPJob<T>& J, const T* pb, const idrs_pp_options* opt, idrs_pp_report& rep) {
-  REQUIRE(!kCplx<T>, "pp_idrs: the complex recycle space is not supported");
   const int s = opt->s;
   J.U0 = DBuf(sizeof(T) * J.n * s, J.cs);
   int nr = 0;
   int st = pp_ritz<T>(J, pb, s, opt->tol, opt->maxit, J.d_x0.template as<T>(), nullptr, 0, 0, 0, nullptr,
-                      J.U0.template as<double>(), s, &rep.recycle_flag, &rep.recycle_relres,
+                      (double*)J.U0.template as<T>(), s, &rep.recycle_flag, &rep.recycle_relres,
                       &rep.recycle_iterations, &nr);
   if (st) return st;
   J.have_U0 = true;
@@ -2020,7 +2038,7 @@ int pp_solve(PPJob<T>& J, const T* pb, T* px, const idrs_pp_options* opt, idrs_p
     int variant = opt->method == 2 ? 2 : 1;
     st = run_idrs<T>(A, (const double*)rb, s, nullptr, &tol, &maxit, &variant, &rep.flag,
                      &rep.relres_solver, &rep.iterations, (const double*)J.d_x0.template as<T>(),
-                     J.have_U0 ? J.U0.template as<double>() : nullptr, om, n_om, nullptr, 0, nullptr, 0, 0,
+                     J.have_U0 ? (const double*)J.U0.template as<T>() : nullptr, om, n_om, nullptr, 0, nullptr, 0, 0,
                      (double*)J.d_y.template as<T>());
   }
   if (st) return st;

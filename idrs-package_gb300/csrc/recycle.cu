@@ -138,110 +138,132 @@ void ritz_omega(const std::complex<double>* Hf, int ldh, int n_omega, std::compl
 namespace {
 
 struct DevVec {
-  double* p = nullptr;
+  void* p = nullptr;
   cudaStream_t st;
-  DevVec(size_t count, cudaStream_t s) : st(s) {
-    IDRS_CUDA(cudaMallocAsync((void**)&p, sizeof(double) * std::max<size_t>(count, 2), s));
+  DevVec(size_t bytes, cudaStream_t s) : st(s) {
+    IDRS_CUDA(cudaMallocAsync(&p, std::max<size_t>(bytes, 16), s));
   }
   DevVec(const DevVec&) = delete;
   DevVec& operator=(const DevVec&) = delete;
   ~DevVec() { if (p) cudaFreeAsync(p, st); }
+  template <class T> T* as() const { return (T*)p; }
 };
 
-// Coefficients of one Ritz step of rcompute_U0.
+// Coefficients of one Ritz step of compute_U0.
+template <class T>
 struct U0Step {
-  double e[MAXS];        // eigvec(i, 1:ns)
-  double h[MAXS + 1];    // H(low:i, i)
+  T e[MAXS];             // eigvec(i, 1:ns)
+  T h[MAXS + 1];         // H(low:i, i)
   int col[MAXS + 1];     // ring columns of v_low .. v_i
   int nl, ns;            // window length, number of U columns
   int cur, next;         // ring columns of v_i and v_{i+1}
-  double hden;           // H(i+1, i)
+  T hden;                // H(i+1, i)
 };
 
 // U(:,j) += e_j v_i;  v_{i+1} = (t - sum_l h_l v_l) / hden.  v_{i+1}
 // overwrites the ring column of v_{i-ns}, which this thread reads first.
-__global__ void __launch_bounds__(kThreads) k_u0_step(long n, const double* __restrict__ t,
-                                                      double* W, double* U, U0Step c) {
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_u0_step(long n, const T* __restrict__ t, T* W, T* U,
+                                                      U0Step<T> c) {
   const long stride = (long)gridDim.x * blockDim.x;
   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += stride) {
-    const double v = W[c.cur * n + q];
+    const T v = W[c.cur * n + q];
     for (int j = 0; j < c.ns; ++j) U[j * n + q] = U[j * n + q] + c.e[j] * v;
-    double acc = 0;
-    for (int l = 0; l < c.nl; ++l) acc += W[c.col[l] * n + q] * c.h[l];
+    T acc = T(0.0);
+    for (int l = 0; l < c.nl; ++l) acc = acc + W[c.col[l] * n + q] * c.h[l];
     W[c.next * n + q] = (t[q] - acc) / c.hden;
   }
 }
 
-// x(:,j) = x(:,j) / d[j]   (d on the device)
-__global__ void k_div_cols(long n, int cols, double* x, const double* d, long dstride) {
+// x(:,j) = x(:,j) / d[j]   (d: real values on the device)
+template <class T>
+__global__ void k_div_cols(long n, int cols, T* x, const double* d) {
   const long stride = (long)gridDim.x * blockDim.x;
   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n * cols; q += stride) {
     const long j = q / n;
-    x[q] = x[q] / d[j * dstride];
+    x[q] = x[q] / T(d[j]);
   }
 }
 
-template <class W> struct TSqrtAt {
-  double* out; bool root;
-  __device__ void operator()(const W* v) const { *out = root ? sqrt((double)v[0]) : (double)v[0]; }
+inline double mag(double v) { return std::fabs(v); }
+inline double mag(c128 v) { return std::hypot(v.x, v.y); }
+
+__device__ inline double re_part(double v) { return v; }
+__device__ inline double re_part(c128 v) { return v.x; }
+
+// stores sqrt(Re v) (a norm) as a real value
+template <class W> struct TNormAt {
+  double* out;
+  __device__ void operator()(const W* v) const { *out = sqrt(re_part(v[0])); }
+};
+
+// R(i, j) = v (an inner product) or sqrt(Re v) (the norm, i = j)
+template <class W> struct TRAt {
+  W* out; bool root;
+  __device__ void operator()(const W* v) const {
+    if (root) *out = W(sqrt(re_part(v[0])));
+    else *out = v[0];
+  }
 };
 
 // One modified Gram-Schmidt pass on column j: with i > 0 first
-// Q_j -= R(i-1,j) Q_{i-1}; then acc0 = Q_i . Q_j (i < j) or |Q_j|^2 (i = j).
+// Q_j -= R(i-1,j) Q_{i-1}; then acc0 = Q_i^H Q_j (i < j) or |Q_j|^2 (i = j).
+template <class T>
 struct BMgsPass {
-  double* Q; long ld; int i, j; const double* Rj;
-  struct Shared { double c; };
+  T* Q; long ld; int i, j; const T* Rj;
+  struct Shared { T c; };
   __device__ void prepare(Shared& sh) const {
-    if (threadIdx.x == 0) sh.c = i > 0 ? Rj[i - 1] : 0.0;
+    if (threadIdx.x == 0) sh.c = i > 0 ? Rj[i - 1] : T(0.0);
   }
   template <int ND, class A>
   __device__ void operator()(long q, Shared& sh, A (&acc)[ND]) const {
-    double qj = Q[j * ld + q];
+    T qj = Q[j * ld + q];
     if (i > 0) {
       qj = qj - sh.c * Q[(i - 1) * ld + q];
       Q[j * ld + q] = qj;
     }
-    const double a = i < j ? Q[i * ld + q] : qj;
-    acc_add(acc[0], a * qj);
+    if (i < j) acc_add(acc[0], conj_(Q[i * ld + q]) * qj);
+    else acc_add(acc[0], abs2_(qj));
   }
 };
 
-// Q_j = Q_j / R(j,j) when R(j,j) > DBL_MIN (else left for the host check)
-__global__ void k_mgs_scale(long n, double* qj, const double* rjj) {
-  const double r = *rjj;
-  if (!(r > DBL_MIN)) return;
+// Q_j = Q_j / R(j,j) when |R(j,j)| > DBL_MIN (else left for the host check)
+template <class T>
+__global__ void k_mgs_scale(long n, T* qj, const T* rjj) {
+  const T r = *rjj;
+  if (!(abs_(r) > DBL_MIN)) return;
   const long stride = (long)gridDim.x * blockDim.x;
   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += stride) qj[q] = qj[q] / r;
 }
 
 }  // namespace
 
-void compute_u0(Operator& A, Operator* M, const double* H, int ldh, int nritz,
-                const double* eigvec, int ns, const double* b, double* U, double* resnrm,
-                cudaStream_t st) {
+template <class T>
+void compute_u0(Operator& A, Operator* M, const T* H, int ldh, int nritz, const T* eigvec, int ns,
+                const T* b, T* U, double* resnrm, cudaStream_t st) {
   if (ns < 1 || ns > MAXS) throw std::runtime_error("compute_U0: dimension of U0 out of range");
   if (nritz < 1 || ldh < nritz + 1) throw std::runtime_error("compute_U0: bad Hessenberg size");
   const long n = A.n();
   const int ring = ns + 1;
-  DevVec W((size_t)n * ring, st), t(n, st), t1(n, st), t2(n, st);
+  DevVec W(sizeof(T) * n * ring, st), t(sizeof(T) * n, st), t1(sizeof(T) * n, st), t2(sizeof(T) * n, st);
   std::unique_ptr<DevVec> u;
-  if (M) u.reset(new DevVec(n, st));
-  IDRS_CUDA(cudaMemsetAsync(U, 0, sizeof(double) * n * ns, st));
-  IDRS_CUDA(cudaMemcpyAsync(W.p, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  if (M) u.reset(new DevVec(sizeof(T) * n, st));
+  IDRS_CUDA(cudaMemsetAsync(U, 0, sizeof(T) * n * ns, st));
+  IDRS_CUDA(cudaMemcpyAsync(W.p, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, st));
   std::vector<int> ind(nritz + 1, 0);
   int k = 0;
   for (int i = 1; i <= nritz; ++i) {
     k = k + 1;
     if (k > ring) k = 1;
     ind[i] = k;
-    const double* v = W.p + (size_t)(k - 1) * n;
+    const T* v = W.as<T>() + (size_t)(k - 1) * n;
     if (M) {
-      op_precon<double>(*M, 64, v, u->p, nullptr, st);
-      op_chain<double>(A.view(64), A.alpha_p, A.degree, u->p, t.p, t1.p, t2.p, nullptr, st);
+      op_precon<T>(*M, 64, v, u->as<T>(), nullptr, st);
+      op_chain<T>(A.view(64), A.alpha_p, A.degree, u->as<T>(), t.as<T>(), t1.as<T>(), t2.as<T>(), nullptr, st);
     } else {
-      op_chain<double>(A.view(64), A.alpha_p, A.degree, v, t.p, t1.p, t2.p, nullptr, st);
+      op_chain<T>(A.view(64), A.alpha_p, A.degree, v, t.as<T>(), t1.as<T>(), t2.as<T>(), nullptr, st);
     }
-    U0Step c{};
+    U0Step<T> c{};
     for (int j = 0; j < ns; ++j) c.e[j] = eigvec[(i - 1) + (size_t)nritz * j];
     const int low = std::max(1, i - ns);
     c.nl = i - low + 1;
@@ -253,47 +275,54 @@ void compute_u0(Operator& A, Operator* M, const double* H, int ldh, int nritz,
     c.cur = k - 1;
     c.next = k % ring;
     c.hden = H[i + (size_t)ldh * (i - 1)];
-    k_u0_step<<<stream_grid(n), kThreads, 0, st>>>(n, t.p, W.p, U, c);
+    k_u0_step<T><<<stream_grid(n), kThreads, 0, st>>>(n, t.as<T>(), W.as<T>(), U, c);
     IDRS_LAUNCH_CHECK();
   }
   if (resnrm) {
     // norms of U(:,j) and of v_{nritz+1}, then U(:,j) /= |U(:,j)|
-    DevVec nr(ns + 1, st);
+    using Wt = typename traits<T>::wide;
+    DevVec nr(sizeof(double) * (ns + 1), st);
     for (int j = 0; j < ns; ++j)
-      launch_fused<1, double>(n, BNorm<double>{U + (size_t)n * j}, TSqrtAt<double>{nr.p + j, true},
-                              A.red, nullptr, st);
-    const double* vlast = W.p + (size_t)(k % ring) * n;
-    launch_fused<1, double>(n, BNorm<double>{vlast}, TSqrtAt<double>{nr.p + ns, true}, A.red,
-                            nullptr, st);
-    k_div_cols<<<stream_grid(n * ns), kThreads, 0, st>>>(n, ns, U, nr.p, 1);
+      launch_fused<1, T>(n, BNorm<T>{U + (size_t)n * j}, TNormAt<Wt>{nr.as<double>() + j}, A.red, nullptr, st);
+    const T* vlast = W.as<T>() + (size_t)(k % ring) * n;
+    launch_fused<1, T>(n, BNorm<T>{vlast}, TNormAt<Wt>{nr.as<double>() + ns}, A.red, nullptr, st);
+    k_div_cols<T><<<stream_grid(n * ns), kThreads, 0, st>>>(n, ns, U, nr.as<double>());
     IDRS_LAUNCH_CHECK();
     std::vector<double> h(ns + 1);
     IDRS_CUDA(cudaMemcpyAsync(h.data(), nr.p, sizeof(double) * (ns + 1), cudaMemcpyDeviceToHost, st));
     IDRS_CUDA(cudaStreamSynchronize(st));
-    const double hl = std::fabs(H[nritz + (size_t)ldh * (nritz - 1)]);
+    const double hl = mag(H[nritz + (size_t)ldh * (nritz - 1)]);
     for (int j = 0; j < ns; ++j)
-      resnrm[j] = h[ns] * hl * std::fabs(eigvec[(nritz - 1) + (size_t)nritz * j]) / h[j];
+      resnrm[j] = h[ns] * hl * mag(eigvec[(nritz - 1) + (size_t)nritz * j]) / h[j];
   }
 }
 
-int global_qr(long n, int s, double* Q, double* R, RedBuf rb, cudaStream_t st) {
-  DevVec dR((size_t)s * s, st);
-  IDRS_CUDA(cudaMemsetAsync(dR.p, 0, sizeof(double) * s * s, st));
+template <class T>
+int global_qr(long n, int s, T* Q, T* R, RedBuf rb, cudaStream_t st) {
+  using Wt = typename traits<T>::wide;
+  DevVec dR(sizeof(T) * s * s, st);
+  IDRS_CUDA(cudaMemsetAsync(dR.p, 0, sizeof(T) * s * s, st));
   for (int j = 0; j < s; ++j) {
-    double* Rj = dR.p + (size_t)s * j;
+    T* Rj = dR.as<T>() + (size_t)s * j;
     for (int i = 0; i <= j; ++i)
-      launch_fused<1, double>(n, BMgsPass{Q, n, i, j, Rj}, TSqrtAt<double>{Rj + i, i == j}, rb,
-                              nullptr, st);
-    k_mgs_scale<<<stream_grid(n), kThreads, 0, st>>>(n, Q + (size_t)n * j, Rj + j);
+      launch_fused<1, T>(n, BMgsPass<T>{Q, n, i, j, Rj}, TRAt<Wt>{(Wt*)(Rj + i), i == j}, rb, nullptr, st);
+    k_mgs_scale<T><<<stream_grid(n), kThreads, 0, st>>>(n, Q + (size_t)n * j, Rj + j);
     IDRS_LAUNCH_CHECK();
   }
-  std::vector<double> h((size_t)s * s);
-  IDRS_CUDA(cudaMemcpyAsync(h.data(), dR.p, sizeof(double) * s * s, cudaMemcpyDeviceToHost, st));
+  std::vector<T> h((size_t)s * s);
+  IDRS_CUDA(cudaMemcpyAsync(h.data(), dR.p, sizeof(T) * s * s, cudaMemcpyDeviceToHost, st));
   IDRS_CUDA(cudaStreamSynchronize(st));
   if (R) std::copy(h.begin(), h.end(), R);
   for (int j = 0; j < s; ++j)
-    if (!(h[j + (size_t)s * j] > DBL_MIN)) return j + 1;
+    if (!(mag(h[j + (size_t)s * j]) > DBL_MIN)) return j + 1;
   return 0;
 }
+
+template void compute_u0<double>(Operator&, Operator*, const double*, int, int, const double*, int,
+                                 const double*, double*, double*, cudaStream_t);
+template void compute_u0<c128>(Operator&, Operator*, const c128*, int, int, const c128*, int,
+                               const c128*, c128*, double*, cudaStream_t);
+template int global_qr<double>(long, int, double*, double*, RedBuf, cudaStream_t);
+template int global_qr<c128>(long, int, c128*, c128*, RedBuf, cudaStream_t);
 
 }  // namespace idrs

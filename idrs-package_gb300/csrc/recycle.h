@@ -36,14 +36,15 @@ void ritz_omega(const std::complex<double>* Hf, int ldh, int n_omega, std::compl
 // returned.  H (ldh >= nritz+1) and eigvec (nritz x ns) are host arrays;
 // b and U (n x ns, leading dimension n) are device arrays.  M: optional
 // preconditioner (the products are A (v / M)).
-void compute_u0(Operator& A, Operator* M, const double* H, int ldh, int nritz,
-                const double* eigvec, int ns, const double* b, double* U, double* resnrm,
-                cudaStream_t st);
+template <class T>
+void compute_u0(Operator& A, Operator* M, const T* H, int ldh, int nritz, const T* eigvec, int ns,
+                const T* b, T* U, double* resnrm, cudaStream_t st);
 
-// global_RQR_factorization (ritz_module.f90:66-96): modified Gram-Schmidt
-// with global inner products, in place on the device matrix Q (n x s,
-// leading dimension n).  R (host, s x s) optional.  Returns 0, or the
-// 1-based index of the first dependent column.
-int global_qr(long n, int s, double* Q, double* R, RedBuf rb, cudaStream_t st);
+// global_RQR_factorization / global_CQR_factorization (ritz_module.f90:36-96):
+// modified Gram-Schmidt with global inner products, in place on the device
+// matrix Q (n x s, leading dimension n).  R (host, s x s) optional.  Returns
+// 0, or the 1-based index of the first dependent column.
+template <class T>
+int global_qr(long n, int s, T* Q, T* R, RedBuf rb, cudaStream_t st);
 
 }  // namespace idrs

@@ -116,11 +116,18 @@ static int cqr_factorization(int m, const cd* V, int ldv, cd* Q, cd* R) {
 }
 
 // RQR_eig / CQR_eig: dense_la_module.f90:192-403 (shifted QR iteration)
-static void qr_eig_core(int n, std::vector<cd>& V, bool real_version, cd* eig, int* converged) {
+static void qr_eig_core(int n, std::vector<cd>& V, bool real_version, cd* eig, int* converged,
+                        cd* U = nullptr) {
   int iter = 0, m = n, maxit = real_version ? 100 * n : 10 * n;
   const double tol = DBL_EPSILON;
   std::vector<cd> Q((size_t)n * n), R((size_t)n * n), RQ((size_t)n * n);
   auto VV = [&](int i, int j) -> cd& { return V[i + (size_t)n * j]; };
+  std::vector<cd> UQ;
+  if (U) {  // Schur vectors: U = I, then U(:, 1:m) = U(:, 1:m) Q after every step
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) U[i + (size_t)n * j] = (i == j) ? cd(1.0) : cd(0.0);
+    UQ.resize((size_t)n * n);
+  }
   cd shift = 0.0;
   if (real_version) {
     for (int i = 0; i < m; ++i) if (std::abs(VV(i, i)) > std::abs(shift)) shift = VV(i, i);
@@ -140,6 +147,16 @@ static void qr_eig_core(int n, std::vector<cd>& V, bool real_version, cd* eig, i
     for (int j = 0; j < m; ++j)
       for (int i = 0; i < m; ++i) VV(i, j) = RQ[i + m * j];
     for (int i = 0; i < m; ++i) VV(i, i) = VV(i, i) + shift;
+    if (U) {
+      for (int j = 0; j < m; ++j)
+        for (int i = 0; i < n; ++i) {
+          cd acc = 0.0;
+          for (int q = 0; q < m; ++q) acc += U[i + (size_t)n * q] * Q[q + m * j];
+          UQ[i + (size_t)n * j] = acc;
+        }
+      for (int j = 0; j < m; ++j)
+        for (int i = 0; i < n; ++i) U[i + (size_t)n * j] = UQ[i + (size_t)n * j];
+    }
     if (std::abs(VV(m - 1, m - 2)) < tol * std::abs(VV(m - 1, m - 1))) m = m - 1;
     if (real_version) {
       shift = 0.0;
@@ -159,11 +176,11 @@ void qr_eig(const double* H, int ldh, int n, cd* eig, int* converged) {
     for (int i = 0; i < n; ++i) V[i + (size_t)n * j] = H[i + (size_t)ldh * j];
   qr_eig_core(n, V, true, eig, converged);
 }
-void qr_eig(const cd* H, int ldh, int n, cd* eig, int* converged) {
+void qr_eig(const cd* H, int ldh, int n, cd* eig, int* converged, cd* U) {
   std::vector<cd> V((size_t)n * n);
   for (int j = 0; j < n; ++j)
     for (int i = 0; i < n; ++i) V[i + (size_t)n * j] = H[i + (size_t)ldh * j];
-  qr_eig_core(n, V, false, eig, converged);
+  qr_eig_core(n, V, false, eig, converged, U);
 }
 
 // filter_ritzval: matrix_module.f90:1059-1077

@@ -15,7 +15,9 @@ int chebyshev(int degree, const std::complex<double>* foci, std::complex<double>
 std::vector<std::complex<double>> neumann_jacobi(int degree, std::complex<double> center);
 std::vector<std::complex<double>> chebyshev_jacobi(int degree, const std::complex<double>* foci);
 void qr_eig(const double* H, int ldh, int n, std::complex<double>* eig, int* converged);
-void qr_eig(const std::complex<double>* H, int ldh, int n, std::complex<double>* eig, int* converged);
+// complex: U (n x n, optional) receives the Schur vectors (CQR_eig's U)
+void qr_eig(const std::complex<double>* H, int ldh, int n, std::complex<double>* eig, int* converged,
+            std::complex<double>* U = nullptr);
 void analyse_spectrum(const double* H, int ldh, int n, double* foci, double* center, double* shift);
 void analyse_spectrum(const std::complex<double>* H, int ldh, int n, std::complex<double>* foci,
                       std::complex<double>* center, std::complex<double>* shift);

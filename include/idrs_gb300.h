@@ -351,6 +351,14 @@ int idrs_ridrs_ritz(idrs_matrix A, const double *b, int s, idrs_matrix M,
                     int *flag, double *relres, int *iterations, const double *x0, double *U0,
                     int dimU0, double *omega, int n_omega, double *resvec, int resvec_len,
                     double *H, int ldh, int nh, int *nritz, double *x);
+/* CIDRS_RITZ (ritz_module.f90:268-387): the same for a complex A (b, x, x0,
+ * U0, omega and H interleaved).  omega = 1/ritz ordered greedily with the
+ * complex Ritz values; U0 from the first dimU0 Schur vectors of QR_eig. */
+int idrs_cidrs_ritz(idrs_matrix A, const double *b, int s, idrs_matrix M,
+                    const double *tolerance, const int *maximum_iterations, const int *variant,
+                    int *flag, double *relres, int *iterations, const double *x0, double *U0,
+                    int dimU0, double *omega, int n_omega, double *resvec, int resvec_len,
+                    double *H, int ldh, int nh, int *nritz, double *x);
 
 /* ---------------------------------------------------------------------- */
 /* pp_idrs: M/PP_IDRS/pp_idrs_module.f90:118-162 (RPP_IDRS) with            */
@@ -403,7 +411,7 @@ int idrs_rpp_idrs(idrs_user_matrix K, const double *b, idrs_user_matrix P, const
 
 /* pp_idrs with every optional input: RPP_IDRS / CPP_IDRS (pp_idrs_module.f90:
  * 64-162; complex: center 2 and foci 4 doubles, b and x interleaved).  The
- * complex pipelines compute the Ritz omegas; the recycle space is real only. */
+ * complex pipelines compute the Ritz omegas and the recycle space like CIDRS_RITZ. */
 int idrs_rpp_idrs_ext(idrs_user_matrix K, const double *b, idrs_user_matrix P, const double *center,
                       const double *foci, const idrs_pp_inputs *in, const idrs_pp_options *opt,
                       idrs_pp_report *report, double *x);

@@ -656,10 +656,21 @@ static int cqr_factorization(int m, or_cplx *V, int ldv, or_cplx *Q, or_cplx *R)
   return 0;
 }
 
+static int qr_eig_core_u(int n, or_cplx *V, int real_version, or_cplx *eig, int *converged,
+                         or_cplx *U);
 static int qr_eig_core(int n, or_cplx *V, int real_version, or_cplx *eig, int *converged) {
+  return qr_eig_core_u(n, V, real_version, eig, converged, NULL);
+}
+/* U (optional): Schur vectors, U = I then U(:,1:m) = U(:,1:m) Q after each step
+ * (CQR_eig, dense_la_module.f90:222-260) */
+static int qr_eig_core_u(int n, or_cplx *V, int real_version, or_cplx *eig, int *converged,
+                         or_cplx *U) {
   int iter = 0, m = n, maxit = real_version ? 100 * n : 10 * n;
   const double tol = DBL_EPSILON;
   or_cplx shift = 0;
+  if (U)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) U[i + n * j] = (i == j) ? 1 : 0;
   or_cplx *Q = malloc(sizeof(or_cplx) * n * n), *R = malloc(sizeof(or_cplx) * n * n),
           *RQ = malloc(sizeof(or_cplx) * n * n);
 #define VV(i, j) V[(i) + n * (j)]
@@ -682,6 +693,17 @@ static int qr_eig_core(int n, or_cplx *V, int real_version, or_cplx *eig, int *c
     for (int j = 0; j < m; ++j)
       for (int i = 0; i < m; ++i) VV(i, j) = RQ[i + m * j];
     for (int i = 0; i < m; ++i) VV(i, i) = VV(i, i) + shift;
+    if (U) {
+      or_cplx *UQ = malloc(sizeof(or_cplx) * n * m);
+      for (int j = 0; j < m; ++j)
+        for (int i = 0; i < n; ++i) {
+          or_cplx acc = 0;
+          for (int q = 0; q < m; ++q) acc += U[i + n * q] * Q[q + m * j];
+          UQ[i + n * j] = acc;
+        }
+      memcpy(U, UQ, sizeof(or_cplx) * n * m);
+      free(UQ);
+    }
     if (cabs(VV(m - 1, m - 2)) < tol * cabs(VV(m - 1, m - 1))) m = m - 1;
     if (real_version) {
       shift = 0;
@@ -1107,6 +1129,165 @@ int or_ritz_omega(const double *Hf, int ldh, int n_omega, double *omega) {
   }
   free(rv); free(p);
   return OR_OK;
+}
+
+/* complex versions: CIDRS_RITZ's omega (ritz_module.f90:335-358, 1/ritz,
+ * complex p), ccompute_U0 (:162-223), global_CQR_factorization (:36-64) */
+int or_ritz_omega_c(const or_cplx *Hf, int ldh, int n_omega, or_cplx *omega) {
+  if (n_omega < 1) return OR_EARG;
+  or_cplx *rv = malloc(sizeof(or_cplx) * n_omega), *p = malloc(sizeof(or_cplx) * n_omega);
+  int converged = 0;
+  or_cqr_eig(Hf, ldh, n_omega, rv, &converged);
+  for (int i = 0; i < n_omega; ++i) {
+    or_cplx w = rv[i];
+    if (cabs(w) < DBL_EPSILON) w = 1.;
+    omega[i] = 1. / w;
+    p[i] = 1.;
+  }
+  for (int i = 0; i < n_omega; ++i) {
+    int mp = i;
+    for (int k = i + 1; k < n_omega; ++k)
+      if (cabs(p[k]) > cabs(p[mp])) mp = k;
+    or_cplx mo = omega[mp];
+    omega[mp] = omega[i];
+    omega[i] = mo;
+    for (int k = 0; k < n_omega; ++k) p[k] = p[k] * (1. - rv[k] * omega[i]);
+  }
+  free(rv); free(p);
+  return OR_OK;
+}
+
+int or_ccompute_U0(const or_mat *A, const or_mat *M, int n, const or_cplx *H, int ldh, int nritz,
+                   const or_cplx *eigvec, int ns, const or_cplx *b, or_cplx *U0, double *resnrm) {
+  const int s = ns;
+  or_cplx *W = calloc((size_t)n * (s + 1), sizeof(or_cplx)), *v = malloc(sizeof(or_cplx) * n),
+          *t = malloc(sizeof(or_cplx) * n), *u = malloc(sizeof(or_cplx) * n);
+  int *ind = calloc(nritz + 1, sizeof(int));
+  for (long q = 0; q < (long)n * s; ++q) U0[q] = 0;
+  memcpy(v, b, sizeof(or_cplx) * n);
+  int k = 0;
+  for (int i = 1; i <= nritz; ++i) {
+    k = k + 1;
+    if (k > s + 1) k = 1;
+    ind[i] = k;
+    memcpy(W + (size_t)n * (k - 1), v, sizeof(or_cplx) * n);
+    for (int j = 0; j < s; ++j) {
+      or_cplx e = eigvec[(i - 1) + (size_t)nritz * j];
+      or_cplx *uj = U0 + (size_t)n * j;
+      for (int q = 0; q < n; ++q) uj[q] = uj[q] + e * v[q];
+    }
+    int low = i - s > 1 ? i - s : 1;
+    if (M) {
+      or_precon_c(M, n, v, u);
+      or_matvec_c(A, n, u, t);
+    } else {
+      or_matvec_c(A, n, v, t);
+    }
+    or_cplx hd = H[i + (size_t)ldh * (i - 1)];
+    for (int q = 0; q < n; ++q) {
+      or_cplx acc = 0;
+      for (int l = low; l <= i; ++l) acc += W[q + (size_t)n * (ind[l] - 1)] * H[(l - 1) + (size_t)ldh * (i - 1)];
+      v[q] = (t[q] - acc) / hd;
+    }
+  }
+  if (resnrm) {
+    double nv = or_norm_c(n, v);
+    for (int j = 0; j < s; ++j) {
+      or_cplx *uj = U0 + (size_t)n * j;
+      double nrm = or_norm_c(n, uj);
+      for (int q = 0; q < n; ++q) uj[q] = uj[q] / nrm;
+      resnrm[j] = nv * cabs(H[nritz + (size_t)ldh * (nritz - 1)]) *
+                  cabs(eigvec[(nritz - 1) + (size_t)nritz * j]) / nrm;
+    }
+  }
+  free(W); free(v); free(t); free(u); free(ind);
+  return OR_OK;
+}
+
+int or_cglobal_qr(int n, int s, const or_cplx *V, or_cplx *Q, or_cplx *R) {
+  if (Q != V) memcpy(Q, V, sizeof(or_cplx) * n * s);
+  or_cplx *Rl = calloc((size_t)s * s, sizeof(or_cplx));
+  int st = OR_OK;
+  for (int j = 0; j < s && st == OR_OK; ++j) {
+    or_cplx *qj = Q + (size_t)n * j;
+    for (int i = 0; i < j; ++i) {
+      const or_cplx *qi = Q + (size_t)n * i;
+      or_cplx r = 0;
+      for (int q = 0; q < n; ++q) r += conj(qi[q]) * qj[q];
+      Rl[i + s * j] = r;
+      for (int q = 0; q < n; ++q) qj[q] = qj[q] - r * qi[q];
+    }
+    Rl[j + s * j] = or_norm_c(n, qj);
+    if (cabs(Rl[j + s * j]) > DBL_MIN) {
+      for (int q = 0; q < n; ++q) qj[q] = qj[q] / Rl[j + s * j];
+    } else {
+      st = OR_EARG;
+    }
+  }
+  if (R) memcpy(R, Rl, sizeof(or_cplx) * s * s);
+  free(Rl);
+  return st;
+}
+
+/* CIDRS_RITZ (ritz_module.f90:268-387): H, omega and U0 (Schur vectors) */
+int or_idrs_ritz_cx(const or_mat *A, int n, const or_cplx *b, int s, const or_opts *o,
+                    or_cplx *x, int *nritz, or_cplx *omega, int n_omega, or_cplx *U0, int dimU0) {
+  double tol = (o && o->tolerance) ? *o->tolerance : (double)1e-6f;
+  if (tol < 0) return OR_EARG;
+  int maxit = (2 * n < 1000) ? 2 * n : 1000;
+  if (o && o->maximum_iterations) maxit = *o->maximum_iterations;
+  int method = (o && o->variant) ? *o->variant : 1;
+  or_cplx *Hf = calloc((size_t)(maxit + 1) * maxit, sizeof(or_cplx));
+  double *resnrm = calloc(maxit + 1, sizeof(double));
+  or_cplx *xs = calloc(n, sizeof(or_cplx));
+  if (o && o->x0) memcpy(xs, o->x0, sizeof(or_cplx) * n);
+  int conv = -1, iter = 0; double relnrm = 1;
+  or_opts io; memset(&io, 0, sizeof io);
+  io.M1 = o ? o->M1 : NULL;
+  io.tolerance = &tol; io.maximum_iterations = &maxit; io.variant = &method;
+  io.flag = &conv; io.relres = &relnrm; io.iterations = &iter; io.x0 = xs;
+  io.resvec = resnrm; io.resvec_len = maxit + 1;
+  io.H = Hf; io.H_rows = maxit + 1; io.H_cols = maxit;
+  io.PT = o ? o->PT : NULL; io.p_seed = o ? o->p_seed : 0;
+  int st = or_idrs_c(A, n, b, s, &io, x);
+  if (st != OR_OK) { free(Hf); free(resnrm); free(xs); return st; }
+  const int nr = (iter / (s + 1)) * s + iter % (s + 1);
+  if (nritz) *nritz = nr;
+  if (o && o->flag) *o->flag = conv;
+  if (o && o->relres) *o->relres = relnrm;
+  if (o && o->iterations) *o->iterations = iter;
+  if (o && o->H) {
+    or_cplx *H = o->H;
+    for (int j = 0; j < o->H_cols; ++j)
+      for (int i = 0; i < o->H_rows; ++i) H[i + (size_t)o->H_rows * j] = Hf[i + (size_t)(maxit + 1) * j];
+  }
+  if (omega && n_omega > 0) {
+    if (nr < n_omega) st = OR_EARG;
+    else or_ritz_omega_c(Hf, maxit + 1, n_omega, omega);
+  }
+  if (st == OR_OK && U0 && dimU0 > 0) {
+    if (nr < dimU0) st = OR_EARG;
+    else {
+      or_cplx *Vs = malloc(sizeof(or_cplx) * nr * nr), *ev = malloc(sizeof(or_cplx) * nr),
+              *V = malloc(sizeof(or_cplx) * nr * nr), *U = malloc(sizeof(or_cplx) * n * dimU0);
+      double *resval = malloc(sizeof(double) * dimU0);
+      for (int j = 0; j < nr; ++j)
+        for (int i = 0; i < nr; ++i) V[i + nr * j] = Hf[i + (size_t)(maxit + 1) * j];
+      int cv = 0;
+      qr_eig_core_u(nr, V, 0, ev, &cv, Vs);
+      const or_mat *M = o ? o->M1 : NULL;
+      or_ccompute_U0(A, M, n, Hf, maxit + 1, nr, Vs, dimU0, b, U, resval);
+      if (M)
+        for (int j = 0; j < dimU0; ++j) {
+          or_precon_c(M, n, U + (size_t)n * j, U0);
+          memcpy(U + (size_t)n * j, U0, sizeof(or_cplx) * n);
+        }
+      st = or_cglobal_qr(n, dimU0, U, U0, NULL);
+      free(Vs); free(ev); free(V); free(U); free(resval);
+    }
+  }
+  free(Hf); free(resnrm); free(xs);
+  return st;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -208,6 +208,13 @@ int or_rcompute_U0(const or_mat *A, const or_mat *M, int n, const double *H, int
                    const double *eigvec, int ns, const double *b, double *U0, double *resnrm);
 int or_rglobal_qr(int n, int s, const double *V, double *Q, double *R);
 int or_ritz_omega(const double *Hf, int ldh, int n_omega, double *omega);
+int or_ritz_omega_c(const or_cplx *Hf, int ldh, int n_omega, or_cplx *omega);
+int or_ccompute_U0(const or_mat *A, const or_mat *M, int n, const or_cplx *H, int ldh, int nritz,
+                   const or_cplx *eigvec, int ns, const or_cplx *b, or_cplx *U0, double *resnrm);
+int or_cglobal_qr(int n, int s, const or_cplx *V, or_cplx *Q, or_cplx *R);
+/* CIDRS_RITZ: complex IDRS_RITZ with H (o->H), omega and U0 (Schur vectors) */
+int or_idrs_ritz_cx(const or_mat *A, int n, const or_cplx *b, int s, const or_opts *o,
+                    or_cplx *x, int *nritz, or_cplx *omega, int n_omega, or_cplx *U0, int dimU0);
 
 /* ---- pp_idrs pipeline (real, single right-hand side) ----
  * method: 1 idrs, 2 bicgstab, 0 qmridr.  preconditioner: 0 none, 1 neumann,

@@ -602,16 +602,22 @@ def pp_mr_idrs(K: UserMatrix, b_all, *, P: UserMatrix | None = None, method=1, s
 
 
 def idrs_ritz(A: Matrix, b, s, *, n_omega=0, dimU0=0, si_seed=0, H_shape=None, **kw):
-    """IDRS_RITZ (ritz_module.f90:389-556) with its H, omega and U0 outputs."""
-    b = np.ascontiguousarray(b, dtype=np.float64)
-    o, keep, outs = _opts(len(b), np.float64, H_shape=H_shape, **kw)
+    """IDRS_RITZ (ritz_module.f90:268-556, real or complex) with its H, omega and U0 outputs."""
+    dt = np.complex128 if A.cplx else np.float64
+    b = np.ascontiguousarray(b, dtype=dt)
+    o, keep, outs = _opts(len(b), dt, H_shape=H_shape, **kw)
     x = np.empty_like(b)
     nritz = C.c_int(0)
-    om = np.zeros(max(n_omega, 1))
-    U0 = np.zeros((len(b), max(dimU0, 1)), order="F")
-    st = lib().or_idrs_ritz_rx(A.ptr, len(b), _p(b), int(s), C.byref(o), _p(x), C.byref(nritz),
-                               _p(om) if n_omega else None, int(n_omega),
-                               _p(U0) if dimU0 else None, int(dimU0), C.c_uint64(si_seed))
+    om = np.zeros(max(n_omega, 1), dtype=dt)
+    U0 = np.zeros((len(b), max(dimU0, 1)), dtype=dt, order="F")
+    if A.cplx:
+        st = lib().or_idrs_ritz_cx(A.ptr, len(b), _p(b), int(s), C.byref(o), _p(x), C.byref(nritz),
+                                   _p(om) if n_omega else None, int(n_omega),
+                                   _p(U0) if dimU0 else None, int(dimU0))
+    else:
+        st = lib().or_idrs_ritz_rx(A.ptr, len(b), _p(b), int(s), C.byref(o), _p(x), C.byref(nritz),
+                                   _p(om) if n_omega else None, int(n_omega),
+                                   _p(U0) if dimU0 else None, int(dimU0), C.c_uint64(si_seed))
     if st:
         raise ValueError(f"or_idrs_ritz status {st}")
     r = _result(x, outs)

@@ -125,3 +125,45 @@ def test_pp_mr_idrs_device_pointers(gpu, P):
     torch.cuda.synchronize()
     assert list(d.iterations) == list(h.iterations)
     np.testing.assert_array_equal(Xd.cpu().numpy().T, h.x)
+
+
+def test_complex_idrs_ritz_outputs_match_oracle(gpu, oracle, P):
+    """CIDRS_RITZ (ritz_module.f90:268-387): complex omegas and the recycle
+    space from the Schur vectors of the complex Hessenberg matrix."""
+    n, s = 8, 4
+    Kg, Ko, _, _ = _cdr(gpu, oracle, P, n)
+    seed = 1.0 + 2.0j
+    A = gpu.Matrix(Kg, seed=seed, complex=True)
+    Ao = oracle.Matrix(Ko, seed=seed, cplx=True)
+    rng = np.random.default_rng(0)
+    b = rng.standard_normal(n ** 3) + 1j * rng.standard_normal(n ** 3)
+    g = gpu.IDRS_RITZ(A, b, s, tolerance=1e-8, n_omega=6, dimU0=s, H_shape=(21, 20))
+    o = oracle.idrs_ritz(Ao, b, s, tolerance=1e-8, n_omega=6, dimU0=s, H_shape=(21, 20))
+    assert g.flag == o.flag == 0 and abs(g.iterations - o.iterations) <= 1
+    np.testing.assert_allclose(g.H, o.H, rtol=1e-9, atol=1e-9 * np.abs(o.H).max())
+    np.testing.assert_allclose(np.sort_complex(g.omega), np.sort_complex(o.omega), rtol=1e-8)
+    assert np.abs(g.U0.conj().T @ g.U0 - np.eye(s)).max() < 1e-12
+    d = g.U0 @ (g.U0.conj().T @ o.U0) - o.U0
+    assert np.linalg.norm(d) < 1e-6
+
+
+def test_complex_pp_mr_idrs_recycle(gpu, oracle, P):
+    """CPP_MR_IDRS with recycle: the recycle solve already solves rhs 1, the
+    sequence meets the tolerance, and the result matches the same steps
+    composed from the oracle."""
+    n = 8
+    _, _, Sg, So = _cdr(gpu, oracle, P, n)
+    rng = np.random.default_rng(9)
+    B = rng.standard_normal((n ** 3, 3)) + 1j * rng.standard_normal((n ** 3, 3))
+    seed = 0.5 + 1.0j
+    g = gpu.PP_MR_IDRS(Sg, B, seed=seed, s=4, tol=1e-8, recycle=True)
+    assert list(g.flags) == [0, 0, 0] and g.iterations[0] == 0
+    assert np.all(g.relres_original < 2e-8)
+    A = oracle.Matrix(So, seed=seed, cplx=True)
+    r = oracle.idrs_ritz(A, B[:, 0], 4, tolerance=1e-8, maximum_iterations=1000, dimU0=4)
+    assert abs(g.recycle_iterations - r.iterations) <= 1
+    x0 = r.x
+    for j in range(3):
+        o = oracle.idrs(A, B[:, j], 4, tolerance=1e-8, x0=x0, U0=r.U0)
+        x0 = o.x
+        np.testing.assert_allclose(g.x[:, j], o.x, rtol=0, atol=1e-6 * np.abs(o.x).max())
