@@ -12,7 +12,10 @@
 !     M/PP_MATRIX/matrix_module.f90:135-167, 306-352, 551-635, 811-849
 !     M/IDRS/idrs_module.f90:66-103, 107-408, 410-713, 787-837
 ! (IDRS package paths, M/ = IDRS/MODULES).  Beyond the reference: the adjoint
-! path (crs_transpose, idrs_backward) for gradients of a scalar loss.  Status codes of the C ABI become
+! path (crs_transpose, idrs_backward) for gradients of a scalar loss.  Also bound: mm_matrix
+! (E/MATRIX_MARKET/mm_module.f90), make_deflation / Pmul, IDRS_RITZ and the real pp_idrs
+! pipelines (single, sequence, multishift) with their options and report as bind(C)
+! types.  Status codes of the C ABI become
 ! `error stop` with the library's message, as the reference stops on illegal
 ! arguments.  Index arrays are 1-based, as in the reference.
 !
@@ -30,6 +33,8 @@ module idrs_gb300_module
    public :: operator(*), operator(/)
    public :: IDRS, QMRIDR, MSIDRS, MSQMRIDR, NORM, INPROD
    public :: crs_transpose, idrs_backward
+   public :: mm_matrix, make_deflation, Pmul, IDRS_RITZ, pp_idrs
+   public :: idrs_pp_options, idrs_pp_report
 
    type :: user_matrix
       type(c_ptr) :: h = c_null_ptr
@@ -50,6 +55,41 @@ module idrs_gb300_module
    interface IDRS
       module procedure RIDRS
    end interface
+   interface IDRS_RITZ
+      module procedure RIDRS_RITZ
+   end interface
+   interface pp_idrs
+      module procedure RPP_IDRS, RPP_MR_IDRS, RPP_MS_IDRS
+   end interface
+
+   ! Options and report of the pp_idrs pipelines (the reference reads the
+   ! options from the command line, M/PP_IDRS/initialize.inc:4-31); the members
+   ! and their order are those of the C structs idrs_pp_options / _report.
+   type, bind(C) :: idrs_pp_options
+      integer(c_int) :: method = 1, s = 4
+      real(c_double) :: tol = 1.0d-6
+      integer(c_int) :: maxit = 1000, in_s = 1, in_it = 0
+      real(c_double) :: in_tol = 0.1d0
+      integer(c_int) :: preconditioner = 0, degree = 0, n_ritz = 32, inner_precision = 64
+      integer(c_int) :: device_pointers = 0, n_omega = 0, recycle = 0
+   end type idrs_pp_options
+
+   type, bind(C) :: idrs_pp_report
+      integer(c_int) :: flag, iterations, ritz_iterations, nritz
+      real(c_double) :: relres_solver, relres_original
+      real(c_double) :: foci(2), center
+      real(c_double) :: seconds_setup, seconds_solve, seconds_total
+      integer(c_int) :: inner_solves, inner_iterations, inner_max
+      integer(c_int) :: recycle_flag, recycle_iterations
+      real(c_double) :: recycle_relres
+      real(c_double) :: foci_imag(2), center_imag
+   end type idrs_pp_report
+
+   type, bind(C) :: idrs_pp_inputs
+      type(c_ptr) :: M = c_null_ptr, C = c_null_ptr, seed = c_null_ptr, shift = c_null_ptr
+      type(c_ptr) :: V = c_null_ptr
+      integer(c_int) :: n_deflation = 0
+   end type idrs_pp_inputs
    interface QMRIDR
       module procedure RQMRIDR
    end interface
@@ -242,6 +282,97 @@ module idrs_gb300_module
          real(c_double), intent(in) :: u(*), v(*)
          real(c_double), intent(out) :: uv(2)
       end function
+      integer(c_int) function c_real_precon_ext(which, K, M, C, shift, P) &
+            bind(C, name='idrs_real_precon_ext')
+         import :: c_int, c_double, c_ptr
+         integer(c_int), value :: which
+         type(c_ptr), value :: K, M, C
+         real(c_double), intent(in), optional :: shift
+         type(c_ptr), intent(out) :: P
+      end function
+      integer(c_int) function c_matrix_create_ext(K, M, C, P, is_complex, seed, shift, &
+            multishift, A) bind(C, name='idrs_matrix_create_ext')
+         import :: c_int, c_double, c_ptr
+         type(c_ptr), value :: K, M, C, P
+         integer(c_int), value :: is_complex, multishift
+         real(c_double), intent(in), optional :: seed(*), shift(*)
+         type(c_ptr), intent(out) :: A
+      end function
+      integer(c_int) function c_mm_matrix(mm_file, which_format, A) bind(C, name='idrs_mm_matrix')
+         import :: c_int, c_char, c_ptr
+         character(kind=c_char), intent(in) :: mm_file(*), which_format(*)
+         type(c_ptr), intent(out) :: A
+      end function
+      integer(c_int) function c_mm_read(mm_file, which_format, rep, field, nrows, ncols, nnz, &
+            ptr, ind, vals) bind(C, name='idrs_mm_read')
+         import :: c_int, c_char, c_long, c_ptr
+         character(kind=c_char), intent(in) :: mm_file(*), which_format(*)
+         integer(c_int), intent(out) :: rep, field, nrows, ncols
+         integer(c_long), intent(out) :: nnz
+         type(c_ptr), value :: ptr, ind, vals
+      end function
+      integer(c_int) function c_make_deflation(A, V, k) bind(C, name='idrs_make_deflation')
+         import :: c_int, c_double, c_ptr
+         type(c_ptr), value :: A
+         real(c_double), intent(in) :: V(*)
+         integer(c_int), value :: k
+      end function
+      integer(c_int) function c_rpmul(A, v, w) bind(C, name='idrs_rpmul')
+         import :: c_int, c_double, c_ptr
+         type(c_ptr), value :: A
+         real(c_double), intent(in) :: v(*)
+         real(c_double), intent(out) :: w(*)
+      end function
+      integer(c_int) function c_ridrs_ritz(A, b, s, M, tolerance, maximum_iterations, variant, &
+            flag, relres, iterations, x0, U0, dimU0, omega, n_omega, resvec, resvec_len, H, ldh, &
+            nh, nritz, x) bind(C, name='idrs_ridrs_ritz')
+         import :: c_int, c_double, c_ptr
+         type(c_ptr), value :: A, M
+         real(c_double), intent(in) :: b(*)
+         integer(c_int), value :: s, dimU0, n_omega, resvec_len, ldh, nh
+         real(c_double), intent(in), optional :: tolerance
+         integer(c_int), intent(in), optional :: maximum_iterations, variant
+         integer(c_int), intent(out), optional :: flag, iterations, nritz
+         real(c_double), intent(out), optional :: relres
+         real(c_double), intent(in), optional :: x0(*)
+         real(c_double), intent(out), optional :: U0(*), omega(*), resvec(*), H(*)
+         real(c_double), intent(out) :: x(*)
+      end function
+      integer(c_int) function c_rpp_idrs_ext(K, b, P, center, foci, inp, opt, report, x) &
+            bind(C, name='idrs_rpp_idrs_ext')
+         import :: c_int, c_double, c_ptr, idrs_pp_options, idrs_pp_report, idrs_pp_inputs
+         type(c_ptr), value :: K, P
+         real(c_double), intent(in) :: b(*)
+         real(c_double), intent(in), optional :: center, foci(2)
+         type(idrs_pp_inputs), intent(in) :: inp
+         type(idrs_pp_options), intent(in) :: opt
+         type(idrs_pp_report), intent(out) :: report
+         real(c_double), intent(out) :: x(*)
+      end function
+      integer(c_int) function c_rpp_mr_idrs_ext(K, nrhs, b_all, P, center, foci, inp, opt, &
+            reports, x_all) bind(C, name='idrs_rpp_mr_idrs_ext')
+         import :: c_int, c_double, c_ptr, idrs_pp_options, idrs_pp_report, idrs_pp_inputs
+         type(c_ptr), value :: K, P
+         integer(c_int), value :: nrhs
+         real(c_double), intent(in) :: b_all(*)
+         real(c_double), intent(in), optional :: center, foci(2)
+         type(idrs_pp_inputs), intent(in) :: inp
+         type(idrs_pp_options), intent(in) :: opt
+         type(idrs_pp_report), intent(out) :: reports(*)
+         real(c_double), intent(out) :: x_all(*)
+      end function
+      integer(c_int) function c_rpp_ms_idrs(K, rhs, n_sigma, sigma, P, center, foci, inp, opt, &
+            report, relres, x) bind(C, name='idrs_rpp_ms_idrs')
+         import :: c_int, c_double, c_ptr, idrs_pp_options, idrs_pp_report, idrs_pp_inputs
+         type(c_ptr), value :: K, P
+         real(c_double), intent(in) :: rhs(*), sigma(*)
+         integer(c_int), value :: n_sigma
+         real(c_double), intent(in), optional :: center, foci(2)
+         type(idrs_pp_inputs), intent(in) :: inp
+         type(idrs_pp_options), intent(in) :: opt
+         type(idrs_pp_report), intent(out) :: report
+         real(c_double), intent(out) :: relres(*), x(*)
+      end function
    end interface
 
 contains
@@ -328,15 +459,43 @@ contains
       A%ncols = A%nrows
    end function stencil7_format
 
-   function real_precon(which_precon, K, shift) result(P)
+   ! REAL_PRECON(which_precon, K, M, C, shift): user_module.f90:1327-1463
+   ! (0 none, 1 diagonal, 2 dense LU, 3 band LU of K + shift C + shift^2 M)
+   function real_precon(which_precon, K, M, C, shift) result(P)
       integer, intent(in) :: which_precon
       type(user_matrix), intent(in) :: K
+      type(user_matrix), intent(in), optional :: M, C
       real(c_double), intent(in), optional :: shift
       type(user_matrix) :: P
-      call check(c_real_precon(which_precon, K%h, shift, P%h))
+      type(c_ptr) :: mh, ch
+      mh = c_null_ptr
+      ch = c_null_ptr
+      if (present(M)) mh = M%h
+      if (present(C)) ch = C%h
+      call check(c_real_precon_ext(which_precon, K%h, mh, ch, shift, P%h))
       P%nrows = K%nrows
       P%ncols = K%ncols
    end function real_precon
+
+   ! mm_matrix(mm_file, which_format): E/MATRIX_MARKET/mm_module.f90:48-154
+   function mm_matrix(mm_file, which_format) result(A)
+      character(len=*), intent(in) :: mm_file
+      character(len=3), intent(in), optional :: which_format
+      type(user_matrix) :: A
+      character(kind=c_char, len=len(mm_file)+1) :: cfile
+      character(kind=c_char, len=4) :: cfmt
+      integer(c_int) :: rep, field, nrows, ncols
+      integer(c_long) :: nnz
+      cfile = trim(mm_file) // c_null_char
+      cfmt = 'coo' // c_null_char
+      if (present(which_format)) cfmt = which_format // c_null_char
+      call check(c_mm_read(cfile, cfmt, rep, field, nrows, ncols, nnz, c_null_ptr, c_null_ptr, &
+                           c_null_ptr))
+      call check(c_mm_matrix(cfile, cfmt, A%h))
+      A%nrows = nrows
+      A%ncols = ncols
+      A%nnz = int(nnz)
+   end function mm_matrix
 
    function user_mv(K, v) result(w)
       type(user_matrix), intent(in) :: K
@@ -346,24 +505,57 @@ contains
    end function user_mv
 
    ! ---------------------------------------------------------- matrix_module
-   ! A%K = K, A%P = P, A%rseed = seed (real_matrix.inc:9-58)
-   function make_matrix(K, P, seed) result(A)
+   ! A%K = K, A%M = M, A%C = C, A%P = P, A%rseed = seed, A%rshift = shift,
+   ! A%multishift (real_matrix.inc:9-58); the block system when multishift and C
+   function make_matrix(K, P, seed, M, C, shift, multishift) result(A)
       type(user_matrix), intent(in) :: K
-      type(user_matrix), intent(in), optional :: P
-      real(c_double), intent(in), optional :: seed
+      type(user_matrix), intent(in), optional :: P, M, C
+      real(c_double), intent(in), optional :: seed, shift
+      logical, intent(in), optional :: multishift
       type(matrix) :: A
-      real(c_double) :: sd(1)
-      type(c_ptr) :: ph
+      real(c_double) :: sd(2), sh(2)
+      type(c_ptr) :: ph, mh, ch
+      integer(c_int) :: ms
       ph = c_null_ptr
+      mh = c_null_ptr
+      ch = c_null_ptr
       if (present(P)) ph = P%h
-      if (present(seed)) then
-         sd(1) = seed
-         call check(c_matrix_create(K%h, ph, 0_c_int, sd, A%h))
+      if (present(M)) mh = M%h
+      if (present(C)) ch = C%h
+      ms = 0
+      if (present(multishift)) then
+         if (multishift) ms = 1
+      end if
+      sd = 0
+      sh = 0
+      if (present(seed)) sd(1) = seed
+      if (present(shift)) sh(1) = shift
+      if (present(seed) .and. present(shift)) then
+         call check(c_matrix_create_ext(K%h, mh, ch, ph, 0_c_int, sd, sh, ms, A%h))
+      elseif (present(seed)) then
+         call check(c_matrix_create_ext(K%h, mh, ch, ph, 0_c_int, seed=sd, multishift=ms, A=A%h))
+      elseif (present(shift)) then
+         call check(c_matrix_create_ext(K%h, mh, ch, ph, 0_c_int, shift=sh, multishift=ms, A=A%h))
       else
-         call check(c_matrix_create(K%h, ph, 0_c_int, A=A%h))
+         call check(c_matrix_create_ext(K%h, mh, ch, ph, 0_c_int, multishift=ms, A=A%h))
       end if
       A%n = K%nrows
+      if (ms == 1 .and. present(C)) A%n = 2 * K%nrows
    end function make_matrix
+
+   ! make_deflation(A, V) and Pmul(A, v): matrix_module.f90:1284-1418
+   subroutine make_deflation(A, V)
+      type(matrix), intent(inout) :: A
+      real(c_double), intent(in) :: V(:,:)
+      call check(c_make_deflation(A%h, V, int(size(V,2), c_int)))
+   end subroutine make_deflation
+
+   function Pmul(A, v) result(w)
+      type(matrix), intent(in) :: A
+      real(c_double), intent(in) :: v(:)
+      real(c_double) :: w(size(v))
+      call check(c_rpmul(A%h, v, w))
+   end function Pmul
 
    subroutine real_preconditioner(A, preconditioner, degree, foci, center, H)
       type(matrix), intent(inout) :: A
@@ -560,6 +752,150 @@ contains
       call check(c_radjoint(AT%h, K%h, x, dLdx, s, tolerance, maximum_iterations, flag, relres, &
            iterations, dLdb, dLdK))
    end subroutine idrs_backward
+
+   ! x = IDRS_RITZ(A, b, s, M, tolerance, maximum_iterations, variant, flag,
+   ! relres, iterations, x0, U0, omega, resvec, H): ritz_module.f90:389-556
+   function RIDRS_RITZ(A, b, s, M, tolerance, maximum_iterations, variant, flag, relres, &
+                       iterations, x0, U0, omega, resvec, H) result(x)
+      type(matrix), intent(in) :: A
+      real(c_double), intent(in) :: b(:)
+      integer, intent(in) :: s
+      type(matrix), intent(in), optional :: M
+      real(c_double), intent(in), optional :: tolerance
+      integer, intent(in), optional :: maximum_iterations, variant
+      integer, intent(out), optional :: flag, iterations
+      real(c_double), intent(out), optional :: relres
+      real(c_double), intent(in), optional :: x0(:)
+      real(c_double), allocatable, intent(inout), optional :: U0(:,:)
+      real(c_double), intent(out), optional :: omega(:), resvec(:), H(:,:)
+      real(c_double) :: x(size(b))
+      type(c_ptr) :: mh
+      integer(c_int) :: dimU0, n_omega, nres, ldh, nh, nritz
+      mh = c_null_ptr
+      if (present(M)) mh = M%h
+      dimU0 = 0
+      n_omega = 0
+      nres = 0
+      ldh = 0
+      nh = 0
+      if (present(omega)) n_omega = size(omega)
+      if (present(resvec)) nres = size(resvec)
+      if (present(H)) then
+         ldh = size(H,1)
+         nh = size(H,2)
+      end if
+      if (present(U0)) then
+         if (allocated(U0)) then
+            dimU0 = size(U0,2)
+            call check(c_ridrs_ritz(A%h, b, s, mh, tolerance, maximum_iterations, variant, flag, &
+                 relres, iterations, x0, U0, dimU0, omega, n_omega, resvec, nres, H, ldh, nh, &
+                 nritz, x))
+            return
+         end if
+      end if
+      call check(c_ridrs_ritz(A%h, b, s, mh, tolerance, maximum_iterations, variant, flag, relres, &
+           iterations, x0=x0, dimU0=dimU0, omega=omega, n_omega=n_omega, resvec=resvec, &
+           resvec_len=nres, H=H, ldh=ldh, nh=nh, nritz=nritz, x=x))
+   end function RIDRS_RITZ
+
+   ! the optional M, C, seed, shift, V of pp_idrs as the C struct
+   subroutine pp_inputs(inp, M, C, seed, shift, V, sd, sh)
+      type(idrs_pp_inputs), intent(out) :: inp
+      type(user_matrix), intent(in), optional :: M, C
+      real(c_double), intent(in), optional, target :: seed, shift
+      real(c_double), intent(in), optional, target, contiguous :: V(:,:)
+      real(c_double), intent(inout), target :: sd(2), sh(2)
+      if (present(M)) inp%M = M%h
+      if (present(C)) inp%C = C%h
+      if (present(seed)) then
+         sd(1) = seed
+         inp%seed = c_loc(sd)
+      end if
+      if (present(shift)) then
+         sh(1) = shift
+         inp%shift = c_loc(sh)
+      end if
+      if (present(V)) then
+         inp%V = c_loc(V)
+         inp%n_deflation = size(V,2)
+      end if
+   end subroutine pp_inputs
+
+   ! x = pp_idrs(K, b, opt, M, C, P, center, foci, seed, shift, V, report):
+   ! RPP_IDRS, pp_idrs_module.f90:118-162
+   function RPP_IDRS(K, b, opt, M, C, P, center, foci, seed, shift, V, report) result(x)
+      type(user_matrix), intent(in) :: K
+      real(c_double), intent(in) :: b(:)
+      type(idrs_pp_options), intent(in) :: opt
+      type(user_matrix), intent(in), optional :: M, C, P
+      real(c_double), intent(in), optional :: center, foci(2), seed, shift
+      real(c_double), intent(in), optional, target, contiguous :: V(:,:)
+      type(idrs_pp_report), intent(out), optional :: report
+      real(c_double) :: x(size(b))
+      type(idrs_pp_inputs) :: inp
+      type(idrs_pp_report) :: rep
+      real(c_double), target :: sd(2), sh(2)
+      type(c_ptr) :: ph
+      sd = 0
+      sh = 0
+      ph = c_null_ptr
+      if (present(P)) ph = P%h
+      call pp_inputs(inp, M, C, seed, shift, V, sd, sh)
+      call check(c_rpp_idrs_ext(K%h, b, ph, center, foci, inp, opt, rep, x))
+      if (present(report)) report = rep
+   end function RPP_IDRS
+
+   ! x_all = pp_idrs(K, b_all, opt, ...): RPP_MR_IDRS, pp_idrs_module.f90:222-279
+   function RPP_MR_IDRS(K, b_all, opt, M, C, P, center, foci, seed, shift, V, reports) result(x_all)
+      type(user_matrix), intent(in) :: K
+      real(c_double), intent(in) :: b_all(:,:)
+      type(idrs_pp_options), intent(in) :: opt
+      type(user_matrix), intent(in), optional :: M, C, P
+      real(c_double), intent(in), optional :: center, foci(2), seed, shift
+      real(c_double), intent(in), optional, target, contiguous :: V(:,:)
+      type(idrs_pp_report), intent(out), optional :: reports(:)
+      real(c_double) :: x_all(size(b_all,1), size(b_all,2))
+      type(idrs_pp_inputs) :: inp
+      type(idrs_pp_report) :: reps(size(b_all,2))
+      real(c_double), target :: sd(2), sh(2)
+      type(c_ptr) :: ph
+      sd = 0
+      sh = 0
+      ph = c_null_ptr
+      if (present(P)) ph = P%h
+      call pp_inputs(inp, M, C, seed, shift, V, sd, sh)
+      call check(c_rpp_mr_idrs_ext(K%h, int(size(b_all,2), c_int), b_all, ph, center, foci, inp, &
+                                   opt, reps, x_all))
+      if (present(reports)) reports = reps
+   end function RPP_MR_IDRS
+
+   ! x(:, 1:n_sigma) = pp_idrs(K, rhs, sigma, opt, ...): RPP_MS_IDRS, pp_idrs_module.f90:346-409
+   function RPP_MS_IDRS(K, rhs, sigma, opt, M, C, P, center, foci, seed, shift, V, report, &
+                        relres) result(x)
+      type(user_matrix), intent(in) :: K
+      real(c_double), intent(in) :: rhs(:), sigma(:)
+      type(idrs_pp_options), intent(in) :: opt
+      type(user_matrix), intent(in), optional :: M, C, P
+      real(c_double), intent(in), optional :: center, foci(2), seed, shift
+      real(c_double), intent(in), optional, target, contiguous :: V(:,:)
+      type(idrs_pp_report), intent(out), optional :: report
+      real(c_double), intent(out), optional :: relres(:)
+      real(c_double) :: x(size(rhs), size(sigma))
+      type(idrs_pp_inputs) :: inp
+      type(idrs_pp_report) :: rep
+      real(c_double) :: rel(size(sigma))
+      real(c_double), target :: sd(2), sh(2)
+      type(c_ptr) :: ph
+      sd = 0
+      sh = 0
+      ph = c_null_ptr
+      if (present(P)) ph = P%h
+      call pp_inputs(inp, M, C, seed, shift, V, sd, sh)
+      call check(c_rpp_ms_idrs(K%h, rhs, int(size(sigma), c_int), sigma, ph, center, foci, inp, &
+                               opt, rep, rel, x))
+      if (present(report)) report = rep
+      if (present(relres)) relres = rel
+   end function RPP_MS_IDRS
 
    function RNORM(A, w) result(nrm)
       type(matrix), intent(in) :: A
