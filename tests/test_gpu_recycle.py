@@ -152,7 +152,7 @@ def test_complex_pp_mr_idrs_recycle(gpu, oracle, P):
     sequence meets the tolerance, and the result matches the same steps
     composed from the oracle."""
     n = 8
-    _, _, Sg, So = _cdr(gpu, oracle, P, n)
+    Sg, So, _, _ = _cdr(gpu, oracle, P, n)  # CRS: a complex seed needs stored values
     rng = np.random.default_rng(9)
     B = rng.standard_normal((n ** 3, 3)) + 1j * rng.standard_normal((n ** 3, 3))
     seed = 0.5 + 1.0j
