@@ -34,7 +34,12 @@ struct unsupported_error : std::runtime_error {
 template <class F>
 int guard(F&& f) {
   try {
-    return f();
+    const int rc = f();
+    if (lu_take_fault()) {
+      set_error("band LU solve: a staged factor chunk never arrived (result set to NaN)");
+      return IDRS_ERR_CUDA;
+    }
+    return rc;
   } catch (const cuda_error& e) {
     set_error(std::string(cudaGetErrorString(e.code)) + " (" + e.where + ")");
     return e.code == cudaErrorMemoryAllocation ? IDRS_ERR_ALLOC : IDRS_ERR_CUDA;

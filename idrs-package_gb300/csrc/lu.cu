@@ -5,12 +5,28 @@
 // :2181-2336).
 //
 // Both factorisations are the reference's: no pivoting, the unit lower
-// factor below the diagonal, a zero pivot is an error.  The elimination and
-// the solves are sequential in the pivot index, so each runs as ONE block of
-// 1024 threads that walks the pivots with a barrier per step; the threads
-// share the rows (and for the factorisation the columns) of each step.  The
-// factor stays in HBM (band: n x (2 hb + 1), dense: n x n, column-major), the
-// band rows a step touches stay in L1/L2.
+// factor below the diagonal, a zero pivot is an error.  The elimination is
+// sequential in the pivot index and runs as ONE block of 1024 threads that
+// walks the pivots with a barrier per step.
+//
+// Band factor layout (n_pad = n rounded up to 32 columns, all zero-padded):
+//   L part  [0, n_pad hb)          L(k+d, k)          at (d-1) + hb k
+//   W part  [n_pad hb, 2 n_pad hb) W(k-d, k)          at n_pad hb + (d-1) + hb k
+//   D part  [2 n_pad hb, +n_pad)   1 / U(k,k)         at 2 n_pad hb + k
+// for d = 1..hb.  During the elimination the W part holds U itself and the D
+// part the diagonal; k_band_finish then stores W(i,k) = U(i,k) / U(k,k) and
+// 1 / U(k,k).  Every column a solve step reads is contiguous, and the
+// backward substitution becomes a unit upper solve plus one diagonal scaling,
+// so each step has a single FP64 FMA on its critical path (GB300 issues one
+// FP64 warp instruction per 64 cycles on an SM sub-partition; the latency is
+// the same).  The dense factor stays column-major n x n with U in place.
+//
+// The band solve (k_band_trsv) is one CTA: TMA bulk copies stage 32-column
+// chunks of the factor in shared memory (double buffered, mbarrier
+// completion), the solution window of hb + 2 chunk rows lives in shared
+// memory as separate real / imaginary planes, and for complex vectors the
+// real and imaginary halves of each row update run on different warps (two
+// FMAs each instead of four).
 #include <stdexcept>
 
 #include "matrix.cuh"
@@ -20,10 +36,34 @@ namespace idrs {
 namespace {
 
 constexpr int kLUThreads = 1024;
+constexpr size_t kTrsvSmemBudget = 200 * 1024;
+// try_wait polls before a staged chunk counts as lost (seconds of waiting)
+constexpr long kTrsvWaitPolls = 1L << 22;
+
+int* g_fault_host = nullptr;  // mapped host word: set by a solve whose copy never landed
+int* g_fault_dev = nullptr;
+
+int* fault_word() {
+  if (!g_fault_dev) {
+    IDRS_CUDA(cudaHostAlloc((void**)&g_fault_host, sizeof(int), cudaHostAllocMapped));
+    *g_fault_host = 0;
+    IDRS_CUDA(cudaHostGetDevicePointer((void**)&g_fault_dev, g_fault_host, 0));
+  }
+  return g_fault_dev;
+}
+
+__host__ __device__ inline long pad32(long n) { return (n + 31) / 32 * 32; }
 
 template <class V> __device__ __forceinline__ bool is_zero(V v);
 template <> __device__ __forceinline__ bool is_zero<double>(double v) { return v == 0.0; }
 template <> __device__ __forceinline__ bool is_zero<c128>(c128 v) { return v.x == 0.0 && v.y == 0.0; }
+
+// index of entry (i, j), |i - j| <= hb, in the band factor layout above
+__host__ __device__ __forceinline__ long band_idx(long n_pad, int hb, long i, long j) {
+  if (i == j) return 2 * n_pad * hb + i;
+  if (i > j) return (i - j - 1) + (long)hb * j;
+  return n_pad * hb + (j - i - 1) + (long)hb * j;
+}
 
 // value k of a CRS/COO user matrix as V
 template <class V>
@@ -38,10 +78,11 @@ __device__ __forceinline__ V entry(const void* val, int vals, long k) {
 template <class V>
 __global__ void k_scatter(int n, const int* __restrict__ rp, const int* __restrict__ ci,
                           const void* __restrict__ val, int vals, V coef, int hb, V* S) {
+  const long n_pad = pad32(n);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     for (int k = rp[i]; k < rp[i + 1]; ++k) {
       const long c = ci[k];
-      const long idx = hb < 0 ? i + (long)n * c : i + (long)n * (c - i + hb);
+      const long idx = hb < 0 ? i + (long)n * c : band_idx(n_pad, hb, i, c);
       S[idx] = S[idx] + coef * entry<V>(val, vals, k);
     }
 }
@@ -49,8 +90,9 @@ __global__ void k_scatter(int n, const int* __restrict__ rp, const int* __restri
 // the diagonal of S += d
 template <class V>
 __global__ void k_add_diag(int n, int hb, V d, V* S) {
+  const long n_pad = pad32(n);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const long idx = hb < 0 ? i + (long)n * i : i + (long)n * hb;
+    const long idx = hb < 0 ? i + (long)n * i : band_idx(n_pad, hb, i, i);
     S[idx] = S[idx] + d;
   }
 }
@@ -68,13 +110,12 @@ __global__ void k_axpby(long cnt, V* S, const V* X, V a, const V* Y, V b) {
 // In-place LU without pivoting.  Dense: hb = n.  For pivot k the rows
 // i in (k, min(k+hb, n-1)] get l = S(i,k)/S(k,k) (rows with S(i,k) = 0 are
 // skipped, as in the reference), then S(i, j) -= l S(k, j) for the columns
-// j in (k, k+hb].  *bad = 1-based index of a zero pivot.
+// j in (k, k+hb].  *bad = 1-based index of a zero pivot.  Consecutive
+// threads take consecutive rows of one column (contiguous in both layouts).
 template <class V>
 __global__ void __launch_bounds__(kLUThreads) k_lu_factor(long n, int hb, bool band, V* S, int* bad) {
-  auto at = [&](long i, long j) -> V& { return band ? S[i + n * (j - i + hb)] : S[i + n * j]; };
-  __shared__ int zero;
-  if (threadIdx.x == 0) zero = 0;
-  __syncthreads();
+  const long n_pad = pad32(n);
+  auto at = [&](long i, long j) -> V& { return band ? S[band_idx(n_pad, hb, i, j)] : S[i + n * j]; };
   const long last_k = band ? n - 1 : n;  // the band form never tests the last pivot
   for (long k = 0; k < last_k; ++k) {
     const V p = at(k, k);
@@ -90,28 +131,40 @@ __global__ void __launch_bounds__(kLUThreads) k_lu_factor(long n, int hb, bool b
     __syncthreads();
     const long rows = last - k, cols = last - k;
     for (long q = threadIdx.x; q < rows * cols; q += blockDim.x) {
-      const long i = k + 1 + q / cols, j = k + 1 + q % cols;
+      const long i = k + 1 + q % rows, j = k + 1 + q / rows;
       const V l = at(i, k);
       if (!is_zero(l)) at(i, j) = at(i, j) - l * at(k, j);
     }
     __syncthreads();
   }
-  (void)zero;
 }
 
-// x = U^-1 L^-1 b (unit lower L), column-oriented like the reference
+// W(i,k) = U(i,k) / U(k,k) and D(k) = 1 / U(k,k), one thread per column
+template <class V>
+__global__ void k_band_finish(long n, int hb, V* S) {
+  const long n_pad = pad32(n);
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += gridDim.x * (long)blockDim.x) {
+    V* d = S + band_idx(n_pad, hb, k, k);
+    const V u = *d;
+    V* w = S + n_pad * hb + (long)hb * k;
+    for (int q = 0; q < hb && q < k; ++q) w[q] = w[q] / u;
+    *d = narrow<V>(c128(1.0, 0.0)) / u;
+  }
+}
+
+// x = U^-1 L^-1 b (unit lower L) for the DENSE factor, column-oriented like
+// the reference (U on the diagonal, divisions as in LU_solve)
 template <class V, class T>
-__global__ void __launch_bounds__(kLUThreads) k_lu_solve(long n, int hb, bool band, const V* __restrict__ S,
-                                                         const T* b, T* x, const int* __restrict__ skip) {
+__global__ void __launch_bounds__(kLUThreads) k_lu_solve(long n, const V* __restrict__ S, const T* b, T* x,
+                                                         const int* __restrict__ skip) {
   if (skip && *(volatile const int*)skip) return;
-  auto at = [&](long i, long j) -> V { return band ? S[i + n * (j - i + hb)] : S[i + n * j]; };
+  auto at = [&](long i, long j) -> V { return S[i + n * j]; };
   if (x != b)
     for (long i = threadIdx.x; i < n; i += blockDim.x) x[i] = b[i];
   __syncthreads();
   for (long k = 0; k < n; ++k) {
     const T xp = x[k];
-    const long up = k + hb < n - 1 ? k + hb : n - 1;
-    for (long i = k + 1 + threadIdx.x; i <= up; i += blockDim.x) x[i] = x[i] - xp * narrow<T>(widen(at(i, k)));
+    for (long i = k + 1 + threadIdx.x; i < n; i += blockDim.x) x[i] = x[i] - xp * narrow<T>(widen(at(i, k)));
     __syncthreads();
   }
   for (long k = n - 1; k >= 0; --k) {
@@ -122,18 +175,317 @@ __global__ void __launch_bounds__(kLUThreads) k_lu_solve(long n, int hb, bool ba
     }
     __syncthreads();
     const T xp = xk;
-    const long low = k - hb > 0 ? k - hb : 0;
-    for (long i = k - 1 - threadIdx.x; i >= low; i -= blockDim.x) x[i] = x[i] - xp * narrow<T>(widen(at(i, k)));
+    for (long i = k - 1 - threadIdx.x; i >= 0; i -= blockDim.x) x[i] = x[i] - xp * narrow<T>(widen(at(i, k)));
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------
+// band solves
+// ---------------------------------------------------------------------------
+// y -= f p as FMAs on the real (part 0) or imaginary (part 1) plane; both
+// band kernels use exactly these operations, so their results are identical
+// (the operands are selected, not the results: one FMA chain per plane)
+__device__ __forceinline__ double band_upd(int part, double f, double y, double pr, double pi) {
+  return fma(-f, part ? pi : pr, y);
+}
+__device__ __forceinline__ double band_upd(int part, c128 f, double y, double pr, double pi) {
+  const double a = part ? pi : pr, c = part ? pr : pi, g = part ? -f.y : f.y;
+  return fma(g, c, fma(-f.x, a, y));
+}
+// (re, im) * d
+__device__ __forceinline__ void band_scale(double& re, double& im, double d) { re *= d; im *= d; }
+__device__ __forceinline__ void band_scale(double& re, double& im, c128 d) {
+  const double r = re * d.x - im * d.y;
+  im = re * d.y + im * d.x;
+  re = r;
+}
+template <class T> __device__ __forceinline__ void split(T v, double& re, double& im) {
+  const c128 w = c128(widen(v));
+  re = w.x;
+  im = w.y;
+}
+template <class T> __device__ __forceinline__ T join(double re, double im) {
+  if constexpr (traits<T>::is_cplx) return T(re, im);
+  else return T(re);
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, unsigned parity) {
+  for (long it = 0; it < kTrsvWaitPolls; ++it)
+    if (mbar_try_wait(b, parity)) return true;
+  return false;
+}
+// bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(b))
+               : "memory");
+}
+
+// Band solve x = D (W^-1 (L^-1 b)), one CTA of parts x rw threads (parts = 2
+// for complex vectors, rw = hb rounded up to a warp).  Thread (part, r)
+// updates row k+1+r (forward) or k-1-r (backward) of step k.  The 2 nc
+// chunks of cc factor columns (forward L chunks 0..nc-1, then backward W
+// chunks nc-1..0) stream through two shared buffers; chunk g uses buffer and
+// mbarrier g & 1 with phase parity (g >> 1) & 1.  Rows enter the ws-slot
+// window (slot = row & (ws-1), ws >= hb + 2 cc) a chunk ahead of their first
+// update and leave it a chunk after they are final, written to x (forward: y;
+// backward: D y).  A chunk whose copy has not landed after kTrsvWaitPolls
+// polls sets *fault and the solve returns NaN.
+template <class V, class T>
+__global__ void __launch_bounds__(kLUThreads) k_band_trsv(long n, int hb, int cc, int ws, const V* __restrict__ F,
+                                                          const T* b, T* x, const int* __restrict__ skip,
+                                                          int* fault) {
+  if (skip && *(volatile const int*)skip) return;
+  constexpr bool TC = traits<T>::is_cplx;
+  extern __shared__ __align__(128) unsigned char sm[];
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm);
+  volatile int* sflag = reinterpret_cast<volatile int*>(sm + 16);
+  const long chunk = (long)cc * hb;
+  V* Fs = reinterpret_cast<V*>(sm + 32);
+  double* yr = reinterpret_cast<double*>(sm + 32 + 2 * chunk * sizeof(V));
+  double* yi = yr + ws;
+  const long m = ws - 1;
+  const int nt = blockDim.x, tid = threadIdx.x;
+  const int rw = TC ? nt / 2 : nt;
+  const int part = tid / rw, r = tid - part * rw;
+  const long n_pad = pad32(n);
+  const long nc = (n + cc - 1) / cc;
+  const V* Wg = F + n_pad * hb;
+  const V* dinv = F + 2 * n_pad * hb;
+  const unsigned bytes = (unsigned)(chunk * sizeof(V));
+  auto src = [&](long g) { return g < nc ? F + g * chunk : Wg + (2 * nc - 1 - g) * chunk; };
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    *sflag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_expect_tx(&mbar[0], bytes);
+    bulk_g2s(Fs, src(0), bytes, &mbar[0]);
+  }
+  __syncthreads();
+  // thread 0: wait for chunk g, then start chunk g + 1 in the other buffer
+  // (free: its last reader finished before the barrier that ended chunk g - 1)
+  auto stage = [&](long g) {
+    if (tid == 0) {
+      if (!mbar_wait_bounded(&mbar[g & 1], (g >> 1) & 1)) {
+        *sflag = 1;
+      } else if (g + 1 < 2 * nc) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&mbar[(g + 1) & 1], bytes);
+        bulk_g2s(Fs + ((g + 1) & 1) * chunk, src(g + 1), bytes, &mbar[(g + 1) & 1]);
+      }
+    }
+  };
+  auto load = [&](const T* v, long i) {
+    double re, im;
+    split(v[i], re, im);
+    yr[i & m] = re;
+    if (TC) yi[i & m] = im;
+  };
+  long g = 0;
+  // forward: y = L^-1 b
+  long hi = 0, wr = 0;
+  for (long c = 0; c < nc; ++c, ++g) {
+    const long k0 = c * cc;
+    stage(g);
+    for (long i = wr + tid; i < k0; i += nt) x[i] = join<T>(yr[i & m], TC ? yi[i & m] : 0.0);
+    wr = k0;
+    const long nh = min(n, k0 + cc + hb);
+    for (long i = hi + tid; i < nh; i += nt) load(b, i);
+    hi = nh;
+    __syncthreads();
+    if (*sflag) break;
+    if (tid) mbar_wait_bounded(&mbar[g & 1], (g >> 1) & 1);  // completed: acquires the chunk
+    const V* Fc = Fs + (g & 1) * chunk;
+    const long kend = min(k0 + cc, n - 1);
+    V fn = r < hb ? Fc[r] : V(0.0);
+    for (long k = k0; k < kend; ++k) {
+      const V f = fn;
+      if (r < hb && k + 1 < k0 + cc) fn = Fc[(k + 1 - k0) * hb + r];
+      const long i = k + 1 + r;
+      if (r < hb && i < n) {
+        double* y = part ? yi : yr;
+        y[i & m] = band_upd(part, f, y[i & m], yr[k & m], TC ? yi[k & m] : 0.0);
+      }
+      __syncthreads();
+    }
+  }
+  if (!*sflag) {
+    for (long i = wr + tid; i < n; i += nt) x[i] = join<T>(yr[i & m], TC ? yi[i & m] : 0.0);
+    __syncthreads();
+    // backward: x = D W^-1 y
+    long lo = n, wl = n;
+    for (long c = nc - 1; c >= 0; --c, ++g) {
+      const long k0 = c * cc, top = min(n, k0 + cc) - 1;
+      stage(g);
+      for (long i = top + 1 + tid; i < wl; i += nt) {
+        double re = yr[i & m], im = TC ? yi[i & m] : 0.0;
+        band_scale(re, im, dinv[i]);
+        x[i] = join<T>(re, im);
+      }
+      wl = top + 1;
+      const long nl = max(0L, k0 - hb);
+      for (long i = nl + tid; i < lo; i += nt) load(x, i);
+      lo = nl;
+      __syncthreads();
+      if (*sflag) break;
+      if (tid) mbar_wait_bounded(&mbar[g & 1], (g >> 1) & 1);
+      const V* Fc = Fs + (g & 1) * chunk;
+      const long kend = max(k0, 1L);
+      V fn = r < hb ? Fc[(top - k0) * hb + r] : V(0.0);
+      for (long k = top; k >= kend; --k) {
+        const V f = fn;
+        if (r < hb && k - 1 >= k0) fn = Fc[(k - 1 - k0) * hb + r];
+        const long i = k - 1 - r;
+        if (r < hb && i >= 0) {
+          double* y = part ? yi : yr;
+          y[i & m] = band_upd(part, f, y[i & m], yr[k & m], TC ? yi[k & m] : 0.0);
+        }
+        __syncthreads();
+      }
+    }
+    if (!*sflag)
+      for (long i = tid; i < wl; i += nt) {
+        double re = yr[i & m], im = TC ? yi[i & m] : 0.0;
+        band_scale(re, im, dinv[i]);
+        x[i] = join<T>(re, im);
+      }
+  }
+  if (*sflag) {
+    // the lost copy may still land: wait once more (bounded), then report
+    if (tid == 0) {
+      mbar_wait_bounded(&mbar[g & 1], (g >> 1) & 1);
+      *(volatile int*)fault = 1;
+    }
+    for (long i = tid; i < n; i += nt) x[i] = join<T>(nan(""), TC ? nan("") : 0.0);
+  }
+}
+
+// The same solve for bands too wide to stage: the solution in HBM, every
+// step's column read directly, the identical FMAs per element.
+template <class V, class T>
+__global__ void __launch_bounds__(kLUThreads) k_band_trsv_g(long n, int hb, const V* __restrict__ F, const T* b,
+                                                            T* x, const int* __restrict__ skip) {
+  if (skip && *(volatile const int*)skip) return;
+  constexpr bool TC = traits<T>::is_cplx;
+  const long n_pad = pad32(n);
+  const V* Wg = F + n_pad * hb;
+  const V* dinv = F + 2 * n_pad * hb;
+  if (x != b)
+    for (long i = threadIdx.x; i < n; i += blockDim.x) x[i] = b[i];
+  __syncthreads();
+  auto step = [&](long k, long i, const V f) {
+    double pr, pi, yr, yi;
+    split(x[k], pr, pi);
+    split(x[i], yr, yi);
+    yr = band_upd(0, f, yr, pr, pi);
+    if (TC) yi = band_upd(1, f, yi, pr, pi);
+    x[i] = join<T>(yr, yi);
+  };
+  for (long k = 0; k + 1 < n; ++k) {
+    for (long r = threadIdx.x; r < hb && k + 1 + r < n; r += blockDim.x) step(k, k + 1 + r, F[(long)hb * k + r]);
+    __syncthreads();
+  }
+  for (long k = n - 1; k >= 1; --k) {
+    for (long r = threadIdx.x; r < hb && k - 1 - r >= 0; r += blockDim.x) step(k, k - 1 - r, Wg[(long)hb * k + r]);
+    __syncthreads();
+  }
+  for (long i = threadIdx.x; i < n; i += blockDim.x) {
+    double re, im;
+    split(x[i], re, im);
+    band_scale(re, im, dinv[i]);
+    x[i] = join<T>(re, im);
+  }
+}
+
+// x = D b (half band 0)
+template <class V, class T>
+__global__ void k_band_diag(long n, const V* __restrict__ dinv, const T* b, T* x, const int* __restrict__ skip) {
+  if (skip && *(volatile const int*)skip) return;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x) {
+    double re, im;
+    split(b[i], re, im);
+    band_scale(re, im, dinv[i]);
+    x[i] = join<T>(re, im);
+  }
+}
+
+struct TrsvShape {
+  int threads = 0, cc = 0, ws = 0;
+  size_t smem = 0;
+};
+
+// the staged kernel's launch shape, or threads = 0 when the band is too wide
+template <class V, class T>
+TrsvShape trsv_shape(int hb) {
+  TrsvShape s;
+  const int parts = traits<T>::is_cplx ? 2 : 1;
+  const int rw = (hb + 31) / 32 * 32;
+  if (hb <= 0 || rw * parts > kLUThreads) return s;
+  for (int cc : {32, 16, 8}) {
+    int ws = 1;
+    while (ws < hb + 2 * cc + 1) ws *= 2;
+    const size_t smem = 32 + 2 * (size_t)cc * hb * sizeof(V) + (size_t)parts * ws * sizeof(double);
+    if (smem <= kTrsvSmemBudget) {
+      s.threads = rw * parts;
+      s.cc = cc;
+      s.ws = ws;
+      s.smem = smem;
+      return s;
+    }
+  }
+  return s;
+}
+
+template <class V, class T>
+void band_solve(const UserMatrix& P, const T* b, T* x, const int* skip, cudaStream_t st) {
+  const long n = P.nrows;
+  const int hb = P.half_band;
+  const V* F = (const V*)P.band;
+  if (n == 0) return;
+  if (hb == 0) {
+    k_band_diag<V, T><<<stream_grid(n), kThreads, 0, st>>>(n, F, b, x, skip);
+    IDRS_LAUNCH_CHECK();
+    return;
+  }
+  const TrsvShape s = trsv_shape<V, T>(hb);
+  if (s.threads) {
+    static bool attr = false;
+    if (!attr) {
+      IDRS_CUDA(cudaFuncSetAttribute(k_band_trsv<V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kTrsvSmemBudget));
+      attr = true;
+    }
+    k_band_trsv<V, T><<<1, s.threads, s.smem, st>>>(n, hb, s.cc, s.ws, F, b, x, skip, fault_word());
+  } else {
+    k_band_trsv_g<V, T><<<1, kLUThreads, 0, st>>>(n, hb, F, b, x, skip);
+  }
+  IDRS_LAUNCH_CHECK();
 }
 
 template <class V>
 void build_typed(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, bool has_shift,
                  c128 shift, bool dense, int hb, UserMatrix& P) {
   const int n = K.nrows;
-  const long w = dense ? n : 2L * hb + 1;
-  const long cnt = (long)n * w;
+  const long cnt = dense ? (long)n * n : (2L * hb + 1) * pad32(n);
   const int hbs = dense ? -1 : hb;
   V* S = nullptr;
   IDRS_CUDA(cudaMalloc((void**)&S, sizeof(V) * std::max<long>(cnt, 1)));
@@ -174,6 +526,10 @@ void build_typed(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, 
   IDRS_CUDA(cudaMemset(bad, 0, sizeof(int)));
   k_lu_factor<V><<<1, kLUThreads>>>(n, dense ? n : hb, !dense, S, bad);
   IDRS_LAUNCH_CHECK();
+  if (!dense) {
+    k_band_finish<V><<<stream_grid(n), kThreads>>>(n, hb, S);
+    IDRS_LAUNCH_CHECK();
+  }
   int h = 0;
   IDRS_CUDA(cudaMemcpy(&h, bad, sizeof(int), cudaMemcpyDeviceToHost));
   cudaFree(bad);
@@ -228,17 +584,29 @@ template <class T>
 void lu_solve(const UserMatrix& P, const T* b, T* x, const int* skip, cudaStream_t st) {
   const bool dense = P.format == FMT_DENSE;
   const long n = P.nrows;
-  const int hb = dense ? (int)n : P.half_band;
-  const void* S = dense ? P.mat : P.band;
-  if (P.vals == 2) {
-    if constexpr (traits<T>::is_cplx)
-      k_lu_solve<c128, T><<<1, kLUThreads, 0, st>>>(n, hb, !dense, (const c128*)S, b, x, skip);
-    else
-      throw std::runtime_error("shift-and-invert: complex factor in a real problem");
-  } else {
-    k_lu_solve<double, T><<<1, kLUThreads, 0, st>>>(n, hb, !dense, (const double*)S, b, x, skip);
+  if (P.vals == 2 && !traits<T>::is_cplx) throw std::runtime_error("shift-and-invert: complex factor in a real problem");
+  if (dense) {
+    if (P.vals == 2) {
+      if constexpr (traits<T>::is_cplx) k_lu_solve<c128, T><<<1, kLUThreads, 0, st>>>(n, (const c128*)P.mat, b, x, skip);
+    } else {
+      k_lu_solve<double, T><<<1, kLUThreads, 0, st>>>(n, (const double*)P.mat, b, x, skip);
+    }
+    IDRS_LAUNCH_CHECK();
+    return;
   }
-  IDRS_LAUNCH_CHECK();
+  if (P.vals == 2) {
+    if constexpr (traits<T>::is_cplx) band_solve<c128, T>(P, b, x, skip, st);
+  } else {
+    band_solve<double, T>(P, b, x, skip, st);
+  }
+}
+
+int lu_take_fault() {
+  if (!g_fault_host) return 0;
+  volatile int* w = g_fault_host;
+  const int v = *w;
+  if (v) *w = 0;
+  return v;
 }
 
 namespace {

@@ -117,7 +117,7 @@ struct UserMatrix {
   int* col_ind = nullptr;
   void* val = nullptr;     // double or c128
   int half_band = 0;
-  void* band = nullptr;    // CDS, column-major nrows x (2hb+1)
+  void* band = nullptr;    // CDS, column-major nrows x (2hb+1); band LU factor: lu.cu's layout
   void* mat = nullptr;     // dense, column-major
   int nx = 0, ny = 0, nz = 0;
   double st[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -259,6 +259,9 @@ void lu_build(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, boo
               c128 shift, int which, bool cplx, UserMatrix& P);
 template <class T>
 void lu_solve(const UserMatrix& P, const T* b, T* x, const int* skip, cudaStream_t st);
+// 1 (and clears it) when a band solve since the last call lost a staged
+// factor chunk (its copy did not complete in time; the solve returned NaN)
+int lu_take_fault();
 // w = v / A for the block system with a shift-and-invert P (n = 2 nn):
 // t1 = v2, t2 = P^-1 (v1 + C v2 + shift M v2) (M absent: + shift v2),
 // w1 = t1 - shift t2, w2 = -t2.  tmp: 2 nn scratch; w must not alias v.

@@ -129,3 +129,37 @@ def test_block_shift_and_invert_matches_oracle(gpu, oracle, P):
     for k, s in enumerate(sig):
         S = D + s * Cd + s ** 2 * Md
         assert np.linalg.norm(rhs - S @ X[:, k]) <= 1e-8 * np.linalg.norm(rhs)
+
+
+def _band_crs(pkg, n, hb, rng, cplx):
+    """random diagonally dominant band matrix (CRS, 1-based) and its dense copy"""
+    A = np.zeros((n, n), complex if cplx else float)
+    for i in range(n):
+        lo, hi = max(0, i - hb), min(n, i + hb + 1)
+        A[i, lo:hi] = rng.standard_normal(hi - lo) + (1j * rng.standard_normal(hi - lo) if cplx else 0)
+        A[i, i] += 2.0 * hb + 2.0
+    r, c = np.nonzero(A)
+    rp = np.concatenate([[1], 1 + np.cumsum(np.bincount(r, minlength=n))]).astype(np.int32)
+    kw = {"cval": A[r, c]} if cplx else {"rval": A[r, c]}
+    return A, pkg.crs_format(n, n, rp, (c + 1).astype(np.int32), **kw), (rp, (c + 1).astype(np.int32), A[r, c])
+
+
+@pytest.mark.parametrize("n,hb,cplx", [(1000, 1, False), (333, 17, True), (95, 94, False), (700, 600, False),
+                                       (700, 600, True), (2048, 64, True)])
+def test_band_lu_shapes_match_oracle(gpu, oracle, n, hb, cplx):
+    """Band LU solves across the staged kernel's shapes (chunk widths 32, 16 and
+    8, ragged last chunk, half band n - 1) and the unstaged kernel of wide
+    complex bands (600 x 2 threads > one block): GPU = oracle and A x = v."""
+    rng = np.random.default_rng(n + hb)
+    A, Kg, (rp, ci, vals) = _band_crs(gpu, n, hb, rng, cplx)
+    Ko = oracle.crs_format(n, n, rp, ci, vals)
+    if cplx:
+        Pg, Po = gpu.complex_precon(3, Kg), oracle.complex_precon(3, Ko)
+    else:
+        Pg, Po = gpu.real_precon(3, Kg), oracle.real_precon(3, Ko)
+    Ag, Ao = gpu.Matrix(Kg, P=Pg, complex=cplx), oracle.Matrix(Ko, P=Po, cplx=cplx)
+    for _ in range(2):
+        v = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0)
+        w = v / Ag
+        np.testing.assert_allclose(w, Ao.precon(v), rtol=1e-11, atol=1e-14)
+        np.testing.assert_allclose(A @ w, v, rtol=1e-10, atol=1e-12)
