@@ -226,7 +226,7 @@ def run_ours(args, rank, world, dist):
     err_exact = float(np.max(np.abs(x_mixed - 1.0)))
 
     # roofline of the dominant kernel: the fp32 Chebyshev(8) chain evaluated by
-    # its three-term recurrence, two stencil steps per pass (k_stencil7_f4x2,
+    # its three-term recurrence, two stencil steps per pass (k_stencil7_f8x2,
     # 4 launches + 1 single step per product).  Algorithmic bytes per product
     # at 4 B per value: pair (y2, y3) reads v, writes y2, y3: 12N; pairs
     # (y4, y5), (y6, y7) read y_{i-1}, y_{i-2}, v and write two: 20N each; pair
@@ -291,7 +291,7 @@ def run_ours(args, rank, world, dist):
                  "stencil_fp64_chain_ms_per_product": ms_prod64, "stencil_fp64_ms_per_launch": ms_launch64,
                  "stencil_fp64_GBps": round(bytes64 / (ms_prod64 * 1e-3) / 1e9, 1),
                  "note": "fp64 stencil is bound by GB300's FP64 pipe, not by HBM"},
-        "roofline": {"bound": "hbm", "kernel": "k_stencil7_f4x2 + k_stencil7_f4 (fp32 Chebyshev(8) recurrence product)",
+        "roofline": {"bound": "hbm", "kernel": "k_stencil7_f8x2 + k_stencil7_f4 (fp32 Chebyshev(8) recurrence product)",
                      "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                      "traffic": traffic,

@@ -14,6 +14,7 @@
 #include "idrs_gpu.cuh"
 #include "ms_gpu.cuh"
 #include "setup.h"
+#include "tma.cuh"
 
 using namespace idrs;
 
@@ -35,8 +36,8 @@ template <class F>
 int guard(F&& f) {
   try {
     const int rc = f();
-    if (lu_take_fault()) {
-      set_error("band LU solve: a staged factor chunk never arrived (result set to NaN)");
+    if (take_device_fault()) {
+      set_error("a staged (TMA) copy never arrived; the result is invalid");
       return IDRS_ERR_CUDA;
     }
     return rc;

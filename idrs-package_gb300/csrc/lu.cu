@@ -30,6 +30,7 @@
 #include <stdexcept>
 
 #include "matrix.cuh"
+#include "tma.cuh"
 
 namespace idrs {
 
@@ -37,20 +38,6 @@ namespace {
 
 constexpr int kLUThreads = 1024;
 constexpr size_t kTrsvSmemBudget = 200 * 1024;
-// try_wait polls before a staged chunk counts as lost (seconds of waiting)
-constexpr long kTrsvWaitPolls = 1L << 22;
-
-int* g_fault_host = nullptr;  // mapped host word: set by a solve whose copy never landed
-int* g_fault_dev = nullptr;
-
-int* fault_word() {
-  if (!g_fault_dev) {
-    IDRS_CUDA(cudaHostAlloc((void**)&g_fault_host, sizeof(int), cudaHostAllocMapped));
-    *g_fault_host = 0;
-    IDRS_CUDA(cudaHostGetDevicePointer((void**)&g_fault_dev, g_fault_host, 0));
-  }
-  return g_fault_dev;
-}
 
 __host__ __device__ inline long pad32(long n) { return (n + 31) / 32 * 32; }
 
@@ -210,35 +197,6 @@ template <class T> __device__ __forceinline__ T join(double re, double im) {
   else return T(re);
 }
 
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(smem_u32(b)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, unsigned parity) {
-  for (long it = 0; it < kTrsvWaitPolls; ++it)
-    if (mbar_try_wait(b, parity)) return true;
-  return false;
-}
-// bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16)
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* b) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(b))
-               : "memory");
-}
-
 // Band solve x = D (W^-1 (L^-1 b)), one CTA of parts x rw threads (parts = 2
 // for complex vectors, rw = hb rounded up to a warp).  Thread (part, r)
 // updates row k+1+r (forward) or k-1-r (backward) of step k.  The 2 nc
@@ -247,8 +205,8 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
 // mbarrier g & 1 with phase parity (g >> 1) & 1.  Rows enter the ws-slot
 // window (slot = row & (ws-1), ws >= hb + 2 cc) a chunk ahead of their first
 // update and leave it a chunk after they are final, written to x (forward: y;
-// backward: D y).  A chunk whose copy has not landed after kTrsvWaitPolls
-// polls sets *fault and the solve returns NaN.
+// backward: D y).  A chunk whose copy has not landed after kTmaWaitCycles
+// sets *fault and the solve returns NaN.
 template <class V, class T>
 __global__ void __launch_bounds__(kLUThreads) k_band_trsv(long n, int hb, int cc, int ws, const V* __restrict__ F,
                                                           const T* b, T* x, const int* __restrict__ skip,
@@ -276,7 +234,7 @@ __global__ void __launch_bounds__(kLUThreads) k_band_trsv(long n, int hb, int cc
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
     *sflag = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_init_fence();
     mbar_expect_tx(&mbar[0], bytes);
     bulk_g2s(Fs, src(0), bytes, &mbar[0]);
   }
@@ -285,10 +243,10 @@ __global__ void __launch_bounds__(kLUThreads) k_band_trsv(long n, int hb, int cc
   // (free: its last reader finished before the barrier that ended chunk g - 1)
   auto stage = [&](long g) {
     if (tid == 0) {
-      if (!mbar_wait_bounded(&mbar[g & 1], (g >> 1) & 1)) {
+      if (!mbar_wait(&mbar[g & 1], (g >> 1) & 1)) {
         *sflag = 1;
       } else if (g + 1 < 2 * nc) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        proxy_async_fence();
         mbar_expect_tx(&mbar[(g + 1) & 1], bytes);
         bulk_g2s(Fs + ((g + 1) & 1) * chunk, src(g + 1), bytes, &mbar[(g + 1) & 1]);
       }
@@ -313,7 +271,7 @@ __global__ void __launch_bounds__(kLUThreads) k_band_trsv(long n, int hb, int cc
     hi = nh;
     __syncthreads();
     if (*sflag) break;
-    if (tid) mbar_wait_bounded(&mbar[g & 1], (g >> 1) & 1);  // completed: acquires the chunk
+    if (tid) mbar_wait(&mbar[g & 1], (g >> 1) & 1);  // completed: acquires the chunk
     const V* Fc = Fs + (g & 1) * chunk;
     const long kend = min(k0 + cc, n - 1);
     V fn = r < hb ? Fc[r] : V(0.0);
@@ -347,7 +305,7 @@ __global__ void __launch_bounds__(kLUThreads) k_band_trsv(long n, int hb, int cc
       lo = nl;
       __syncthreads();
       if (*sflag) break;
-      if (tid) mbar_wait_bounded(&mbar[g & 1], (g >> 1) & 1);
+      if (tid) mbar_wait(&mbar[g & 1], (g >> 1) & 1);
       const V* Fc = Fs + (g & 1) * chunk;
       const long kend = max(k0, 1L);
       V fn = r < hb ? Fc[(top - k0) * hb + r] : V(0.0);
@@ -372,7 +330,7 @@ __global__ void __launch_bounds__(kLUThreads) k_band_trsv(long n, int hb, int cc
   if (*sflag) {
     // the lost copy may still land: wait once more (bounded), then report
     if (tid == 0) {
-      mbar_wait_bounded(&mbar[g & 1], (g >> 1) & 1);
+      mbar_wait(&mbar[g & 1], (g >> 1) & 1);
       *(volatile int*)fault = 1;
     }
     for (long i = tid; i < n; i += nt) x[i] = join<T>(nan(""), TC ? nan("") : 0.0);
@@ -474,7 +432,7 @@ void band_solve(const UserMatrix& P, const T* b, T* x, const int* skip, cudaStre
                                      (int)kTrsvSmemBudget));
       attr = true;
     }
-    k_band_trsv<V, T><<<1, s.threads, s.smem, st>>>(n, hb, s.cc, s.ws, F, b, x, skip, fault_word());
+    k_band_trsv<V, T><<<1, s.threads, s.smem, st>>>(n, hb, s.cc, s.ws, F, b, x, skip, device_fault_word());
   } else {
     k_band_trsv_g<V, T><<<1, kLUThreads, 0, st>>>(n, hb, F, b, x, skip);
   }
@@ -601,9 +559,21 @@ void lu_solve(const UserMatrix& P, const T* b, T* x, const int* skip, cudaStream
   }
 }
 
-int lu_take_fault() {
-  if (!g_fault_host) return 0;
+static int* g_fault_host = nullptr;  // mapped host word
+static int* g_fault_dev = nullptr;
+
+int* device_fault_word() {
+  if (!g_fault_dev) {
+    IDRS_CUDA(cudaHostAlloc((void**)&g_fault_host, sizeof(int), cudaHostAllocMapped));
+    *g_fault_host = 0;
+    IDRS_CUDA(cudaHostGetDevicePointer((void**)&g_fault_dev, g_fault_host, 0));
+  }
+  return g_fault_dev;
+}
+
+int take_device_fault() {
   volatile int* w = g_fault_host;
+  if (!w) return 0;
   const int v = *w;
   if (v) *w = 0;
   return v;

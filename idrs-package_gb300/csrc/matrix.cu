@@ -235,6 +235,35 @@ __global__ void __launch_bounds__(256) k_stencil7(int nx, int ny, int nz, int zc
 // per point.  Needs nx % 4 == 0 and 16-byte aligned vectors (checked by the
 // launcher).  SCALE == false form: a and the centre term are folded into the
 // coefficients.
+struct St7 {
+  float c0, cw, ce, cs, cn, cf, cb;
+};
+// one point: centre product, then the six neighbours fused in a fixed order
+// (explicit FMAs, so every fp32 stencil kernel rounds identically whatever
+// contraction the compiler would pick)
+__device__ __forceinline__ float st7_point(const St7& c, float xc, float w, float e, float s, float n, float f,
+                                           float b) {
+  float r = c.c0 * xc;
+  r = fmaf(c.cw, w, r);
+  r = fmaf(c.ce, e, r);
+  r = fmaf(c.cs, s, r);
+  r = fmaf(c.cn, n, r);
+  r = fmaf(c.cf, f, r);
+  return fmaf(c.cb, b, r);
+}
+__device__ __forceinline__ float4 st7_apply(const St7& c, float4 xm, float4 xc, float4 xp, float4 xs,
+                                            float4 xn, float left, float right) {
+  float4 r;
+  r.x = st7_point(c, xc.x, left, xc.y, xs.x, xn.x, xm.x, xp.x);
+  r.y = st7_point(c, xc.y, xc.x, xc.z, xs.y, xn.y, xm.y, xp.y);
+  r.z = st7_point(c, xc.z, xc.y, xc.w, xs.z, xn.z, xm.z, xp.z);
+  r.w = st7_point(c, xc.w, xc.z, right, xs.w, xn.w, xm.w, xp.w);
+  return r;
+}
+__device__ __forceinline__ void axpy4(float4& r, float a, float4 x) {
+  r.x = fmaf(a, x.x, r.x); r.y = fmaf(a, x.y, r.y); r.z = fmaf(a, x.z, r.z); r.w = fmaf(a, x.w, r.w);
+}
+
 constexpr int kF4Rows = 8;
 
 __device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
@@ -273,13 +302,9 @@ __global__ void __launch_bounds__(32 * kF4Rows, 4) k_stencil7_f4(
     if (lane == 0) left = (in && i0 > 0) ? __ldg(x + p - 1) : 0.f;
     if (lane == 31) right = (in && i0 + 4 < nx) ? __ldg(x + p + 4) : 0.f;
     if (in) {
-      float4 r;
-      r.x = c0 * xc.x + cw * left + ce * xc.y + cs * xs.x + cn * xn.x + cf * xm.x + cb * xp.x;
-      r.y = c0 * xc.y + cw * xc.x + ce * xc.z + cs * xs.y + cn * xn.y + cf * xm.y + cb * xp.y;
-      r.z = c0 * xc.z + cw * xc.y + ce * xc.w + cs * xs.z + cn * xn.z + cf * xm.z + cb * xp.z;
-      r.w = c0 * xc.w + cw * xc.z + ce * right + cs * xs.w + cn * xn.w + cf * xm.w + cb * xp.w;
-      if (u) { r.x += cu * uc.x; r.y += cu * uc.y; r.z += cu * uc.z; r.w += cu * uc.w; }
-      if (v) { r.x += cv * vc.x; r.y += cv * vc.y; r.z += cv * vc.z; r.w += cv * vc.w; }
+      float4 r = st7_apply(St7{c0, cw, ce, cs, cn, cf, cb}, xm, xc, xp, xs, xn, left, right);
+      if (u) axpy4(r, cu, uc);
+      if (v) axpy4(r, cv, vc);
       *reinterpret_cast<float4*>(y + p) = r;
     }
     xm = xc;
@@ -304,25 +329,10 @@ static inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; 
 // written out only when a later step reads it).  Per pair of steps it moves
 // xin, u, v, vb and the outputs once instead of twice: 5 vectors instead of 8
 // in the middle of a Chebyshev recurrence.
-struct St7 {
-  float c0, cw, ce, cs, cn, cf, cb;
-};
 constexpr int kX2Rows = 8;
 constexpr int kX2Halo = kX2Rows + 2;
 constexpr int kX2MaxNx = 256;
 
-__device__ __forceinline__ float4 st7_apply(const St7& c, float4 xm, float4 xc, float4 xp, float4 xs,
-                                            float4 xn, float left, float right) {
-  float4 r;
-  r.x = c.c0 * xc.x + c.cw * left + c.ce * xc.y + c.cs * xs.x + c.cn * xn.x + c.cf * xm.x + c.cb * xp.x;
-  r.y = c.c0 * xc.y + c.cw * xc.x + c.ce * xc.z + c.cs * xs.y + c.cn * xn.y + c.cf * xm.y + c.cb * xp.y;
-  r.z = c.c0 * xc.z + c.cw * xc.y + c.ce * xc.w + c.cs * xs.z + c.cn * xn.z + c.cf * xm.z + c.cb * xp.z;
-  r.w = c.c0 * xc.w + c.cw * xc.z + c.ce * right + c.cs * xs.w + c.cn * xn.w + c.cf * xm.w + c.cb * xp.w;
-  return r;
-}
-__device__ __forceinline__ void axpy4(float4& r, float a, float4 x) {
-  r.x += a * x.x; r.y += a * x.y; r.z += a * x.z; r.w += a * x.w;
-}
 
 __global__ void __launch_bounds__(64 * kX2Halo, 2) k_stencil7_f4x2(
     int nx, int ny, int nz, int zc, St7 ca, float cua, float cva, St7 cb, float cub, float cvb,
@@ -402,6 +412,115 @@ __global__ void __launch_bounds__(64 * kX2Halo, 2) k_stencil7_f4x2(
 }
 
 
+
+// The same two steps with eight x-points per thread: one warp spans a row of
+// nx <= 256 points (nx % 8 == 0), so the x-neighbours are shuffles with zero
+// fill at both ends (no edge loads), and every per-thread overhead (address
+// arithmetic, bounds predicates, shuffles, the barrier) is spread over twice
+// as many points.  The kernel is instruction-issue bound (ncu: 72 % issue
+// active against 29 % DRAM throughput with four points per thread), so points
+// per instruction is what sets its speed.  yA planes live in shared memory
+// as two half-planes (points 0-3 and 4-7 of every lane) so that each 16-byte
+// shared access of a warp is conflict-free.  Streams advance by one plane
+// pointer increment per iteration.
+constexpr int kX8Rows = 8;
+constexpr int kX8Halo = kX8Rows + 2;
+
+struct F8 {
+  float4 a, b;
+};
+__device__ __forceinline__ F8 ld8(const float* p) { return F8{ld4(p), ld4(p + 4)}; }
+__device__ __forceinline__ F8 zero8() { return F8{make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)}; }
+__device__ __forceinline__ void axpy8(F8& r, float a, const F8& x) { axpy4(r.a, a, x.a); axpy4(r.b, a, x.b); }
+// 7-point stencil on eight consecutive points: left / right are the x-neighbours
+// of the first / last point
+__device__ __forceinline__ F8 st7_apply8(const St7& c, const F8& xm, const F8& xc, const F8& xp, const F8& xs,
+                                         const F8& xn, float left, float right) {
+  F8 r;
+  r.a = st7_apply(c, xm.a, xc.a, xp.a, xs.a, xn.a, left, xc.b.x);
+  r.b = st7_apply(c, xm.b, xc.b, xp.b, xs.b, xn.b, xc.a.w, right);
+  return r;
+}
+
+__global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2(
+    int nx, int ny, int nz, int zc, St7 ca, float cua, float cva, St7 cb, float cub, float cvb,
+    const float* __restrict__ xin, const float* __restrict__ u, const float* __restrict__ v,
+    const float* __restrict__ vb, float* __restrict__ ya, float* __restrict__ yb,
+    const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  // [plane ring 4][row][half][lane * 4]
+  __shared__ __align__(16) float sA[4][kX8Halo][2][128];
+  const int lane = threadIdx.x, ty = threadIdx.y;
+  const int i0 = lane * 8;
+  const int j = blockIdx.x * kX8Rows - 1 + ty;
+  const int z0 = blockIdx.y * zc;
+  const int z1 = min(nz, z0 + zc);
+  const bool act = i0 < nx && j >= 0 && j < ny;
+  const bool interior = act && ty >= 1 && ty <= kX8Rows;
+  const bool has_s = act && j > 0, has_n = act && j + 1 < ny;
+  const long plane = (long)nx * ny;
+  const long roff = act ? (long)j * nx + i0 : 0;
+  auto at = [&](const float* a, int z) { return a + (long)z * plane + roff; };
+  auto atw = [&](float* a, int z) { return a + (long)z * plane + roff; };
+  auto ld = [&](const float* a, int z) -> F8 { return (a && act && z >= 0 && z < nz) ? ld8(at(a, z)) : zero8(); };
+  auto put = [&](int zp, const F8& r) {
+    float* q = &sA[(zp + 4) & 3][ty][0][lane * 4];
+    *reinterpret_cast<float4*>(q) = r.a;
+    *reinterpret_cast<float4*>(q + 128) = r.b;
+  };
+  // step A at plane zp from xm, xc, xp = xin(zp-1 .. zp+1)
+  auto stepA = [&](int zp, const F8& xm, const F8& xc, const F8& xp) {
+    F8 r = zero8();
+    if (zp >= 0 && zp < nz) {  // uniform over the block
+      const float* o = at(xin, zp);
+      const F8 xs = has_s ? ld8(o - nx) : zero8();
+      const F8 xn = has_n ? ld8(o + nx) : zero8();
+      float left = __shfl_up_sync(0xffffffffu, xc.b.w, 1);
+      float right = __shfl_down_sync(0xffffffffu, xc.a.x, 1);
+      if (lane == 0) left = 0.f;
+      if (lane == 31) right = 0.f;
+      if (act) {
+        r = st7_apply8(ca, xm, xc, xp, xs, xn, left, right);
+        if (u) axpy8(r, cua, ld8(at(u, zp)));
+        if (v) axpy8(r, cva, ld8(at(v, zp)));
+        if (ya && interior && zp >= z0 && zp < z1) {
+          float* w = atw(ya, zp);
+          *reinterpret_cast<float4*>(w) = r.a;
+          *reinterpret_cast<float4*>(w + 4) = r.b;
+        }
+      }
+    }
+    put(zp, r);
+  };
+  F8 m = ld(xin, z0 - 2), c = ld(xin, z0 - 1), p = ld(xin, z0);
+  stepA(z0 - 1, m, c, p);
+  m = c; c = p; p = ld(xin, z0 + 1);
+  stepA(z0, m, c, p);
+  for (int z = z0; z < z1; ++z) {
+    m = c; c = p; p = ld(xin, z + 2);  // m = xin(z)
+    stepA(z + 1, m, c, p);
+    __syncthreads();
+    // step B at plane z; every lane runs the shuffles (lanes past the grid hold zeros)
+    const int s0 = (z + 3) & 3, s1 = z & 3, s2 = (z + 1) & 3;  // planes z-1, z, z+1
+    auto get = [&](int s, int row) {
+      const float* q = &sA[s][row][0][lane * 4];
+      return F8{*reinterpret_cast<const float4*>(q), *reinterpret_cast<const float4*>(q + 128)};
+    };
+    const F8 bc = interior ? get(s1, ty) : zero8();
+    float bl = __shfl_up_sync(0xffffffffu, bc.b.w, 1);
+    float br = __shfl_down_sync(0xffffffffu, bc.a.x, 1);
+    if (lane == 0) bl = 0.f;
+    if (lane == 31) br = 0.f;
+    if (interior) {
+      F8 r = st7_apply8(cb, get(s0, ty), bc, get(s2, ty), get(s1, ty - 1), get(s1, ty + 1), bl, br);
+      axpy8(r, cub, m);
+      if (vb) axpy8(r, cvb, ld8(at(vb, z)));
+      float* w = atw(yb, z);
+      *reinterpret_cast<float4*>(w) = r.a;
+      *reinterpret_cast<float4*>(w + 4) = r.b;
+    }
+  }
+}
 
 // CRS, G lanes per row (G | 32).  Warp-uniform loop so the shuffles are
 // always executed by the full warp.
@@ -1002,6 +1121,15 @@ static int f4x2_resident() {
   return b;
 }
 
+static int f8x2_resident() {
+  static const int b = [] {
+    int r = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_stencil7_f8x2, 32 * kX8Halo, 0) != cudaSuccess) r = 0;
+    return r > 0 ? r : 1;
+  }();
+  return b;
+}
+
 // Can two fp32 steps share one k_stencil7_f4x2 pass?
 static bool f4x2_ok(const MatView& M, const ChainStep<float>& A, const ChainStep<float>& B) {
   if (M.format != FMT_STENCIL7 || M.nx % 4 != 0 || M.nx > kX2MaxNx) return false;
@@ -1036,8 +1164,22 @@ static void run_chain(const MatView& Ks, const std::vector<ChainStep<T>>& steps,
           if (steps[q].in == A.out || steps[q].e.u == A.out) { need = true; break; }
           if (steps[q].out == A.out) break;
         }
-        // two full waves of resident blocks (each SM holds f4x2_resident() blocks)
         const int gy = (Ks.ny + kX2Rows - 1) / kX2Rows;
+        if (Ks.nx % 8 == 0) {
+          const long target = 2L * num_sms() * f8x2_resident();
+          const long chunks = std::max(1L, std::min((long)Ks.nz, (target + gy - 1) / gy));
+          const int zc = (int)std::max(4L, ((long)Ks.nz + chunks - 1) / chunks);
+          dim3 blk(32, kX8Halo, 1);
+          dim3 grid((Ks.ny + kX8Rows - 1) / kX8Rows, (Ks.nz + zc - 1) / zc, 1);
+          k_stencil7_f8x2<<<grid, blk, 0, st>>>(
+              Ks.nx, Ks.ny, Ks.nz, zc, st7_of(Ks, A.e.a, A.e.cx), A.e.u ? A.e.cu : 0.f,
+              A.e.v ? A.e.cv : 0.f, st7_of(Ks, B.e.a, B.e.cx), B.e.u ? B.e.cu : 0.f, B.e.v ? B.e.cv : 0.f,
+              A.in, A.e.u, A.e.v, B.e.v, need ? A.out : nullptr, B.out, skip);
+          IDRS_LAUNCH_CHECK();
+          k += 2;
+          continue;
+        }
+        // two full waves of resident blocks (each SM holds f4x2_resident() blocks)
         const long target = 2L * num_sms() * f4x2_resident();
         const long chunks = std::max(1L, std::min((long)Ks.nz, (target + gy - 1) / gy));
         int zc = (int)std::max(4L, ((long)Ks.nz + chunks - 1) / chunks);

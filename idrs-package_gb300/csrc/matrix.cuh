@@ -259,9 +259,6 @@ void lu_build(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, boo
               c128 shift, int which, bool cplx, UserMatrix& P);
 template <class T>
 void lu_solve(const UserMatrix& P, const T* b, T* x, const int* skip, cudaStream_t st);
-// 1 (and clears it) when a band solve since the last call lost a staged
-// factor chunk (its copy did not complete in time; the solve returned NaN)
-int lu_take_fault();
 // w = v / A for the block system with a shift-and-invert P (n = 2 nn):
 // t1 = v2, t2 = P^-1 (v1 + C v2 + shift M v2) (M absent: + shift v2),
 // w1 = t1 - shift t2, w2 = -t2.  tmp: 2 nn scratch; w must not alias v.

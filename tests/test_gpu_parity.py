@@ -300,12 +300,14 @@ def test_mixed_precision_with_chebyshev(gpu, P):
     np.testing.assert_allclose(r.x, 1.0, atol=1e-6)
 
 
-@pytest.mark.parametrize("dims", [(12, 12, 12), (256, 3, 5), (20, 9, 33), (30, 30, 30), (260, 4, 4), (4, 1, 7)])
+@pytest.mark.parametrize("dims", [(12, 12, 12), (256, 3, 5), (20, 9, 33), (30, 30, 30), (260, 4, 4), (4, 1, 7),
+                                  (64, 7, 9), (8, 5, 3), (128, 33, 20), (16, 16, 16), (256, 17, 6)])
 @pytest.mark.parametrize("poly", ["chebyshev", "neumann"])
 def test_fp32_chain_matches_fp64(gpu, P, dims, poly):
     """The fp32 operator of the inner solves (polynomial by its recurrence,
-    two stencil steps per pass where nx % 4 == 0 and nx <= 256, single steps
-    otherwise) against the fp64 operator: agreement to fp32 accuracy."""
+    two stencil steps per pass where nx <= 256 -- eight x-points per thread
+    for nx % 8 == 0, four for nx % 4 == 0 -- single steps otherwise) against
+    the fp64 operator: agreement to fp32 accuracy."""
     nx, ny, nz = dims
     coef = P.cdr_coefficients(max(nx, ny, nz))
     K = gpu.stencil7_format(nx, ny, nz, coef)
