@@ -34,7 +34,7 @@ extern "C" {
 
 #define IDRS_OK 0
 #define IDRS_ERR_ARG 1         /* illegal argument (reference: error stop / stop) */
-#define IDRS_ERR_CUDA 2        /* CUDA runtime error */
+#define IDRS_ERR_CUDA 2        /* CUDA runtime error, or a staged (TMA) copy that never completed */
 #define IDRS_ERR_ALLOC 3       /* out of device or host memory */
 #define IDRS_ERR_STATE 4       /* handle used in the wrong state */
 #define IDRS_ERR_UNSUPPORTED 5 /* valid in the reference, not in this build */
