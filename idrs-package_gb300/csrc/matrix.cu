@@ -497,6 +497,9 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2(
   m = c; c = p; p = ld(xin, z0 + 1);
   stepA(z0, m, c, p);
   for (int z = z0; z < z1; ++z) {
+    // step B's vb row is requested before step A and the barrier, so its
+    // latency overlaps them instead of stalling every warp after the barrier
+    const F8 vbz = (vb && interior) ? ld8(at(vb, z)) : zero8();
     m = c; c = p; p = ld(xin, z + 2);  // m = xin(z)
     stepA(z + 1, m, c, p);
     __syncthreads();
@@ -514,7 +517,7 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2(
     if (interior) {
       F8 r = st7_apply8(cb, get(s0, ty), bc, get(s2, ty), get(s1, ty - 1), get(s1, ty + 1), bl, br);
       axpy8(r, cub, m);
-      if (vb) axpy8(r, cvb, ld8(at(vb, z)));
+      if (vb) axpy8(r, cvb, vbz);
       float* w = atw(yb, z);
       *reinterpret_cast<float4*>(w) = r.a;
       *reinterpret_cast<float4*>(w + 4) = r.b;
