@@ -61,7 +61,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
     objs = [obj for _, obj, _ in procs]
     tmp = LIB + ".tmp"
-    subprocess.run([nvcc, "-shared", "-o", tmp, *objs, "-lcudart"], check=True)
+    subprocess.run([nvcc, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"], check=True)
     os.replace(tmp, LIB)
     return LIB
 

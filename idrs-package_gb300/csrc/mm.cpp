@@ -12,16 +12,23 @@
 // Hermitian coordinate files are expanded entry by entry, each mirrored entry
 // right after its original (so rows keep the file's order).  Pattern files
 // get unit values.  Host code only: idrs_mm_read makes no CUDA call.
+#include <algorithm>
 #include <cctype>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <fstream>
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
+
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include "../../include/idrs_gb300.h"
 
@@ -48,32 +55,97 @@ std::string lower(std::string s) {
   return s;
 }
 
-// Fortran list-directed input also accepts D exponents
-double to_double(std::string tok) {
+bool is_ws(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r'; }
+
+// An index token as strtol reads it (0 when it holds no number, so the range
+// check rejects it).  std::from_chars is strtol's grammar without the '+' sign.
+long tok_long(const char* b, const char* e) {
+  if (e - b > 1 && *b == '+' && b[1] != '+' && b[1] != '-') ++b;
+  long v = 0;
+  const auto r = std::from_chars(b, e, v);
+  return r.ec == std::errc() ? v : 0;
+}
+
+// A value token as the reference reads it (Fortran list-directed input also
+// accepts D exponents).  std::from_chars rounds decimal input exactly like
+// strtod; tokens it does not cover (D exponents, hexadecimal, values out of
+// the double range) go through strtod itself.  False when there is no number.
+bool tok_double(const char* b, const char* e, double& v) {
+  bool slow = e - b > 100;
+  for (const char* q = b; q < e && !slow; ++q)
+    slow = *q == 'd' || *q == 'D' || *q == 'x' || *q == 'X';
+  if (!slow) {
+    const char* s = (e - b > 1 && *b == '+' && b[1] != '+' && b[1] != '-') ? b + 1 : b;
+    const auto r = std::from_chars(s, e, v);
+    if (r.ec == std::errc()) return true;
+    if (r.ec != std::errc::result_out_of_range) return false;
+  }
+  std::string tok(b, e);
   for (char& c : tok)
     if (c == 'd' || c == 'D') c = 'e';
   char* end = nullptr;
-  double v = std::strtod(tok.c_str(), &end);
-  if (end == tok.c_str()) throw std::runtime_error("mm: bad number '" + tok + "'");
-  return v;
+  v = std::strtod(tok.c_str(), &end);
+  return end != tok.c_str();
 }
 
-bool next_data_line(std::istream& in, std::string& line) {
-  while (std::getline(in, line)) {
-    size_t p = line.find_first_not_of(" \t\r");
-    if (p == std::string::npos) continue;
-    if (line[p] == '%') continue;
-    return true;
+// The whole file, read-only: mapped when the system allows it (no copy; the
+// parsing threads fault the pages in), else read into a heap buffer.
+class FileView {
+ public:
+  explicit FileView(const char* path) {
+    const int fd = ::open(path, O_RDONLY);
+    if (fd < 0) throw std::runtime_error(std::string("Error while opening matrix-market file ") + path);
+    struct stat st;
+    if (::fstat(fd, &st) == 0 && S_ISREG(st.st_mode) && st.st_size > 0) {
+      void* m = ::mmap(nullptr, (size_t)st.st_size, PROT_READ, MAP_PRIVATE, fd, 0);
+      if (m != MAP_FAILED) {
+        map_ = m;
+        size_ = (size_t)st.st_size;
+      }
+    }
+    if (!map_) {  // pipes, special files, or no mapping: read it
+      char tmp[1 << 16];
+      for (ssize_t got; (got = ::read(fd, tmp, sizeof tmp)) > 0;) heap_.insert(heap_.end(), tmp, tmp + got);
+      size_ = heap_.size();
+    }
+    ::close(fd);
   }
-  return false;
-}
+  ~FileView() {
+    if (map_) ::munmap(map_, size_);
+  }
+  FileView(const FileView&) = delete;
+  FileView& operator=(const FileView&) = delete;
+  const char* data() const { return map_ ? static_cast<const char*>(map_) : heap_.data(); }
+  size_t size() const { return size_; }
 
+ private:
+  void* map_ = nullptr;
+  size_t size_ = 0;
+  std::vector<char> heap_;
+};
+
+// The data section after the size line is a stream of whitespace-separated
+// tokens (values may be spread over lines arbitrarily: list-directed input).
+// It is cut into one chunk per host thread at whitespace, each thread counts
+// its tokens, a prefix sum gives every chunk its first token number, and the
+// threads then parse their tokens into place (token t is field t % per of
+// entry t / per).  The first error in token order is reported, as a
+// sequential read would.
 MMFile parse(const char* path) {
-  std::ifstream in(path);
-  if (!in) throw std::runtime_error(std::string("Error while opening matrix-market file ") + path);
+  const FileView file(path);
+  const char* p = file.data();
+  const char* const end = p + file.size();
+  auto getline = [&](std::string& line) -> bool {
+    if (p >= end) return false;
+    const char* q = static_cast<const char*>(std::memchr(p, '\n', (size_t)(end - p)));
+    if (!q) q = end;
+    line.assign(p, q);
+    p = q < end ? q + 1 : end;
+    return true;
+  };
   MMFile f;
   std::string line;
-  if (!std::getline(in, line)) throw std::runtime_error("mm: empty file");
+  if (!getline(line)) throw std::runtime_error("mm: empty file");
   std::istringstream banner(line);
   std::string tag, object, rep, field, symm;
   banner >> tag >> object >> rep >> field >> symm;
@@ -95,7 +167,13 @@ MMFile parse(const char* path) {
   else throw std::runtime_error("mm: unknown symmetry " + symm);
   if (f.rep == REP_ARRAY && f.field == F_PATTERN) throw std::runtime_error("mm: pattern arrays are invalid");
   if (f.symm == S_HERMITIAN && f.field != F_COMPLEX) throw std::runtime_error("mm: Hermitian needs complex");
-  if (!next_data_line(in, line)) throw std::runtime_error("mm: missing size line");
+  // size line: the first line that is neither blank nor a '%' comment
+  bool have = false;
+  while (!have && getline(line)) {
+    const size_t q = line.find_first_not_of(" \t\r");
+    have = q != std::string::npos && line[q] != '%';
+  }
+  if (!have) throw std::runtime_error("mm: missing size line");
   std::istringstream sz(line);
   long rows = -1, cols = -1, nnz = -1;
   sz >> rows >> cols;
@@ -114,31 +192,75 @@ MMFile parse(const char* path) {
   if (f.rep == REP_COORD) { f.i.resize(nnz); f.j.resize(nnz); }
   if (f.field != F_PATTERN) f.re.resize(nnz);
   if (f.field == F_COMPLEX) f.im.resize(nnz);
-  // values may be spread over lines arbitrarily (list-directed input)
-  std::string tok;
-  auto need = [&](std::string& t) {
-    if (!(in >> t)) throw std::runtime_error("mm: file ends before all entries were read");
-  };
-  for (long k = 0; k < nnz; ++k) {
-    if (f.rep == REP_COORD) {
-      need(tok); long a = std::strtol(tok.c_str(), nullptr, 10);
-      need(tok); long b = std::strtol(tok.c_str(), nullptr, 10);
-      if (a < 1 || a > rows || b < 1 || b > cols) throw std::runtime_error("mm: entry index out of range");
-      f.i[k] = (int)a;
-      f.j[k] = (int)b;
-    }
-    if (f.field == F_PATTERN) continue;
-    need(tok);
-    double re = to_double(tok);
-    if (f.field == F_COMPLEX) {
-      need(tok);
-      double im = to_double(tok);
-      f.re[k] = (double)(float)re;  // default-kind COMPLEX in mmread
-      f.im[k] = (double)(float)im;
-    } else {
-      f.re[k] = re;
-    }
+
+  const bool coord = f.rep == REP_COORD;
+  const int nval = f.field == F_PATTERN ? 0 : (f.field == F_COMPLEX ? 2 : 1);
+  const int per = (coord ? 2 : 0) + nval;
+  const long need = nnz * per;
+  const long len = end - p;
+  int nth = 1;
+  if (len >= (1L << 20)) nth = (int)std::min(64u, std::max(1u, std::thread::hardware_concurrency()));
+  std::vector<const char*> cb(nth + 1);
+  cb[0] = p;
+  cb[nth] = end;
+  for (int c = 1; c < nth; ++c) {
+    const char* q = std::max(cb[c - 1], p + len * c / nth);
+    while (q < end && !is_ws(*q)) ++q;  // chunks end at whitespace: no token is split
+    cb[c] = q;
   }
+  std::vector<long> first(nth + 1, 0);
+  std::vector<long> err_tok(nth, -1);
+  std::vector<std::string> err_msg(nth);
+  auto run = [&](auto&& body) {
+    std::vector<std::thread> th;
+    for (int c = 1; c < nth; ++c) th.emplace_back(body, c);
+    body(0);
+    for (auto& t : th) t.join();
+  };
+  run([&](int c) {  // tokens per chunk
+    long n = 0;
+    for (const char *q = cb[c], *e = cb[c + 1]; q < e;) {
+      while (q < e && is_ws(*q)) ++q;
+      if (q >= e) break;
+      ++n;
+      while (q < e && !is_ws(*q)) ++q;
+    }
+    first[c + 1] = n;
+  });
+  for (int c = 0; c < nth; ++c) first[c + 1] += first[c];
+  run([&](int c) {  // parse into place
+    long t = first[c];
+    for (const char *q = cb[c], *e = cb[c + 1]; q < e && t < need; ++t) {
+      while (q < e && is_ws(*q)) ++q;
+      if (q >= e) break;
+      const char* b = q;
+      while (q < e && !is_ws(*q)) ++q;
+      const long k = t / per;
+      const int fld = (int)(t % per);
+      if (coord && fld < 2) {
+        const long a = tok_long(b, q);
+        if (a < 1 || a > (fld == 0 ? rows : cols)) {
+          err_tok[c] = t;
+          err_msg[c] = "mm: entry index out of range";
+          return;
+        }
+        (fld == 0 ? f.i : f.j)[k] = (int)a;
+        continue;
+      }
+      double v;
+      if (!tok_double(b, q, v)) {
+        err_tok[c] = t;
+        err_msg[c] = "mm: bad number '" + std::string(b, q) + "'";
+        return;
+      }
+      const int vi = fld - (coord ? 2 : 0);
+      if (f.field == F_COMPLEX) (vi == 0 ? f.re : f.im)[k] = (double)(float)v;  // default-kind COMPLEX in mmread
+      else f.re[k] = v;
+    }
+  });
+  for (int c = 0; c < nth; ++c)  // chunks are in token order: the first error is the earliest
+    if (err_tok[c] >= 0) throw std::runtime_error(err_msg[c]);
+  if (first[nth] < need) throw std::runtime_error("mm: file ends before all entries were read");
   return f;
 }
 

@@ -152,3 +152,66 @@ def test_reference_example_files(pkg, name):
         r = pkg.mm_read(path, fmt)
         np.testing.assert_array_equal(_dense_from(r, r.field == "complex"),
                                       _scipy_dense(path, r.field == "complex"))
+
+
+def _spread(tokens, rng):
+    """tokens joined by irregular whitespace: spaces, tabs, CRLF and LF line
+    breaks anywhere (list-directed input allows values spread over lines)"""
+    seps = np.array([" ", "  ", "\t", "\n", "\r\n", " \n "])
+    pick = rng.integers(0, len(seps), size=len(tokens))
+    return "".join(t + seps[k] for t, k in zip(tokens, pick))
+
+
+def test_large_coordinate_file_parsed_in_parallel(pkg, tmp_path):
+    """A multi-megabyte file takes the multi-threaded scan (chunks cut at
+    whitespace, tokens numbered by a prefix sum): every index and value comes
+    back exactly as written, in file order."""
+    rng = np.random.default_rng(11)
+    n, k = 5000, 150000
+    i = rng.integers(1, n + 1, size=k)
+    j = rng.integers(1, n + 1, size=k)
+    v = rng.standard_normal(k) * 10.0 ** rng.integers(-5, 6, size=k)
+    toks = []
+    for a, b, x in zip(i.tolist(), j.tolist(), v.tolist()):
+        toks += [str(a), str(b), repr(x) if rng.random() < 0.9 else repr(x).replace("e", "D")]
+    p = tmp_path / "big.mtx"
+    p.write_text("%%MatrixMarket matrix coordinate real general\n% big\n" + f"{n} {n} {k}\n" + _spread(toks, rng))
+    assert p.stat().st_size > 3 << 20
+    r = pkg.mm_read(str(p), "coo")
+    np.testing.assert_array_equal(r.indx, i)
+    np.testing.assert_array_equal(r.jndx, j)
+    np.testing.assert_array_equal(r.vals, v)
+
+
+def test_large_complex_array_file_parsed_in_parallel(pkg, tmp_path):
+    rng = np.random.default_rng(12)
+    n, m = 40000, 3
+    Z = rng.standard_normal((n, m)) + 1j * rng.standard_normal((n, m))
+    toks = []
+    for z in Z.T.ravel().tolist():
+        toks += [repr(z.real), "+" + repr(z.imag) if z.imag >= 0 else repr(z.imag)]
+    p = tmp_path / "bigz.mtx"
+    p.write_text("%%MatrixMarket matrix array complex general\n" + f"{n} {m}\n" + _spread(toks, rng))
+    assert p.stat().st_size > 2 << 20
+    r = pkg.mm_read(str(p))
+    np.testing.assert_array_equal(r.vals, Z.astype(np.complex64).astype(np.complex128))
+
+
+@pytest.mark.parametrize("damage", ["bad_value", "bad_index", "truncated"])
+def test_large_file_errors_are_reported(pkg, tmp_path, damage):
+    rng = np.random.default_rng(13)
+    n, k = 3000, 120000
+    lines = [f"{a} {b} {x!r}" for a, b, x in zip(rng.integers(1, n + 1, size=k).tolist(),
+                                                   rng.integers(1, n + 1, size=k).tolist(),
+                                                   rng.standard_normal(k).tolist())]
+    if damage == "bad_value":
+        lines[k * 2 // 3] = "7 7 abc"  # no number (a numeric prefix is read, as strtod does)
+    elif damage == "bad_index":
+        lines[k // 2] = f"{n + 1} 1 1.0"
+    else:
+        lines = lines[:-5]
+    p = tmp_path / "dmg.mtx"
+    p.write_text("%%MatrixMarket matrix coordinate real general\n" + f"{n} {n} {k}\n" + "\n".join(lines) + "\n")
+    assert p.stat().st_size > 1 << 20
+    with pytest.raises(pkg.IDRSError):
+        pkg.mm_read(str(p))
