@@ -178,8 +178,8 @@ def run_ours(args, rank, world, dist):
     torch.cuda.synchronize()
 
     def solve(mode, tol, host=False):
-        if host:
-            return pkg.PP_IDRS(K, b_host.numpy(), P=D, tol=tol, **solve_kw(mode, args))
+        if host:  # pinned b in, pinned x out
+            return pkg.PP_IDRS(K, b_host.numpy(), P=D, tol=tol, x_out=x_host.numpy(), **solve_kw(mode, args))
         return pkg.PP_IDRS(K, b_dev.data_ptr(), P=D, tol=tol, x_out=x_dev.data_ptr(), **solve_kw(mode, args))
 
     # warm-up, and the solver tolerance that meets 1e-8 on the original system

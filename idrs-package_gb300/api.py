@@ -825,7 +825,9 @@ def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=Non
     are keyword arguments.
 
     b may be a numpy array (host) or an int device address; with a device b,
-    x_out must be the device address of the solution vector."""
+    x_out must be the device address of the solution vector.  With a host b,
+    x_out may be a contiguous numpy array of b's length and kind (for
+    example pinned memory) that receives the solution."""
     dev = isinstance(b, int)
     cplx = _pp_kind(K, None if dev else b, M, C_, seed, shift, complex)
     if dev:
@@ -834,7 +836,13 @@ def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=Non
         x = x_out
     else:
         b = _arr(b, cplx, K.nrows)
-        x = np.empty_like(b)
+        if x_out is None:
+            x = np.empty_like(b)
+        elif (isinstance(x_out, np.ndarray) and x_out.dtype == b.dtype and x_out.shape == b.shape
+              and x_out.flags.c_contiguous and x_out.flags.writeable):
+            x = x_out
+        else:
+            raise ValueError("x_out must be a writeable contiguous array of b's length and kind")
     o = _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
                     inner_precision, dev, n_omega, False)
     rep = PPReport()

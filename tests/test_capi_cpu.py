@@ -37,3 +37,34 @@ def test_argument_errors_without_gpu(pkg):
     assert st == pkg.api.IDRS_ERR_ARG
     assert lib.idrs_matrix_create(None, None, 0, None, C.byref(h)) == pkg.api.IDRS_ERR_ARG
     assert lib.idrs_version() >= 10000
+
+
+def test_pp_idrs_host_output_buffer(pkg, monkeypatch):
+    """PP_IDRS with a host b writes the solution into a caller's x_out (for
+    example pinned memory) and rejects an unsuitable one; a fake library
+    stands in for the device call."""
+    import types
+    import numpy as np
+    import pytest
+    api = pkg.api
+    n = 7
+    seen = {}
+
+    def fake_pp(K, pb, P, c, f, inp, o, rep, px):
+        seen["px"] = px
+        (C.c_double * n).from_address(px)[:] = [float(i) for i in range(n)]
+        return 0
+
+    fake = types.SimpleNamespace(idrs_rpp_idrs_ext=fake_pp, idrs_last_error=lambda: b"")
+    monkeypatch.setattr(api, "_lib", fake)
+    K = types.SimpleNamespace(handle=None, nrows=n, cplx=False)
+    b = np.ones(n)
+    out = np.full(n, -1.0)
+    r = api.PP_IDRS(K, b, x_out=out)
+    assert r.x is out and seen["px"] == out.ctypes.data
+    np.testing.assert_array_equal(out, np.arange(n, dtype=float))
+    r = api.PP_IDRS(K, b)  # no x_out: a fresh array
+    assert r.x is not out and seen["px"] == r.x.ctypes.data
+    for bad in (np.zeros(n + 1), np.zeros(n, dtype=np.float32), np.zeros((n, 2))[:, 0], [0.0] * n):
+        with pytest.raises(ValueError):
+            api.PP_IDRS(K, b, x_out=bad)
