@@ -125,22 +125,36 @@ class ClockSampler:
     def summary(self):
         if self.proc is None or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        rows = []
-        for line in open(self.path):
-            f = [x.strip() for x in line.split(",")]
-            if len(f) >= 9:
-                rows.append(f)
-        if not rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
-        power = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
-        loaded = [s for s, p in zip(sm, power) if p > 300] or sm
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
-        return {"sm_mhz": statistics.median(loaded) if loaded else None,
-                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(rows), "power_w_max": max(power) if power else None}
+        with open(self.path) as f:
+            return summarize_clocks(f.read().splitlines())
+
+
+def summarize_clocks(lines):
+    """Median SM clock under load (samples above 300 W, else all), maximum SM
+    clock, and the throttle reasons seen active, from `nvidia-smi
+    --query-gpu=ClockSampler.Q --format=csv,noheader,nounits` lines.  Each
+    sample is parsed as a whole, so a field reading [N/A] drops only its own
+    value."""
+    def num(x):
+        try:
+            return float(x)
+        except ValueError:
+            return None
+    rows = [[x.strip() for x in ln.split(",")] for ln in lines]
+    rows = [r for r in rows if len(r) >= 9]
+    if not rows:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+    sm = [num(r[1]) for r in rows]
+    mx = [v for v in (num(r[2]) for r in rows) if v is not None]
+    power = [num(r[3]) for r in rows]
+    loaded = [s for s, p in zip(sm, power) if s is not None and p is not None and p > 300]
+    loaded = loaded or [s for s in sm if s is not None]
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+    pw = [p for p in power if p is not None]
+    return {"sm_mhz": statistics.median(loaded) if loaded else None,
+            "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+            "samples": len(rows), "power_w_max": max(pw) if pw else None}
 
 
 # ------------------------------------------------------------------- solves

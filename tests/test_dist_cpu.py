@@ -1,4 +1,5 @@
-"""The multi-replica path of bench.py on CPU (gloo, world size 2).
+"""bench.py's host logic on CPU: the multi-replica path (gloo, world size 2)
+and the clock summary of the bench line.
 
 The solve path does not shard, so `bench.py --gpus N` runs N replicas: each
 rank solves its own copy, the ranks meet at barriers around the timed region,
@@ -85,3 +86,26 @@ def test_reference_arm_under_torchrun_prints_once():
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["steps"] == 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] == "port" and d["value"] > 0
+
+
+def test_clock_summary_parses_each_sample_whole():
+    """The bench line's clocks: median SM clock over loaded samples, the
+    maximum clock, throttle reasons seen active; an [N/A] field drops only
+    its own value (no misaligned clock/power pairs)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    lines = [
+        "0, 1965, 2070, 120.5, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "0, 2070, 2070, [N/A], 0x0, Not Active, Not Active, Not Active, Not Active",
+        "0, 2070, 2070, 790.1, 0x4, Not Active, Not Active, Not Active, Active",
+        "0, 2055, 2070, 805.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "garbage line",
+    ]
+    s = bench.summarize_clocks(lines)
+    assert s["samples"] == 4
+    assert s["sm_mhz"] == 2062.5  # median of the two samples above 300 W
+    assert s["sm_max_mhz"] == 2070.0 and s["power_w_max"] == 805.0
+    assert s["reasons"] == ["sw_power_cap"]
+    idle = bench.summarize_clocks(["0, 1200, 2070, 90.0, 0x0, Not Active, Active, Not Active, Not Active"])
+    assert idle["sm_mhz"] == 1200.0 and idle["reasons"] == ["hw_thermal_slowdown"]
+    assert bench.summarize_clocks([])["reasons"] == ["no samples"]
