@@ -519,3 +519,23 @@ def test_block_shift_and_invert_oracle(oracle, P):
     for k, s in enumerate(sig):
         S = D + s * Cd + s ** 2 * Md
         assert np.linalg.norm(rhs - S @ X[:, k]) <= 1e-8 * np.linalg.norm(rhs)
+
+
+@pytest.mark.parametrize("n,hb,cplx", [(1000, 1, False), (333, 17, True), (95, 94, False), (300, 250, True)])
+def test_band_lu_oracle_wide_and_ragged_bands(oracle, n, hb, cplx):
+    """The oracle's band LU (band_LU_solve, user_module.f90:2181-2336) on the
+    band shapes the GPU solves are checked with: tridiagonal, odd n, half band
+    n - 1 and wide complex bands -- against numpy solves."""
+    rng = np.random.default_rng(n + hb)
+    A = np.zeros((n, n), complex if cplx else float)
+    for i in range(n):
+        lo, hi = max(0, i - hb), min(n, i + hb + 1)
+        A[i, lo:hi] = rng.standard_normal(hi - lo) + (1j * rng.standard_normal(hi - lo) if cplx else 0)
+        A[i, i] += 2.0 * hb + 2.0
+    r, c = np.nonzero(A)
+    rp = np.concatenate([[1], 1 + np.cumsum(np.bincount(r, minlength=n))]).astype(np.int32)
+    K = oracle.crs_format(n, n, rp, (c + 1).astype(np.int32), A[r, c])
+    Pm = oracle.complex_precon(3, K) if cplx else oracle.real_precon(3, K)
+    Ao = oracle.Matrix(K, P=Pm, cplx=cplx)
+    v = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0)
+    np.testing.assert_allclose(Ao.precon(v), np.linalg.solve(A, v), rtol=1e-10, atol=1e-13)
