@@ -439,6 +439,49 @@ void band_solve(const UserMatrix& P, const T* b, T* x, const int* skip, cudaStre
   IDRS_LAUNCH_CHECK();
 }
 
+// X's terms for the formats the scatter kernel does not read: a CDS matrix
+// into the band factor, a dense matrix into the dense factor, each built on
+// the host from X's values and uploaded into the ZEROED buffer dst (every
+// caller adds its terms with coefficient one into a fresh buffer).  Band
+// entries whose column lies outside the matrix are left out (the
+// elimination never reads them).  The reference has no band form of a dense
+// matrix and no dense form of a CDS one (real_band / real_dense leave the
+// result zero, user_module.f90:1163-1235, :1981-2066), so those
+// combinations add nothing here either.
+template <class V>
+void host_form(const UserMatrix& X, V* dst, bool dense, int hb) {
+  const long n = X.nrows;
+  auto fetch = [&](const void* src, long cnt) {  // X's values widened to complex
+    std::vector<c128> v((size_t)std::max(cnt, 1L));
+    if (X.vals == 2) {
+      IDRS_CUDA(cudaMemcpy(v.data(), src, sizeof(c128) * cnt, cudaMemcpyDeviceToHost));
+    } else {
+      std::vector<double> r((size_t)std::max(cnt, 1L));
+      IDRS_CUDA(cudaMemcpy(r.data(), src, sizeof(double) * cnt, cudaMemcpyDeviceToHost));
+      for (long k = 0; k < cnt; ++k) v[k] = c128(r[k], 0.0);
+    }
+    return v;
+  };
+  if (dense && X.format == FMT_DENSE) {
+    const long cnt = n * std::min<long>(n, X.ncols);
+    const std::vector<c128> v = fetch(X.mat, cnt);
+    std::vector<V> h((size_t)std::max(cnt, 1L));
+    for (long k = 0; k < cnt; ++k) h[k] = narrow<V>(v[k]);
+    IDRS_CUDA(cudaMemcpy(dst, h.data(), sizeof(V) * cnt, cudaMemcpyHostToDevice));
+  } else if (!dense && X.format == FMT_CDS) {
+    const long n_pad = pad32(n), hx = X.half_band;
+    const std::vector<c128> v = fetch(X.band, n * (2 * hx + 1));
+    const long cnt = (2L * hb + 1) * n_pad;
+    std::vector<V> h((size_t)std::max(cnt, 1L), narrow<V>(c128(0.0, 0.0)));
+    for (long d = -hx; d <= hx; ++d)
+      for (long i = 0; i < n; ++i) {
+        const long j = i + d;
+        if (j >= 0 && j < n) h[band_idx(n_pad, hb, i, j)] = narrow<V>(v[i + n * (d + hx)]);
+      }
+    IDRS_CUDA(cudaMemcpy(dst, h.data(), sizeof(V) * cnt, cudaMemcpyHostToDevice));
+  }
+}
+
 template <class V>
 void build_typed(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, bool has_shift,
                  c128 shift, bool dense, int hb, UserMatrix& P) {
@@ -449,8 +492,12 @@ void build_typed(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, 
   IDRS_CUDA(cudaMalloc((void**)&S, sizeof(V) * std::max<long>(cnt, 1)));
   IDRS_CUDA(cudaMemset(S, 0, sizeof(V) * std::max<long>(cnt, 1)));
   auto scatter = [&](const UserMatrix& X, V* dst, V coef) {
-    k_scatter<V><<<stream_grid(n), kThreads>>>(n, X.row_ptr, X.col_ind, X.val, X.vals, coef, hbs, dst);
-    IDRS_LAUNCH_CHECK();
+    if (X.format == FMT_CRS || X.format == FMT_COO) {
+      k_scatter<V><<<stream_grid(n), kThreads>>>(n, X.row_ptr, X.col_ind, X.val, X.vals, coef, hbs, dst);
+      IDRS_LAUNCH_CHECK();
+    } else {
+      host_form<V>(X, dst, dense, hb);  // coef is one at every call
+    }
   };
   const V one = narrow<V>(c128(1.0, 0.0));
   const V sh = narrow<V>(shift);
@@ -523,8 +570,8 @@ int band_of(const UserMatrix& X) {
 void lu_build(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, bool has_shift,
               c128 shift, int which, bool cplx, UserMatrix& P) {
   for (const UserMatrix* X : {&K, M, C})
-    if (X && X->format != FMT_CRS && X->format != FMT_COO)
-      throw std::runtime_error("shift-and-invert: K, M and C must be CRS or COO");
+    if (X && X->format != FMT_CRS && X->format != FMT_COO && X->format != FMT_CDS && X->format != FMT_DENSE)
+      throw std::runtime_error("shift-and-invert: K, M and C must be CRS, COO, CDS or dense");
   const bool dense = which == 2;
   int hb = 0;
   if (!dense) {

@@ -87,8 +87,9 @@ int idrs_complex_precon(int which_precon, idrs_user_matrix K, const double *shif
  * + shift^2; M only: K - shift M), each matrix's diagonal with zeros -> 1.
  * which_precon 2 / 3: the dense / band LU factor (no pivoting, as the
  * reference; a zero pivot is IDRS_ERR_ARG) of that shifted matrix, factored
- * on the device; K, M, C must be CRS or COO.  v/P is then two triangular
- * solves on the device. */
+ * on the device; K, M, C may be CRS, COO, CDS or dense (as in the reference,
+ * a CDS matrix has no dense form and a dense matrix no band form: they add
+ * nothing there).  v/P is then two triangular solves on the device. */
 int idrs_real_precon_ext(int which_precon, idrs_user_matrix K, idrs_user_matrix M,
                          idrs_user_matrix C, const double *shift, idrs_user_matrix *P);
 int idrs_complex_precon_ext(int which_precon, idrs_user_matrix K, idrs_user_matrix M,

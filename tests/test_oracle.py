@@ -539,3 +539,42 @@ def test_band_lu_oracle_wide_and_ragged_bands(oracle, n, hb, cplx):
     Ao = oracle.Matrix(K, P=Pm, cplx=cplx)
     v = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0)
     np.testing.assert_allclose(Ao.precon(v), np.linalg.solve(A, v), rtol=1e-10, atol=1e-13)
+
+
+def _random_example(kind, n, hb, rng):
+    """E/RANDOM: uniform random band (CDS, entries outside the matrix zeroed,
+    band_real.f90:58-70) or dense matrix (dense_complex.f90:56-64); returns
+    the dense copy, the band or matrix as stored, and whether it is complex."""
+    cplx = kind.endswith("complex")
+    if kind.startswith("band"):
+        R = rng.uniform(size=(n, 2 * hb + 1)) + (1j * rng.uniform(size=(n, 2 * hb + 1)) if cplx else 0)
+        A = np.zeros((n, n), R.dtype)
+        for d in range(-hb, hb + 1):
+            for i in range(n):
+                if 0 <= i + d < n:
+                    A[i, i + d] = R[i, d + hb]
+                else:
+                    R[i, d + hb] = 0
+        return A, R, cplx
+    A = rng.uniform(size=(n, n)) + (1j * rng.uniform(size=(n, n)) if cplx else 0)
+    return A, A, cplx
+
+
+@pytest.mark.parametrize("kind", ["band_real", "band_complex", "dense_real", "dense_complex"])
+def test_random_examples_oracle(oracle, kind):
+    """The reference's RANDOM examples (band_real.f90:39-82, dense_complex.f90:
+    38-71): A from cds_format / dense_format, b = A 1, P = its band / dense LU
+    (real_precon 3 / 2), the solution of A x = b is 1."""
+    rng = np.random.default_rng({"band_real": 1, "band_complex": 2, "dense_real": 3, "dense_complex": 4}[kind])
+    n, hb = (400, 6) if kind.startswith("band") else (120, 0)
+    A, R, cplx = _random_example(kind, n, hb, rng)
+    K = oracle.cds_format(n, n, hb, R) if kind.startswith("band") else oracle.dense_format(R)
+    which = 3 if kind.startswith("band") else 2
+    P = oracle.complex_precon(which, K) if cplx else oracle.real_precon(which, K)
+    Ao = oracle.Matrix(K, P=P, cplx=cplx)
+    v = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0)
+    np.testing.assert_allclose(Ao.precon(v), np.linalg.solve(A, v), rtol=1e-8, atol=1e-10)
+    b = A @ np.ones(n)
+    r = oracle.idrs(Ao, b, 4, tolerance=1e-10)  # pp_idrs without a polynomial: IDR(4) on A P^-1
+    assert r.flag == 0
+    np.testing.assert_allclose(Ao.scaleback(b, r.x), 1.0, atol=1e-6)
