@@ -32,9 +32,16 @@ struct unsupported_error : std::runtime_error {
   using std::runtime_error::runtime_error;
 };
 
+// A lost staged copy (k_band_trsv) sets the process's fault word.  The word
+// is cleared when a call starts, so a fault is charged only to the call that
+// saw it.  A call in host-pointer mode has synchronised its stream (its
+// results are copied back) before the word is read; a call in device-pointer
+// mode may return while its kernels still run, and then reports a lost copy
+// only through the NaN values the solve writes.
 template <class F>
 int guard(F&& f) {
   try {
+    take_device_fault();
     const int rc = f();
     if (take_device_fault()) {
       set_error("a staged (TMA) copy never arrived; the result is invalid");

@@ -21,6 +21,8 @@
 //    on the symbol address, no allocation) at the start of each call, and
 //    calls that overlap on the GPU -- on different streams, or from different
 //    threads without ordering -- race on the scratch.  Order them.
+//  * u, v and uv must be device memory of the current device (or managed
+//    memory); any other pointer is refused with IDRS_ERR_ARG before a launch.
 //  * The call is asynchronous on `stream`; *uv is valid once it completes.
 #include <mutex>
 
@@ -102,6 +104,24 @@ extern "C" int idrs_rinprod_noalloc(long n, const double* u, const double* v, do
   if (e != cudaSuccess || dev < 0 || dev >= 256) {
     idrs::set_error(std::string("rinprod_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
     return IDRS_ERR_CUDA;
+  }
+  // u, v and uv must be memory this device can address: device memory of
+  // this device, or managed memory.  A host pointer is refused here, before
+  // anything is launched.
+  for (const void* p : {(const void*)u, (const void*)v, (const void*)uv}) {
+    if (!p) continue;
+    cudaPointerAttributes at{};
+    e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      idrs::set_error(std::string("rinprod_noalloc: cudaPointerGetAttributes: ") + cudaGetErrorString(e));
+      return IDRS_ERR_ARG;
+    }
+    const bool ok = at.type == cudaMemoryTypeManaged || (at.type == cudaMemoryTypeDevice && at.device == dev);
+    if (!ok) {
+      idrs::set_error("rinprod_noalloc: u, v and uv must be device (or managed) pointers of the current device");
+      return IDRS_ERR_ARG;
+    }
   }
   void* scratch = nullptr;
   {

@@ -331,7 +331,9 @@ int idrs_cinprod(idrs_matrix A, const double *u, const double *v, double *uv);
  * limited to 67,108,864 (IDRS_ERR_ARG beyond).  The first call on each device
  * performs a one-time set-up; make it before any stream capture.  The call
  * is asynchronous on `stream` (a cudaStream_t, NULL for the default stream);
- * calls that overlap on the GPU share the scratch and race. */
+ * calls that overlap on the GPU share the scratch and race.  u, v and uv must
+ * be device memory of the current device (or managed memory); other pointers
+ * return IDRS_ERR_ARG before anything is launched. */
 int idrs_rinprod_noalloc(long n, const double *u, const double *v, double *uv, void *stream);
 
 /* x = IDRS_RITZ(A, b, s[, M, tolerance, maximum_iterations, variant, flag,

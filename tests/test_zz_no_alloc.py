@@ -42,3 +42,21 @@ def test_rinprod_noalloc_rejects_oversize(gpu):
     # rejected on the host before any launch: the buffers are never read
     st = lib.idrs_rinprod_noalloc((1 << 26) + 1, small.data_ptr(), small.data_ptr(), small.data_ptr(), None)
     assert st == 1 and b"no-allocation limit" in lib.idrs_last_error()
+
+
+def test_rinprod_noalloc_rejects_host_pointers(gpu):
+    """Pointers the GPU cannot use as device memory are refused on the host
+    (cudaPointerGetAttributes) before any launch."""
+    import torch
+    lib = gpu.lib()
+    host = np.ones(16)
+    dev = torch.ones(16, dtype=torch.float64, device="cuda")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    for args in ((host.ctypes.data, dev.data_ptr(), out.data_ptr()),
+                 (dev.data_ptr(), dev.data_ptr(), host.ctypes.data)):
+        st = lib.idrs_rinprod_noalloc(16, *args, None)
+        assert st == 1 and b"device (or managed) pointers" in lib.idrs_last_error()
+    # the entry point still works afterwards
+    assert lib.idrs_rinprod_noalloc(16, dev.data_ptr(), dev.data_ptr(), out.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    assert float(out.item()) == 16.0
