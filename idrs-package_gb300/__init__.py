@@ -13,6 +13,6 @@ from .api import (  # noqa: F401
     IDRSError,
     Matrix,
     POINTER_DEVICE, crs_transpose, sparse_outer_grad, mm_matrix, mm_read,
-    POINTER_HOST, Result, UserMatrix, cds_format, complex_diagonal, complex_precon, coo_format,
+    POINTER_HOST, POLY_HORNER, POLY_RECURRENCE, Result, UserMatrix, cds_format, complex_diagonal, complex_precon, coo_format,
     crs_format, dense_format, lib, load, real_diagonal, real_precon, stencil7_format,
 )

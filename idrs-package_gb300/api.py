@@ -29,6 +29,8 @@ LIB_PATH = os.path.join(_HERE, "_build", "libidrs_gb300.so")
 
 IDRS_OK, IDRS_ERR_ARG, IDRS_ERR_CUDA, IDRS_ERR_ALLOC, IDRS_ERR_STATE, IDRS_ERR_UNSUPPORTED = range(6)
 POINTER_HOST, POINTER_DEVICE = 0, 1
+# fp64 evaluation of the polynomial preconditioner (idrs_matrix_set_poly_eval)
+POLY_HORNER, POLY_RECURRENCE = 0, 1
 
 
 class IDRSError(RuntimeError):
@@ -73,6 +75,7 @@ _PROTOS = {
     "idrs_matrix_free": (_i, [_vp]),
     "idrs_matrix_set_stream": (_i, [_vp, _vp]),
     "idrs_matrix_set_pointer_mode": (_i, [_vp, _i]),
+    "idrs_matrix_set_poly_eval": (_i, [_vp, _i]),
     "idrs_matrix_set_shadow": (_i, [_vp, _i, _vp]),
     "idrs_real_preconditioner": (_i, [_vp, _i, _i, _vp, _vp, _vp, _i, _i]),
     "idrs_complex_preconditioner": (_i, [_vp, _i, _i, _vp, _vp, _vp, _i, _i]),
@@ -136,7 +139,7 @@ class PPOptions(C.Structure):
                 ("in_s", C.c_int), ("in_it", C.c_int), ("in_tol", C.c_double),
                 ("preconditioner", C.c_int), ("degree", C.c_int), ("n_ritz", C.c_int),
                 ("inner_precision", C.c_int), ("device_pointers", C.c_int),
-                ("n_omega", C.c_int), ("recycle", C.c_int)]
+                ("n_omega", C.c_int), ("recycle", C.c_int), ("poly_eval", C.c_int)]
 
 
 class PPReport(C.Structure):
@@ -436,6 +439,11 @@ class Matrix:
         _check(lib().idrs_matrix_set_pointer_mode(self.handle, int(mode)))
         self.device_pointers = mode == POINTER_DEVICE
 
+    def set_poly_eval(self, mode: int):
+        """POLY_HORNER (the reference's rpolpre) or POLY_RECURRENCE (the Jacobi
+        three-term recurrence) for the fp64 products of this operator."""
+        _check(lib().idrs_matrix_set_poly_eval(self.handle, int(mode)))
+
     def set_shadow(self, s, PT):
         """Inject the shadow space P (s x n, rows contiguous) for solves with this s."""
         pt = None if PT is None else np.ascontiguousarray(PT, dtype=self.dtype)
@@ -607,6 +615,20 @@ def QMRIDR(A: Matrix, b, s, M1: Matrix | None = None, tolerance=None, maximum_it
     return r
 
 
+def _shift_masks(r: Result, tolerance):
+    """Per-shift status of a multishift result (no counterpart in the
+    reference, which reports one flag for all shifts and, like gfortran's
+    maxval, lets a NaN residual pass the flag test): converged_mask[k] is
+    relres[k] <= tol, nonfinite_mask[k] marks a shift whose residual or
+    solution holds a NaN or an infinity (a breakdown of that shift)."""
+    tol = 1e-6 if tolerance is None else float(tolerance)
+    rel = np.asarray(r.relres, dtype=float)
+    fin = np.isfinite(rel) & np.all(np.isfinite(r.x), axis=0)
+    r["nonfinite_mask"] = ~fin
+    r["converged_mask"] = fin & (rel <= tol)
+    return r
+
+
 def _shifts(A: Matrix, sigma):
     sig = np.ascontiguousarray(np.atleast_1d(sigma), dtype=np.complex128 if A.cplx else np.float64)
     if sig.ndim != 1 or len(sig) < 1:
@@ -640,7 +662,7 @@ def MSIDRS(A: Matrix, b, sigma, s, M1: Matrix | None = None, tolerance=None,
         r["resvec"] = rv
     if cf is not None:
         r["colfac"] = cf
-    return r
+    return _shift_masks(r, tolerance)
 
 
 def MSQMRIDR(A: Matrix, b, sigma, s, M1: Matrix | None = None, tolerance=None,
@@ -668,7 +690,7 @@ def MSQMRIDR(A: Matrix, b, sigma, s, M1: Matrix | None = None, tolerance=None,
     r = Result(x=x, flag=flag.value, relres=relres, iterations=iters.value)
     if rv is not None:
         r["resvec"] = rv
-    return r
+    return _shift_masks(r, tolerance)
 
 
 # ------------------------------------------------------------------ adjoint
@@ -760,9 +782,9 @@ def IDRS_RITZ(A: Matrix, b, s, M: Matrix | None = None, tolerance=None, maximum_
 
 
 def _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
-                inner_precision, dev, n_omega, recycle):
+                inner_precision, dev, n_omega, recycle, poly_eval=POLY_HORNER):
     return PPOptions(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
-                     inner_precision, int(dev), int(n_omega), int(bool(recycle)))
+                     inner_precision, int(dev), int(n_omega), int(bool(recycle)), int(poly_eval))
 
 
 def _pp_result(rep: PPReport, **extra) -> Result:
@@ -819,7 +841,7 @@ def _pp_cf(cplx, center, foci):
 def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=None, *, method=1,
             s=4, tol=1e-6, maxit=1000, in_s=1, in_it=0, in_tol=0.1, preconditioner=0, degree=0,
             n_ritz=32, inner_precision=64, n_omega=0, M=None, C_=None, seed=None, shift=None,
-            V=None, complex=None, x_out=None) -> Result:
+            V=None, complex=None, x_out=None, poly_eval=0) -> Result:
     """x = pp_idrs(K, b[, M, C, P, center, foci, seed, shift, V]) (RPP_IDRS / CPP_IDRS,
     pp_idrs_module.f90:64-162); the command-line options of initialize.inc:4-31
     are keyword arguments.
@@ -844,7 +866,7 @@ def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=Non
         else:
             raise ValueError("x_out must be a writeable contiguous array of b's length and kind")
     o = _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
-                    inner_precision, dev, n_omega, False)
+                    inner_precision, dev, n_omega, False, poly_eval)
     rep = PPReport()
     keep = []
     c, f = _pp_cf(cplx, center, foci)
@@ -859,7 +881,7 @@ def PP_MR_IDRS(K: UserMatrix, b_all, P: UserMatrix | None = None, center=None, f
                method=1, s=4, tol=1e-6, maxit=1000, in_s=1, in_it=0, in_tol=0.1,
                preconditioner=0, degree=0, n_ritz=32, inner_precision=64, n_omega=0,
                recycle=False, M=None, C_=None, seed=None, shift=None, V=None, complex=None,
-               nrhs=None, x_out=None) -> Result:
+               nrhs=None, x_out=None, poly_eval=0) -> Result:
     """x_all = pp_idrs(K, b_all[, M, C, P, center, foci, seed, shift, V]) for a sequence
     of right-hand sides (RPP_MR_IDRS / CPP_MR_IDRS, pp_idrs_module.f90:164-279,
     recycle.inc, run_mr_idrs.inc).
@@ -883,7 +905,7 @@ def PP_MR_IDRS(K: UserMatrix, b_all, P: UserMatrix | None = None, center=None, f
         nrhs = b_all.shape[1]
         x = np.zeros((n, nrhs), dtype=dt, order="F")
     o = _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
-                    inner_precision, dev, n_omega, recycle)
+                    inner_precision, dev, n_omega, recycle, poly_eval)
     reps = (PPReport * nrhs)()
     keep = []
     c, f = _pp_cf(cplx, center, foci)

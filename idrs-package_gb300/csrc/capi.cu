@@ -773,7 +773,9 @@ static int matvec_t(idrs_matrix A, const double* v, double* w) {
   const T* dv = (const T*)sv.in(v);
   T* dw = (T*)sv.out(w);
   DBuf t1(sizeof(T) * n, A->stream), t2(sizeof(T) * n, A->stream);
-  op_chain<T>(A->view(64), A->alpha_p, A->degree, dv, dw, t1.as<T>(), t2.as<T>(), nullptr, A->stream, T(1), T(0), nullptr);
+  DBuf t3(use_recurrence(*A, 64) ? sizeof(T) * n : 0, A->stream);
+  op_apply<T>(*A, 64, dv, dw, t1.as<T>(), t2.as<T>(), use_recurrence(*A, 64) ? t3.as<T>() : nullptr, nullptr,
+              nullptr, A->stream);
   sv.finish(w, dw);
   IDRS_CUDA(cudaStreamSynchronize(A->stream));
   return IDRS_OK;
@@ -1452,6 +1454,14 @@ int idrs_matrix_set_pointer_mode(idrs_matrix A, int mode) {
   });
 }
 
+int idrs_matrix_set_poly_eval(idrs_matrix A, int mode) {
+  return guard([&] {
+    REQUIRE(A && (mode == IDRS_POLY_HORNER || mode == IDRS_POLY_RECURRENCE), "set_poly_eval: bad arguments");
+    A->poly_eval = mode;
+    return IDRS_OK;
+  });
+}
+
 int idrs_matrix_set_shadow(idrs_matrix A, int s, const double* PT) {
   return guard([&] {
     REQUIRE(A && s >= 1, "set_shadow: bad arguments");
@@ -1502,21 +1512,15 @@ int idrs_time_matvec(idrs_matrix A, int prec, int warmup, int reps, double* ms_p
     size_t es = (A->cplx ? 2 : 1) * (prec == 64 ? 8 : 4);
     DBuf v(es * n, st), w(es * n, st), t1(es * n, st), t2(es * n, st), t3(es * n, st), t4(es * n, st);
     IDRS_CUDA(cudaMemsetAsync(v.p, 0, es * n, st));
-    const MatView& M = A->view(prec);
-    const bool recur = (prec == 32 && A->jac.valid());
     auto once = [&] {
-      if (prec == 64 && !A->cplx)
-        op_chain<double>(M, A->alpha_p, A->degree, v.as<double>(), w.as<double>(), t1.as<double>(), t2.as<double>(), nullptr, st, 1.0, 0.0, nullptr);
-      else if (prec == 32 && !A->cplx && recur)
-        op_chain_recur<float>(M, A->jac, A->degree, v.as<float>(), w.as<float>(), t1.as<float>(), t2.as<float>(), t3.as<float>(), t4.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
-      else if (prec == 32 && !A->cplx)
-        op_chain<float>(M, A->alpha_p, A->degree, v.as<float>(), w.as<float>(), t1.as<float>(), t2.as<float>(), nullptr, st, 1.0f, 0.0f, nullptr);
-      else if (prec == 64)
-        op_chain<c128>(M, A->alpha_p, A->degree, v.as<c128>(), w.as<c128>(), t1.as<c128>(), t2.as<c128>(), nullptr, st, c128(1.0), c128(0.0), nullptr);
-      else if (recur)
-        op_chain_recur<c64>(M, A->jac, A->degree, v.as<c64>(), w.as<c64>(), t1.as<c64>(), t2.as<c64>(), t3.as<c64>(), t4.as<c64>(), nullptr, st, c64(1.0f), c64(0.0f), nullptr);
-      else
-        op_chain<c64>(M, A->alpha_p, A->degree, v.as<c64>(), w.as<c64>(), t1.as<c64>(), t2.as<c64>(), nullptr, st, c64(1.0f), c64(0.0f), nullptr);
+      auto run = [&](auto z) {
+        using T = decltype(z);
+        op_apply<T>(*A, prec, v.as<T>(), w.as<T>(), t1.as<T>(), t2.as<T>(), t3.as<T>(), t4.as<T>(), nullptr, st);
+      };
+      if (prec == 64 && !A->cplx) run(0.0);
+      else if (prec == 32 && !A->cplx) run(0.0f);
+      else if (prec == 64) run(c128(0.0));
+      else run(c64(0.0f));
     };
     for (int i = 0; i < warmup; ++i) once();
     cudaEvent_t e0, e1;
@@ -1937,6 +1941,9 @@ int pp_setup(PPJob<T>& J, const T* pb, const double* center, const double* foci,
              const idrs_pp_options* opt, idrs_pp_report& rep) {
   const int s = opt->s;
   constexpr int vw = kCplx<T> ? 2 : 1;
+  REQUIRE(opt->poly_eval == IDRS_POLY_HORNER || opt->poly_eval == IDRS_POLY_RECURRENCE,
+          "pp_idrs: poly_eval must be IDRS_POLY_HORNER or IDRS_POLY_RECURRENCE");
+  J.A->poly_eval = opt->poly_eval;
   int preconditioner = opt->degree == 0 ? 0 : opt->preconditioner;
   bool estimate = preconditioner != 0;
   if (preconditioner == 1 && center) estimate = false;

@@ -744,7 +744,8 @@ class QmrGpu {
   long n;
   cudaStream_t st;
   RedBuf rb;
-  T *gpool = nullptr, *wpool = nullptr, *v = nullptr, *vt = nullptr, *t1 = nullptr, *t2 = nullptr, *PT = nullptr;
+  T *gpool = nullptr, *wpool = nullptr, *v = nullptr, *vt = nullptr, *t1 = nullptr, *t2 = nullptr, *t3 = nullptr,
+    *PT = nullptr;
   Tin *v_in = nullptr, *vt_in = nullptr;
   IdrsGpu<Tin>* inner = nullptr;
   QmrState<W>* d_st = nullptr;

@@ -33,6 +33,8 @@ IdrsGpu<T>::IdrsGpu(Operator& A_, int prec_, int s_, int method_)
   if (prec == 32) {
     t3 = dalloc<T>(n, st);
     t4 = dalloc<T>(n, st);
+  } else if (use_recurrence(A, prec)) {
+    t3 = dalloc<T>(n, st);  // the fp64 recurrence rotates three vectors
   }
   PT = dalloc<T>((long)rows * n, st);
   IDRS_CUDA(cudaMallocAsync((void**)&d_st, sizeof(IdrsState<W>), st));
@@ -58,10 +60,8 @@ template <class T>
 void IdrsGpu<T>::matvec(const T* in, T* out, const int* skip, T fa, T fcv, const T* fv) {
   // fp32 evaluates the polynomial by its stable three-term recurrence; fp64
   // keeps the monomial Horner form of rpolpre (matrix_module.f90:266-284)
-  if (prec == 32 && A.jac.valid())
-    op_chain_recur<T>(A.view(prec), A.jac, A.degree, in, out, t1, t2, t3, t4, skip, st, fa, fcv, fv);
-  else
-    op_chain<T>(A.view(prec), A.alpha_p, A.degree, in, out, t1, t2, skip, st, fa, fcv, fv);
+  // unless the operator asks for the recurrence (poly_eval 1)
+  op_apply<T>(A, prec, in, out, t1, t2, t3, t4, skip, st, fa, fcv, fv);
 }
 
 template <class T>
@@ -191,6 +191,7 @@ QmrGpu<T, Tin>::QmrGpu(Operator& A_, int s_, const SolveOpts& o) : A(A_), s(s_) 
   vt = dalloc<T>(n, st);
   t1 = dalloc<T>(n, st);
   t2 = dalloc<T>(n, st);
+  if (use_recurrence(A, 64)) t3 = dalloc<T>(n, st);
   PT = dalloc<T>((long)s * n, st);
   IDRS_CUDA(cudaMallocAsync((void**)&d_st, sizeof(QmrState<W>), st));
   IDRS_CUDA(cudaMemsetAsync(d_st, 0, sizeof(QmrState<W>), st));
@@ -211,7 +212,7 @@ QmrGpu<T, Tin>::QmrGpu(Operator& A_, int s_, const SolveOpts& o) : A(A_), s(s_) 
 template <class T, class Tin>
 QmrGpu<T, Tin>::~QmrGpu() {
   delete inner;
-  for (void* p : {(void*)gpool, (void*)wpool, (void*)v, (void*)vt, (void*)t1, (void*)t2, (void*)PT,
+  for (void* p : {(void*)gpool, (void*)wpool, (void*)v, (void*)vt, (void*)t1, (void*)t2, (void*)t3, (void*)PT,
                   (void*)d_st, (void*)d_scratch, (void*)d_rho, (void*)v_in, (void*)vt_in})
     if (p) cudaFreeAsync(p, st);
   if (h_stop) cudaFreeHost(h_stop);
@@ -246,7 +247,7 @@ void QmrGpu<T, Tin>::solve(const T* b, T* x, const SolveOpts& o) {
   T* gn = G(gn_idx);
   const bool have_x0 = (o.x0 != nullptr);
   auto matvec = [&](const T* in, T* out, const int* skip, T fa, T fcv, const T* fv) {
-    op_chain<T>(A.view(64), A.alpha_p, A.degree, in, out, t1, t2, skip, st, fa, fcv, fv);
+    op_apply<T>(A, 64, in, out, t1, t2, t3, nullptr, skip, st, fa, fcv, fv);
   };
   if (have_x0) {
     vec_copy<T>(n, (const T*)o.x0, x, stop, st);

@@ -1212,17 +1212,13 @@ static void run_chain(const MatView& Ks, const std::vector<ChainStep<T>>& steps,
 // form keeps its accuracy where the monomial coefficients (|alpha| ~ 10^3-10^4
 // with alternating signs for a degree-8 Chebyshev polynomial) cancel.
 // fp32 stencil chains run two steps per pass (k_stencil7_f4x2).
+// The steps y_2 .. y_{d+1} of the recurrence (degree d >= 1), y_i written
+// to buf[(i - 2) % nbuf]; `last` (if given) receives y_{d+1} instead.
 template <class T>
-void op_chain_recur(const MatView& Ks, const JacobiCols& J, int degree, const T* v, T* w, T* t1,
-                    T* t2, T* t3, T* t4, const int* skip, cudaStream_t st, T fa, T fcv, const T* fv) {
-  if (degree == 0) {
-    spmv<T>(Ks, v, w, fa, fcv, fv, skip, st);
-    return;
-  }
+static std::vector<ChainStep<T>> recur_steps(const JacobiCols& J, int degree, const T* v, T* const* buf,
+                                             int nbuf, T* last) {
   auto C = [](c128 z) { return narrow<T>(z); };
   std::vector<ChainStep<T>> steps;
-  T* buf[4] = {t1, t2, t3, t4};
-  const int nbuf = t4 ? 4 : 3;
   const T* ym2 = nullptr;  // y_{i-2}
   const T* ym1 = nullptr;  // y_{i-1}
   {
@@ -1255,12 +1251,35 @@ void op_chain_recur(const MatView& Ks, const JacobiCols& J, int degree, const T*
     ym1 = sk.out;
     ++nb;
   }
-  ChainStep<T> fin{ym1, w, Epi<T>()};
+  if (last) steps.back().out = last;
+  return steps;
+}
+
+template <class T>
+void op_chain_recur(const MatView& Ks, const JacobiCols& J, int degree, const T* v, T* w, T* t1,
+                    T* t2, T* t3, T* t4, const int* skip, cudaStream_t st, T fa, T fcv, const T* fv) {
+  if (degree == 0) {
+    spmv<T>(Ks, v, w, fa, fcv, fv, skip, st);
+    return;
+  }
+  T* buf[4] = {t1, t2, t3, t4};
+  std::vector<ChainStep<T>> steps = recur_steps<T>(J, degree, v, buf, t4 ? 4 : 3, nullptr);
+  ChainStep<T> fin{steps.back().out, w, Epi<T>()};
   fin.e.a = fa;
   fin.e.cv = fcv;
   fin.e.v = fv;
   steps.push_back(fin);
   run_chain<T>(Ks, steps, skip, st);
+}
+
+template <class T>
+void op_apply(Operator& A, int prec, const T* v, T* w, T* t1, T* t2, T* t3, T* t4, const int* skip,
+              cudaStream_t st, T fa, T fcv, const T* fv) {
+  const MatView& Ks = A.view(prec);
+  if (use_recurrence(A, prec) && t3)
+    op_chain_recur<T>(Ks, A.jac, A.degree, v, w, t1, t2, t3, t4, skip, st, fa, fcv, fv);
+  else
+    op_chain<T>(Ks, A.alpha_p, A.degree, v, w, t1, t2, skip, st, fa, fcv, fv);
 }
 
 // ---------------------------------------------------------------------------
@@ -1390,6 +1409,25 @@ void op_scaleback(Operator& A, int prec, const std::vector<c128>& alpha, int deg
     return;
   }
   T du = (A.dkind == 1) ? narrow<T>(A.dinv_u) : T(1);
+  if (use_recurrence(A, prec) && alpha.data() == A.alpha_p.data() && degree == A.degree) {
+    // p(Ks) y = y_{d+1} of the three-term recurrence; the rotation puts
+    // y_{d+1} into x (x never holds y_d or y_{d-1} when it is written)
+    T* buf[3];
+    buf[(degree - 1) % 3] = x;
+    buf[degree % 3] = t1;
+    buf[(degree + 1) % 3] = t2;
+    std::vector<ChainStep<T>> steps = recur_steps<T>(A.jac, degree, y, buf, 3, nullptr);
+    if (A.dkind == 1) {
+      Epi<T>& e = steps.back().e;
+      e.a = e.a * du; e.cx = e.cx * du; e.cu = e.cu * du; e.cv = e.cv * du;
+    }
+    run_chain<T>(Ks, steps, skip, st);
+    if (A.dkind == 2) {
+      if (prec == 32 && !A.dinv32) A.view(32);
+      vec_scale_vec<T>(n, prec == 32 ? A.dinv32 : A.dinv64, A.dinv_cplx, x, x, skip, st);
+    }
+    return;
+  }
   const T* cur = y;
   T* bufs[2] = {t1, t2};
   int nb = 0;
@@ -1696,6 +1734,8 @@ void operator_free(Operator* A) {
   template void spmv_ex<T>(const MatView&, const T*, T*, const Epi<T>&, const int*, cudaStream_t); \
   template void op_chain_recur<T>(const MatView&, const JacobiCols&, int, const T*, T*, T*, T*, T*, T*, \
                                   const int*, cudaStream_t, T, T, const T*);                       \
+  template void op_apply<T>(Operator&, int, const T*, T*, T*, T*, T*, T*, const int*, cudaStream_t, T, T, \
+                            const T*);                                                             \
   template void op_chain<T>(const MatView&, const std::vector<c128>&, int, const T*, T*, T*, T*,   \
                             const int*, cudaStream_t, T, T, const T*);                            \
   template void op_scaleback<T>(Operator&, int, const std::vector<c128>&, int, const T*, T*, T*,  \

@@ -161,6 +161,9 @@ struct Operator {
   int preconditioner = 0, degree = 0;
   std::vector<c128> alpha_p;  // 0..degree
   JacobiCols jac;             // tridiagonal Jacobi matrix of the polynomial (Chebyshev/Neumann)
+  // fp64 evaluation of p: 0 Horner on the monomial coefficients (rpolpre),
+  // 1 the three-term recurrence of jac (fp32 products always use it)
+  int poly_eval = 0;
   int n_sigma = 0;
   std::vector<c128> alpha_s;  // (degree+1) x n_sigma
   cudaStream_t stream = nullptr;
@@ -211,6 +214,16 @@ struct Operator {
   const MatView& view(int prec);
 };
 
+// Does a product of precision prec evaluate p by its three-term recurrence?
+// fp32: whenever p has a Jacobi matrix; fp64: on request (poly_eval 1), for
+// operators without deflation and without a shift-and-invert LU factor.
+inline bool use_recurrence(const Operator& A, int prec) {
+  if (A.degree <= 0 || !A.jac.valid()) return false;
+  if (prec == 32) return true;
+  const bool lu = A.P && (A.P->which_precon == 2 || A.P->which_precon == 3);
+  return A.poly_eval == 1 && !lu && !(A.defl && A.defl->k > 0);
+}
+
 int build_operator(Operator* A);  // (re)builds the scaled data; returns status
 void operator_free(Operator* A);
 RedBuf alloc_redbuf(cudaStream_t st);
@@ -234,6 +247,12 @@ template <class T>
 void op_chain_recur(const MatView& Ks, const JacobiCols& J, int degree, const T* v, T* w, T* t1,
                     T* t2, T* t3, T* t4, const int* skip, cudaStream_t st, T fa = T(1), T fcv = T(0),
                     const T* fv = nullptr);
+
+// w = fa * Ks p(Ks) v + fcv * fv, p evaluated as use_recurrence() says
+// (t3 null: Horner); t1..t4 as for op_chain_recur.
+template <class T>
+void op_apply(Operator& A, int prec, const T* v, T* w, T* t1, T* t2, T* t3, T* t4, const int* skip,
+              cudaStream_t st, T fa = T(1), T fcv = T(0), const T* fv = nullptr);
 
 // w = Ks p(Ks) v, then the final product gets the epilogue
 //   w = fa * (Ks u) + fcv * fv.

@@ -72,6 +72,9 @@ module idrs_gb300_module
       real(c_double) :: in_tol = 0.1d0
       integer(c_int) :: preconditioner = 0, degree = 0, n_ritz = 32, inner_precision = 64
       integer(c_int) :: device_pointers = 0, n_omega = 0, recycle = 0
+      ! 0: the reference's Horner evaluation of the polynomial in fp64,
+      ! 1: its three-term recurrence (see idrs_matrix_set_poly_eval)
+      integer(c_int) :: poly_eval = 0
    end type idrs_pp_options
 
    type, bind(C) :: idrs_pp_report

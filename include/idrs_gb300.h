@@ -149,6 +149,24 @@ int idrs_matrix_create_ext(idrs_user_matrix K, idrs_user_matrix M, idrs_user_mat
 int idrs_matrix_free(idrs_matrix A);
 int idrs_matrix_set_stream(idrs_matrix A, void *cuda_stream);
 int idrs_matrix_set_pointer_mode(idrs_matrix A, int mode);
+/* How fp64 products evaluate the polynomial preconditioner (no counterpart
+ * in the reference, which always uses rpolpre's Horner scheme on the
+ * monomial coefficients, matrix_module.f90:266-284):
+ *   IDRS_POLY_HORNER (default): Horner, as the reference;
+ *   IDRS_POLY_RECURRENCE: the three-term recurrence of the polynomial's
+ *     tridiagonal Jacobi matrix (Chebyshev and Neumann, matrix_module.f90:
+ *     851-941), for A*v, IDRS/QMRIDR and scaleback.  A degree-8 Chebyshev
+ *     polynomial fitted to a wide spectrum has monomial coefficients of
+ *     +-10^3..10^4 with alternating signs, so Horner cancels digits and the
+ *     true residual of an fp64 solve stalls above 1e-8 at 256^3; the
+ *     recurrence keeps its iterates of the size of A^-1 v.
+ * fp32 products always use the recurrence.  Multishift solves, their
+ * per-shift scale-back, the recycle space and operators with deflation or a
+ * shift-and-invert preconditioner keep Horner, as does the Hessenberg
+ * polynomial (no Jacobi matrix). */
+#define IDRS_POLY_HORNER 0
+#define IDRS_POLY_RECURRENCE 1
+int idrs_matrix_set_poly_eval(idrs_matrix A, int mode);
 /* Injects the shadow space used by solves with this s (row j of PT is
  * PT + j*n, real or interleaved complex).  PT = NULL removes it.  The
  * reference draws P from gfortran's RANDOM_NUMBER (idrs_module.f90:839-937);
@@ -383,6 +401,9 @@ typedef struct idrs_pp_options {
   int device_pointers; /* 1: b and x are device pointers */
   int n_omega;         /* -omega: number of Ritz-value omegas (default 0) */
   int recycle;         /* -recycle: 1 builds the s-dimensional recycle space U0 */
+  int poly_eval;       /* IDRS_POLY_HORNER (0, the reference) or IDRS_POLY_RECURRENCE for
+                          the fp64 products (see idrs_matrix_set_poly_eval); no
+                          counterpart in the reference */
 } idrs_pp_options;
 
 typedef struct idrs_pp_report {

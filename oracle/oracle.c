@@ -594,10 +594,16 @@ int or_matrix_create(const or_umat *K, const or_umat *P, const double *seed, int
   *out = A;
   return OR_OK;
 }
+int or_matrix_set_poly_eval(or_mat *A, int mode) {
+  if (!A || (mode != 0 && mode != 1)) return OR_EARG;
+  A->poly_eval = mode;
+  return OR_OK;
+}
 void or_matrix_free(or_mat *A) {
   if (!A) return;
   free(A->ralpha_p); free(A->calpha_p); free(A->ralpha_s); free(A->calpha_s);
   free(A->sigma_s); free(A->sigma); free(A->defl_V); free(A->defl_AV); free(A->defl_E);
+  free(A->jac);
   free(A);
 }
 
@@ -629,8 +635,23 @@ DEF_COMPUTE_ALPHA(or_rcompute_alpha, double)
 /* ccompute_alpha: matrix_module.f90:1021-1057 */
 DEF_COMPUTE_ALPHA(or_ccompute_alpha, or_cplx)
 
-#define DEF_NEUMANN(NAME, TT, CA)                                                       \
-  int NAME(int degree, TT center, TT *alpha) {                                          \
+/* The Jacobi matrix's tridiagonal columns (a_i, b_i, c_i) = (J(i-1,i),
+ * J(i,i), J(i+1,i)), i = 1..degree+1, kept for the recurrence evaluation */
+#define DEF_JCOLS(NAME, TT)                                                             \
+  static void NAME(int degree, const TT *J, TT *cols) {                                 \
+    int ld = degree + 2;                                                                \
+    if (!cols) return;                                                                  \
+    for (int i = 1; i <= degree + 1; ++i) {                                             \
+      cols[3 * (i - 1)] = i >= 2 ? J[(i - 2) + ld * (i - 1)] : 0;                       \
+      cols[3 * (i - 1) + 1] = J[(i - 1) + ld * (i - 1)];                                \
+      cols[3 * (i - 1) + 2] = J[i + ld * (i - 1)];                                      \
+    }                                                                                   \
+  }
+DEF_JCOLS(or_jcols_r, double)
+DEF_JCOLS(or_jcols_c, or_cplx)
+
+#define DEF_NEUMANN(NAME, TT, CA, JC)                                                   \
+  int NAME##_j(int degree, TT center, TT *alpha, TT *cols) {                            \
     int ld = degree + 2;                                                                \
     TT *J = calloc((size_t)ld * (degree + 1), sizeof(TT));                              \
     for (int i = 1; i <= degree + 1; ++i) {                                             \
@@ -638,15 +659,17 @@ DEF_COMPUTE_ALPHA(or_ccompute_alpha, or_cplx)
       J[i + ld * (i - 1)] = -center;                                                    \
     }                                                                                   \
     int st = CA(degree, J, ld, degree + 1, alpha);                                      \
+    JC(degree, J, cols);                                                                \
     free(J);                                                                            \
     return st;                                                                          \
-  }
+  }                                                                                     \
+  int NAME(int degree, TT center, TT *alpha) { return NAME##_j(degree, center, alpha, NULL); }
 /* rneumann: matrix_module.f90:851-875; cneumann :877-901 */
-DEF_NEUMANN(or_rneumann, double, or_rcompute_alpha)
-DEF_NEUMANN(or_cneumann, or_cplx, or_ccompute_alpha)
+DEF_NEUMANN(or_rneumann, double, or_rcompute_alpha, or_jcols_r)
+DEF_NEUMANN(or_cneumann, or_cplx, or_ccompute_alpha, or_jcols_c)
 
-#define DEF_CHEBYSHEV(NAME, TT, CA)                                                     \
-  int NAME(int degree, const TT foci[2], TT *alpha) {                                   \
+#define DEF_CHEBYSHEV(NAME, TT, CA, JC)                                                 \
+  int NAME##_j(int degree, const TT foci[2], TT *alpha, TT *cols) {                     \
     TT theta = (foci[0] + foci[1]) / 2.;                                                \
     TT delta = (foci[0] - foci[1]) / 2.;                                                \
     TT sigma = theta / delta;                                                           \
@@ -662,12 +685,14 @@ DEF_NEUMANN(or_cneumann, or_cplx, or_ccompute_alpha)
       rho = 1. / (2. * sigma - rho);                                                    \
     }                                                                                   \
     int st = CA(degree, J, ld, degree + 1, alpha);                                      \
+    JC(degree, J, cols);                                                                \
     free(J);                                                                            \
     return st;                                                                          \
-  }
+  }                                                                                     \
+  int NAME(int degree, const TT foci[2], TT *alpha) { return NAME##_j(degree, foci, alpha, NULL); }
 /* rchebyshev: matrix_module.f90:903-941; cchebyshev :943-981 */
-DEF_CHEBYSHEV(or_rchebyshev, double, or_rcompute_alpha)
-DEF_CHEBYSHEV(or_cchebyshev, or_cplx, or_ccompute_alpha)
+DEF_CHEBYSHEV(or_rchebyshev, double, or_rcompute_alpha, or_jcols_r)
+DEF_CHEBYSHEV(or_cchebyshev, or_cplx, or_ccompute_alpha, or_jcols_c)
 
 /* ------------------------------------------------------------------------ */
 /* QR eigenvalues: dense_la_module.f90:42-83 (CQR_factorization, refine=2), */
@@ -885,6 +910,7 @@ int or_real_preconditioner(or_mat *A, int preconditioner, int degree, const doub
   A->preconditioner = preconditioner;
   A->degree = (preconditioner == 0) ? 0 : degree;
   free(A->ralpha_p); A->ralpha_p = NULL;
+  free(A->jac); A->jac = NULL;
   if (preconditioner == 0) return OR_OK;
   A->ralpha_p = calloc(degree + 1, sizeof(double));
   if (preconditioner == 1) {
@@ -892,13 +918,15 @@ int or_real_preconditioner(or_mat *A, int preconditioner, int degree, const doub
     if (center) c = *center - A->rseed;
     else if (H) or_ranalyse_spectrum(H, ldh, nh, NULL, &c, NULL);
     else c = 1.;
-    return or_rneumann(degree, c, A->ralpha_p);
+    A->jac = calloc(3 * (size_t)(degree + 1), sizeof(double));
+    return or_rneumann_j(degree, c, A->ralpha_p, A->jac);
   } else if (preconditioner == 2) {
     double f[2];
     if (foci) { f[0] = foci[0] - A->rseed; f[1] = foci[1] - A->rseed; }
     else if (H) or_ranalyse_spectrum(H, ldh, nh, f, NULL, NULL);
     else { f[0] = 0.25; f[1] = 1.75; }
-    return or_rchebyshev(degree, f, A->ralpha_p);
+    A->jac = calloc(3 * (size_t)(degree + 1), sizeof(double));
+    return or_rchebyshev_j(degree, f, A->ralpha_p, A->jac);
   } else if (preconditioner == 3) {
     if (!H) return OR_EARG;
     return or_rcompute_alpha(degree, H, ldh, nh, A->ralpha_p);
@@ -911,6 +939,7 @@ int or_complex_preconditioner(or_mat *A, int preconditioner, int degree, const o
   A->preconditioner = preconditioner;
   A->degree = (preconditioner == 0) ? 0 : degree;
   free(A->calpha_p); A->calpha_p = NULL;
+  free(A->jac); A->jac = NULL;
   if (preconditioner == 0) return OR_OK;
   A->calpha_p = calloc(degree + 1, sizeof(or_cplx));
   if (preconditioner == 1) {
@@ -918,13 +947,15 @@ int or_complex_preconditioner(or_mat *A, int preconditioner, int degree, const o
     if (center) c = *center - A->cseed;
     else if (H) or_canalyse_spectrum(H, ldh, nh, NULL, &c, NULL);
     else c = 1.;
-    return or_cneumann(degree, c, A->calpha_p);
+    A->jac = calloc(3 * (size_t)(degree + 1), sizeof(or_cplx));
+    return or_cneumann_j(degree, c, A->calpha_p, A->jac);
   } else if (preconditioner == 2) {
     or_cplx f[2];
     if (foci) { f[0] = foci[0] - A->cseed; f[1] = foci[1] - A->cseed; }
     else if (H) or_canalyse_spectrum(H, ldh, nh, f, NULL, NULL);
     else { f[0] = 0.25; f[1] = 1.75; }
-    return or_cchebyshev(degree, f, A->calpha_p);
+    A->jac = calloc(3 * (size_t)(degree + 1), sizeof(or_cplx));
+    return or_cchebyshev_j(degree, f, A->calpha_p, A->jac);
   } else if (preconditioner == 3) {
     if (!H) return OR_EARG;
     return or_ccompute_alpha(degree, H, ldh, nh, A->calpha_p);
@@ -1455,6 +1486,7 @@ static int or_pp_setup_r(or_mat *A, int n, const double *b, or_pp_args *a, doubl
   }
   if (st == OR_OK)
     for (int i = 0; i <= A->degree && i < 64; ++i) a->alpha_p[i] = A->ralpha_p ? A->ralpha_p[i] : 1.;
+  A->poly_eval = a->poly_eval;
   free(H);
   return st;
 }

@@ -71,6 +71,11 @@ typedef struct or_mat {
   double rshift; or_cplx cshift;
   int n_deflation;             /* deflation: V, AV (n x k), V^H A V (k x k) */
   void *defl_V, *defl_AV, *defl_E;
+  /* evaluation of the polynomial: 0 Horner (rpolpre), 1 the three-term
+   * recurrence of its Jacobi matrix (no counterpart in the reference);
+   * jac = (a_i, b_i, c_i), i = 1..degree+1, of the kind of the operator */
+  int poly_eval;
+  void *jac;
 } or_mat;
 
 /* Optional arguments of the solvers: a NULL pointer means "not present". */
@@ -131,6 +136,8 @@ int or_matrix_create(const or_umat *K, const or_umat *P, const double *seed, int
 int or_matrix_create_ext(const or_umat *K, const or_umat *M, const or_umat *C,
                          const or_umat *P, const double *seed, const double *shift, int cplx,
                          int multishift, or_mat **out);
+/* 0: Horner (the reference), 1: the Jacobi three-term recurrence */
+int or_matrix_set_poly_eval(or_mat *A, int mode);
 void or_matrix_free(or_mat *A);
 int or_real_preconditioner(or_mat *A, int preconditioner, int degree, const double *foci,
                            const double *center, const double *H, int ldh, int nh);
@@ -239,6 +246,7 @@ typedef struct or_pp_args {
   /* per right-hand side outputs of or_pp_mr_idrs_r (arrays of nrhs; may be NULL) */
   int *flags, *iters;
   double *relres_solver_all, *relres_original_all;
+  int poly_eval;               /* as or_mat.poly_eval, for the pipeline's operator */
 } or_pp_args;
 int or_pp_idrs_r(const or_umat *K, const or_umat *P, int n, const double *b, or_pp_args *a,
                  double *x);

@@ -70,6 +70,7 @@ class PPArgs(C.Structure):
         ("recycle_relres", C.c_double),
         ("flags", c_int_p), ("iters", c_int_p),
         ("relres_solver_all", c_dbl_p), ("relres_original_all", c_dbl_p),
+        ("poly_eval", C.c_int),
     ]
 
 
@@ -281,6 +282,12 @@ class Matrix:
         st = fn(self.ptr, int(preconditioner), int(degree), _p(f), _p(c), _p(Hf), ldh, nh)
         if st:
             raise ValueError(f"preconditioner status {st}")
+
+    def set_poly_eval(self, mode):
+        """0: Horner (the reference's rpolpre), 1: the Jacobi three-term recurrence."""
+        st = lib().or_matrix_set_poly_eval(self.ptr, int(mode))
+        if st:
+            raise ValueError(f"set_poly_eval status {st}")
 
     def ms_parameters(self, sigma):
         sigma = np.ascontiguousarray(sigma, dtype=np.complex128 if self.cplx else np.float64)
@@ -543,7 +550,7 @@ def analyse_spectrum(H):
 
 
 def _pp_args(method, s, tol, maxit, in_s, in_tol, in_it, preconditioner, degree, n_ritz, foci,
-             center, p_seed, n_omega=0, recycle=False, si_seed=0):
+             center, p_seed, n_omega=0, recycle=False, si_seed=0, poly_eval=0):
     a = PPArgs()
     a.method, a.s, a.maxit, a.in_s, a.in_it = method, s, maxit, in_s, in_it
     a.preconditioner, a.degree, a.n_ritz = preconditioner, degree, n_ritz
@@ -555,6 +562,7 @@ def _pp_args(method, s, tol, maxit, in_s, in_tol, in_it, preconditioner, degree,
         c = C.c_double(center); keep.append(c); a.center = C.pointer(c)
     a.p_seed = p_seed
     a.n_omega, a.recycle, a.si_seed = int(n_omega), int(bool(recycle)), int(si_seed)
+    a.poly_eval = int(poly_eval)
     return a, keep
 
 
@@ -568,9 +576,9 @@ def _pp_common(a, degree):
 
 def pp_idrs(K: UserMatrix, b, *, P: UserMatrix | None = None, method=1, s=4, tol=1e-6, maxit=1000,
             in_s=4, in_tol=0.1, in_it=0, preconditioner=0, degree=0, n_ritz=32, foci=None,
-            center=None, p_seed=1, n_omega=0):
+            center=None, p_seed=1, n_omega=0, poly_eval=0):
     a, keep = _pp_args(method, s, tol, maxit, in_s, in_tol, in_it, preconditioner, degree, n_ritz,
-                       foci, center, p_seed, n_omega)
+                       foci, center, p_seed, n_omega, poly_eval=poly_eval)
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.empty_like(b)
     st = lib().or_pp_idrs_r(K.ptr, P.ptr if P else None, len(b), _p(b), C.byref(a), _p(x))

@@ -68,3 +68,19 @@ def test_pp_idrs_host_output_buffer(pkg, monkeypatch):
     for bad in (np.zeros(n + 1), np.zeros(n, dtype=np.float32), np.zeros((n, 2))[:, 0], [0.0] * n):
         with pytest.raises(ValueError):
             api.PP_IDRS(K, b, x_out=bad)
+
+
+def test_multishift_shift_masks(pkg):
+    """The per-shift status a multishift result carries: a NaN residual or
+    solution column is non-finite (never converged), the others converge by
+    relres <= tol."""
+    import numpy as np
+    x = np.ones((4, 3))
+    x[2, 1] = np.nan
+    r = pkg.api.Result(x=x, relres=np.array([1e-9, 1e-9, np.nan]), flag=0, iterations=5)
+    pkg.api._shift_masks(r, 1e-8)
+    np.testing.assert_array_equal(r.nonfinite_mask, [False, True, True])
+    np.testing.assert_array_equal(r.converged_mask, [True, False, False])
+    r = pkg.api.Result(x=np.ones((4, 2)), relres=np.array([1e-7, 1e-9]), flag=2, iterations=5)
+    pkg.api._shift_masks(r, 1e-8)
+    np.testing.assert_array_equal(r.converged_mask, [False, True])

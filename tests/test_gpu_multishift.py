@@ -196,7 +196,11 @@ def test_msqmridr_nested_inner_msidrs(gpu, oracle, P, prec):
     kw = dict(tolerance=tol, inner_s=4, inner_iterations=10, inner_tolerance=0.1)
     g = gpu.MSQMRIDR(A, b, sd, 4, inner_precision=prec, **kw)
     o = oracle.msqmridr(Ao, b, sd, 4, **kw)
+    # the per-shift masks of the result (no reference counterpart)
+    assert not g.nonfinite_mask.any()
+    np.testing.assert_array_equal(g.converged_mask, g.relres <= tol)
     if prec == 64:
+        assert g.converged_mask.all()
         assert g.flag == o.flag == 0 and np.max(g.relres) <= tol
         assert g.iterations == o.iterations
         for k in range(len(sd)):

@@ -583,3 +583,28 @@ def test_random_examples_oracle(oracle, kind):
     r = oracle.idrs(Ao, b, 4, tolerance=1e-10)  # pp_idrs without a polynomial: IDR(4) on A P^-1
     assert r.flag == 0
     np.testing.assert_allclose(Ao.scaleback(b, r.x), 1.0, atol=1e-6)
+
+
+@pytest.mark.parametrize("prec,kw", [(2, dict(foci=[0.05, 1.9])), (1, dict(center=1.0))])
+@pytest.mark.parametrize("degree", [1, 2, 8])
+def test_recurrence_evaluation_oracle(oracle, P, prec, kw, degree):
+    """The Jacobi three-term recurrence of the Chebyshev / Neumann polynomial
+    (matrix_module.f90:851-941) gives the same A p(A) v and D^-1 p(A) y as
+    the reference's Horner rpolpre (:266-284) and the dense closed form."""
+    N, K, D, As = _scaled_cdr(oracle, P)
+    rng = np.random.default_rng(degree)
+    v = rng.standard_normal(N)
+    A = oracle.Matrix(K, P=oracle.real_precon(1, K))
+    A.preconditioner(prec, degree, **kw)
+    a = oracle.chebyshev(degree, kw["foci"]) if prec == 2 else oracle.neumann(degree, kw["center"])
+    pv = sum(a[k] * np.linalg.matrix_power(As, k) @ v for k in range(degree + 1))
+    w_h = A.matvec(v)
+    y_h = A.scaleback(v, v)
+    A.set_poly_eval(1)
+    w_r = A.matvec(v)
+    y_r = A.scaleback(v, v)
+    np.testing.assert_allclose(w_r, As @ pv, rtol=1e-10, atol=1e-10 * np.abs(As @ pv).max())
+    np.testing.assert_allclose(w_r, w_h, rtol=1e-10, atol=1e-10 * np.abs(w_h).max())
+    dinv = 1.0 / np.diag(D)
+    np.testing.assert_allclose(y_r, dinv * pv, rtol=1e-10, atol=1e-10 * np.abs(dinv * pv).max())
+    np.testing.assert_allclose(y_r, y_h, rtol=1e-10, atol=1e-10 * np.abs(y_h).max())
