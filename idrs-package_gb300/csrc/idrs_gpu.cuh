@@ -110,13 +110,15 @@ template <class T>
 struct BPdot {
   const T* PT; long ld; const T* w; int nd;
   using Shared = NoShared;
+  static constexpr bool kPack = true;
+  bool pack_ok() const { return aligned_f4(PT) && aligned_f4(w) && ld % 4 == 0; }
   __device__ void prepare(Shared&) const {}
-  template <int ND, class A>
-  __device__ void operator()(long i, Shared&, A (&acc)[ND]) const {
-    T wi = w[i];
+  template <int W, int ND, class A>
+  __device__ void run(long i, Shared&, A (&acc)[ND]) const {
+    const Pk<T, W> wi = pk_ld<W>(w, i);
 #pragma unroll
     for (int d = 0; d < ND; ++d)
-      if (d < nd) acc_add(acc[d], PT[d * ld + i] * wi);
+      if (d < nd) pk_acc_mul(acc[d], pk_ld<W>(PT + d * ld, i), wi);
   }
 };
 
@@ -135,13 +137,15 @@ template <class T>
 struct BOmDots {
   const T* t; const T* r;
   using Shared = NoShared;
+  static constexpr bool kPack = true;
+  bool pack_ok() const { return aligned_f4(t) && aligned_f4(r); }
   __device__ void prepare(Shared&) const {}
-  template <int ND, class A>
-  __device__ void operator()(long i, Shared&, A (&acc)[ND]) const {
-    T ti = t[i], ri = r[i];
-    acc_add(acc[0], conj_(ti) * ri);
-    acc_add(acc[1], abs2_(ti));
-    acc_add(acc[2], abs2_(ri));
+  template <int W, int ND, class A>
+  __device__ void run(long i, Shared&, A (&acc)[ND]) const {
+    const Pk<T, W> ti = pk_ld<W>(t, i), ri = pk_ld<W>(r, i);
+    pk_acc_dot(acc[0], ti, ri);
+    pk_acc_abs2(acc[1], ti);
+    pk_acc_abs2(acc[2], ri);
   }
 };
 
@@ -254,14 +258,20 @@ struct BBuildU {  // U_k = om*(r - sum_{q>=k} g_q G_q) + sum_{q>=k} g_q U_q   (i
     for (int q = threadIdx.x; q < s; q += blockDim.x) sh.g[q] = narrow<T>(st->gamma[q]);
     if (threadIdx.x == 0) sh.om = narrow<T>(st->om);
   }
-  template <int ND, class A>
-  __device__ void operator()(long i, Shared& sh, A (&)[ND]) const {
-    T v = r[i];
-    for (int q = k; q < s; ++q) v = v - sh.g[q] * G[q * ld + i];
-    if (vout) { vout[i] = v; return; }  // preconditioned variant: v only
-    T t = sh.om * v;
-    for (int q = k; q < s; ++q) t = t + sh.g[q] * U[q * ld + i];
-    U[k * ld + i] = t;
+  static constexpr bool kPack = true;
+  bool pack_ok() const {
+    return aligned_f4(r) && aligned_f4(G) && aligned_f4(U) && (!vout || aligned_f4(vout)) && ld % 4 == 0;
+  }
+  template <int L, int ND, class A>
+  __device__ void run(long i, Shared& sh, A (&)[ND]) const {
+    Pk<T, L> v = pk_ld<L>(r, i);
+#pragma unroll 4
+    for (int q = k; q < s; ++q) v = pk_msub(v, sh.g[q], pk_ld<L>(G + q * ld, i));
+    if (vout) { pk_st<L>(vout, i, v); return; }  // preconditioned variant: v only
+    Pk<T, L> t = pk_scale(sh.om, v);
+#pragma unroll 4
+    for (int q = k; q < s; ++q) t = pk_madd(t, sh.g[q], pk_ld<L>(U + q * ld, i));
+    pk_st<L>(U + k * ld, i, t);
   }
 };
 template <class T, class W>
@@ -288,19 +298,22 @@ struct BIdrUpd {  // bi-orthogonalise G_k,U_k; r -= beta G_k; x += beta U_k; acc
     for (int q = threadIdx.x; q < k; q += blockDim.x) sh.a[q] = narrow<T>(st->alpha[q]);
     if (threadIdx.x == 0) sh.beta = narrow<T>(st->beta[k]);
   }
-  template <int ND, class A>
-  __device__ void operator()(long i, Shared& sh, A (&acc)[ND]) const {
-    T g = G[k * ld + i], u = U[k * ld + i];
+  static constexpr bool kPack = true;
+  bool pack_ok() const { return aligned_f4(G) && aligned_f4(U) && aligned_f4(r) && aligned_f4(x) && ld % 4 == 0; }
+  template <int L, int ND, class A>
+  __device__ void run(long i, Shared& sh, A (&acc)[ND]) const {
+    Pk<T, L> g = pk_ld<L>(G + k * ld, i), u = pk_ld<L>(U + k * ld, i);
+#pragma unroll 4
     for (int q = 0; q < k; ++q) {
-      g = g - G[q * ld + i] * sh.a[q];
-      u = u - U[q * ld + i] * sh.a[q];
+      g = pk_msub(g, sh.a[q], pk_ld<L>(G + q * ld, i));
+      u = pk_msub(u, sh.a[q], pk_ld<L>(U + q * ld, i));
     }
-    G[k * ld + i] = g;
-    U[k * ld + i] = u;
-    T rr = r[i] - sh.beta * g;
-    r[i] = rr;
-    x[i] = x[i] + sh.beta * u;
-    acc_add(acc[0], abs2_(rr));
+    pk_st<L>(G + k * ld, i, g);
+    pk_st<L>(U + k * ld, i, u);
+    const Pk<T, L> rr = pk_msub(pk_ld<L>(r, i), sh.beta, g);
+    pk_st<L>(r, i, rr);
+    pk_st<L>(x, i, pk_madd(pk_ld<L>(x, i), sh.beta, u));
+    pk_acc_abs2(acc[0], rr);
   }
 };
 
@@ -308,17 +321,21 @@ template <class T, class W>
 struct BOmUpd {  // r -= om t; x += om v; acc0 = |r|^2, acc_{1+j} = PT_j . r
   T* r; const T* t; T* x; const T* v; const T* PT; long ld; int s; const W* om;
   struct Shared { T om; };
+  static constexpr bool kPack = true;
+  bool pack_ok() const {
+    return aligned_f4(r) && aligned_f4(t) && aligned_f4(x) && aligned_f4(v) && aligned_f4(PT) && ld % 4 == 0;
+  }
   __device__ void prepare(Shared& sh) const { if (threadIdx.x == 0) sh.om = narrow<T>(*om); }
-  template <int ND, class A>
-  __device__ void operator()(long i, Shared& sh, A (&acc)[ND]) const {
-    T vi = v[i];
-    T ri = r[i] - sh.om * t[i];
-    x[i] = x[i] + sh.om * vi;
-    r[i] = ri;
-    acc_add(acc[0], abs2_(ri));
+  template <int L, int ND, class A>
+  __device__ void run(long i, Shared& sh, A (&acc)[ND]) const {
+    const Pk<T, L> vi = pk_ld<L>(v, i);
+    const Pk<T, L> ri = pk_msub(pk_ld<L>(r, i), sh.om, pk_ld<L>(t, i));
+    pk_st<L>(x, i, pk_madd(pk_ld<L>(x, i), sh.om, vi));
+    pk_st<L>(r, i, ri);
+    pk_acc_abs2(acc[0], ri);
 #pragma unroll
     for (int d = 1; d < ND; ++d)
-      if (d <= s) acc_add(acc[d], PT[(d - 1) * ld + i] * ri);
+      if (d <= s) pk_acc_mul(acc[d], pk_ld<L>(PT + (d - 1) * ld, i), ri);
   }
 };
 

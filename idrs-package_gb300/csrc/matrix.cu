@@ -1,11 +1,13 @@
 // matrix.cu -- SpMV kernels (stencil, CRS, CDS, dense), the scaled operator
 // build and the Horner chain of the polynomial preconditioner.
 #include <algorithm>
+#include <cstdlib>
 #include <climits>
 #include <atomic>
 #include <mutex>
 
 #include "matrix.cuh"
+#include "tma.cuh"
 
 namespace idrs {
 
@@ -60,6 +62,30 @@ __device__ __forceinline__ c128 shfl_idx_t(c128 v, int l) { return c128(shfl_idx
 __device__ __forceinline__ c64 shfl_idx_t(c64 v, int l) { return c64(shfl_idx_t(v.x, l), shfl_idx_t(v.y, l)); }
 
 template <class V, class T> __device__ __forceinline__ T mulvt(V a, T b) { return a * b; }
+
+// Matrix values and column indices are read once per product.  Where a
+// warp consumes every line it loads in one instruction (the long-row
+// segments), evict-first loads (ld.global.cs) keep them from displacing the
+// gathered vector x from L2; the row kernels re-read a line across their
+// loop steps and load normally (evict-first measured slower there).
+__device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
+__device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
+__device__ __forceinline__ int ld_stream(const int* p) { return __ldcs(p); }
+__device__ __forceinline__ c128 ld_stream(const c128* p) {
+  const double2 v = __ldcs(reinterpret_cast<const double2*>(p));
+  return c128(v.x, v.y);
+}
+__device__ __forceinline__ c64 ld_stream(const c64* p) {
+  const float2 v = __ldcs(reinterpret_cast<const float2*>(p));
+  return c64(v.x, v.y);
+}
+// val[k] * x[ci[k]], the streamed operands evict-first when STREAM
+template <bool STREAM = false, class V, class T>
+__device__ __forceinline__ T crs_term(const V* __restrict__ val, const int* __restrict__ ci, const T* __restrict__ x,
+                                      long k) {
+  if constexpr (STREAM) return mulvt(ld_stream(val + k), x[ld_stream(ci + k)]);
+  else return mulvt(val[k], x[ci[k]]);
+}
 
 MatView UserMatrix::view64() const {
   MatView v;
@@ -525,6 +551,194 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2(
   }
 }
 
+// The same pair with its HBM streams staged in shared memory one plane
+// ahead by bulk asynchronous copies (cp.async.bulk, mbarrier completion), so
+// no warp waits for HBM inside an iteration: while a block computes plane
+// zp, the copies of xin(zp+2) and u, v(zp+1) are in flight.  xin rows
+// j0-2 .. j0+9 of a plane (the block's rows, their halo rows and the halo
+// rows' y-neighbours) are one contiguous run, u and v rows j0-1 .. j0+8
+// another, so each plane is three copies issued by one thread.  Three xin
+// stages, two u / v stages and a ring of three yA planes (two barriers per
+// plane) keep the block at about 106 KB of shared memory, two blocks per SM.
+// Each thread owns two half-rows of four points (i0 = 4 lane and nx/2 + i0),
+// so every 16-byte shared-memory access of a warp is conflict-free; each
+// point is computed by the same FMAs as in k_stencil7_f8x2 (bitwise equal
+// results).  A copy that has not landed after kTmaWaitCycles sets a shared
+// flag: the block then stops waiting, writes NaN into its output rows and
+// records the fault.
+constexpr int kT8XRows = kX8Rows + 4;
+constexpr int kT8XStages = 3;
+constexpr int kT8UStages = 2;
+constexpr int kT8ARing = 3;
+
+static size_t t8_smem(int nx) {
+  return 128 + sizeof(float) * (size_t)nx *
+                   ((size_t)kT8XStages * kT8XRows + 2 * (size_t)kT8UStages * kX8Halo + (size_t)kT8ARing * kX8Halo);
+}
+
+// two half-rows of four points: [i0, i0+4) and [hx+i0, hx+i0+4)
+__device__ __forceinline__ F8 ld8h(const float* row, int i0, int hx) {
+  return F8{*reinterpret_cast<const float4*>(row + i0), *reinterpret_cast<const float4*>(row + hx + i0)};
+}
+__device__ __forceinline__ F8 ld8hg(const float* row, int i0, int hx) { return F8{ld4(row + i0), ld4(row + hx + i0)}; }
+__device__ __forceinline__ void st8h(float* row, int i0, int hx, const F8& r) {
+  *reinterpret_cast<float4*>(row + i0) = r.a;
+  *reinterpret_cast<float4*>(row + hx + i0) = r.b;
+}
+// the x-neighbours of both half-rows (lane L holds the last points of each
+// half; the domain ends are zero); every lane runs the shuffles
+struct XNb {
+  float la, ra, lb, rb;
+};
+__device__ __forceinline__ XNb x_neighbours(const F8& c, int lane, int L) {
+  const float ua = __shfl_up_sync(0xffffffffu, c.a.w, 1), da = __shfl_down_sync(0xffffffffu, c.a.x, 1);
+  const float ub = __shfl_up_sync(0xffffffffu, c.b.w, 1), db = __shfl_down_sync(0xffffffffu, c.b.x, 1);
+  const float b0 = __shfl_sync(0xffffffffu, c.b.x, 0), aL = __shfl_sync(0xffffffffu, c.a.w, L);
+  return XNb{lane == 0 ? 0.f : ua, lane == L ? b0 : da, lane == 0 ? aL : ub, lane == L ? 0.f : db};
+}
+__device__ __forceinline__ F8 st7_apply8h(const St7& c, const F8& xm, const F8& xc, const F8& xp, const F8& xs,
+                                          const F8& xn, const XNb& nb) {
+  return F8{st7_apply(c, xm.a, xc.a, xp.a, xs.a, xn.a, nb.la, nb.ra),
+            st7_apply(c, xm.b, xc.b, xp.b, xs.b, xn.b, nb.lb, nb.rb)};
+}
+
+__global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
+    int nx, int ny, int nz, int zc, St7 ca, float cua, float cva, St7 cb, float cub, float cvb,
+    const float* __restrict__ xin, const float* __restrict__ u, const float* __restrict__ v,
+    const float* __restrict__ vb, float* __restrict__ ya, float* __restrict__ yb,
+    const int* __restrict__ skip, int* fault) {
+  if (skip && *skip) return;
+  extern __shared__ __align__(128) unsigned char sm[];
+  uint64_t* mbX = reinterpret_cast<uint64_t*>(sm);
+  uint64_t* mbU = mbX + kT8XStages;
+  volatile int* sflag = reinterpret_cast<volatile int*>(sm + 64);
+  float* Xs = reinterpret_cast<float*>(sm + 128);
+  float* Us = Xs + (long)kT8XStages * kT8XRows * nx;
+  float* Vs = Us + (long)kT8UStages * kX8Halo * nx;
+  float* sA = Vs + (long)kT8UStages * kX8Halo * nx;
+  const int lane = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + lane;
+  const int hx = nx >> 1, L = (nx >> 3) - 1, i0 = lane * 4;
+  const int j0 = blockIdx.x * kX8Rows, j = j0 - 1 + ty;
+  const int z0 = blockIdx.y * zc, z1 = min(nz, z0 + zc), zb = z0 - 1;
+  const bool lact = lane <= L;
+  const bool act = lact && j >= 0 && j < ny;
+  const bool interior = act && ty >= 1 && ty <= kX8Rows;
+  const long plane = (long)nx * ny;
+  const int xr0 = max(j0 - 2, 0), xr1 = min(j0 + kX8Rows + 1, ny - 1);
+  const int ur0 = max(j0 - 1, 0), ur1 = min(j0 + kX8Rows, ny - 1);
+  const unsigned xbytes = (unsigned)((xr1 - xr0 + 1) * nx * 4);
+  const unsigned ubytes = (unsigned)((ur1 - ur0 + 1) * nx * 4);
+  const bool have_uv = (u != nullptr) || (v != nullptr);
+  // planes of the stage sequences: xin zb .. z1+1, u / v zb .. z1 (inside the
+  // grid); they are copied in order from qa, the first one inside the grid,
+  // so the k-th copy (k = q - qa) goes to stage k % stages and completes that
+  // stage's mbarrier phase k / stages
+  const int qa = max(zb, 0);
+  auto x_ok = [&](int q) { return q >= qa && q < nz && q <= z1 + 1; };
+  auto u_ok = [&](int q) { return have_uv && q >= qa && q < nz && q <= z1; };
+  auto issueX = [&](int q) {
+    if (!x_ok(q)) return;
+    const int s = (q - qa) % kT8XStages;
+    mbar_expect_tx(&mbX[s], xbytes);
+    bulk_g2s(Xs + ((long)s * kT8XRows + (xr0 - (j0 - 2))) * nx, xin + q * plane + (long)xr0 * nx, xbytes, &mbX[s]);
+  };
+  auto issueU = [&](int q) {
+    if (!u_ok(q)) return;
+    const int s = (q - qa) % kT8UStages;
+    mbar_expect_tx(&mbU[s], (u ? ubytes : 0u) + (v ? ubytes : 0u));
+    const long off = ((long)s * kX8Halo + (ur0 - (j0 - 1))) * nx;
+    if (u) bulk_g2s(Us + off, u + q * plane + (long)ur0 * nx, ubytes, &mbU[s]);
+    if (v) bulk_g2s(Vs + off, v + q * plane + (long)ur0 * nx, ubytes, &mbU[s]);
+  };
+  auto waitX = [&](int q) {
+    if (!x_ok(q) || *sflag) return;
+    if (!mbar_wait(&mbX[(q - qa) % kT8XStages], ((q - qa) / kT8XStages) & 1)) *sflag = 1;
+  };
+  auto waitU = [&](int q) {
+    if (!u_ok(q) || *sflag) return;
+    if (!mbar_wait(&mbU[(q - qa) % kT8UStages], ((q - qa) / kT8UStages) & 1)) *sflag = 1;
+  };
+  auto xrow = [&](int q, int r) { return Xs + ((long)((q - qa) % kT8XStages) * kT8XRows + r) * nx; };
+  auto arow = [&](int q, int r) { return sA + ((long)((q - zb) % kT8ARing) * kX8Halo + r) * nx; };
+  if (tid == 0) {
+    for (int s = 0; s < kT8XStages; ++s) mbar_init(&mbX[s], 1);
+    for (int s = 0; s < kT8UStages; ++s) mbar_init(&mbU[s], 1);
+    *sflag = 0;
+    mbar_init_fence();
+    issueX(zb);
+    issueX(zb + 1);
+    issueU(zb);
+  }
+  __syncthreads();
+  const F8 z8 = zero8();
+  F8 xm = (act && zb - 1 >= 0) ? ld8hg(xin + (long)(zb - 1) * plane + (long)j * nx, i0, hx) : z8;
+  for (int zp = zb; zp <= z1; ++zp) {
+    if (zp > zb) __syncthreads();  // step B of plane zp-2 is done with the yA slot step A reuses
+    if (tid == 0) {
+      proxy_async_fence();
+      issueX(zp + 2);
+      issueU(zp + 1);
+    }
+    const bool doB = zp - 1 >= z0;
+    const F8 vbz = (vb && interior && doB) ? ld8hg(vb + (long)(zp - 1) * plane + (long)j * nx, i0, hx) : z8;
+    // the stages step A reads (no-ops for planes outside the sequences)
+    if (zp == zb) waitX(zp);
+    waitX(zp + 1);
+    waitU(zp);
+    // step A at plane zp
+    F8 r = z8, xc = z8;
+    if (zp >= 0 && zp < nz) {  // uniform over the block
+      xc = act ? ld8h(xrow(zp, ty + 1), i0, hx) : z8;
+      const F8 xp = (act && x_ok(zp + 1)) ? ld8h(xrow(zp + 1, ty + 1), i0, hx) : z8;
+      const F8 xs = (act && j > 0) ? ld8h(xrow(zp, ty), i0, hx) : z8;
+      const F8 xn = (act && j + 1 < ny) ? ld8h(xrow(zp, ty + 2), i0, hx) : z8;
+      const XNb nb = x_neighbours(xc, lane, L);
+      if (act) {
+        r = st7_apply8h(ca, xm, xc, xp, xs, xn, nb);
+        const long uo = ((long)((zp - qa) % kT8UStages) * kX8Halo + ty) * nx;
+        if (u) axpy8(r, cua, ld8h(Us + uo, i0, hx));
+        if (v) axpy8(r, cva, ld8h(Vs + uo, i0, hx));
+        if (ya && interior && zp >= z0 && zp < z1) st8h(ya + (long)zp * plane + (long)j * nx, i0, hx, r);
+      }
+    }
+    if (lact) st8h(arow(zp, ty), i0, hx, r);
+    __syncthreads();
+    // step B at plane zp-1 from yA(zp-2 .. zp) and xin(zp-1) (= xm)
+    if (doB) {
+      const int zq = zp - 1;
+      const F8 bc = interior ? ld8h(arow(zq, ty), i0, hx) : z8;
+      const XNb nb = x_neighbours(bc, lane, L);
+      if (interior) {
+        F8 rb = st7_apply8h(cb, ld8h(arow(zq - 1, ty), i0, hx), bc, ld8h(arow(zp, ty), i0, hx),
+                            ld8h(arow(zq, ty - 1), i0, hx), ld8h(arow(zq, ty + 1), i0, hx), nb);
+        axpy8(rb, cub, xm);
+        if (vb) axpy8(rb, cvb, vbz);
+        st8h(yb + (long)zq * plane + (long)j * nx, i0, hx, rb);
+      }
+    }
+    xm = xc;
+  }
+  __syncthreads();  // every wait is behind: the flag is final and the same for all threads
+  if (*sflag) {
+    // a copy never landed: let the last copy of every stage finish (bounded),
+    // then poison this block's outputs and report
+    if (tid == 0) {
+      for (int q = z1 + 1, c = 0; q >= qa && c < kT8XStages; --q)
+        if (x_ok(q)) mbar_wait(&mbX[(q - qa) % kT8XStages], ((q - qa) / kT8XStages) & 1), ++c;
+      for (int q = z1, c = 0; q >= qa && c < kT8UStages; --q)
+        if (u_ok(q)) mbar_wait(&mbU[(q - qa) % kT8UStages], ((q - qa) / kT8UStages) & 1), ++c;
+      *(volatile int*)fault = 1;
+    }
+    const float qn = nanf("");
+    const F8 nan8 = F8{make_float4(qn, qn, qn, qn), make_float4(qn, qn, qn, qn)};
+    if (interior)
+      for (int z = z0; z < z1; ++z) {
+        st8h(yb + (long)z * plane + (long)j * nx, i0, hx, nan8);
+        if (ya) st8h(ya + (long)z * plane + (long)j * nx, i0, hx, nan8);
+      }
+  }
+}
+
 // CRS, G lanes per row (G | 32).  Warp-uniform loop so the shuffles are
 // always executed by the full warp.
 template <int G, class T, class V>
@@ -549,7 +763,7 @@ __global__ void __launch_bounds__(256) k_crs(int nrows, const int* __restrict__ 
       const int beg = rp[row], end = rp[row + 1];
       mine = (end - beg) <= max_len;  // longer rows: the bin kernels
       if (mine)
-        for (int k = beg + gl; k < end; k += G) sum = sum + mulvt(val[k], x[ci[k]]);
+        for (int k = beg + gl; k < end; k += G) sum = sum + crs_term(val, ci, x, k);
     }
 #pragma unroll
     for (int m = G / 2; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
@@ -579,7 +793,7 @@ __global__ void __launch_bounds__(256) k_crs_row(int nrows, const int* __restric
     if (end - beg > max_len) continue;  // written by the bin kernels
     T sum = T(0);
 #pragma unroll 4
-    for (int k = beg; k < end; ++k) sum = sum + mulvt(val[k], x[ci[k]]);
+    for (int k = beg; k < end; ++k) sum = sum + crs_term(val, ci, x, k);
     T out = a * sum;
     if (cx != T(0)) out = out + cx * x[row];
     if (u) out = out + cu * u[row];
@@ -621,7 +835,7 @@ __global__ void __launch_bounds__(256) k_crs_list(int nlist, const int* __restri
       row = rows[idx];
       const int beg = rp[row], end = rp[row + 1];
 #pragma unroll 4
-      for (int k = beg + gl; k < end; k += G) sum = sum + mulvt(val[k], x[ci[k]]);
+      for (int k = beg + gl; k < end; k += G) sum = sum + crs_term(val, ci, x, k);
     }
 #pragma unroll
     for (int m = G / 2; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
@@ -652,7 +866,7 @@ __global__ void __launch_bounds__(256) k_crs_seg(int n_seg, int n_long, const in
 #pragma unroll
   for (int j = 0; j < kBinLong / 32; ++j) {
     const long k = beg + lane + 32L * j;
-    if (k < end) sum = sum + mulvt(val[k], x[ci[k]]);
+    if (k < end) sum = sum + crs_term<true>(val, ci, x, k);
   }
 #pragma unroll
   for (int m = 16; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
@@ -1124,6 +1338,43 @@ static int f4x2_resident() {
   return b;
 }
 
+// The staged pair (k_stencil7_f8x2t) for this nx on the current device:
+// resident blocks per SM, or 0 when it cannot run (shared memory) or
+// IDRS_STAGED_PAIR=0 asks for the unstaged kernel.
+static int f8x2t_resident(int nx) {
+  static const bool enabled = [] {
+    const char* e = getenv("IDRS_STAGED_PAIR");
+    return !(e && e[0] == '0');
+  }();
+  if (!enabled) return 0;
+  static std::mutex mu;
+  static std::atomic<uint64_t> attr_set{0};
+  static int cache_dev = -1, cache_nx = -1, cache_r = 0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev == cache_dev && nx == cache_nx) return cache_r;
+  const uint64_t bit = dev < 64 ? uint64_t(1) << dev : 0;
+  if (!bit || !(attr_set.load() & bit)) {
+    if (cudaFuncSetAttribute(k_stencil7_f8x2t, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)t8_smem(kX2MaxNx)) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    attr_set.fetch_or(bit);
+  }
+  int r = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_stencil7_f8x2t, 32 * kX8Halo, t8_smem(nx)) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    r = 0;
+  }
+  cache_dev = dev;
+  cache_nx = nx;
+  cache_r = r;
+  return r;
+}
+
 static int f8x2_resident() {
   static const int b = [] {
     int r = 0;
@@ -1168,6 +1419,21 @@ static void run_chain(const MatView& Ks, const std::vector<ChainStep<T>>& steps,
           if (steps[q].out == A.out) break;
         }
         const int gy = (Ks.ny + kX2Rows - 1) / kX2Rows;
+        const int staged = Ks.nx % 8 == 0 ? f8x2t_resident(Ks.nx) : 0;
+        if (staged > 0) {
+          const long target = 2L * num_sms() * staged;
+          const long chunks = std::max(1L, std::min((long)Ks.nz, (target + gy - 1) / gy));
+          const int zc = (int)std::max(4L, ((long)Ks.nz + chunks - 1) / chunks);
+          dim3 blk(32, kX8Halo, 1);
+          dim3 grid((Ks.ny + kX8Rows - 1) / kX8Rows, (Ks.nz + zc - 1) / zc, 1);
+          k_stencil7_f8x2t<<<grid, blk, t8_smem(Ks.nx), st>>>(
+              Ks.nx, Ks.ny, Ks.nz, zc, st7_of(Ks, A.e.a, A.e.cx), A.e.u ? A.e.cu : 0.f,
+              A.e.v ? A.e.cv : 0.f, st7_of(Ks, B.e.a, B.e.cx), B.e.u ? B.e.cu : 0.f, B.e.v ? B.e.cv : 0.f,
+              A.in, A.e.u, A.e.v, B.e.v, need ? A.out : nullptr, B.out, skip, device_fault_word());
+          IDRS_LAUNCH_CHECK();
+          k += 2;
+          continue;
+        }
         if (Ks.nx % 8 == 0) {
           const long target = 2L * num_sms() * f8x2_resident();
           const long chunks = std::max(1L, std::min((long)Ks.nz, (target + gy - 1) / gy));
