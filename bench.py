@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--grid", type=int, default=256)
     p.add_argument("--in-it", type=int, default=400)
-    p.add_argument("--in-tol", type=float, default=1e-2)
+    p.add_argument("--in-tol", type=float, default=5e-3)
     p.add_argument("--in-s", type=int, default=4)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-other-configs", action="store_true",

@@ -79,12 +79,51 @@ __device__ __forceinline__ c64 ld_stream(const c64* p) {
   const float2 v = __ldcs(reinterpret_cast<const float2*>(p));
   return c64(v.x, v.y);
 }
+// L2-only evict-first loads: an L2 cache-policy hint on a read-only load,
+// L1 allocation unchanged (the row kernels re-read their lines from L1)
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ double ld_l2ef(const double* a, uint64_t pol) {
+  double v;
+  asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float ld_l2ef(const float* a, uint64_t pol) {
+  float v;
+  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ int ld_l2ef(const int* a, uint64_t pol) {
+  int v;
+  asm("ld.global.nc.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ c128 ld_l2ef(const c128* a, uint64_t pol) {
+  double x, y;
+  asm("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(x), "=d"(y) : "l"(a), "l"(pol));
+  return c128(x, y);
+}
+__device__ __forceinline__ c64 ld_l2ef(const c64* a, uint64_t pol) {
+  float x, y;
+  asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(x), "=f"(y) : "l"(a), "l"(pol));
+  return c64(x, y);
+}
+
 // val[k] * x[ci[k]], the streamed operands evict-first when STREAM
 template <bool STREAM = false, class V, class T>
 __device__ __forceinline__ T crs_term(const V* __restrict__ val, const int* __restrict__ ci, const T* __restrict__ x,
                                       long k) {
   if constexpr (STREAM) return mulvt(ld_stream(val + k), x[ld_stream(ci + k)]);
   else return mulvt(val[k], x[ci[k]]);
+}
+// the same with the L2-only evict-first policy pol
+template <class V, class T>
+__device__ __forceinline__ T crs_term_l2(const V* __restrict__ val, const int* __restrict__ ci,
+                                         const T* __restrict__ x, long k, uint64_t pol) {
+  return mulvt(ld_l2ef(val + k, pol), x[ld_l2ef(ci + k, pol)]);
 }
 
 MatView UserMatrix::view64() const {
@@ -554,26 +593,26 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2(
 // The same pair with its HBM streams staged in shared memory one plane
 // ahead by bulk asynchronous copies (cp.async.bulk, mbarrier completion), so
 // no warp waits for HBM inside an iteration: while a block computes plane
-// zp, the copies of xin(zp+2) and u, v(zp+1) are in flight.  xin rows
-// j0-2 .. j0+9 of a plane (the block's rows, their halo rows and the halo
-// rows' y-neighbours) are one contiguous run, u and v rows j0-1 .. j0+8
-// another, so each plane is three copies issued by one thread.  Three xin
-// stages, two u / v stages and a ring of three yA planes (two barriers per
-// plane) keep the block at about 106 KB of shared memory, two blocks per SM.
-// Each thread owns two half-rows of four points (i0 = 4 lane and nx/2 + i0),
-// so every 16-byte shared-memory access of a warp is conflict-free; each
-// point is computed by the same FMAs as in k_stencil7_f8x2 (bitwise equal
-// results).  A copy that has not landed after kTmaWaitCycles sets a shared
-// flag: the block then stops waiting, writes NaN into its output rows and
-// records the fault.
-constexpr int kT8XRows = kX8Rows + 4;
+// zp, the copies of xin(zp+2) and u, v(zp+1) are in flight.  The block's rows
+// j0-1 .. j0+8 of a plane are one contiguous run of each vector, so a plane
+// is three copies issued by one thread.  The halo rows' outer y-neighbours
+// (rows j0-2 and j0+9, read by two warps only) are loaded into registers a
+// plane ahead instead.  Three xin stages, two u / v stages and a ring of
+// four yA planes (one barrier per plane) keep the block at 110 KB of shared
+// memory, two blocks per SM.  Stage slots and mbarrier phases advance by
+// counters (every copied plane is waited for once, in order).  Each thread
+// owns two half-rows of four points (i0 = 4 lane and nx/2 + i0), so every
+// 16-byte shared-memory access of a warp is conflict-free; each point is
+// computed by the same FMAs as in k_stencil7_f8x2 (bitwise equal results).
+// A copy that has not landed after kTmaWaitCycles sets a shared flag: the
+// block then stops waiting, writes NaN into its output rows and records the
+// fault.
 constexpr int kT8XStages = 3;
 constexpr int kT8UStages = 2;
-constexpr int kT8ARing = 3;
+constexpr int kT8ARing = 4;
 
 static size_t t8_smem(int nx) {
-  return 128 + sizeof(float) * (size_t)nx *
-                   ((size_t)kT8XStages * kT8XRows + 2 * (size_t)kT8UStages * kX8Halo + (size_t)kT8ARing * kX8Halo);
+  return 128 + sizeof(float) * (size_t)nx * kX8Halo * (kT8XStages + 2 * kT8UStages + kT8ARing);
 }
 
 // two half-rows of four points: [i0, i0+4) and [hx+i0, hx+i0+4)
@@ -601,6 +640,7 @@ __device__ __forceinline__ F8 st7_apply8h(const St7& c, const F8& xm, const F8& 
   return F8{st7_apply(c, xm.a, xc.a, xp.a, xs.a, xn.a, nb.la, nb.ra),
             st7_apply(c, xm.b, xc.b, xp.b, xs.b, xn.b, nb.lb, nb.rb)};
 }
+__device__ __forceinline__ int next_slot(int s, int n) { return s + 1 == n ? 0 : s + 1; }
 
 __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
     int nx, int ny, int nz, int zc, St7 ca, float cua, float cva, St7 cb, float cub, float cvb,
@@ -612,10 +652,11 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
   uint64_t* mbX = reinterpret_cast<uint64_t*>(sm);
   uint64_t* mbU = mbX + kT8XStages;
   volatile int* sflag = reinterpret_cast<volatile int*>(sm + 64);
+  const long rstride = (long)kX8Halo * nx;  // one stage / ring slot
   float* Xs = reinterpret_cast<float*>(sm + 128);
-  float* Us = Xs + (long)kT8XStages * kT8XRows * nx;
-  float* Vs = Us + (long)kT8UStages * kX8Halo * nx;
-  float* sA = Vs + (long)kT8UStages * kX8Halo * nx;
+  float* Us = Xs + kT8XStages * rstride;
+  float* Vs = Us + kT8UStages * rstride;
+  float* sA = Vs + kT8UStages * rstride;
   const int lane = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + lane;
   const int hx = nx >> 1, L = (nx >> 3) - 1, i0 = lane * 4;
   const int j0 = blockIdx.x * kX8Rows, j = j0 - 1 + ty;
@@ -624,42 +665,50 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
   const bool act = lact && j >= 0 && j < ny;
   const bool interior = act && ty >= 1 && ty <= kX8Rows;
   const long plane = (long)nx * ny;
-  const int xr0 = max(j0 - 2, 0), xr1 = min(j0 + kX8Rows + 1, ny - 1);
-  const int ur0 = max(j0 - 1, 0), ur1 = min(j0 + kX8Rows, ny - 1);
-  const unsigned xbytes = (unsigned)((xr1 - xr0 + 1) * nx * 4);
-  const unsigned ubytes = (unsigned)((ur1 - ur0 + 1) * nx * 4);
+  const int r0 = max(j0 - 1, 0), r1 = min(j0 + kX8Rows, ny - 1);
+  const unsigned rbytes = (unsigned)((r1 - r0 + 1) * nx * 4);
+  const long roff = (long)(r0 - (j0 - 1)) * nx;
   const bool have_uv = (u != nullptr) || (v != nullptr);
-  // planes of the stage sequences: xin zb .. z1+1, u / v zb .. z1 (inside the
-  // grid); they are copied in order from qa, the first one inside the grid,
-  // so the k-th copy (k = q - qa) goes to stage k % stages and completes that
-  // stage's mbarrier phase k / stages
+  // planes of the stage sequences: xin zb .. z1+1, u / v zb .. z1, inside the
+  // grid, copied and waited for in order from qa
   const int qa = max(zb, 0);
   auto x_ok = [&](int q) { return q >= qa && q < nz && q <= z1 + 1; };
   auto u_ok = [&](int q) { return have_uv && q >= qa && q < nz && q <= z1; };
+  // the halo warps' outer neighbour row (ty 0: j-1, ty 9: j+1) of plane q
+  const int hrow = ty == 0 ? j - 1 : j + 1;
+  const bool hact = lact && j >= 0 && j < ny && (ty == 0 || ty == kX8Halo - 1) && hrow >= 0 && hrow < ny;
+  auto ld_halo = [&](int q) -> F8 {
+    return (hact && q >= 0 && q < nz) ? ld8hg(xin + (long)q * plane + (long)hrow * nx, i0, hx) : zero8();
+  };
+  int ix = 0, iu = 0;  // thread 0: next stage to fill
   auto issueX = [&](int q) {
     if (!x_ok(q)) return;
-    const int s = (q - qa) % kT8XStages;
-    mbar_expect_tx(&mbX[s], xbytes);
-    bulk_g2s(Xs + ((long)s * kT8XRows + (xr0 - (j0 - 2))) * nx, xin + q * plane + (long)xr0 * nx, xbytes, &mbX[s]);
+    mbar_expect_tx(&mbX[ix], rbytes);
+    bulk_g2s(Xs + ix * rstride + roff, xin + q * plane + (long)r0 * nx, rbytes, &mbX[ix]);
+    ix = next_slot(ix, kT8XStages);
   };
   auto issueU = [&](int q) {
     if (!u_ok(q)) return;
-    const int s = (q - qa) % kT8UStages;
-    mbar_expect_tx(&mbU[s], (u ? ubytes : 0u) + (v ? ubytes : 0u));
-    const long off = ((long)s * kX8Halo + (ur0 - (j0 - 1))) * nx;
-    if (u) bulk_g2s(Us + off, u + q * plane + (long)ur0 * nx, ubytes, &mbU[s]);
-    if (v) bulk_g2s(Vs + off, v + q * plane + (long)ur0 * nx, ubytes, &mbU[s]);
+    mbar_expect_tx(&mbU[iu], (u ? rbytes : 0u) + (v ? rbytes : 0u));
+    if (u) bulk_g2s(Us + iu * rstride + roff, u + q * plane + (long)r0 * nx, rbytes, &mbU[iu]);
+    if (v) bulk_g2s(Vs + iu * rstride + roff, v + q * plane + (long)r0 * nx, rbytes, &mbU[iu]);
+    iu = next_slot(iu, kT8UStages);
   };
+  int wx = 0, wu = 0;          // next stage to wait for
+  unsigned phx = 0, phu = 0;   // expected phase parity of each stage (bit s)
   auto waitX = [&](int q) {
-    if (!x_ok(q) || *sflag) return;
-    if (!mbar_wait(&mbX[(q - qa) % kT8XStages], ((q - qa) / kT8XStages) & 1)) *sflag = 1;
+    if (!x_ok(q)) return;
+    if (!*sflag && !mbar_wait_sleep(&mbX[wx], (phx >> wx) & 1u)) *sflag = 1;
+    phx ^= 1u << wx;
+    wx = next_slot(wx, kT8XStages);
   };
   auto waitU = [&](int q) {
-    if (!u_ok(q) || *sflag) return;
-    if (!mbar_wait(&mbU[(q - qa) % kT8UStages], ((q - qa) / kT8UStages) & 1)) *sflag = 1;
+    if (!u_ok(q)) return;
+    if (!*sflag && !mbar_wait_sleep(&mbU[wu], (phu >> wu) & 1u)) *sflag = 1;
+    phu ^= 1u << wu;
+    wu = next_slot(wu, kT8UStages);
   };
-  auto xrow = [&](int q, int r) { return Xs + ((long)((q - qa) % kT8XStages) * kT8XRows + r) * nx; };
-  auto arow = [&](int q, int r) { return sA + ((long)((q - zb) % kT8ARing) * kX8Halo + r) * nx; };
+  auto arow = [&](int q, int r) { return sA + ((q - zb) & (kT8ARing - 1)) * rstride + (long)r * nx; };
   if (tid == 0) {
     for (int s = 0; s < kT8XStages; ++s) mbar_init(&mbX[s], 1);
     for (int s = 0; s < kT8UStages; ++s) mbar_init(&mbU[s], 1);
@@ -671,39 +720,49 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
   }
   __syncthreads();
   const F8 z8 = zero8();
+  // stage slots of xin(zp), xin(zp+1) and u / v(zp) for the reads
+  int rx1 = zb + 1 - qa;                      // 0 or 1
+  int rx0 = rx1 == 0 ? kT8XStages - 1 : 0;    // plane zb (unused when zb < 0)
+  int ru = 0;
   F8 xm = (act && zb - 1 >= 0) ? ld8hg(xin + (long)(zb - 1) * plane + (long)j * nx, i0, hx) : z8;
+  F8 hcur = ld_halo(zb);
   for (int zp = zb; zp <= z1; ++zp) {
-    if (zp > zb) __syncthreads();  // step B of plane zp-2 is done with the yA slot step A reuses
     if (tid == 0) {
-      proxy_async_fence();
+      proxy_async_fence();  // the reads of the refilled stages were before the last barrier
       issueX(zp + 2);
       issueU(zp + 1);
     }
     const bool doB = zp - 1 >= z0;
     const F8 vbz = (vb && interior && doB) ? ld8hg(vb + (long)(zp - 1) * plane + (long)j * nx, i0, hx) : z8;
-    // the stages step A reads (no-ops for planes outside the sequences)
+    const F8 hnext = ld_halo(zp + 1);
     if (zp == zb) waitX(zp);
     waitX(zp + 1);
     waitU(zp);
     // step A at plane zp
     F8 r = z8, xc = z8;
     if (zp >= 0 && zp < nz) {  // uniform over the block
-      xc = act ? ld8h(xrow(zp, ty + 1), i0, hx) : z8;
-      const F8 xp = (act && x_ok(zp + 1)) ? ld8h(xrow(zp + 1, ty + 1), i0, hx) : z8;
-      const F8 xs = (act && j > 0) ? ld8h(xrow(zp, ty), i0, hx) : z8;
-      const F8 xn = (act && j + 1 < ny) ? ld8h(xrow(zp, ty + 2), i0, hx) : z8;
+      const float* X0 = Xs + rx0 * rstride;
+      xc = act ? ld8h(X0 + (long)ty * nx, i0, hx) : z8;
+      const F8 xp = (act && x_ok(zp + 1)) ? ld8h(Xs + rx1 * rstride + (long)ty * nx, i0, hx) : z8;
+      F8 xs = z8, xn = z8;
+      if (act) {
+        if (ty == 0) xs = hcur;
+        else if (j > 0) xs = ld8h(X0 + (long)(ty - 1) * nx, i0, hx);
+        if (ty == kX8Halo - 1) xn = hcur;
+        else if (j + 1 < ny) xn = ld8h(X0 + (long)(ty + 1) * nx, i0, hx);
+      }
       const XNb nb = x_neighbours(xc, lane, L);
       if (act) {
         r = st7_apply8h(ca, xm, xc, xp, xs, xn, nb);
-        const long uo = ((long)((zp - qa) % kT8UStages) * kX8Halo + ty) * nx;
-        if (u) axpy8(r, cua, ld8h(Us + uo, i0, hx));
-        if (v) axpy8(r, cva, ld8h(Vs + uo, i0, hx));
+        if (u) axpy8(r, cua, ld8h(Us + ru * rstride + (long)ty * nx, i0, hx));
+        if (v) axpy8(r, cva, ld8h(Vs + ru * rstride + (long)ty * nx, i0, hx));
         if (ya && interior && zp >= z0 && zp < z1) st8h(ya + (long)zp * plane + (long)j * nx, i0, hx, r);
       }
     }
     if (lact) st8h(arow(zp, ty), i0, hx, r);
     __syncthreads();
-    // step B at plane zp-1 from yA(zp-2 .. zp) and xin(zp-1) (= xm)
+    // step B at plane zp-1 from yA(zp-2 .. zp) and xin(zp-1) (= xm); step A
+    // of the next plane writes the ring slot of zp-3, which nothing reads now
     if (doB) {
       const int zq = zp - 1;
       const F8 bc = interior ? ld8h(arow(zq, ty), i0, hx) : z8;
@@ -717,6 +776,10 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
       }
     }
     xm = xc;
+    hcur = hnext;
+    rx0 = rx1;
+    rx1 = next_slot(rx1, kT8XStages);
+    if (u_ok(zp)) ru = next_slot(ru, kT8UStages);
   }
   __syncthreads();  // every wait is behind: the flag is final and the same for all threads
   if (*sflag) {
@@ -755,6 +818,7 @@ __global__ void __launch_bounds__(256) k_crs(int nrows, const int* __restrict__ 
   const int gl = lane & (G - 1);
   const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
   const long nwarps = (gridDim.x * (long)blockDim.x) >> 5;
+  const uint64_t pol = l2_evict_first_policy();
   for (long base = warp * RPW; base < nrows; base += nwarps * RPW) {
     const long row = base + sub;
     T sum = T(0);
@@ -763,7 +827,7 @@ __global__ void __launch_bounds__(256) k_crs(int nrows, const int* __restrict__ 
       const int beg = rp[row], end = rp[row + 1];
       mine = (end - beg) <= max_len;  // longer rows: the bin kernels
       if (mine)
-        for (int k = beg + gl; k < end; k += G) sum = sum + crs_term(val, ci, x, k);
+        for (int k = beg + gl; k < end; k += G) sum = sum + crs_term_l2(val, ci, x, k, pol);
     }
 #pragma unroll
     for (int m = G / 2; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);
@@ -787,13 +851,14 @@ __global__ void __launch_bounds__(256) k_crs_row(int nrows, const int* __restric
                                                  const T* __restrict__ u,
                                                  const int* __restrict__ skip, int max_len) {
   if (skip && *skip) return;
+  const uint64_t pol = l2_evict_first_policy();
   for (long row = blockIdx.x * (long)blockDim.x + threadIdx.x; row < nrows;
        row += gridDim.x * (long)blockDim.x) {
     const int beg = rp[row], end = rp[row + 1];
     if (end - beg > max_len) continue;  // written by the bin kernels
     T sum = T(0);
 #pragma unroll 4
-    for (int k = beg; k < end; ++k) sum = sum + crs_term(val, ci, x, k);
+    for (int k = beg; k < end; ++k) sum = sum + crs_term_l2(val, ci, x, k, pol);
     T out = a * sum;
     if (cx != T(0)) out = out + cx * x[row];
     if (u) out = out + cu * u[row];
@@ -827,6 +892,7 @@ __global__ void __launch_bounds__(256) k_crs_list(int nlist, const int* __restri
   const int gl = lane & (G - 1);
   const long warp = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
   const long nwarps = (gridDim.x * (long)blockDim.x) >> 5;
+  const uint64_t pol = l2_evict_first_policy();
   for (long base = warp * RPW; base < nlist; base += nwarps * RPW) {
     const long idx = base + sub;
     T sum = T(0);
@@ -835,7 +901,7 @@ __global__ void __launch_bounds__(256) k_crs_list(int nlist, const int* __restri
       row = rows[idx];
       const int beg = rp[row], end = rp[row + 1];
 #pragma unroll 4
-      for (int k = beg + gl; k < end; k += G) sum = sum + crs_term(val, ci, x, k);
+      for (int k = beg + gl; k < end; k += G) sum = sum + crs_term_l2(val, ci, x, k, pol);
     }
 #pragma unroll
     for (int m = G / 2; m >= 1; m >>= 1) sum = sum + shfl_x(sum, m);

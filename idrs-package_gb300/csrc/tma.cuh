@@ -51,6 +51,17 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
     if (clock64() - t0 > kTmaWaitCycles) return false;
   return true;
 }
+// the same for many waiting threads: between polls a thread sleeps, so
+// waiting warps leave the issue slots to the warps that compute
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* b, unsigned parity) {
+  if (mbar_try_wait(b, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(b, parity)) {
+    __nanosleep(32);
+    if (clock64() - t0 > kTmaWaitCycles) return false;
+  }
+  return true;
+}
 // bulk copy global -> shared: both addresses 16-byte aligned, bytes a
 // multiple of 16; completes `bytes` of transactions on b
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* b) {
