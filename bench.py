@@ -44,8 +44,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--grid", type=int, default=256)
-    p.add_argument("--in-it", type=int, default=400)
-    p.add_argument("--in-tol", type=float, default=5e-3)
+    p.add_argument("--in-it", type=int, default=300)
+    p.add_argument("--in-tol", type=float, default=3e-3)
     p.add_argument("--in-s", type=int, default=4)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-other-configs", action="store_true",
@@ -269,6 +269,19 @@ def run_ours(args, rank, world, dist):
     t_horner, r_horner = timed("fp64_horner", 1, tol=TOL)
     err_horner = errors(x_dev.cpu().numpy())[0]
     t_e2e, r_e2e = timed("mixed", args.steps, host=True)
+    # the number of fp32 inner iterations reacts to rounding: the same solve
+    # on three right-hand sides perturbed by 1e-13 relative (x moves by less
+    # than 1e-8) shows the spread of the headline time
+    spread = []
+    rng = np.random.default_rng(7)
+    for _ in range(3):
+        b_dev.copy_(torch.from_numpy(b_host.numpy() * (1.0 + 1e-13 * rng.standard_normal(N))).to("cuda"))
+        tq, rq = timed("mixed", 1)
+        eq = errors(x_dev.cpu().numpy())[1]
+        spread.append({"seconds": round(tq[0], 5), "outer": rq.iterations, "inner": rq.inner_iterations,
+                       "relres_original": rq.relres_original, "rel_err_vs_exact": eq,
+                       "meets_bar": rq.flag == 0 and rq.relres_original <= TOL and eq <= 10 * TOL})
+    b_dev.copy_(b_host.to("cuda"))
     fp64_met = r_fp64.flag == 0 and r_fp64.relres_original <= TOL
     mixed_met = r_mixed.flag == 0 and r_mixed.relres_original <= TOL and err_mixed <= 10 * TOL
 
@@ -346,12 +359,15 @@ def run_ours(args, rank, world, dist):
         "speedup_mixed_vs_fp64": (round(statistics.mean(t_fp64) / value, 3) if fp64_met and mixed_met
                                   else None),
         "bar": "relres_original <= 1e-8 and ||x - x_ref|| <= 10 tol ||x_ref|| (x_ref: FP64 to 1e-11)",
+        "mixed_perturbed_rhs": {"runs": spread,
+                                "mean_seconds_4rhs": round((value + sum(q["seconds"] for q in spread)) / 4, 5),
+                                "what": "b (value) and b (1 + 1e-13 xi_k), k = 1..3; error against x = 1"},
         "spmv": {"stencil_fp32_chain_ms_per_product": ms_prod32, "stencil_fp32_ms_per_launch": ms_launch32,
                  "stencil_fp32_GBps": round(achieved, 1),
                  "stencil_fp64_chain_ms_per_product": ms_prod64, "stencil_fp64_ms_per_launch": ms_launch64,
                  "stencil_fp64_GBps": round(bytes64 / (ms_prod64 * 1e-3) / 1e9, 1),
                  "note": "fp64 stencil is bound by GB300's FP64 pipe, not by HBM"},
-        "roofline": {"bound": "hbm", "kernel": "k_stencil7_f8x2 + k_stencil7_f4 (fp32 Chebyshev(8) recurrence product)",
+        "roofline": {"bound": "hbm", "kernel": "k_stencil7_f8x2t + k_stencil7_f4 (fp32 Chebyshev(8) recurrence product)",
                      "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                      "traffic": traffic,

@@ -222,12 +222,16 @@ __device__ __forceinline__ kc64 load_cg(const kc64* p) { return kc64{load_cg(&p-
 // tail(vals) on thread 0 with the totals widened to double / c128.  Partials
 // are combined in a fixed order, so the result does not depend on block
 // scheduling.  Must be reached by every thread of every block.
+// The same for blocks of any shape with kThreads threads: tid is the
+// thread's linear index in its block, bid the block's linear index and
+// nblocks the number of blocks (<= kMaxRedBlocks).
 template <int ND, class A, class Tail>
-__device__ __forceinline__ void grid_reduce_tail(A (&acc)[ND], RedBuf rb, const Tail& tail) {
+__device__ __forceinline__ void grid_reduce_tail_at(A (&acc)[ND], RedBuf rb, const Tail& tail, int tid, int bid,
+                                                    int nblocks) {
   using W = decltype(acc_value(acc[0]));
   __shared__ A sh[kThreads / 32][ND];
   __shared__ bool is_last;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int lane = tid & 31, wid = tid >> 5;
 #pragma unroll
   for (int d = 0; d < ND; ++d) warp_reduce(acc[d]);
   if (lane == 0) {
@@ -236,16 +240,16 @@ __device__ __forceinline__ void grid_reduce_tail(A (&acc)[ND], RedBuf rb, const 
   }
   __syncthreads();
   A* part = reinterpret_cast<A*>(rb.partials);
-  if (threadIdx.x < ND) {
-    A t = sh[0][threadIdx.x];
-    for (int w = 1; w < kThreads / 32; ++w) acc_merge(t, sh[w][threadIdx.x]);
-    part[(size_t)blockIdx.x * ND + threadIdx.x] = t;
+  if (tid < ND) {
+    A t = sh[0][tid];
+    for (int w = 1; w < kThreads / 32; ++w) acc_merge(t, sh[w][tid]);
+    part[(size_t)bid * ND + tid] = t;
   }
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     unsigned int prev = atomicAdd(rb.ticket, 1u);
-    is_last = (prev == gridDim.x - 1);
+    is_last = (prev == (unsigned)nblocks - 1);
   }
   __syncthreads();
   if (!is_last) return;
@@ -253,7 +257,7 @@ __device__ __forceinline__ void grid_reduce_tail(A (&acc)[ND], RedBuf rb, const 
   A t[ND];
 #pragma unroll
   for (int d = 0; d < ND; ++d) acc_zero(t[d]);
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += kThreads) {
+  for (int b = tid; b < nblocks; b += kThreads) {
 #pragma unroll
     for (int d = 0; d < ND; ++d) acc_merge(t[d], load_cg(part + (size_t)b * ND + d));
   }
@@ -265,7 +269,7 @@ __device__ __forceinline__ void grid_reduce_tail(A (&acc)[ND], RedBuf rb, const 
     for (int d = 0; d < ND; ++d) sh[wid][d] = t[d];
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     W vals[ND];
 #pragma unroll
     for (int d = 0; d < ND; ++d) {
@@ -276,6 +280,11 @@ __device__ __forceinline__ void grid_reduce_tail(A (&acc)[ND], RedBuf rb, const 
     *rb.ticket = 0u;
     tail(vals);
   }
+}
+
+template <int ND, class A, class Tail>
+__device__ __forceinline__ void grid_reduce_tail(A (&acc)[ND], RedBuf rb, const Tail& tail) {
+  grid_reduce_tail_at<ND>(acc, rb, tail, (int)threadIdx.x, (int)blockIdx.x, (int)gridDim.x);
 }
 
 // Tail that does nothing (plain reductions whose result is not needed).

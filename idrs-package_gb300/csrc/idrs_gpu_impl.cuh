@@ -3,6 +3,7 @@
 #pragma once
 
 #include "idrs_gpu.cuh"
+#include "stencil_dot.cuh"
 
 namespace idrs {
 
@@ -156,8 +157,15 @@ void IdrsGpu<T>::enqueue_cycle(const T* b, T* x, const SolveOpts& o, int cycle, 
     } else {
       launch_fused<0, T>(n, BBuildU<T, W>{r, G, U, n, k, s, d_st, nullptr}, NoTail(), rb, stop, st);
     }
-    matvec(Uk, Gk, stop);
-    launch_fused_nd<T>(s, n, BPdot<T>{PT, n, Gk, s}, TIdrsMu<W>{d_st, k}, rb, stop, st);
+    // G_k = A U_k and mu = P^T G_k: on the fp32 stencil the projection is
+    // accumulated by the chain's last pass (G_k is not read back)
+    bool fused = false;
+    if constexpr (std::is_same<T, float>::value)
+      fused = prec == 32 && chain_with_pdot(A, Uk, Gk, t1, t2, t3, t4, PT, n, s, rb, TIdrsMu<W>{d_st, k}, stop, st);
+    if (!fused) {
+      matvec(Uk, Gk, stop);
+      launch_fused_nd<T>(s, n, BPdot<T>{PT, n, Gk, s}, TIdrsMu<W>{d_st, k}, rb, stop, st);
+    }
     launch_fused<1, T>(n, BIdrUpd<T, W>{G, U, n, k, r, x, d_st}, TIdrsNorm<W>{d_st, k}, rb, stop, st);
   }
   // omega step (idrs.inc:254-299)

@@ -7,6 +7,7 @@
 #include <mutex>
 
 #include "matrix.cuh"
+#include "stencil.cuh"
 #include "tma.cuh"
 
 namespace idrs {
@@ -300,38 +301,7 @@ __global__ void __launch_bounds__(256) k_stencil7(int nx, int ny, int nz, int zc
 // per point.  Needs nx % 4 == 0 and 16-byte aligned vectors (checked by the
 // launcher).  SCALE == false form: a and the centre term are folded into the
 // coefficients.
-struct St7 {
-  float c0, cw, ce, cs, cn, cf, cb;
-};
-// one point: centre product, then the six neighbours fused in a fixed order
-// (explicit FMAs, so every fp32 stencil kernel rounds identically whatever
-// contraction the compiler would pick)
-__device__ __forceinline__ float st7_point(const St7& c, float xc, float w, float e, float s, float n, float f,
-                                           float b) {
-  float r = c.c0 * xc;
-  r = fmaf(c.cw, w, r);
-  r = fmaf(c.ce, e, r);
-  r = fmaf(c.cs, s, r);
-  r = fmaf(c.cn, n, r);
-  r = fmaf(c.cf, f, r);
-  return fmaf(c.cb, b, r);
-}
-__device__ __forceinline__ float4 st7_apply(const St7& c, float4 xm, float4 xc, float4 xp, float4 xs,
-                                            float4 xn, float left, float right) {
-  float4 r;
-  r.x = st7_point(c, xc.x, left, xc.y, xs.x, xn.x, xm.x, xp.x);
-  r.y = st7_point(c, xc.y, xc.x, xc.z, xs.y, xn.y, xm.y, xp.y);
-  r.z = st7_point(c, xc.z, xc.y, xc.w, xs.z, xn.z, xm.z, xp.z);
-  r.w = st7_point(c, xc.w, xc.z, right, xs.w, xn.w, xm.w, xp.w);
-  return r;
-}
-__device__ __forceinline__ void axpy4(float4& r, float a, float4 x) {
-  r.x = fmaf(a, x.x, r.x); r.y = fmaf(a, x.y, r.y); r.z = fmaf(a, x.z, r.z); r.w = fmaf(a, x.w, r.w);
-}
-
-constexpr int kF4Rows = 8;
-
-__device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+// St7, st7_point, st7_apply, axpy4, ld4 and kF4Rows: stencil.cuh
 
 __global__ void __launch_bounds__(32 * kF4Rows, 4) k_stencil7_f4(
     int nx, int ny, int nz, int zc, float c0, float cw, float ce, float cs, float cn, float cf,
@@ -1605,6 +1575,16 @@ void op_chain_recur(const MatView& Ks, const JacobiCols& J, int degree, const T*
 }
 
 template <class T>
+const T* op_chain_recur_head(const MatView& Ks, const JacobiCols& J, int degree, const T* v, T* t1, T* t2, T* t3,
+                             T* t4, const int* skip, cudaStream_t st) {
+  if (degree == 0) return v;
+  T* buf[4] = {t1, t2, t3, t4};
+  const std::vector<ChainStep<T>> steps = recur_steps<T>(J, degree, v, buf, t4 ? 4 : 3, nullptr);
+  run_chain<T>(Ks, steps, skip, st);
+  return steps.back().out;
+}
+
+template <class T>
 void op_apply(Operator& A, int prec, const T* v, T* w, T* t1, T* t2, T* t3, T* t4, const int* skip,
               cudaStream_t st, T fa, T fcv, const T* fv) {
   const MatView& Ks = A.view(prec);
@@ -2066,6 +2046,8 @@ void operator_free(Operator* A) {
   template void spmv_ex<T>(const MatView&, const T*, T*, const Epi<T>&, const int*, cudaStream_t); \
   template void op_chain_recur<T>(const MatView&, const JacobiCols&, int, const T*, T*, T*, T*, T*, T*, \
                                   const int*, cudaStream_t, T, T, const T*);                       \
+  template const T* op_chain_recur_head<T>(const MatView&, const JacobiCols&, int, const T*, T*, T*, T*, T*, \
+                                           const int*, cudaStream_t);                                     \
   template void op_apply<T>(Operator&, int, const T*, T*, T*, T*, T*, T*, const int*, cudaStream_t, T, T, \
                             const T*);                                                             \
   template void op_chain<T>(const MatView&, const std::vector<c128>&, int, const T*, T*, T*, T*,   \

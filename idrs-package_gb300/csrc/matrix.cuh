@@ -254,6 +254,12 @@ template <class T>
 void op_apply(Operator& A, int prec, const T* v, T* w, T* t1, T* t2, T* t3, T* t4, const int* skip,
               cudaStream_t st, T fa = T(1), T fcv = T(0), const T* fv = nullptr);
 
+// every step of op_chain_recur but the last product; returns the vector
+// that product multiplies (y_{d+1}; v itself for degree 0)
+template <class T>
+const T* op_chain_recur_head(const MatView& Ks, const JacobiCols& J, int degree, const T* v, T* t1, T* t2, T* t3,
+                             T* t4, const int* skip, cudaStream_t st);
+
 // w = Ks p(Ks) v, then the final product gets the epilogue
 //   w = fa * (Ks u) + fcv * fv.
 // t1, t2: scratch vectors (length n).  alpha: polynomial coefficients (host).
