@@ -494,11 +494,15 @@ class IdrsGpu {
   IdrsState<W>* d_st = nullptr;
   int* h_stop = nullptr;  // pinned, 2 slots
   cudaEvent_t ev[2];
+  // the cycles after the first one, captured once per solve and replayed
+  cudaGraphExec_t cycle_graph = nullptr;
+  long cycle_launches = 0;
   bool p_ready = false;
   const void* p_injected = nullptr;
 
  private:
   void enqueue_cycle(const T* b, T* x, const SolveOpts& o, int cycle, bool inispace);
+  bool capture_cycle(const T* b, T* x, const SolveOpts& o, bool inispace);
   void matvec(const T* in, T* out, const int* skip, T fa = T(1), T fcv = T(0), const T* fv = nullptr);
 };
 

@@ -53,8 +53,43 @@ IdrsGpu<T>::~IdrsGpu() {
                   (void*)PT, (void*)d_st})
     if (p) cudaFreeAsync(p, st);
   if (h_stop) cudaFreeHost(h_stop);
+  if (cycle_graph) cudaGraphExecDestroy(cycle_graph);
   cudaEventDestroy(ev[0]);
   cudaEventDestroy(ev[1]);
+}
+
+// Every IDR(s) cycle after the first launches the same kernels with the same
+// arguments (fixed vectors, coefficients read from the device state, the
+// stop flag read by each kernel), so a standalone solve captures one such
+// cycle as a CUDA graph and replays it: one launch per cycle instead of one
+// per pass, which is what bounds small problems (2 MB vectors at 64^3).
+// Anything the capture cannot hold ends it with an error; the solve then
+// launches its cycles directly.  Returns whether the graph is ready.
+template <class T>
+bool IdrsGpu<T>::capture_cycle(const T* b, T* x, const SolveOpts& o, bool inispace) {
+  if (cycle_graph) return true;
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const long l0 = launch_count();
+  bool ok = true;
+  try {
+    enqueue_cycle(b, x, o, 1, inispace);
+  } catch (const cuda_error&) {
+    ok = false;
+  }
+  const cudaError_t e = cudaStreamEndCapture(st, &g);
+  if (!ok || e != cudaSuccess || !g || cudaGraphInstantiate(&cycle_graph, g, 0) != cudaSuccess) {
+    cudaGetLastError();
+    if (g) cudaGraphDestroy(g);
+    cycle_graph = nullptr;
+    return false;
+  }
+  cudaGraphDestroy(g);
+  cycle_launches = launch_count() - l0;
+  return true;
 }
 
 template <class T>
@@ -121,8 +156,20 @@ void IdrsGpu<T>::solve(const T* b, T* x, const SolveOpts& o) {
   // stop flag of cycle c-1, so the GPU never waits for the host.  An inner
   // solve polls too (its outer iteration waits for its result anyway) so that
   // it launches no cycles beyond the one after convergence.
+  const bool lu = A.P && (A.P->which_precon == 2 || A.P->which_precon == 3);
+  bool graphs = !o.inner && !(o.M1 && o.M1->dkind != 0) && !lu && !(A.defl && A.defl->k > 0);
+  if (cycle_graph) {
+    cudaGraphExecDestroy(cycle_graph);  // captured for another solve's vectors
+    cycle_graph = nullptr;
+  }
   for (int c = 0; c < max_cycles; ++c) {
-    enqueue_cycle(b, x, o, c, inispace);
+    if (c >= 1 && graphs) graphs = capture_cycle(b, x, o, inispace);
+    if (c >= 1 && graphs) {
+      IDRS_CUDA(cudaGraphLaunch(cycle_graph, st));
+      for (long q = 0; q < cycle_launches; ++q) count_launch();
+    } else {
+      enqueue_cycle(b, x, o, c, inispace);
+    }
     IDRS_CUDA(cudaMemcpyAsync(&h_stop[c & 1], stop, sizeof(int), cudaMemcpyDeviceToHost, st));
     IDRS_CUDA(cudaEventRecord(ev[c & 1], st));
     if (c >= 1) {

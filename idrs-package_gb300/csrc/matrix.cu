@@ -622,7 +622,7 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
   uint64_t* mbX = reinterpret_cast<uint64_t*>(sm);
   uint64_t* mbU = mbX + kT8XStages;
   volatile int* sflag = reinterpret_cast<volatile int*>(sm + 64);
-  const long rstride = (long)kX8Halo * nx;  // one stage / ring slot
+  const int rstride = kX8Halo * nx;  // one stage / ring slot (floats)
   float* Xs = reinterpret_cast<float*>(sm + 128);
   float* Us = Xs + kT8XStages * rstride;
   float* Vs = Us + kT8UStages * rstride;
@@ -634,31 +634,46 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
   const bool lact = lane <= L;
   const bool act = lact && j >= 0 && j < ny;
   const bool interior = act && ty >= 1 && ty <= kX8Rows;
+  const bool has_s = act && j > 0, has_n = act && j + 1 < ny;
   const long plane = (long)nx * ny;
   const int r0 = max(j0 - 1, 0), r1 = min(j0 + kX8Rows, ny - 1);
   const unsigned rbytes = (unsigned)((r1 - r0 + 1) * nx * 4);
-  const long roff = (long)(r0 - (j0 - 1)) * nx;
+  const int roff = (r0 - (j0 - 1)) * nx;
   const bool have_uv = (u != nullptr) || (v != nullptr);
   // planes of the stage sequences: xin zb .. z1+1, u / v zb .. z1, inside the
   // grid, copied and waited for in order from qa
   const int qa = max(zb, 0);
-  auto x_ok = [&](int q) { return q >= qa && q < nz && q <= z1 + 1; };
-  auto u_ok = [&](int q) { return have_uv && q >= qa && q < nz && q <= z1; };
-  // the halo warps' outer neighbour row (ty 0: j-1, ty 9: j+1) of plane q
+  const int xlast = min(nz - 1, z1 + 1), ulast = have_uv ? min(nz - 1, z1) : qa - 1;
+  // this thread's element in every stage and ring slot (row ty, first half)
+  const int toff = ty * nx + i0;
+  float* const X0 = Xs + toff;
+  float* const X1 = X0 + rstride;
+  float* const X2 = X1 + rstride;
+  const float* const U0 = Us + toff;
+  const float* const U1 = U0 + rstride;
+  const float* const V0 = Vs + toff;
+  const float* const V1 = V0 + rstride;
+  float* const A0 = sA + toff;
+  auto xslot = [&](int s) { return s == 0 ? X0 : (s == 1 ? X1 : X2); };
+  auto aslot = [&](int q) { return A0 + ((q - zb) & (kT8ARing - 1)) * rstride; };
+  // global streams of this thread, advanced one plane per iteration
+  const long goff = (long)j * nx + i0;
+  const float* gvb = vb ? vb + (long)(zb - 1) * plane + goff : nullptr;  // vb(zp-1)
+  float* gya = ya ? ya + (long)zb * plane + goff : nullptr;              // ya(zp)
+  float* gyb = yb + (long)(zb - 1) * plane + goff;                        // yb(zp-1)
+  // the halo warps' outer neighbour row (ty 0: j-1, ty 9: j+1)
   const int hrow = ty == 0 ? j - 1 : j + 1;
   const bool hact = lact && j >= 0 && j < ny && (ty == 0 || ty == kX8Halo - 1) && hrow >= 0 && hrow < ny;
-  auto ld_halo = [&](int q) -> F8 {
-    return (hact && q >= 0 && q < nz) ? ld8hg(xin + (long)q * plane + (long)hrow * nx, i0, hx) : zero8();
-  };
+  const float* ghalo = hact ? xin + (long)zb * plane + (long)hrow * nx + i0 : xin;  // plane zp
   int ix = 0, iu = 0;  // thread 0: next stage to fill
   auto issueX = [&](int q) {
-    if (!x_ok(q)) return;
+    if (q < qa || q > xlast) return;
     mbar_expect_tx(&mbX[ix], rbytes);
     bulk_g2s(Xs + ix * rstride + roff, xin + q * plane + (long)r0 * nx, rbytes, &mbX[ix]);
     ix = next_slot(ix, kT8XStages);
   };
   auto issueU = [&](int q) {
-    if (!u_ok(q)) return;
+    if (q < qa || q > ulast) return;
     mbar_expect_tx(&mbU[iu], (u ? rbytes : 0u) + (v ? rbytes : 0u));
     if (u) bulk_g2s(Us + iu * rstride + roff, u + q * plane + (long)r0 * nx, rbytes, &mbU[iu]);
     if (v) bulk_g2s(Vs + iu * rstride + roff, v + q * plane + (long)r0 * nx, rbytes, &mbU[iu]);
@@ -666,19 +681,22 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
   };
   int wx = 0, wu = 0;          // next stage to wait for
   unsigned phx = 0, phu = 0;   // expected phase parity of each stage (bit s)
+  auto wait_on = [&](uint64_t* bar, unsigned par) {
+    if (mbar_try_wait(bar, par)) return;
+    if (!*sflag && !mbar_wait_sleep(bar, par)) *sflag = 1;
+  };
   auto waitX = [&](int q) {
-    if (!x_ok(q)) return;
-    if (!*sflag && !mbar_wait_sleep(&mbX[wx], (phx >> wx) & 1u)) *sflag = 1;
+    if (q < qa || q > xlast) return;
+    wait_on(&mbX[wx], (phx >> wx) & 1u);
     phx ^= 1u << wx;
     wx = next_slot(wx, kT8XStages);
   };
   auto waitU = [&](int q) {
-    if (!u_ok(q)) return;
-    if (!*sflag && !mbar_wait_sleep(&mbU[wu], (phu >> wu) & 1u)) *sflag = 1;
+    if (q < qa || q > ulast) return;
+    wait_on(&mbU[wu], (phu >> wu) & 1u);
     phu ^= 1u << wu;
     wu = next_slot(wu, kT8UStages);
   };
-  auto arow = [&](int q, int r) { return sA + ((q - zb) & (kT8ARing - 1)) * rstride + (long)r * nx; };
   if (tid == 0) {
     for (int s = 0; s < kT8XStages; ++s) mbar_init(&mbX[s], 1);
     for (int s = 0; s < kT8UStages; ++s) mbar_init(&mbU[s], 1);
@@ -691,11 +709,13 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
   __syncthreads();
   const F8 z8 = zero8();
   // stage slots of xin(zp), xin(zp+1) and u / v(zp) for the reads
-  int rx1 = zb + 1 - qa;                      // 0 or 1
-  int rx0 = rx1 == 0 ? kT8XStages - 1 : 0;    // plane zb (unused when zb < 0)
+  int rx1 = zb + 1 - qa;                    // 0 or 1
+  int rx0 = rx1 == 0 ? kT8XStages - 1 : 0;  // plane zb (unused when zb < 0)
   int ru = 0;
-  F8 xm = (act && zb - 1 >= 0) ? ld8hg(xin + (long)(zb - 1) * plane + (long)j * nx, i0, hx) : z8;
-  F8 hcur = ld_halo(zb);
+  F8 xm = (act && zb - 1 >= 0) ? ld8hg(xin + (long)(zb - 1) * plane + goff - i0, i0, hx) : z8;
+  F8 hcur = (hact && zb >= 0) ? ld8hg(ghalo, 0, hx) : z8;
+  if (zb == qa) waitX(zb);
+  F8 xc = (act && zb >= 0) ? ld8h(xslot(rx0), 0, hx) : z8;  // xin(zp), carried in registers
   for (int zp = zb; zp <= z1; ++zp) {
     if (tid == 0) {
       proxy_async_fence();  // the reads of the refilled stages were before the last barrier
@@ -703,71 +723,74 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
       issueU(zp + 1);
     }
     const bool doB = zp - 1 >= z0;
-    const F8 vbz = (vb && interior && doB) ? ld8hg(vb + (long)(zp - 1) * plane + (long)j * nx, i0, hx) : z8;
-    const F8 hnext = ld_halo(zp + 1);
-    if (zp == zb) waitX(zp);
+    const F8 vbz = (gvb && interior && doB) ? ld8hg(gvb, 0, hx) : z8;
+    ghalo += plane;
+    const F8 hnext = (hact && zp + 1 < nz) ? ld8hg(ghalo, 0, hx) : z8;
     waitX(zp + 1);
     waitU(zp);
+    // xin(zp+1): this step's upper z-neighbour and the next plane's centre
+    // (loaded also when step A is outside the grid, zp = -1)
+    const F8 xp = (act && zp + 1 >= qa && zp + 1 <= xlast) ? ld8h(xslot(rx1), 0, hx) : z8;
     // step A at plane zp
-    F8 r = z8, xc = z8;
+    F8 r = z8;
     if (zp >= 0 && zp < nz) {  // uniform over the block
-      const float* X0 = Xs + rx0 * rstride;
-      xc = act ? ld8h(X0 + (long)ty * nx, i0, hx) : z8;
-      const F8 xp = (act && x_ok(zp + 1)) ? ld8h(Xs + rx1 * rstride + (long)ty * nx, i0, hx) : z8;
+      const float* Xc = xslot(rx0);
       F8 xs = z8, xn = z8;
-      if (act) {
-        if (ty == 0) xs = hcur;
-        else if (j > 0) xs = ld8h(X0 + (long)(ty - 1) * nx, i0, hx);
-        if (ty == kX8Halo - 1) xn = hcur;
-        else if (j + 1 < ny) xn = ld8h(X0 + (long)(ty + 1) * nx, i0, hx);
-      }
+      if (ty == 0) xs = hcur;
+      else if (has_s) xs = ld8h(Xc - nx, 0, hx);
+      if (ty == kX8Halo - 1) xn = hcur;
+      else if (has_n) xn = ld8h(Xc + nx, 0, hx);
       const XNb nb = x_neighbours(xc, lane, L);
       if (act) {
         r = st7_apply8h(ca, xm, xc, xp, xs, xn, nb);
-        if (u) axpy8(r, cua, ld8h(Us + ru * rstride + (long)ty * nx, i0, hx));
-        if (v) axpy8(r, cva, ld8h(Vs + ru * rstride + (long)ty * nx, i0, hx));
-        if (ya && interior && zp >= z0 && zp < z1) st8h(ya + (long)zp * plane + (long)j * nx, i0, hx, r);
+        if (u) axpy8(r, cua, ld8h(ru ? U1 : U0, 0, hx));
+        if (v) axpy8(r, cva, ld8h(ru ? V1 : V0, 0, hx));
+        if (gya && interior && zp >= z0 && zp < z1) st8h(gya, 0, hx, r);
       }
     }
-    if (lact) st8h(arow(zp, ty), i0, hx, r);
+    if (lact) st8h(aslot(zp), 0, hx, r);
     __syncthreads();
     // step B at plane zp-1 from yA(zp-2 .. zp) and xin(zp-1) (= xm); step A
     // of the next plane writes the ring slot of zp-3, which nothing reads now
     if (doB) {
-      const int zq = zp - 1;
-      const F8 bc = interior ? ld8h(arow(zq, ty), i0, hx) : z8;
+      const float* Aq = aslot(zp - 1);
+      const F8 bc = interior ? ld8h(Aq, 0, hx) : z8;
       const XNb nb = x_neighbours(bc, lane, L);
       if (interior) {
-        F8 rb = st7_apply8h(cb, ld8h(arow(zq - 1, ty), i0, hx), bc, ld8h(arow(zp, ty), i0, hx),
-                            ld8h(arow(zq, ty - 1), i0, hx), ld8h(arow(zq, ty + 1), i0, hx), nb);
+        F8 rb = st7_apply8h(cb, ld8h(aslot(zp - 2), 0, hx), bc, ld8h(aslot(zp), 0, hx), ld8h(Aq - nx, 0, hx),
+                            ld8h(Aq + nx, 0, hx), nb);
         axpy8(rb, cub, xm);
         if (vb) axpy8(rb, cvb, vbz);
-        st8h(yb + (long)zq * plane + (long)j * nx, i0, hx, rb);
+        st8h(gyb, 0, hx, rb);
       }
     }
     xm = xc;
+    xc = xp;
     hcur = hnext;
     rx0 = rx1;
     rx1 = next_slot(rx1, kT8XStages);
-    if (u_ok(zp)) ru = next_slot(ru, kT8UStages);
+    if (zp >= qa && zp <= ulast) ru ^= 1;
+    if (gvb) gvb += plane;
+    if (gya) gya += plane;
+    gyb += plane;
   }
   __syncthreads();  // every wait is behind: the flag is final and the same for all threads
   if (*sflag) {
     // a copy never landed: let the last copy of every stage finish (bounded),
     // then poison this block's outputs and report
     if (tid == 0) {
-      for (int q = z1 + 1, c = 0; q >= qa && c < kT8XStages; --q)
-        if (x_ok(q)) mbar_wait(&mbX[(q - qa) % kT8XStages], ((q - qa) / kT8XStages) & 1), ++c;
-      for (int q = z1, c = 0; q >= qa && c < kT8UStages; --q)
-        if (u_ok(q)) mbar_wait(&mbU[(q - qa) % kT8UStages], ((q - qa) / kT8UStages) & 1), ++c;
+      for (int q = xlast, c = 0; q >= qa && c < kT8XStages; --q, ++c)
+        mbar_wait(&mbX[(q - qa) % kT8XStages], ((q - qa) / kT8XStages) & 1);
+      for (int q = ulast, c = 0; q >= qa && c < kT8UStages; --q, ++c)
+        mbar_wait(&mbU[(q - qa) % kT8UStages], ((q - qa) / kT8UStages) & 1);
       *(volatile int*)fault = 1;
     }
     const float qn = nanf("");
     const F8 nan8 = F8{make_float4(qn, qn, qn, qn), make_float4(qn, qn, qn, qn)};
     if (interior)
       for (int z = z0; z < z1; ++z) {
-        st8h(yb + (long)z * plane + (long)j * nx, i0, hx, nan8);
-        if (ya) st8h(ya + (long)z * plane + (long)j * nx, i0, hx, nan8);
+        st8h(yb + (long)z * plane + goff, 0, hx, nan8);
+        if (ya) st8h(ya + (long)z * plane + goff, 0, hx, nan8);
       }
   }
 }

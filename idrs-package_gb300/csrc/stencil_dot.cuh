@@ -48,17 +48,22 @@ __global__ void __launch_bounds__(32 * kF4Rows) k_stencil7_f4_dot(int nx, int ny
     float right = __shfl_down_sync(0xffffffffu, xc.x, 1);
     if (lane == 0) left = (in && i0 > 0) ? __ldg(x + p - 1) : 0.f;
     if (lane == 31) right = (in && i0 + 4 < nx) ? __ldg(x + p + 4) : 0.f;
+    // the shadow rows of this quad, requested before the stencil arithmetic
+    float4 q[ND];
+#pragma unroll
+    for (int d = 0; d < ND; ++d) q[d] = (in && d < nd) ? ld4(PT + d * ld + p) : zero;
     if (in) {
       const float4 r = st7_apply(c, xm, xc, xp, xs, xn, left, right);
       *reinterpret_cast<float4*>(y + p) = r;
+      // every product added to the compensated accumulator, as in the
+      // separate pass (the projection's accuracy steers the fp32 IDR(s))
 #pragma unroll
       for (int d = 0; d < ND; ++d)
         if (d < nd) {
-          const float4 q = ld4(PT + d * ld + p);
-          acc_add(acc[d], q.x * r.x);
-          acc_add(acc[d], q.y * r.y);
-          acc_add(acc[d], q.z * r.z);
-          acc_add(acc[d], q.w * r.w);
+          acc_add(acc[d], q[d].x * r.x);
+          acc_add(acc[d], q[d].y * r.y);
+          acc_add(acc[d], q[d].z * r.z);
+          acc_add(acc[d], q[d].w * r.w);
         }
     }
     xm = xc;
