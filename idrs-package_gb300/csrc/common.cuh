@@ -168,6 +168,7 @@ struct cuda_error {
                                                      __FILE__ ":" + std::to_string(__LINE__)}; \
   } while (0)
 void count_launch();
+void uncount_launches(long k);  // launches that were captured into a graph, not run
 long launch_count();
 #define IDRS_LAUNCH_CHECK()   \
   do {                        \

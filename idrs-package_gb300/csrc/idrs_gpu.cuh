@@ -494,9 +494,12 @@ class IdrsGpu {
   IdrsState<W>* d_st = nullptr;
   int* h_stop = nullptr;  // pinned, 2 slots
   cudaEvent_t ev[2];
-  // the cycles after the first one, captured once per solve and replayed
+  // the cycles after the first one, captured once per solve and replayed;
+  // an inner solver keeps the graph for the next inner solve into the same x
+  // (its operator and work vectors do not change during the outer solve)
   cudaGraphExec_t cycle_graph = nullptr;
   long cycle_launches = 0;
+  const T* graph_x = nullptr;
   bool p_ready = false;
   const void* p_injected = nullptr;
 

@@ -60,11 +60,23 @@ IdrsGpu<T>::~IdrsGpu() {
 
 // Every IDR(s) cycle after the first launches the same kernels with the same
 // arguments (fixed vectors, coefficients read from the device state, the
-// stop flag read by each kernel), so a standalone solve captures one such
-// cycle as a CUDA graph and replays it: one launch per cycle instead of one
-// per pass, which is what bounds small problems (2 MB vectors at 64^3).
+// stop flag read by each kernel), so a solve captures one such cycle as a
+// CUDA graph and replays it: one launch per cycle instead of one per pass,
+// which is what bounds small problems (2 MB vectors at 64^3).  The inner
+// solves of a flexible QMRIDR(s) all write the same x, so the graph captured
+// by the first one serves the whole outer solve.
 // Anything the capture cannot hold ends it with an error; the solve then
 // launches its cycles directly.  Returns whether the graph is ready.
+// IDRS_CYCLE_GRAPHS=0 in the environment launches every cycle directly
+// (read once per process; for comparisons)
+inline bool cycle_graphs_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("IDRS_CYCLE_GRAPHS");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 template <class T>
 bool IdrsGpu<T>::capture_cycle(const T* b, T* x, const SolveOpts& o, bool inispace) {
   if (cycle_graph) return true;
@@ -81,6 +93,8 @@ bool IdrsGpu<T>::capture_cycle(const T* b, T* x, const SolveOpts& o, bool inispa
     ok = false;
   }
   const cudaError_t e = cudaStreamEndCapture(st, &g);
+  const long captured = launch_count() - l0;
+  uncount_launches(captured);  // captured, not run: each replay counts them
   if (!ok || e != cudaSuccess || !g || cudaGraphInstantiate(&cycle_graph, g, 0) != cudaSuccess) {
     cudaGetLastError();
     if (g) cudaGraphDestroy(g);
@@ -88,7 +102,8 @@ bool IdrsGpu<T>::capture_cycle(const T* b, T* x, const SolveOpts& o, bool inispa
     return false;
   }
   cudaGraphDestroy(g);
-  cycle_launches = launch_count() - l0;
+  cycle_launches = captured;
+  graph_x = x;
   return true;
 }
 
@@ -157,8 +172,8 @@ void IdrsGpu<T>::solve(const T* b, T* x, const SolveOpts& o) {
   // solve polls too (its outer iteration waits for its result anyway) so that
   // it launches no cycles beyond the one after convergence.
   const bool lu = A.P && (A.P->which_precon == 2 || A.P->which_precon == 3);
-  bool graphs = !o.inner && !(o.M1 && o.M1->dkind != 0) && !lu && !(A.defl && A.defl->k > 0);
-  if (cycle_graph) {
+  bool graphs = cycle_graphs_enabled() && !(o.M1 && o.M1->dkind != 0) && !lu && !(A.defl && A.defl->k > 0);
+  if (cycle_graph && !(o.inner && graphs && x == graph_x)) {
     cudaGraphExecDestroy(cycle_graph);  // captured for another solve's vectors
     cycle_graph = nullptr;
   }

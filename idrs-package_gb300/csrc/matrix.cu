@@ -18,6 +18,7 @@ namespace idrs {
 static thread_local std::string g_error;
 static std::atomic<long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void uncount_launches(long k) { g_launches.fetch_sub(k, std::memory_order_relaxed); }
 long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 void set_error(const std::string& msg) { g_error = msg; }
 const char* last_error() { return g_error.c_str(); }
@@ -612,12 +613,16 @@ __device__ __forceinline__ F8 st7_apply8h(const St7& c, const F8& xm, const F8& 
 }
 __device__ __forceinline__ int next_slot(int s, int n) { return s + 1 == n ? 0 : s + 1; }
 
+// NXC: the row length as a compile-time constant (0: nx at run time), so the
+// row, half-row and slot offsets of the common 256-point rows are immediates
+template <int NXC>
 __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
-    int nx, int ny, int nz, int zc, St7 ca, float cua, float cva, St7 cb, float cub, float cvb,
+    int nx_rt, int ny, int nz, int zc, St7 ca, float cua, float cva, St7 cb, float cub, float cvb,
     const float* __restrict__ xin, const float* __restrict__ u, const float* __restrict__ v,
     const float* __restrict__ vb, float* __restrict__ ya, float* __restrict__ yb,
     const int* __restrict__ skip, int* fault) {
   if (skip && *skip) return;
+  const int nx = NXC ? NXC : nx_rt;
   extern __shared__ __align__(128) unsigned char sm[];
   uint64_t* mbX = reinterpret_cast<uint64_t*>(sm);
   uint64_t* mbU = mbX + kT8XStages;
@@ -1415,7 +1420,9 @@ static int f8x2t_resident(int nx) {
   if (dev == cache_dev && nx == cache_nx) return cache_r;
   const uint64_t bit = dev < 64 ? uint64_t(1) << dev : 0;
   if (!bit || !(attr_set.load() & bit)) {
-    if (cudaFuncSetAttribute(k_stencil7_f8x2t, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_stencil7_f8x2t<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)t8_smem(kX2MaxNx)) != cudaSuccess ||
+        cudaFuncSetAttribute(k_stencil7_f8x2t<kX2MaxNx>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)t8_smem(kX2MaxNx)) != cudaSuccess) {
       cudaGetLastError();
       return 0;
@@ -1423,7 +1430,8 @@ static int f8x2t_resident(int nx) {
     attr_set.fetch_or(bit);
   }
   int r = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_stencil7_f8x2t, 32 * kX8Halo, t8_smem(nx)) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &r, nx == kX2MaxNx ? k_stencil7_f8x2t<kX2MaxNx> : k_stencil7_f8x2t<0>, 32 * kX8Halo, t8_smem(nx)) !=
       cudaSuccess) {
     cudaGetLastError();
     r = 0;
@@ -1485,7 +1493,8 @@ static void run_chain(const MatView& Ks, const std::vector<ChainStep<T>>& steps,
           const int zc = (int)std::max(4L, ((long)Ks.nz + chunks - 1) / chunks);
           dim3 blk(32, kX8Halo, 1);
           dim3 grid((Ks.ny + kX8Rows - 1) / kX8Rows, (Ks.nz + zc - 1) / zc, 1);
-          k_stencil7_f8x2t<<<grid, blk, t8_smem(Ks.nx), st>>>(
+          auto kern = Ks.nx == kX2MaxNx ? k_stencil7_f8x2t<kX2MaxNx> : k_stencil7_f8x2t<0>;
+          kern<<<grid, blk, t8_smem(Ks.nx), st>>>(
               Ks.nx, Ks.ny, Ks.nz, zc, st7_of(Ks, A.e.a, A.e.cx), A.e.u ? A.e.cu : 0.f,
               A.e.v ? A.e.cv : 0.f, st7_of(Ks, B.e.a, B.e.cx), B.e.u ? B.e.cu : 0.f, B.e.v ? B.e.cv : 0.f,
               A.in, A.e.u, A.e.v, B.e.v, need ? A.out : nullptr, B.out, skip, device_fault_word());
