@@ -51,6 +51,7 @@ _PROTOS = {
     "idrs_last_error": (C.c_char_p, []),
     "idrs_version": (_i, []),
     "idrs_launch_count": (C.c_long, []),
+    "idrs_pp_struct_size": (C.c_long, [_i]),
     "idrs_crs_format": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp]),
     "idrs_coo_format": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "idrs_cds_format": (_i, [_i, _i, _i, _vp, _vp, _vp]),
@@ -139,7 +140,8 @@ class PPOptions(C.Structure):
                 ("in_s", C.c_int), ("in_it", C.c_int), ("in_tol", C.c_double),
                 ("preconditioner", C.c_int), ("degree", C.c_int), ("n_ritz", C.c_int),
                 ("inner_precision", C.c_int), ("device_pointers", C.c_int),
-                ("n_omega", C.c_int), ("recycle", C.c_int), ("poly_eval", C.c_int)]
+                ("n_omega", C.c_int), ("recycle", C.c_int), ("poly_eval", C.c_int),
+                ("fp64_check_tol", C.c_double)]
 
 
 class PPReport(C.Structure):
@@ -151,7 +153,9 @@ class PPReport(C.Structure):
                 ("inner_iterations", C.c_int), ("inner_max", C.c_int),
                 ("recycle_flag", C.c_int), ("recycle_iterations", C.c_int),
                 ("recycle_relres", C.c_double), ("foci_imag", C.c_double * 2),
-                ("center_imag", C.c_double)]
+                ("center_imag", C.c_double), ("rel_err_vs_fp64", C.c_double),
+                ("fp64_relres_original", C.c_double), ("fp64_flag", C.c_int),
+                ("fp64_iterations", C.c_int), ("seconds_fp64_check", C.c_double)]
 
 
 class PPInputs(C.Structure):
@@ -590,11 +594,31 @@ def IDRS(A: Matrix, b, s, M1: Matrix | None = None, tolerance=None, maximum_iter
     return r
 
 
+def _rel_err(x, xr):
+    """||x - xr|| / ||xr|| (per column of a multishift x)."""
+    return np.linalg.norm(x - xr, axis=0) / np.linalg.norm(xr, axis=0)
+
+
+def _is_mixed(inner_iterations, inner_precision):
+    return bool(inner_iterations) and inner_iterations > 0 and inner_precision == 32
+
+
+def _check_maxit(maxit, n):
+    """Iteration bound of the FP64 check solve: a mixed call's bound counts
+    outer iterations, so the check gets at least min(2n, 5000)."""
+    return max(maxit or 0, min(2 * n, 5000))
+
+
 def QMRIDR(A: Matrix, b, s, M1: Matrix | None = None, tolerance=None, maximum_iterations=None,
            inner_s=None, inner_tolerance=None, inner_iterations=None, x0=None, omega=None,
-           resvec=False, inner_precision=None) -> Result:
+           resvec=False, inner_precision=None, fp64_check=None) -> Result:
     """x = QMRIDR(A, b, s, ...) (RQMRIDR/CQMRIDR, idrs_module.f90:253-408).
-    inner_precision=32 runs the inner IDR(inner_s) in fp32 / complex64."""
+    inner_precision=32 runs the inner IDR(inner_s) in fp32 / complex64.
+
+    fp64_check (see fp64_check_tolerance; by default on for the mixed form)
+    adds rel_err_vs_fp64 = ||x - x64|| / ||x64||, x64 the FP64 QMRIDR(s)
+    solution of the same system (no inner solves) at the check's tolerance,
+    with its fp64_flag and fp64_iterations."""
     b = _solver_common(A, b)
     n = len(b)
     maxit = maximum_iterations if maximum_iterations is not None else min(2 * n, 1000)
@@ -612,6 +636,12 @@ def QMRIDR(A: Matrix, b, s, M1: Matrix | None = None, tolerance=None, maximum_it
     r = Result(x=x, flag=flag.value, relres=relres.value, iterations=iters.value)
     if rv is not None:
         r["resvec"] = rv
+    tc = fp64_check_tolerance(1e-6 if tolerance is None else tolerance, fp64_check,
+                              _is_mixed(inner_iterations, inner_precision))
+    if tc > 0:
+        q = QMRIDR(A, b, s, M1=M1, tolerance=tc, maximum_iterations=_check_maxit(maximum_iterations, n),
+                   omega=omega, inner_iterations=0, fp64_check=False)
+        r.update(rel_err_vs_fp64=float(_rel_err(x, q.x)), fp64_flag=q.flag, fp64_iterations=q.iterations)
     return r
 
 
@@ -667,10 +697,12 @@ def MSIDRS(A: Matrix, b, sigma, s, M1: Matrix | None = None, tolerance=None,
 
 def MSQMRIDR(A: Matrix, b, sigma, s, M1: Matrix | None = None, tolerance=None,
              maximum_iterations=None, inner_s=None, inner_tolerance=None,
-             inner_iterations=None, omega=None, resvec=False, inner_precision=None) -> Result:
+             inner_iterations=None, omega=None, resvec=False, inner_precision=None,
+             fp64_check=None) -> Result:
     """x(:, k) = MSQMRIDR(A, b, sigma, s, ...) (RMSQMRIDR/CMSQMRIDR,
     idrs_module.f90:410-570).  inner_precision=32 runs the inner MSIDRS in
-    fp32 / complex64."""
+    fp32 / complex64.  fp64_check as in QMRIDR: rel_err_vs_fp64 per shift
+    against the FP64 MSQMRIDR(s) solutions (no inner solves)."""
     b = _solver_common(A, b)
     n = len(b)
     sig = _shifts(A, sigma)
@@ -690,6 +722,12 @@ def MSQMRIDR(A: Matrix, b, sigma, s, M1: Matrix | None = None, tolerance=None,
     r = Result(x=x, flag=flag.value, relres=relres, iterations=iters.value)
     if rv is not None:
         r["resvec"] = rv
+    tc = fp64_check_tolerance(1e-6 if tolerance is None else tolerance, fp64_check,
+                              _is_mixed(inner_iterations, inner_precision))
+    if tc > 0:
+        q = MSQMRIDR(A, b, sig, s, M1=M1, tolerance=tc, maximum_iterations=_check_maxit(maximum_iterations, n),
+                     omega=omega, inner_iterations=0, fp64_check=False)
+        r.update(rel_err_vs_fp64=_rel_err(x, q.x), fp64_flag=q.flag, fp64_iterations=q.iterations)
     return _shift_masks(r, tolerance)
 
 
@@ -781,10 +819,32 @@ def IDRS_RITZ(A: Matrix, b, s, M: Matrix | None = None, tolerance=None, maximum_
     return r
 
 
+def fp64_check_tolerance(tol, fp64_check, mixed, dev=False):
+    """The tolerance of the FP64 solve that a result's relative error is
+    measured against (0.0: no check).  fp64_check: None (default) checks every
+    mixed-precision result (fp32 / complex64 inner solves) of a call with host
+    arrays; True checks any result; False none; a float is the tolerance
+    itself.  The default tolerance is tol * 1e-3 (at least 1e-14), tight
+    enough that the FP64 solution's own error is small beside the 10 tol
+    that a mixed result may differ from it."""
+    if fp64_check is None:
+        fp64_check = bool(mixed) and not dev
+    if fp64_check is False:
+        return 0.0
+    if fp64_check is True:
+        return max(float(tol) * 1e-3, 1e-14)
+    t = float(fp64_check)
+    if not t > 0.0:
+        raise IDRSError(IDRS_ERR_ARG, "fp64_check must be None, a bool or a positive tolerance")
+    return t
+
+
 def _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
-                inner_precision, dev, n_omega, recycle, poly_eval=POLY_HORNER):
+                inner_precision, dev, n_omega, recycle, poly_eval=POLY_HORNER, fp64_check=False):
+    mixed = method == 0 and in_it > 0 and inner_precision == 32
     return PPOptions(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
-                     inner_precision, int(dev), int(n_omega), int(bool(recycle)), int(poly_eval))
+                     inner_precision, int(dev), int(n_omega), int(bool(recycle)), int(poly_eval),
+                     fp64_check_tolerance(tol, fp64_check, mixed, dev))
 
 
 def _pp_result(rep: PPReport, **extra) -> Result:
@@ -799,7 +859,16 @@ def _pp_result(rep: PPReport, **extra) -> Result:
                   inner_solves=rep.inner_solves, inner_iterations=rep.inner_iterations,
                   inner_max=rep.inner_max, recycle_flag=rep.recycle_flag,
                   recycle_iterations=rep.recycle_iterations, recycle_relres=rep.recycle_relres,
-                  **extra)
+                  **_fp64_fields(rep), **extra)
+
+
+def _fp64_fields(rep: PPReport) -> dict:
+    """rel_err_vs_fp64 (None without a check) and the FP64 solve's record."""
+    if rep.fp64_flag < 0:
+        return dict(rel_err_vs_fp64=None)
+    return dict(rel_err_vs_fp64=rep.rel_err_vs_fp64, fp64_flag=rep.fp64_flag,
+                fp64_iterations=rep.fp64_iterations, fp64_relres_original=rep.fp64_relres_original,
+                seconds_fp64_check=rep.seconds_fp64_check)
 
 
 def _pp_kind(K, b, M, C_, seed, shift, complex_):
@@ -841,7 +910,7 @@ def _pp_cf(cplx, center, foci):
 def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=None, *, method=1,
             s=4, tol=1e-6, maxit=1000, in_s=1, in_it=0, in_tol=0.1, preconditioner=0, degree=0,
             n_ritz=32, inner_precision=64, n_omega=0, M=None, C_=None, seed=None, shift=None,
-            V=None, complex=None, x_out=None, poly_eval=0) -> Result:
+            V=None, complex=None, x_out=None, poly_eval=0, fp64_check=None) -> Result:
     """x = pp_idrs(K, b[, M, C, P, center, foci, seed, shift, V]) (RPP_IDRS / CPP_IDRS,
     pp_idrs_module.f90:64-162); the command-line options of initialize.inc:4-31
     are keyword arguments.
@@ -849,7 +918,12 @@ def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=Non
     b may be a numpy array (host) or an int device address; with a device b,
     x_out must be the device address of the solution vector.  With a host b,
     x_out may be a contiguous numpy array of b's length and kind (for
-    example pinned memory) that receives the solution."""
+    example pinned memory) that receives the solution.
+
+    fp64_check (see fp64_check_tolerance; by default on for mixed-precision
+    solves with host arrays) adds rel_err_vs_fp64 = ||x - x64|| / ||x64||
+    against an FP64 solve of the same system, with that solve's fp64_flag,
+    fp64_iterations and fp64_relres_original."""
     dev = isinstance(b, int)
     cplx = _pp_kind(K, None if dev else b, M, C_, seed, shift, complex)
     if dev:
@@ -866,7 +940,7 @@ def PP_IDRS(K: UserMatrix, b, P: UserMatrix | None = None, center=None, foci=Non
         else:
             raise ValueError("x_out must be a writeable contiguous array of b's length and kind")
     o = _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
-                    inner_precision, dev, n_omega, False, poly_eval)
+                    inner_precision, dev, n_omega, False, poly_eval, fp64_check)
     rep = PPReport()
     keep = []
     c, f = _pp_cf(cplx, center, foci)
@@ -881,7 +955,7 @@ def PP_MR_IDRS(K: UserMatrix, b_all, P: UserMatrix | None = None, center=None, f
                method=1, s=4, tol=1e-6, maxit=1000, in_s=1, in_it=0, in_tol=0.1,
                preconditioner=0, degree=0, n_ritz=32, inner_precision=64, n_omega=0,
                recycle=False, M=None, C_=None, seed=None, shift=None, V=None, complex=None,
-               nrhs=None, x_out=None, poly_eval=0) -> Result:
+               nrhs=None, x_out=None, poly_eval=0, fp64_check=None) -> Result:
     """x_all = pp_idrs(K, b_all[, M, C, P, center, foci, seed, shift, V]) for a sequence
     of right-hand sides (RPP_MR_IDRS / CPP_MR_IDRS, pp_idrs_module.f90:164-279,
     recycle.inc, run_mr_idrs.inc).
@@ -889,7 +963,8 @@ def PP_MR_IDRS(K: UserMatrix, b_all, P: UserMatrix | None = None, center=None, f
     b_all: n x nrhs numpy array, or the int device address of a column-major
     n x nrhs array (then nrhs and the device address x_out are required).
     Returns x (n x nrhs, host case) and per right-hand side arrays flags,
-    iterations, relres, relres_original, seconds_solve."""
+    iterations, relres, relres_original, seconds_solve (and rel_err_vs_fp64
+    with fp64_check, as in PP_IDRS)."""
     dev = isinstance(b_all, int)
     n = K.nrows
     cplx = _pp_kind(K, None if dev else b_all, M, C_, seed, shift, complex)
@@ -905,7 +980,7 @@ def PP_MR_IDRS(K: UserMatrix, b_all, P: UserMatrix | None = None, center=None, f
         nrhs = b_all.shape[1]
         x = np.zeros((n, nrhs), dtype=dt, order="F")
     o = _pp_options(method, s, tol, maxit, in_s, in_it, in_tol, preconditioner, degree, n_ritz,
-                    inner_precision, dev, n_omega, recycle, poly_eval)
+                    inner_precision, dev, n_omega, recycle, poly_eval, fp64_check)
     reps = (PPReport * nrhs)()
     keep = []
     c, f = _pp_cf(cplx, center, foci)
@@ -919,19 +994,39 @@ def PP_MR_IDRS(K: UserMatrix, b_all, P: UserMatrix | None = None, center=None, f
     r["relres"] = np.array([q.relres_solver for q in reps])
     r["relres_original"] = np.array([q.relres_original for q in reps])
     r["seconds_solve"] = np.array([q.seconds_solve for q in reps])
+    if o.fp64_check_tol > 0:
+        r["rel_err_vs_fp64"] = np.array([q.rel_err_vs_fp64 for q in reps])
+        r["fp64_flags"] = np.array([q.fp64_flag for q in reps])
     return r
 
 
 def PP_MS_IDRS(K: UserMatrix, rhs, sigma, P: UserMatrix | None = None, center=None, foci=None, *,
                method=1, s=4, tol=1e-6, maxit=1000, in_s=1, in_it=0, in_tol=0.1,
                preconditioner=0, degree=0, n_ritz=32, inner_precision=64, n_omega=0, M=None,
-               C_=None, seed=None, shift=None, V=None, complex=None) -> Result:
+               C_=None, seed=None, shift=None, V=None, complex=None, fp64_check=None) -> Result:
     """x(n, n_sigma) = pp_idrs(K, rhs, sigma[, M, C, P, center, foci, seed, shift, V])
     (RPP_MS_IDRS / CPP_MS_IDRS with run_ms_idrs.inc).  With C the block system
     is solved and x is the second half of each solution.  relres_sigma: the
     true residual of every shifted system.  A 2-D rhs (n x nrhs) runs the
     sequence form RPP_MS_MR_IDRS / CPP_MS_MR_IDRS: x is n x n_sigma x nrhs,
-    relres_sigma n_sigma x nrhs, flags and iterations per right-hand side."""
+    relres_sigma n_sigma x nrhs, flags and iterations per right-hand side.
+    fp64_check as in PP_IDRS: rel_err_vs_fp64 per shift (and right-hand side)
+    against the same pipeline in FP64 without inner solves."""
+    r = _pp_ms_idrs(K, rhs, sigma, P, center, foci, method, s, tol, maxit, in_s, in_it, in_tol,
+                    preconditioner, degree, n_ritz, inner_precision, n_omega, M, C_, seed, shift,
+                    V, complex)
+    tc = fp64_check_tolerance(tol, fp64_check, method == 0 and _is_mixed(in_it, inner_precision))
+    if tc > 0:
+        q = _pp_ms_idrs(K, rhs, sigma, P, center, foci, method, s, tc, _check_maxit(maxit, K.nrows),
+                        in_s, 0, in_tol, preconditioner, degree, n_ritz, 64, n_omega, M, C_, seed,
+                        shift, V, complex)
+        r.update(rel_err_vs_fp64=_rel_err(r.x, q.x), fp64_flag=q.flag, fp64_iterations=q.iterations)
+    return r
+
+
+def _pp_ms_idrs(K, rhs, sigma, P, center, foci, method, s, tol, maxit, in_s, in_it, in_tol,
+                preconditioner, degree, n_ritz, inner_precision, n_omega, M, C_, seed, shift, V,
+                complex):
     cplx = _pp_kind(K, rhs, M, C_, seed, shift, complex) or np.iscomplexobj(sigma)
     dt = np.complex128 if cplx else np.float64
     seq = np.ndim(rhs) == 2

@@ -954,6 +954,14 @@ int idrs_cinprod(idrs_matrix A, const double* u, const double* v, double* uv) { 
 
 const char* idrs_last_error(void) { return idrs::last_error(); }
 long idrs_launch_count(void) { return idrs::launch_count(); }
+long idrs_pp_struct_size(int which) {
+  switch (which) {
+    case 0: return (long)sizeof(idrs_pp_options);
+    case 1: return (long)sizeof(idrs_pp_report);
+    case 2: return (long)sizeof(idrs_pp_inputs);
+    default: return 0;
+  }
+}
 int idrs_version(void) { return 10000; }
 
 int idrs_crs_format(int nrows, int ncols, const int* row_ptr, const int* col_ind,
@@ -1889,6 +1897,8 @@ int pp_open(PPJob<T>& J, idrs_user_matrix K, idrs_user_matrix P, const idrs_pp_i
             bool multishift, const idrs_pp_options* opt) {
   REQUIRE(K, "pp_idrs: K is required");
   REQUIRE(opt->s >= 1, "rpp_idrs: s must be positive");
+  REQUIRE(std::isfinite(opt->fp64_check_tol) && opt->fp64_check_tol >= 0.0,
+          "pp_idrs: fp64_check_tol must be 0 (no check) or a positive tolerance");
   REQUIRE(opt->n_omega >= 0, "rpp_idrs: n_omega must not be negative");
   idrs_user_matrix M = in ? in->M : nullptr, C = in ? in->C : nullptr;
   int st = idrs_matrix_create_ext(K, M, C, P, kCplx<T> ? 1 : 0, in ? in->seed : nullptr,
@@ -2071,6 +2081,66 @@ int pp_solve(PPJob<T>& J, const T* pb, T* px, const idrs_pp_options* opt, idrs_p
   return IDRS_OK;
 }
 
+// ||x - xr|| / ||xr|| on the device (J.r is the scratch vector)
+template <class T>
+double rel_diff(PPJob<T>& J, const T* x, const T* xr) {
+  cudaStream_t cs = J.cs;
+  T* d = J.r.template as<T>();
+  IDRS_CUDA(cudaMemcpyAsync(d, x, sizeof(T) * J.n, cudaMemcpyDeviceToDevice, cs));
+  axpy<T>(J.n, T(-1.0), xr, d, cs);
+  using W = typename traits<T>::wide;
+  launch_fused<1, T>(J.n, BNorm<T>{d}, TStoreRe<W>{J.res.template as<double>()}, J.A->red, nullptr, cs);
+  launch_fused<1, T>(J.n, BNorm<T>{xr}, TStoreRe<W>{J.res.template as<double>() + 1}, J.A->red, nullptr, cs);
+  double h[2] = {0, 0};
+  IDRS_CUDA(cudaMemcpyAsync(h, J.res.p, 16, cudaMemcpyDeviceToHost, cs));
+  IDRS_CUDA(cudaStreamSynchronize(cs));
+  return std::sqrt(h[0]) / std::sqrt(h[1]);
+}
+
+// The FP64 solve a result is checked against (no counterpart in the
+// reference): the same preconditioned system solved again from x0 = 0 by the
+// FP64 form of the method (QMRIDR(s) without inner solves, or IDR(s)) to
+// opt->fp64_check_tol, with at least min(2n, 5000) iterations;
+// rel_err_vs_fp64 = ||x - x64|| / ||x64||.  The warm start of the next
+// right-hand side (J.d_x0) is kept.
+// the iteration bound of the check's FP64 solve (at least)
+int fp64_check_maxit(long n) { return (int)std::min<long>(2 * n, 5000); }
+
+void no_fp64_check(idrs_pp_report& rep) {
+  rep.rel_err_vs_fp64 = -1.0;
+  rep.fp64_relres_original = -1.0;
+  rep.fp64_flag = -1;
+  rep.fp64_iterations = 0;
+  rep.seconds_fp64_check = 0.0;
+}
+
+template <class T>
+int pp_fp64_check(PPJob<T>& J, const T* pb, const T* px, const idrs_pp_options* opt, idrs_pp_report& rep) {
+  no_fp64_check(rep);
+  if (!(opt->fp64_check_tol > 0.0)) return IDRS_OK;
+  auto t0 = clk::now();
+  const size_t vb = sizeof(T) * J.n;
+  DBuf keep(vb, J.cs), xr(vb, J.cs);
+  IDRS_CUDA(cudaMemcpyAsync(keep.p, J.d_x0.p, vb, cudaMemcpyDeviceToDevice, J.cs));
+  IDRS_CUDA(cudaMemsetAsync(J.d_x0.p, 0, vb, J.cs));
+  idrs_pp_options o = *opt;
+  o.tol = opt->fp64_check_tol;
+  o.maxit = std::max(opt->maxit, fp64_check_maxit(J.n));  // a mixed call bounds outer iterations only
+  o.in_it = 0;
+  o.inner_precision = 64;
+  idrs_pp_report r{};
+  int st = pp_solve<T>(J, pb, xr.template as<T>(), &o, r);
+  if (st) return st;
+  rep.rel_err_vs_fp64 = rel_diff<T>(J, px, xr.template as<T>());
+  rep.fp64_relres_original = r.relres_original;
+  rep.fp64_flag = r.flag;
+  rep.fp64_iterations = r.iterations;
+  IDRS_CUDA(cudaMemcpyAsync(J.d_x0.p, keep.p, vb, cudaMemcpyDeviceToDevice, J.cs));
+  IDRS_CUDA(cudaStreamSynchronize(J.cs));
+  rep.seconds_fp64_check = std::chrono::duration<double>(clk::now() - t0).count();
+  return IDRS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -2127,6 +2197,8 @@ int pp_idrs_t(idrs_user_matrix K, const double* b, idrs_user_matrix P, const dou
   rep.seconds_setup = std::chrono::duration<double>(t1 - t0).count();
   rep.seconds_solve = std::chrono::duration<double>(t2 - t1).count();
   rep.seconds_total = std::chrono::duration<double>(t2 - t0).count();
+  st = pp_fp64_check<T>(J, pb, px, opt, rep);
+  if (st) return st;
   if (report) *report = rep;
   return IDRS_OK;
 }
@@ -2186,6 +2258,8 @@ int pp_mr_idrs_t(idrs_user_matrix K, int nrhs, const double* b_all, idrs_user_ma
     rep.seconds_setup = setup;
     rep.seconds_solve = std::chrono::duration<double>(te - ts).count();
     rep.seconds_total = std::chrono::duration<double>(te - t0).count();
+    st = pp_fp64_check<T>(J, pb, px, opt, rep);
+    if (st) return st;
     if (reports) reports[irhs] = rep;
   }
   return IDRS_OK;
@@ -2319,6 +2393,7 @@ int pp_ms_t(idrs_user_matrix K, int nrhs, const double* rhs_all, int n_sigma, co
     rep.seconds_setup = setup;
     rep.seconds_solve = std::chrono::duration<double>(te - ts).count();
     rep.seconds_total = std::chrono::duration<double>(te - t0).count();
+    no_fp64_check(rep);  // the multishift pipelines have no built-in check
     if (reports) reports[irhs] = rep;
   }
   return IDRS_OK;

@@ -75,6 +75,9 @@ module idrs_gb300_module
       ! 0: the reference's Horner evaluation of the polynomial in fp64,
       ! 1: its three-term recurrence (see idrs_matrix_set_poly_eval)
       integer(c_int) :: poly_eval = 0
+      ! > 0: solve again in FP64 (no inner solves) to this tolerance and report
+      ! the relative error against that solution (rel_err_vs_fp64)
+      real(c_double) :: fp64_check_tol = 0.0d0
    end type idrs_pp_options
 
    type, bind(C) :: idrs_pp_report
@@ -86,6 +89,9 @@ module idrs_gb300_module
       integer(c_int) :: recycle_flag, recycle_iterations
       real(c_double) :: recycle_relres
       real(c_double) :: foci_imag(2), center_imag
+      real(c_double) :: rel_err_vs_fp64, fp64_relres_original
+      integer(c_int) :: fp64_flag, fp64_iterations
+      real(c_double) :: seconds_fp64_check
    end type idrs_pp_report
 
    type, bind(C) :: idrs_pp_inputs

@@ -404,6 +404,12 @@ typedef struct idrs_pp_options {
   int poly_eval;       /* IDRS_POLY_HORNER (0, the reference) or IDRS_POLY_RECURRENCE for
                           the fp64 products (see idrs_matrix_set_poly_eval); no
                           counterpart in the reference */
+  double fp64_check_tol; /* > 0: after each solve, solve the same preconditioned system
+                            again from x0 = 0 with the FP64 form of the method (no inner
+                            solves; at least min(2n, 5000) iterations) to this tolerance
+                            and report the relative error of x against that solution
+                            (report->rel_err_vs_fp64); 0: no check.  Not counted in
+                            seconds_solve.  No counterpart in the reference. */
 } idrs_pp_options;
 
 typedef struct idrs_pp_report {
@@ -415,7 +421,18 @@ typedef struct idrs_pp_report {
   int recycle_flag, recycle_iterations;            /* the recycle.inc solve (recycle = 1) */
   double recycle_relres;
   double foci_imag[2], center_imag;                 /* complex pipelines: imaginary parts */
+  /* opt->fp64_check_tol > 0: ||x - x64|| / ||x64|| against the FP64 solve x64,
+   * and that solve's flag, iterations, true residual and wall time; otherwise
+   * rel_err_vs_fp64 = fp64_relres_original = -1 and fp64_flag = -1 */
+  double rel_err_vs_fp64, fp64_relres_original;
+  int fp64_flag, fp64_iterations;
+  double seconds_fp64_check;
 } idrs_pp_report;
+
+/* sizeof(idrs_pp_options) (which 0), sizeof(idrs_pp_report) (1) or
+ * sizeof(idrs_pp_inputs) (2), for bindings that declare the structs
+ * themselves; 0 for another value.  Needs no GPU. */
+long idrs_pp_struct_size(int which);
 
 /* The optional inputs of pp_idrs beyond P, center and foci
  * (pp_idrs_module.f90: M, C, seed, shift, V); NULL = all absent.  seed and

@@ -27,6 +27,36 @@ def test_python_prototypes_cover_the_header(pkg):
     assert set(_declared()) <= set(pkg.api._PROTOS)
 
 
+def test_pp_structs_match_the_c_layout(pkg):
+    """The ctypes mirrors of idrs_pp_options / _report / _inputs have the
+    C structs' sizes (a field added on one side only changes them)."""
+    lib = pkg.load()
+    api = pkg.api
+    for which, cls in enumerate((api.PPOptions, api.PPReport, api.PPInputs)):
+        assert lib.idrs_pp_struct_size(which) == C.sizeof(cls), cls.__name__
+    assert lib.idrs_pp_struct_size(3) == 0
+
+
+def test_fp64_check_tolerance_rules(pkg):
+    """fp64_check: None checks mixed results of host-array calls only, True
+    any result at tol * 1e-3 (at least 1e-14), a float is the tolerance."""
+    import pytest
+    f = pkg.api.fp64_check_tolerance
+    assert f(1e-8, None, True) == pytest.approx(1e-11)
+    assert f(1e-8, None, False) == 0.0
+    assert f(1e-8, None, True, dev=True) == 0.0
+    assert f(1e-8, True, False, dev=True) == pytest.approx(1e-11)
+    assert f(1e-13, True, True) == 1e-14
+    assert f(1e-8, False, True) == 0.0
+    assert f(1e-8, 3e-12, False) == 3e-12
+    with pytest.raises(pkg.api.IDRSError):
+        f(1e-8, -1.0, True)
+    o = pkg.api._pp_options(0, 8, 1e-8, 60, 4, 300, 3e-3, 2, 8, 20, 32, False, 0, False, 1, None)
+    assert o.fp64_check_tol == pytest.approx(1e-11) and o.poly_eval == 1
+    o = pkg.api._pp_options(0, 8, 1e-8, 60, 4, 0, 3e-3, 2, 8, 20, 64, False, 0, False, 1, None)
+    assert o.fp64_check_tol == 0.0
+
+
 def test_argument_errors_without_gpu(pkg):
     lib = pkg.load()
     h = C.c_void_p()
