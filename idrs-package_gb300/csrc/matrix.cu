@@ -1203,6 +1203,47 @@ static void launch_seg_reduce(const MatView& M, Rows R, const V* val, const T* x
   }
 }
 
+// A side stream of the calling thread on the current device, with the two
+// events that fork it from and join it to a caller's stream (a pattern a
+// stream capture records too).  IDRS_CRS_OVERLAP=0 in the environment keeps
+// every bin on the caller's stream (read once per process; for comparisons).
+struct SideStream {
+  int dev = -1;
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+static bool side_stream(SideStream*& out) {
+  static const bool on = [] {
+    const char* e = getenv("IDRS_CRS_OVERLAP");
+    return !(e && e[0] == '0');
+  }();
+  if (!on) return false;
+  static thread_local SideStream ss;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (ss.dev != dev) {
+    if (ss.s) {
+      cudaStreamDestroy(ss.s);
+      cudaEventDestroy(ss.fork);
+      cudaEventDestroy(ss.join);
+      ss = SideStream{};
+    }
+    if (cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ss.join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      ss = SideStream{};
+      return false;
+    }
+    ss.dev = dev;
+  }
+  out = &ss;
+  return true;
+}
+
 template <class T, class V>
 static void launch_crs(const MatView& M, const V* val, const T* x, T* y, T a, T cv, const T* v,
                        T cx, T cu, const T* u, const int* skip, cudaStream_t st) {
@@ -1214,6 +1255,25 @@ static void launch_crs(const MatView& M, const V* val, const T* x, T* y, T a, T 
   long need = (M.nrows + rows_per_block - 1) / rows_per_block;
   int grid = (int)std::max(1L, std::min(need, (long)num_sms() * 8));
   const int max_len = (M.bin_short > 0) ? M.bin_short : INT_MAX;
+  // the long bin writes rows of its own: it runs beside the short and middle
+  // bins on a side stream forked here and joined at the end
+  auto launch_long = [&](cudaStream_t ls) {
+    const long sb = ((long)M.n_seg * 32 + kThreads - 1) / kThreads;
+    k_crs_seg<T, V><<<(unsigned)sb, kThreads, 0, ls>>>(M.n_seg, M.n_long, M.long_rows, M.seg_ptr, M.rp, M.ci, val,
+                                                       x, (T*)M.partial, skip);
+    IDRS_LAUNCH_CHECK();
+    const long fb = ((long)M.n_long * 32 + kThreads - 1) / kThreads;
+    k_crs_fin<T><<<(unsigned)fb, kThreads, 0, ls>>>(M.n_long, M.long_rows, M.seg_ptr, (const T*)M.partial, x, y,
+                                                    a, cv, v, cx, cu, u, skip);
+  };
+  SideStream* side = nullptr;
+  const bool forked = M.n_long > 0 && side_stream(side);
+  if (forked) {
+    IDRS_CUDA(cudaEventRecord(side->fork, st));
+    IDRS_CUDA(cudaStreamWaitEvent(side->s, side->fork, 0));
+    launch_long(side->s);
+    IDRS_LAUNCH_CHECK();
+  }
   if (M.group == 1) {
     k_crs_row<T, V><<<stream_grid(M.nrows), kThreads, 0, st>>>(M.nrows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu,
                                                                u, skip, max_len);
@@ -1232,15 +1292,12 @@ static void launch_crs(const MatView& M, const V* val, const T* x, T* y, T a, T 
     k_crs_list<kBinLanes, T, V><<<(unsigned)std::max(mb, 1L), kThreads, 0, st>>>(
         M.n_med, M.med_rows, M.rp, M.ci, val, x, y, a, cv, v, cx, cu, u, skip);
   }
-  if (M.n_long > 0) {
+  if (forked) {  // the caller counts and checks the last launch on st
+    IDRS_CUDA(cudaEventRecord(side->join, side->s));
+    IDRS_CUDA(cudaStreamWaitEvent(st, side->join, 0));
+  } else if (M.n_long > 0) {
     IDRS_LAUNCH_CHECK();
-    const long sb = ((long)M.n_seg * 32 + kThreads - 1) / kThreads;
-    k_crs_seg<T, V><<<(unsigned)sb, kThreads, 0, st>>>(M.n_seg, M.n_long, M.long_rows, M.seg_ptr, M.rp, M.ci, val,
-                                                       x, (T*)M.partial, skip);
-    IDRS_LAUNCH_CHECK();
-    const long fb = ((long)M.n_long * 32 + kThreads - 1) / kThreads;
-    k_crs_fin<T><<<(unsigned)fb, kThreads, 0, st>>>(M.n_long, M.long_rows, M.seg_ptr, (const T*)M.partial, x, y,
-                                                    a, cv, v, cx, cu, u, skip);
+    launch_long(st);
   }
 }
 
