@@ -93,6 +93,7 @@ _PROTOS = {
     "idrs_ms_rscaleback": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
     "idrs_ms_cscaleback": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
     "idrs_time_matvec": (_i, [_vp, _i, _i, _i, _vp, _vp]),
+    "idrs_time_sparse_outer_grad": (_i, [_vp, _i, _i, _vp]),
     "idrs_ridrs": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp,
                         _i, _vp, _i, _i, _vp]),
     "idrs_cidrs": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp,

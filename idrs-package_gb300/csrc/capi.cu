@@ -1548,6 +1548,33 @@ int idrs_time_matvec(idrs_matrix A, int prec, int warmup, int reps, double* ms_p
   });
 }
 
+int idrs_time_sparse_outer_grad(idrs_matrix A, int warmup, int reps, double* ms_per_call) {
+  return guard([&] {
+    REQUIRE(A && reps >= 1 && warmup >= 0 && ms_per_call, "time_sparse_outer_grad: bad arguments");
+    REQUIRE(A->K->format == FMT_CRS && A->K->vals != 2, "time_sparse_outer_grad: real CRS matrix required");
+    const long n = A->n(), nnz = A->K->nnz;
+    cudaStream_t st = A->stream;
+    DBuf lam(sizeof(double) * n, st), x(sizeof(double) * n, st), g(sizeof(double) * std::max(nnz, 1L), st);
+    IDRS_CUDA(cudaMemsetAsync(lam.p, 0, sizeof(double) * n, st));
+    IDRS_CUDA(cudaMemsetAsync(x.p, 0, sizeof(double) * n, st));
+    auto once = [&] { sparse_outer_grad(*A->K, lam.as<double>(), x.as<double>(), g.as<double>(), st); };
+    for (int i = 0; i < warmup; ++i) once();
+    cudaEvent_t e0, e1;
+    IDRS_CUDA(cudaEventCreate(&e0));
+    IDRS_CUDA(cudaEventCreate(&e1));
+    IDRS_CUDA(cudaEventRecord(e0, st));
+    for (int i = 0; i < reps; ++i) once();
+    IDRS_CUDA(cudaEventRecord(e1, st));
+    IDRS_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    IDRS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms_per_call = ms / reps;
+    return IDRS_OK;
+  });
+}
+
 int idrs_ridrs(idrs_matrix A, const double* b, int s, idrs_matrix M1, const double* tolerance,
                const int* maximum_iterations, const int* variant, int* flag, double* relres,
                int* iterations, const double* x0, const double* U0, const double* omega,

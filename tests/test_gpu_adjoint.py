@@ -86,6 +86,28 @@ def test_sparse_outer_grad_exact(gpu, oracle, P):
     np.testing.assert_array_equal(g, go)
 
 
+def test_sparse_outer_grad_ragged_blocks(gpu):
+    """Row blocks whose nonzeros fit the shared-memory row ids and blocks that
+    overflow them (a 256-row block with more than 4096 nonzeros takes the
+    binary search), empty rows and a row count that is not a multiple of the
+    block's 256 rows: bitwise equal to -lambda_i x_j in numpy."""
+    rng = np.random.default_rng(11)
+    n = 5000
+    L = rng.integers(0, 12, n)
+    L[1024:2048] = rng.integers(10, 40, 1024)  # these blocks overflow the row ids
+    L[rng.integers(0, n, 200)] = 0
+    rp = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(L, out=rp[1:])
+    assert rp[1280] - rp[1024] > 4096 and rp[256] - rp[0] <= 4096
+    ci = rng.integers(0, n, int(rp[-1]))
+    vals = rng.standard_normal(int(rp[-1]))
+    K = gpu.crs_format(n, n, (rp + 1).astype(np.int32), (ci + 1).astype(np.int32), rval=vals)
+    lam, x = rng.standard_normal(n), rng.standard_normal(n)
+    g = gpu.sparse_outer_grad(gpu.Matrix(K), lam, x)
+    rows = np.repeat(np.arange(n), L)
+    np.testing.assert_array_equal(g, -lam[rows] * x[ci])
+
+
 def _setup(gpu, P, n, seed=9):
     N = n ** 3
     rp, ci, vals = _cdr_crs(P, n)
