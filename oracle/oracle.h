@@ -97,6 +97,10 @@ typedef struct or_opts {
   void *colfac;
   uint64_t p_seed;              /* seed of the shadow-space generator (default 1) */
   int skip_inner_true_residual; /* unused by the oracle (always faithful) */
+  int inner_round32;            /* test probe, 0 = the reference: each nested MSIDRS result of
+                                   MSQMRIDR (solutions and collinearity factors) rounded to
+                                   single precision, the way a complex64 inner solve hands its
+                                   output to the FP64 outer iteration */
 } or_opts;
 
 /* ---- counter-based uniform generator shared with the CUDA library ---- */

@@ -46,6 +46,7 @@ class Opts(C.Structure):
         ("colfac", C.c_void_p),
         ("p_seed", C.c_uint64),
         ("skip_inner_true_residual", C.c_int),
+        ("inner_round32", C.c_int),
     ]
 
 
@@ -354,7 +355,7 @@ class Result(dict):
 def _opts(n, dt, *, tolerance=None, maximum_iterations=None, variant=None, M1=None,
           inner_s=None, inner_tolerance=None, inner_iterations=None, x0=None, U0=None,
           omega=None, PT=None, resvec_len=None, n_sigma=1, H_shape=None, colfac_len=None,
-          p_seed=1):
+          p_seed=1, inner_round32=False):
     keep = []
     o = Opts()
     o.tolerance = _dp(tolerance)
@@ -390,6 +391,7 @@ def _opts(n, dt, *, tolerance=None, maximum_iterations=None, variant=None, M1=No
         colfac = np.zeros(colfac_len, dtype=dt)
         o.colfac = _p(colfac)
     o.p_seed = p_seed
+    o.inner_round32 = int(bool(inner_round32))  # MSQMRIDR probe: nested results rounded to fp32
     return o, keep, (flag, relres, iters, resvec, H, colfac)
 
 

@@ -147,6 +147,32 @@ def test_pp_idrs_pipeline(oracle, P):
     np.testing.assert_allclose(r.x, 1.0, atol=1e-6)
 
 
+def test_nested_msqmridr_single_precision_inner_floor(oracle, P):
+    """The nested MSQMRIDR(4) with MSIDRS(4) inner (msqmridr.inc:162-175)
+    forms every shift's residual from the inner collinearity factors.  With
+    the inner results rounded to single precision (the oracle's
+    inner_round32 probe, as a complex64 inner solve hands them on) the
+    shifted systems stop near 3e-8 with flag 2, where the exact nested solve
+    reaches 1e-8 on every shift: the floor of the complex64 inner form is the
+    method's, not the GPU's arithmetic."""
+    n = 10
+    N = n ** 3
+    K = oracle.stencil7_format(n, n, n, P.laplace_coefficients(n))
+    A = oracle.Matrix(K, cplx=True)
+    b = P.complex_unit_normal(N)
+    sd, _ = P.multishift_shifts(n, n_shifts=6, lo=1.2, hi=4.0)
+    kw = dict(tolerance=1e-8, inner_s=4, inner_iterations=10, inner_tolerance=0.1, maximum_iterations=200)
+
+    def true_relres(x):
+        return np.array([np.linalg.norm(b - (K.mv(x[:, k]) - sd[k] * x[:, k])) / np.linalg.norm(b)
+                         for k in range(len(sd))])
+    exact = oracle.msqmridr(A, b, sd, 4, **kw)
+    rounded = oracle.msqmridr(A, b, sd, 4, inner_round32=True, **kw)
+    assert exact.flag == 0 and np.all(true_relres(exact.x) <= 1e-8)
+    rr = true_relres(rounded.x)
+    assert rounded.flag == 2 and np.all(rr > 1e-8) and np.all(rr < 1e-6)
+
+
 def test_multishift_oracle(oracle, P):
     """MSIDRS / MSQMRIDR on a small shifted Laplacian: every shifted system's
     true residual meets the tolerance."""
