@@ -1,6 +1,8 @@
 // capi.cu -- the extern "C" boundary (include/idrs_gb300.h).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <mutex>
 #include <complex>
 #include <cstring>
 #include <memory>
@@ -71,17 +73,25 @@ int guard(F&& f) {
     if (!(cond)) throw arg_error(msg); \
   } while (0)
 
+// The stream-ordered pool of each device keeps the memory of finished calls
+// (release threshold: never), so the per-call work vectors of a solve are
+// reused instead of mapped again; set once per device, from any thread.
 void init_runtime() {
-  static bool done = false;
-  if (done) return;
-  done = true;
+  static std::atomic<uint64_t> done{0};
+  static std::mutex mu;
   int dev = 0;
   IDRS_CUDA(cudaGetDevice(&dev));
+  const uint64_t bit = dev < 64 ? uint64_t(1) << dev : 0;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return;
+  std::lock_guard<std::mutex> lock(mu);
+  if (bit && (done.load() & bit)) return;
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
     uint64_t thr = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
+  cudaGetLastError();
+  done.fetch_or(bit, std::memory_order_release);
 }
 
 // device buffer owned for the duration of one call

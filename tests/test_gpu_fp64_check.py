@@ -101,3 +101,19 @@ def test_bad_check_tolerance_is_rejected(gpu, prob):
     K, D, b = prob
     with pytest.raises(gpu.IDRSError):
         gpu.PP_IDRS(K, b, P=D, tol=TOL, fp64_check=-1e-3, **MIXED)
+
+
+def test_complex_pipeline_states_its_error(gpu, oracle):
+    """CPP_IDRS (damped Helmholtz, seed 2 pi i, Neumann(4)) with QMRIDR(4) and
+    a complex64 inner IDR(4): the check runs the complex FP64 form."""
+    from test_gpu_pp import _helmholtz
+    n, K, M, C, b = _helmholtz(gpu, oracle)
+    kw = dict(method=0, s=4, tol=TOL, maxit=200, preconditioner=1, degree=4, n_ritz=12, in_s=4,
+              in_it=20, in_tol=1e-2, inner_precision=32, M=M[0], C_=C[0], seed=2j * np.pi)
+    g = gpu.PP_IDRS(K[0], b.astype(complex), **kw)
+    assert g.flag == 0 and g.relres_original <= 2 * TOL
+    assert g.fp64_flag == 0 and 0 < g.rel_err_vs_fp64 <= 1e-5
+    q = gpu.PP_IDRS(K[0], b.astype(complex), **dict(kw, inner_precision=64, in_it=0, tol=1e-11, maxit=5000))
+    assert q.flag == 0
+    # both FP64 solutions carry errors of order kappa * 1e-11 of their own
+    assert abs(g.rel_err_vs_fp64 - _rel(g.x, q.x)) <= 1e-8 + 0.05 * g.rel_err_vs_fp64
