@@ -110,7 +110,9 @@ bool chain_with_pdot(Operator& A, const float* v, float* w, float* t1, float* t2
   const St7 c{float(M.st[0]), float(M.st[1]), float(M.st[2]), float(M.st[3]), float(M.st[4]), float(M.st[5]),
               float(M.st[6])};
   dim3 blk(32, kF4Rows, 1), grid(gx, gy, (M.nz + zc - 1) / zc);
-  if (nd <= 4)
+  if (nd <= 2)
+    k_stencil7_f4_dot<2, Tail><<<grid, blk, 0, st>>>(M.nx, M.ny, M.nz, zc, c, y, w, PT, ld, nd, rb, tail, skip);
+  else if (nd <= 4)
     k_stencil7_f4_dot<4, Tail><<<grid, blk, 0, st>>>(M.nx, M.ny, M.nz, zc, c, y, w, PT, ld, nd, rb, tail, skip);
   else
     k_stencil7_f4_dot<8, Tail><<<grid, blk, 0, st>>>(M.nx, M.ny, M.nz, zc, c, y, w, PT, ld, nd, rb, tail, skip);

@@ -23,15 +23,16 @@ n = 24
 K = pkg.stencil7_format(n, n, n, pkg.problems.cdr_coefficients(n))
 b = K * np.ones(n ** 3)
 out = []
-for in_it in (6, 40):
+for in_s, in_it in ((4, 6), (4, 40), (2, 40)):
     r = pkg.PP_IDRS(K, b, P=pkg.real_precon(1, K), method=0, s=8, tol=1e-8, maxit=60, preconditioner=2,
-                    degree=8, n_ritz=20, in_s=4, in_it=in_it, in_tol=1e-2, inner_precision=32, poly_eval=1)
+                    degree=8, n_ritz=20, in_s=in_s, in_it=in_it, in_tol=1e-2, inner_precision=32, poly_eval=1,
+                    fp64_check=False)
     out += [r.x, np.array([r.flag, r.iterations, r.inner_iterations, r.relres_original])]
 A = pkg.Matrix(K, P=pkg.real_precon(1, K))
 A.preconditioner(2, 8, foci=[0.05, 1.9])
 for inner in (1, 8):
     q = pkg.QMRIDR(A, b, 8, tolerance=1e-8, maximum_iterations=3, inner_s=4, inner_iterations=inner,
-                   inner_tolerance=1e-12, inner_precision=32, resvec=True)
+                   inner_tolerance=1e-12, inner_precision=32, resvec=True, fp64_check=False)
     out.append(q.resvec[:4])
 np.savez(sys.argv[2], *out)
 """
@@ -47,7 +48,7 @@ def _run(tmp_path, fused):
 
 def test_fused_projection_matches_separate_pass(gpu, tmp_path):
     f, p = _run(tmp_path, True), _run(tmp_path, False)
-    for k in (0, 2):  # PP_IDRS mixed solves with short and long inner solves
+    for k in (0, 2, 4):  # PP_IDRS mixed: IDR(4) short and long inner solves, IDR(2)
         xf, sf, xp, sp = f[k], f[k + 1], p[k], p[k + 1]
         assert sf[0] == sp[0] == 0 and sf[3] <= 1e-8 and sp[3] <= 1e-8
         assert np.linalg.norm(xf - xp) / np.linalg.norm(xp) <= 1e-7
@@ -56,5 +57,5 @@ def test_fused_projection_matches_separate_pass(gpu, tmp_path):
     # projection's sum; with eight inner iterations that difference grows
     # through the inner solve (measured 1.1e-4 after one outer iteration,
     # 1.7e-3 after three); a wrong projection would differ by O(1)
-    np.testing.assert_allclose(f[4], p[4], rtol=1e-5)
-    np.testing.assert_allclose(f[5], p[5], rtol=1e-2)
+    np.testing.assert_allclose(f[6], p[6], rtol=1e-5)
+    np.testing.assert_allclose(f[7], p[7], rtol=1e-2)
