@@ -308,8 +308,10 @@ struct BIdrUpd {  // bi-orthogonalise G_k,U_k; r -= beta G_k; x += beta U_k; acc
       g = pk_msub(g, sh.a[q], pk_ld<L>(G + q * ld, i));
       u = pk_msub(u, sh.a[q], pk_ld<L>(U + q * ld, i));
     }
-    pk_st<L>(G + k * ld, i, g);
-    pk_st<L>(U + k * ld, i, u);
+    if (k > 0) {  // step 0 has nothing to orthogonalise against: G_0, U_0 stay as they are
+      pk_st<L>(G + k * ld, i, g);
+      pk_st<L>(U + k * ld, i, u);
+    }
     const Pk<T, L> rr = pk_msub(pk_ld<L>(r, i), sh.beta, g);
     pk_st<L>(r, i, rr);
     pk_st<L>(x, i, pk_madd(pk_ld<L>(x, i), sh.beta, u));

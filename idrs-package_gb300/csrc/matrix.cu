@@ -218,7 +218,7 @@ void build_row_plan(UserMatrix& M, const int* rp) {
       med.emplace_back((int)len, i);
     } else {
       longr.push_back(i);
-      segp.push_back(segp.back() + (int)((len + kBinLong - 1) / kBinLong));
+      segp.push_back(segp.back() + (int)((len + kSegNnz - 1) / kSegNnz));
     }
   }
   // longest first, rows ascending within a length: the rows of one warp have
@@ -614,8 +614,13 @@ __device__ __forceinline__ F8 st7_apply8h(const St7& c, const F8& xm, const F8& 
 __device__ __forceinline__ int next_slot(int s, int n) { return s + 1 == n ? 0 : s + 1; }
 
 // NXC: the row length as a compile-time constant (0: nx at run time), so the
-// row, half-row and slot offsets of the common 256-point rows are immediates
-template <int NXC>
+// row, half-row and slot offsets of the common 256-point rows are immediates.
+// VBM: where step B's vb term comes from.  In a polynomial chain vb is the
+// chain's input, which is also step A's v (VBM 1) or, in the first pair,
+// step A's xin (VBM 2); the thread then already holds vb(zp-1) from the
+// previous plane (step A's v, kept one plane in registers, or xm), and no
+// global load sits in step B.  VBM 0 loads vb from global memory.
+template <int NXC, int VBM>
 __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
     int nx_rt, int ny, int nz, int zc, St7 ca, float cua, float cva, St7 cb, float cub, float cvb,
     const float* __restrict__ xin, const float* __restrict__ u, const float* __restrict__ v,
@@ -663,7 +668,8 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
   auto aslot = [&](int q) { return A0 + ((q - zb) & (kT8ARing - 1)) * rstride; };
   // global streams of this thread, advanced one plane per iteration
   const long goff = (long)j * nx + i0;
-  const float* gvb = vb ? vb + (long)(zb - 1) * plane + goff : nullptr;  // vb(zp-1)
+  const float* gvb = (VBM == 0 && vb) ? vb + (long)(zb - 1) * plane + goff : nullptr;  // vb(zp-1)
+  F8 vprev = zero8();  // VBM 1: v(zp-1) of this thread's row, from step A of the previous plane
   float* gya = ya ? ya + (long)zb * plane + goff : nullptr;              // ya(zp)
   float* gyb = yb + (long)(zb - 1) * plane + goff;                        // yb(zp-1)
   // the halo warps' outer neighbour row (ty 0: j-1, ty 9: j+1)
@@ -728,7 +734,8 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
       issueU(zp + 1);
     }
     const bool doB = zp - 1 >= z0;
-    const F8 vbz = (gvb && interior && doB) ? ld8hg(gvb, 0, hx) : z8;
+    const F8 vbz = (VBM == 0 && gvb && interior && doB) ? ld8hg(gvb, 0, hx) : z8;
+    F8 vcur = z8;
     ghalo += plane;
     const F8 hnext = (hact && zp + 1 < nz) ? ld8hg(ghalo, 0, hx) : z8;
     waitX(zp + 1);
@@ -749,7 +756,10 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
       if (act) {
         r = st7_apply8h(ca, xm, xc, xp, xs, xn, nb);
         if (u) axpy8(r, cua, ld8h(ru ? U1 : U0, 0, hx));
-        if (v) axpy8(r, cva, ld8h(ru ? V1 : V0, 0, hx));
+        if (v) {
+          vcur = ld8h(ru ? V1 : V0, 0, hx);
+          axpy8(r, cva, vcur);
+        }
         if (gya && interior && zp >= z0 && zp < z1) st8h(gya, 0, hx, r);
       }
     }
@@ -765,13 +775,16 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
         F8 rb = st7_apply8h(cb, ld8h(aslot(zp - 2), 0, hx), bc, ld8h(aslot(zp), 0, hx), ld8h(Aq - nx, 0, hx),
                             ld8h(Aq + nx, 0, hx), nb);
         axpy8(rb, cub, xm);
-        if (vb) axpy8(rb, cvb, vbz);
+        if (VBM == 1) axpy8(rb, cvb, vprev);
+        else if (VBM == 2) axpy8(rb, cvb, xm);
+        else if (vb) axpy8(rb, cvb, vbz);
         st8h(gyb, 0, hx, rb);
       }
     }
     xm = xc;
     xc = xp;
     hcur = hnext;
+    if (VBM == 1) vprev = vcur;
     rx0 = rx1;
     rx1 = next_slot(rx1, kT8XStages);
     if (zp >= qa && zp <= ulast) ru ^= 1;
@@ -907,7 +920,7 @@ __global__ void __launch_bounds__(256) k_crs_list(int nlist, const int* __restri
   }
 }
 
-// CRS long bin: one warp per kBinLong-nonzero segment of a long row.
+// CRS long bin: one warp per kSegNnz-nonzero segment of a long row.
 template <class T, class V>
 __global__ void __launch_bounds__(256) k_crs_seg(int n_seg, int n_long, const int* __restrict__ long_rows,
                                                  const int* __restrict__ seg_ptr,
@@ -924,11 +937,11 @@ __global__ void __launch_bounds__(256) k_crs_seg(int n_seg, int n_long, const in
     if (seg_ptr[mid] <= g) lo = mid; else hi = mid;
   }
   const int row = long_rows[lo];
-  const long beg = rp[row] + (g - seg_ptr[lo]) * (long)kBinLong;
-  const long end = min((long)rp[row + 1], beg + kBinLong);
+  const long beg = rp[row] + (g - seg_ptr[lo]) * (long)kSegNnz;
+  const long end = min((long)rp[row + 1], beg + kSegNnz);
   T sum = T(0);
-#pragma unroll
-  for (int j = 0; j < kBinLong / 32; ++j) {
+#pragma unroll 8
+  for (int j = 0; j < kSegNnz / 32; ++j) {
     const long k = beg + lane + 32L * j;
     if (k < end) sum = sum + crs_term<true>(val, ci, x, k);
   }
@@ -1477,10 +1490,12 @@ static int f8x2t_resident(int nx) {
   if (dev == cache_dev && nx == cache_nx) return cache_r;
   const uint64_t bit = dev < 64 ? uint64_t(1) << dev : 0;
   if (!bit || !(attr_set.load() & bit)) {
-    if (cudaFuncSetAttribute(k_stencil7_f8x2t<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)t8_smem(kX2MaxNx)) != cudaSuccess ||
-        cudaFuncSetAttribute(k_stencil7_f8x2t<kX2MaxNx>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)t8_smem(kX2MaxNx)) != cudaSuccess) {
+    bool ok = true;
+    for (auto kern : {k_stencil7_f8x2t<0, 0>, k_stencil7_f8x2t<0, 1>, k_stencil7_f8x2t<0, 2>,
+                      k_stencil7_f8x2t<kX2MaxNx, 0>, k_stencil7_f8x2t<kX2MaxNx, 1>, k_stencil7_f8x2t<kX2MaxNx, 2>})
+      ok = ok && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t8_smem(kX2MaxNx)) ==
+                     cudaSuccess;
+    if (!ok) {
       cudaGetLastError();
       return 0;
     }
@@ -1488,7 +1503,7 @@ static int f8x2t_resident(int nx) {
   }
   int r = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &r, nx == kX2MaxNx ? k_stencil7_f8x2t<kX2MaxNx> : k_stencil7_f8x2t<0>, 32 * kX8Halo, t8_smem(nx)) !=
+          &r, nx == kX2MaxNx ? k_stencil7_f8x2t<kX2MaxNx, 1> : k_stencil7_f8x2t<0, 1>, 32 * kX8Halo, t8_smem(nx)) !=
       cudaSuccess) {
     cudaGetLastError();
     r = 0;
@@ -1550,11 +1565,17 @@ static void run_chain(const MatView& Ks, const std::vector<ChainStep<T>>& steps,
           const int zc = (int)std::max(4L, ((long)Ks.nz + chunks - 1) / chunks);
           dim3 blk(32, kX8Halo, 1);
           dim3 grid((Ks.ny + kX8Rows - 1) / kX8Rows, (Ks.nz + zc - 1) / zc, 1);
-          auto kern = Ks.nx == kX2MaxNx ? k_stencil7_f8x2t<kX2MaxNx> : k_stencil7_f8x2t<0>;
+          // step B's vb: step A's v, step A's xin, or a vector of its own
+          const int vbm = (B.e.v && B.e.v == A.e.v) ? 1 : (B.e.v && B.e.v == A.in) ? 2 : 0;
+          const bool c256 = Ks.nx == kX2MaxNx;
+          auto kern = vbm == 1 ? (c256 ? k_stencil7_f8x2t<kX2MaxNx, 1> : k_stencil7_f8x2t<0, 1>)
+                    : vbm == 2 ? (c256 ? k_stencil7_f8x2t<kX2MaxNx, 2> : k_stencil7_f8x2t<0, 2>)
+                               : (c256 ? k_stencil7_f8x2t<kX2MaxNx, 0> : k_stencil7_f8x2t<0, 0>);
           kern<<<grid, blk, t8_smem(Ks.nx), st>>>(
               Ks.nx, Ks.ny, Ks.nz, zc, st7_of(Ks, A.e.a, A.e.cx), A.e.u ? A.e.cu : 0.f,
               A.e.v ? A.e.cv : 0.f, st7_of(Ks, B.e.a, B.e.cx), B.e.u ? B.e.cu : 0.f, B.e.v ? B.e.cv : 0.f,
-              A.in, A.e.u, A.e.v, B.e.v, need ? A.out : nullptr, B.out, skip, device_fault_word());
+              A.in, A.e.u, A.e.v, vbm == 0 ? B.e.v : nullptr, need ? A.out : nullptr, B.out, skip,
+              device_fault_word());
           IDRS_LAUNCH_CHECK();
           k += 2;
           continue;

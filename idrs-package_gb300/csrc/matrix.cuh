@@ -41,7 +41,7 @@ struct MatView {
   int group = 8;                          // CRS lanes per row
   // CRS with skewed rows: length bins.  Rows up to bin_short nonzeros stay
   // with the row kernels; rows up to kBinLong in med_rows (sorted by length)
-  // get kBinLanes lanes each; longer rows are cut into kBinLong-nonzero warp
+  // get kBinLanes lanes each; longer rows are cut into kSegNnz-nonzero warp
   // segments whose partial sums are added per row in a fixed order.
   int bin_short = 0, n_med = 0, n_long = 0, n_seg = 0;
   const int* med_rows = nullptr;
@@ -89,8 +89,9 @@ struct Deflation {
 
 constexpr int kCooWarpNnz = 256;   // entries per warp of the segmented reduction (8 per lane)
 constexpr int kBinShort = 8;       // CRS length bins (rows with one lane per row)
-constexpr int kBinLanes = 8;       // lanes per row of the middle bin
-constexpr int kBinLong = 256;      // longer rows: warp segments of this many nonzeros
+constexpr int kBinLanes = 4;       // lanes per row of the middle bin
+constexpr int kBinLong = 256;      // longer rows: warp segments
+constexpr int kSegNnz = 1024;      // nonzeros per warp segment of a long row
 
 // Three diagonals of a tridiagonal Jacobi matrix J((d+2) x (d+1)):
 // a[i-1] = J(i-1,i), b[i-1] = J(i,i), c[i-1] = J(i+1,i), i = 1..d+1.
