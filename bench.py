@@ -308,7 +308,10 @@ def run_ours(args, rank, world, dist):
     # (Nine unfused steps would need 124N.)
     A = pkg.Matrix(K, P=D)
     A.preconditioner(2, 8, foci=list(r_mixed.foci))
-    ms_prod32, ms_launch32 = A.time_matvec(32, 5, 20)
+    ms_direct32, ms_launch32 = A.time_matvec(32, 5, 20)
+    # the same product captured once as a CUDA graph and replayed: how the
+    # solve's captured inner cycles run it (the roofline figure)
+    ms_prod32 = A.time_matvec_graph(32, 5, 20)
     ms_prod64, ms_launch64 = A.time_matvec(64, 3, 10)
     bytes32 = 76.0 * N
     bytes64 = 200.0 * N
@@ -377,7 +380,9 @@ def run_ours(args, rank, world, dist):
         "mixed_perturbed_rhs": {"runs": spread,
                                 "mean_seconds_4rhs": round((value + sum(q["seconds"] for q in spread)) / 4, 5),
                                 "what": "b (value) and b (1 + 1e-13 xi_k), k = 1..3; error against x = 1"},
-        "spmv": {"stencil_fp32_chain_ms_per_product": ms_prod32, "stencil_fp32_ms_per_launch": ms_launch32,
+        "spmv": {"stencil_fp32_chain_ms_per_product": ms_prod32,
+                 "stencil_fp32_chain_ms_per_product_direct_launches": ms_direct32,
+                 "stencil_fp32_ms_per_launch_direct": ms_launch32,
                  "stencil_fp32_GBps": round(achieved, 1),
                  "stencil_fp64_chain_ms_per_product": ms_prod64, "stencil_fp64_ms_per_launch": ms_launch64,
                  "stencil_fp64_GBps": round(bytes64 / (ms_prod64 * 1e-3) / 1e9, 1),
@@ -388,6 +393,9 @@ def run_ours(args, rank, world, dist):
                      "traffic": traffic,
                      "algorithmic_bytes": "76 N per 5-launch product (12N + 20N + 20N + 16N + 8N), N = 256^3; "
                                           "traffic = ncu DRAM bytes per product",
+                     "timing": "CUDA events over 20 replays of the product captured as a CUDA graph (as the "
+                               "solve's captured inner cycles run it)",
+                     "achieved_direct_launches": round(bytes32 / (ms_direct32 * 1e-3) / 1e9, 1),
                      "unfused_equivalent_GBps": round(124.0 * N / (ms_prod32 * 1e-3) / 1e9, 1)},
         "e2e": {"value": round(statistics.mean(t_e2e), 5), "unit": "s",
                 "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N,
@@ -541,7 +549,9 @@ def run_profile(args):
         A.preconditioner(2, 8, foci=[0.041648375561015305, 1.8404453336520692])
         prec = 32 if args.profile == "chain32" else 64
         ms, msl = A.time_matvec(prec, 5, 20)
-        print(json.dumps({"profile": args.profile, "grid": n, "ms_per_product": ms, "ms_per_launch": msl}))
+        msg = A.time_matvec_graph(prec, 5, 20)
+        print(json.dumps({"profile": args.profile, "grid": n, "ms_per_product": ms, "ms_per_launch": msl,
+                          "ms_per_product_graph": msg}))
 
 
 # ------------------------------------------------------- other configurations

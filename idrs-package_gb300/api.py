@@ -93,6 +93,7 @@ _PROTOS = {
     "idrs_ms_rscaleback": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
     "idrs_ms_cscaleback": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
     "idrs_time_matvec": (_i, [_vp, _i, _i, _i, _vp, _vp]),
+    "idrs_time_matvec_graph": (_i, [_vp, _i, _i, _i, _vp]),
     "idrs_time_sparse_outer_grad": (_i, [_vp, _i, _i, _vp]),
     "idrs_ridrs": (_i, [_vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp,
                         _i, _vp, _i, _i, _vp]),
@@ -481,6 +482,13 @@ class Matrix:
         _check(lib().idrs_time_matvec(self.handle, int(prec), int(warmup), int(reps), C.byref(a),
                                       C.byref(b)))
         return a.value, b.value
+
+    def time_matvec_graph(self, prec=64, warmup=3, reps=20):
+        """CUDA-event time (ms) of one product A*v captured as a CUDA graph and
+        replayed, as the IDR(s) cycles run their products."""
+        a = C.c_double()
+        _check(lib().idrs_time_matvec_graph(self.handle, int(prec), int(warmup), int(reps), C.byref(a)))
+        return a.value
 
     def ms_parameters(self, sigma):
         sigma = np.ascontiguousarray(sigma, dtype=self.dtype)

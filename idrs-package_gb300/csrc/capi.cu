@@ -1558,6 +1558,67 @@ int idrs_time_matvec(idrs_matrix A, int prec, int warmup, int reps, double* ms_p
   });
 }
 
+int idrs_time_matvec_graph(idrs_matrix A, int prec, int warmup, int reps, double* ms_per_product) {
+  return guard([&] {
+    REQUIRE(A && (prec == 64 || prec == 32) && reps >= 1 && warmup >= 0 && ms_per_product,
+            "time_matvec_graph: bad arguments");
+    long n = A->n();
+    cudaStream_t st = A->stream;
+    size_t es = (A->cplx ? 2 : 1) * (prec == 64 ? 8 : 4);
+    DBuf v(es * n, st), w(es * n, st), t1(es * n, st), t2(es * n, st), t3(es * n, st), t4(es * n, st);
+    IDRS_CUDA(cudaMemsetAsync(v.p, 0, es * n, st));
+    auto once = [&] {
+      auto run = [&](auto z) {
+        using T = decltype(z);
+        op_apply<T>(*A, prec, v.as<T>(), w.as<T>(), t1.as<T>(), t2.as<T>(), t3.as<T>(), t4.as<T>(), nullptr, st);
+      };
+      if (prec == 64 && !A->cplx) run(0.0);
+      else if (prec == 32 && !A->cplx) run(0.0f);
+      else if (prec == 64) run(c128(0.0));
+      else run(c64(0.0f));
+    };
+    for (int i = 0; i < warmup; ++i) once();
+    IDRS_CUDA(cudaStreamSynchronize(st));
+    // one product captured as a graph (as the IDR(s) cycles run it), then replayed
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    IDRS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const long l0 = launch_count();
+    bool ok = true;
+    try {
+      once();
+    } catch (const cuda_error&) {
+      ok = false;
+    }
+    const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    const long captured = launch_count() - l0;
+    uncount_launches(captured);  // captured, not run: the replays count them
+    if (!ok || ce != cudaSuccess || !g || cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) {
+      cudaGetLastError();
+      if (g) cudaGraphDestroy(g);
+      REQUIRE(false, "time_matvec_graph: the product cannot be captured as a CUDA graph");
+    }
+    cudaGraphDestroy(g);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float ms = 0;
+    cudaError_t re = cudaGraphLaunch(ge, st);
+    if (re == cudaSuccess) re = cudaEventCreate(&e0);
+    if (re == cudaSuccess) re = cudaEventCreate(&e1);
+    if (re == cudaSuccess) re = cudaEventRecord(e0, st);
+    for (int i = 0; i < reps && re == cudaSuccess; ++i) re = cudaGraphLaunch(ge, st);
+    if (re == cudaSuccess) re = cudaEventRecord(e1, st);
+    if (re == cudaSuccess) re = cudaEventSynchronize(e1);
+    if (re == cudaSuccess) re = cudaEventElapsedTime(&ms, e0, e1);
+    for (long q = 0; q < captured * (reps + 1); ++q) count_launch();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaGraphExecDestroy(ge);
+    IDRS_CUDA(re);
+    *ms_per_product = ms / reps;
+    return IDRS_OK;
+  });
+}
+
 int idrs_time_sparse_outer_grad(idrs_matrix A, int warmup, int reps, double* ms_per_call) {
   return guard([&] {
     REQUIRE(A && reps >= 1 && warmup >= 0 && ms_per_call, "time_sparse_outer_grad: bad arguments");

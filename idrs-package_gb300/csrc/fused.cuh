@@ -95,6 +95,8 @@ struct has_pack<B, std::void_t<decltype(B::kPack)>> : std::bool_constant<B::kPac
 template <int ND, class T, class Body, class Tail, int W = 1>
 __global__ void __launch_bounds__(kThreads) k_fused(long n, Body body, Tail tail, RedBuf rb,
                                                     const int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip && *(volatile const int*)skip) return;
   using A = typename acc_of<T>::type;
   __shared__ typename Body::Shared sh;
@@ -141,13 +143,13 @@ inline void launch_fused(long n, const Body& body, const Tail& tail, RedBuf rb, 
     if (body.pack_ok()) {
       const long np = (n + 3) / 4;
       int grid = (ND > 0) ? red_grid(np, resident_blocks<ND, T, Body, Tail, 4>()) : stream_grid(np);
-      k_fused<ND, T, Body, Tail, 4><<<grid, kThreads, 0, st>>>(n, body, tail, rb, skip);
+      launch_pdl(k_fused<ND, T, Body, Tail, 4>, dim3(grid), dim3(kThreads), 0, st, n, body, tail, rb, skip);
       IDRS_LAUNCH_CHECK();
       return;
     }
   }
   int grid = (ND > 0) ? red_grid(n, resident_blocks<ND, T, Body, Tail>()) : stream_grid(n);
-  k_fused<ND, T, Body, Tail><<<grid, kThreads, 0, st>>>(n, body, tail, rb, skip);
+  launch_pdl(k_fused<ND, T, Body, Tail>, dim3(grid), dim3(kThreads), 0, st, n, body, tail, rb, skip);
   IDRS_LAUNCH_CHECK();
 }
 

@@ -236,8 +236,16 @@ void IdrsGpu<T>::enqueue_cycle(const T* b, T* x, const SolveOpts& o, int cycle, 
     op_precon<T>(*M1, prec, r, v, stop, st);
     vv = v;
   }
-  matvec(vv, t, stop);
-  launch_fused<3, T>(n, BOmDots<T>{t, r}, TIdrsOm<W>{d_st}, rb, stop, st);
+  // t = A vv and t.r, t.t, r.r: on the fp32 stencil accumulated by the
+  // chain's last pass (t is not read back for them)
+  bool fused = false;
+  if constexpr (std::is_same<T, float>::value)
+    fused = prec == 32 && chain_with_pdot<TIdrsOm<W>, true>(A, vv, t, t1, t2, t3, t4, r, n, 1, rb, TIdrsOm<W>{d_st},
+                                                            stop, st);
+  if (!fused) {
+    matvec(vv, t, stop);
+    launch_fused<3, T>(n, BOmDots<T>{t, r}, TIdrsOm<W>{d_st}, rb, stop, st);
+  }
   launch_fused_nd<T>(s + 1, n, BOmUpd<T, W>{r, t, x, vv, PT, n, s, &d_st->om}, TIdrsNormOm<W>{d_st}, rb, stop, st);
 }
 

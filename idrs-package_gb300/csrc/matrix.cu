@@ -20,6 +20,13 @@ static std::atomic<long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void uncount_launches(long k) { g_launches.fetch_sub(k, std::memory_order_relaxed); }
 long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("IDRS_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
 void set_error(const std::string& msg) { g_error = msg; }
 const char* last_error() { return g_error.c_str(); }
 
@@ -309,6 +316,8 @@ __global__ void __launch_bounds__(32 * kF4Rows, 4) k_stencil7_f4(
     float cb, const float* __restrict__ x, float* __restrict__ y, float cv,
     const float* __restrict__ v, float cu, const float* __restrict__ u,
     const int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip && *skip) return;
   const int lane = threadIdx.x;
   const int i0 = (blockIdx.x * 32 + lane) * 4;
@@ -626,6 +635,8 @@ __global__ void __launch_bounds__(32 * kX8Halo, 2) k_stencil7_f8x2t(
     const float* __restrict__ xin, const float* __restrict__ u, const float* __restrict__ v,
     const float* __restrict__ vb, float* __restrict__ ya, float* __restrict__ yb,
     const int* __restrict__ skip, int* fault) {
+  pdl_wait();
+  pdl_trigger();
   if (skip && *skip) return;
   const int nx = NXC ? NXC : nx_rt;
   extern __shared__ __align__(128) unsigned char sm[];
@@ -1355,10 +1366,9 @@ static void launch_stencil(const MatView& M, const T* x, T* y, T a, T cv, const 
       if (zc4 < 4 && M.nz >= 4) zc4 = 4;
       dim3 grid4(gx4, gy4, (M.nz + zc4 - 1) / zc4);
       const double ar = (double)a;
-      k_stencil7_f4<<<grid4, blk4, 0, st>>>(
-          M.nx, M.ny, M.nz, zc4, float(ar * M.st[0] + (double)cx), float(ar * M.st[1]),
-          float(ar * M.st[2]), float(ar * M.st[3]), float(ar * M.st[4]), float(ar * M.st[5]),
-          float(ar * M.st[6]), x, y, cv, v, cu, u, skip);
+      launch_pdl(k_stencil7_f4, grid4, blk4, 0, st, M.nx, M.ny, M.nz, zc4, float(ar * M.st[0] + (double)cx),
+                 float(ar * M.st[1]), float(ar * M.st[2]), float(ar * M.st[3]), float(ar * M.st[4]),
+                 float(ar * M.st[5]), float(ar * M.st[6]), x, y, cv, v, cu, u, skip);
       return;
     }
   }
@@ -1571,11 +1581,10 @@ static void run_chain(const MatView& Ks, const std::vector<ChainStep<T>>& steps,
           auto kern = vbm == 1 ? (c256 ? k_stencil7_f8x2t<kX2MaxNx, 1> : k_stencil7_f8x2t<0, 1>)
                     : vbm == 2 ? (c256 ? k_stencil7_f8x2t<kX2MaxNx, 2> : k_stencil7_f8x2t<0, 2>)
                                : (c256 ? k_stencil7_f8x2t<kX2MaxNx, 0> : k_stencil7_f8x2t<0, 0>);
-          kern<<<grid, blk, t8_smem(Ks.nx), st>>>(
-              Ks.nx, Ks.ny, Ks.nz, zc, st7_of(Ks, A.e.a, A.e.cx), A.e.u ? A.e.cu : 0.f,
-              A.e.v ? A.e.cv : 0.f, st7_of(Ks, B.e.a, B.e.cx), B.e.u ? B.e.cu : 0.f, B.e.v ? B.e.cv : 0.f,
-              A.in, A.e.u, A.e.v, vbm == 0 ? B.e.v : nullptr, need ? A.out : nullptr, B.out, skip,
-              device_fault_word());
+          launch_pdl(kern, grid, blk, t8_smem(Ks.nx), st, Ks.nx, Ks.ny, Ks.nz, zc, st7_of(Ks, A.e.a, A.e.cx),
+                     A.e.u ? A.e.cu : 0.f, A.e.v ? A.e.cv : 0.f, st7_of(Ks, B.e.a, B.e.cx),
+                     B.e.u ? B.e.cu : 0.f, B.e.v ? B.e.cv : 0.f, A.in, A.e.u, A.e.v,
+                     vbm == 0 ? B.e.v : nullptr, need ? A.out : nullptr, B.out, skip, device_fault_word());
           IDRS_LAUNCH_CHECK();
           k += 2;
           continue;

@@ -18,12 +18,17 @@ namespace idrs {
 
 // One thread owns four consecutive x-points of a row and marches in z like
 // k_stencil7_f4 (same point arithmetic, so w is bitwise the same); acc_d +=
-// PT_d . w over the thread's points for d < nd.
-template <int ND, class Tail>
+// PT_d . w over the thread's points for d < nd.  OM: the omega step's three
+// inner products instead (idrs.inc:254-270, the separate pass BOmDots):
+// acc_0 += w . r, acc_1 += w . w, acc_2 += r . r with r = PT's row 0 (ND 3,
+// nd 1), so the new t = w is not read back for them.
+template <int ND, class Tail, bool OM = false>
 __global__ void __launch_bounds__(32 * kF4Rows) k_stencil7_f4_dot(int nx, int ny, int nz, int zc, St7 c,
                                                                   const float* __restrict__ x, float* __restrict__ y,
                                                                   const float* __restrict__ PT, long ld, int nd,
                                                                   RedBuf rb, Tail tail, const int* __restrict__ skip) {
+  pdl_wait();
+  pdl_trigger();
   if (skip && *(volatile const int*)skip) return;
   const int lane = threadIdx.x;
   const int i0 = (blockIdx.x * 32 + lane) * 4;
@@ -57,14 +62,29 @@ __global__ void __launch_bounds__(32 * kF4Rows) k_stencil7_f4_dot(int nx, int ny
       *reinterpret_cast<float4*>(y + p) = r;
       // every product added to the compensated accumulator, as in the
       // separate pass (the projection's accuracy steers the fp32 IDR(s))
+      if constexpr (OM) {
+        acc_add(acc[0], q[0].x * r.x);
+        acc_add(acc[0], q[0].y * r.y);
+        acc_add(acc[0], q[0].z * r.z);
+        acc_add(acc[0], q[0].w * r.w);
+        acc_add(acc[1], r.x * r.x);
+        acc_add(acc[1], r.y * r.y);
+        acc_add(acc[1], r.z * r.z);
+        acc_add(acc[1], r.w * r.w);
+        acc_add(acc[2], q[0].x * q[0].x);
+        acc_add(acc[2], q[0].y * q[0].y);
+        acc_add(acc[2], q[0].z * q[0].z);
+        acc_add(acc[2], q[0].w * q[0].w);
+      } else {
 #pragma unroll
-      for (int d = 0; d < ND; ++d)
-        if (d < nd) {
-          acc_add(acc[d], q[d].x * r.x);
-          acc_add(acc[d], q[d].y * r.y);
-          acc_add(acc[d], q[d].z * r.z);
-          acc_add(acc[d], q[d].w * r.w);
-        }
+        for (int d = 0; d < ND; ++d)
+          if (d < nd) {
+            acc_add(acc[d], q[d].x * r.x);
+            acc_add(acc[d], q[d].y * r.y);
+            acc_add(acc[d], q[d].z * r.z);
+            acc_add(acc[d], q[d].w * r.w);
+          }
+      }
     }
     xm = xc;
     xc = xp;
@@ -87,11 +107,12 @@ inline bool fused_pdot_enabled() {
 // w = Ks p(Ks) v and the tail of P^T w in the last pass when the operator is
 // the fp32 matrix-free stencil with its polynomial by the recurrence (or no
 // polynomial), the vectors are 16-byte aligned and nd <= 8; false (nothing
-// launched) otherwise.
-template <class Tail>
+// launched) otherwise.  OM: the omega step's w . r, w . w, r . r with r = PT
+// (nd 1) instead.
+template <class Tail, bool OM = false>
 bool chain_with_pdot(Operator& A, const float* v, float* w, float* t1, float* t2, float* t3, float* t4,
                      const float* PT, long ld, int nd, RedBuf rb, Tail tail, const int* skip, cudaStream_t st) {
-  if (nd < 1 || nd > 8 || !fused_pdot_enabled()) return false;
+  if (nd < 1 || nd > 8 || (OM && nd != 1) || !fused_pdot_enabled()) return false;
   if (A.degree > 0 && !use_recurrence(A, 32)) return false;
   const MatView& M = A.view(32);
   if (M.format != FMT_STENCIL7 || M.nx % 4 != 0) return false;
@@ -110,12 +131,9 @@ bool chain_with_pdot(Operator& A, const float* v, float* w, float* t1, float* t2
   const St7 c{float(M.st[0]), float(M.st[1]), float(M.st[2]), float(M.st[3]), float(M.st[4]), float(M.st[5]),
               float(M.st[6])};
   dim3 blk(32, kF4Rows, 1), grid(gx, gy, (M.nz + zc - 1) / zc);
-  if (nd <= 2)
-    k_stencil7_f4_dot<2, Tail><<<grid, blk, 0, st>>>(M.nx, M.ny, M.nz, zc, c, y, w, PT, ld, nd, rb, tail, skip);
-  else if (nd <= 4)
-    k_stencil7_f4_dot<4, Tail><<<grid, blk, 0, st>>>(M.nx, M.ny, M.nz, zc, c, y, w, PT, ld, nd, rb, tail, skip);
-  else
-    k_stencil7_f4_dot<8, Tail><<<grid, blk, 0, st>>>(M.nx, M.ny, M.nz, zc, c, y, w, PT, ld, nd, rb, tail, skip);
+  auto kern = OM ? k_stencil7_f4_dot<3, Tail, true>
+             : nd <= 2 ? k_stencil7_f4_dot<2, Tail> : nd <= 4 ? k_stencil7_f4_dot<4, Tail> : k_stencil7_f4_dot<8, Tail>;
+  launch_pdl(kern, grid, blk, 0, st, M.nx, M.ny, M.nz, zc, c, y, w, PT, ld, nd, rb, tail, skip);
   IDRS_LAUNCH_CHECK();
   return true;
 }

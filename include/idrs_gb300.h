@@ -229,6 +229,11 @@ int idrs_ms_cscaleback(idrs_matrix A, int n_sigma, const double *sigma, const do
  * Each vector is larger than the GPU's L2 for n >= 2^24 (fp64). */
 int idrs_time_matvec(idrs_matrix A, int prec, int warmup, int reps, double *ms_per_product,
                      double *ms_per_launch);
+/* The same products as idrs_time_matvec, captured once as a CUDA graph and
+ * replayed `reps` times between CUDA events (no counterpart in the
+ * reference): the product as the IDR(s) cycles run it, whose captured cycles
+ * are replayed graphs too. */
+int idrs_time_matvec_graph(idrs_matrix A, int prec, int warmup, int reps, double *ms_per_product);
 /* Device time of the sparse gradient kernel (idrs_rsparse_outer_grad) on A's
  * CRS matrix: reps launches back to back on A's stream between CUDA events,
  * after warmup launches, with vectors the call allocates (no host copies, no
