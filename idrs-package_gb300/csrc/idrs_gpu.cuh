@@ -37,6 +37,9 @@ template <class W> __device__ inline W wdiv(W a, W b) { return a / b; }
 template <class W>
 struct IdrsState {
   int info, stop, early, iter, ii, jj, maxit, method, s, out_H, nritz, n_omega;
+  // x += beta_k U_k of the steps of the current cycle is deferred to the
+  // omega step's pass: xpend steps are pending (xdone = 1 when none are)
+  int xpend, xdone;
   double tol, tolb, normb, normr, kappa, relres, rho;
   W om;
   W M[MAXS * MAXS];
@@ -291,48 +294,83 @@ struct BCombineU {  // U_k = om*t + sum_{q>=k} g_q U_q  (t = v/M1)
 };
 
 template <class T, class W>
-struct BIdrUpd {  // bi-orthogonalise G_k,U_k; r -= beta G_k; x += beta U_k; acc0 = |r|^2
-  T* G; T* U; long ld; int k; T* r; T* x; const IdrsState<W>* st;
+struct BIdrUpd {  // bi-orthogonalise G_k,U_k; r -= beta G_k; acc0 = |r|^2 (x += beta U_k: BOmUpd / BXFlush)
+  T* G; T* U; long ld; int k; T* r; const IdrsState<W>* st;
   struct Shared { T a[MAXS]; T beta; };
   __device__ void prepare(Shared& sh) const {
     for (int q = threadIdx.x; q < k; q += blockDim.x) sh.a[q] = narrow<T>(st->alpha[q]);
     if (threadIdx.x == 0) sh.beta = narrow<T>(st->beta[k]);
   }
   static constexpr bool kPack = true;
-  bool pack_ok() const { return aligned_f4(G) && aligned_f4(U) && aligned_f4(r) && aligned_f4(x) && ld % 4 == 0; }
+  bool pack_ok() const { return aligned_f4(G) && aligned_f4(U) && aligned_f4(r) && ld % 4 == 0; }
   template <int L, int ND, class A>
   __device__ void run(long i, Shared& sh, A (&acc)[ND]) const {
-    Pk<T, L> g = pk_ld<L>(G + k * ld, i), u = pk_ld<L>(U + k * ld, i);
-#pragma unroll 4
-    for (int q = 0; q < k; ++q) {
-      g = pk_msub(g, sh.a[q], pk_ld<L>(G + q * ld, i));
-      u = pk_msub(u, sh.a[q], pk_ld<L>(U + q * ld, i));
-    }
+    Pk<T, L> g = pk_ld<L>(G + k * ld, i);
     if (k > 0) {  // step 0 has nothing to orthogonalise against: G_0, U_0 stay as they are
+      Pk<T, L> u = pk_ld<L>(U + k * ld, i);
+#pragma unroll 4
+      for (int q = 0; q < k; ++q) {
+        g = pk_msub(g, sh.a[q], pk_ld<L>(G + q * ld, i));
+        u = pk_msub(u, sh.a[q], pk_ld<L>(U + q * ld, i));
+      }
       pk_st<L>(G + k * ld, i, g);
       pk_st<L>(U + k * ld, i, u);
     }
     const Pk<T, L> rr = pk_msub(pk_ld<L>(r, i), sh.beta, g);
     pk_st<L>(r, i, rr);
-    pk_st<L>(x, i, pk_madd(pk_ld<L>(x, i), sh.beta, u));
     pk_acc_abs2(acc[0], rr);
   }
 };
 
+// x += beta_q U_q for the q < n pending steps, in step order (so x is rounded
+// exactly as if each step had updated it)
 template <class T, class W>
-struct BOmUpd {  // r -= om t; x += om v; acc0 = |r|^2, acc_{1+j} = PT_j . r
-  T* r; const T* t; T* x; const T* v; const T* PT; long ld; int s; const W* om;
-  struct Shared { T om; };
+struct XPending {
+  T b[MAXS];
+  int n;
+  __device__ void load(const IdrsState<W>* st, int nmax) {
+    if (threadIdx.x == 0) n = min(st->xpend, nmax);
+    for (int q = threadIdx.x; q < nmax; q += blockDim.x) b[q] = narrow<T>(st->beta[q]);
+  }
+};
+template <int L, class T, class W>
+__device__ __forceinline__ Pk<T, L> x_pending(Pk<T, L> xi, const XPending<T, W>& p, const T* U, long ld, long i) {
+  for (int q = 0; q < p.n; ++q) xi = pk_madd(xi, p.b[q], pk_ld<L>(U + q * ld, i));
+  return xi;
+}
+
+template <class T, class W>
+struct BXFlush {  // the deferred x += beta_q U_q of a cycle the solve stopped in
+  T* x; const T* U; long ld; int s; const IdrsState<W>* st;
+  struct Shared { XPending<T, W> p; };
+  __device__ void prepare(Shared& sh) const { sh.p.load(st, s); }
+  static constexpr bool kPack = true;
+  bool pack_ok() const { return aligned_f4(x) && aligned_f4(U) && ld % 4 == 0; }
+  template <int L, int ND, class A>
+  __device__ void run(long i, Shared& sh, A (&)[ND]) const {
+    pk_st<L>(x, i, x_pending<L>(pk_ld<L>(x, i), sh.p, U, ld, i));
+  }
+};
+
+template <class T, class W>
+struct BOmUpd {  // r -= om t; x += beta_q U_q (the cycle's steps) + om v; acc0 = |r|^2, acc_{1+j} = PT_j . r
+  T* r; const T* t; T* x; const T* v; const T* PT; long ld; int s; const W* om; const T* U;
+  const IdrsState<W>* st;
+  struct Shared { T om; XPending<T, W> p; };
   static constexpr bool kPack = true;
   bool pack_ok() const {
-    return aligned_f4(r) && aligned_f4(t) && aligned_f4(x) && aligned_f4(v) && aligned_f4(PT) && ld % 4 == 0;
+    return aligned_f4(r) && aligned_f4(t) && aligned_f4(x) && aligned_f4(v) && aligned_f4(PT) &&
+           aligned_f4(U) && ld % 4 == 0;
   }
-  __device__ void prepare(Shared& sh) const { if (threadIdx.x == 0) sh.om = narrow<T>(*om); }
+  __device__ void prepare(Shared& sh) const {
+    if (threadIdx.x == 0) sh.om = narrow<T>(*om);
+    sh.p.load(st, s);
+  }
   template <int L, int ND, class A>
   __device__ void run(long i, Shared& sh, A (&acc)[ND]) const {
     const Pk<T, L> vi = pk_ld<L>(v, i);
     const Pk<T, L> ri = pk_msub(pk_ld<L>(r, i), sh.om, pk_ld<L>(t, i));
-    pk_st<L>(x, i, pk_madd(pk_ld<L>(x, i), sh.om, vi));
+    pk_st<L>(x, i, pk_madd(x_pending<L>(pk_ld<L>(x, i), sh.p, U, ld, i), sh.om, vi));
     pk_st<L>(r, i, ri);
     pk_acc_abs2(acc[0], ri);
 #pragma unroll
@@ -403,6 +441,8 @@ template <class W> struct TIdrsNorm {  // idrs.inc:226-249
   IdrsState<W>* st; int k;
   __device__ void operator()(const W* v) const {
     const int s = st->s;
+    st->xpend = k + 1;  // x += beta_q U_q, q <= k, still to come
+    st->xdone = 0;
     if (k < s - 1)
       for (int q = k + 1; q < s; ++q) st->f[q] = st->f[q] - st->beta[k] * Mat(st->M, q, k);
     const int ii = st->ii;
@@ -444,6 +484,8 @@ template <class W> struct TIdrsOm {  // idrs.inc:260, 273-284 with COMP_OM idrs_
 template <class W> struct TIdrsNormOm {  // idrs.inc:291-299, then f = P_DOT of the next cycle
   IdrsState<W>* st;
   __device__ void operator()(const W* v) const {
+    st->xpend = 0;  // BOmUpd applied the cycle's x updates
+    st->xdone = 1;
     st->normr = sqrt(real_(v[0]));
     st->iter += 1;
     if (st->resvec) st->resvec[st->iter] = st->normr;
@@ -469,6 +511,12 @@ __global__ void k_idrs_state_init(IdrsState<W>* st, IdrsState<W> init, const int
 }
 template <class W>
 __global__ void k_set_stop(int* stop) { *stop = 1; }
+// after BXFlush: no x update is pending any more
+template <class W>
+__global__ void k_xflush_done(IdrsState<W>* st) {
+  st->xpend = 0;
+  st->xdone = 1;
+}
 
 // ---------------------------------------------------------------------------
 // IDR(s) driver

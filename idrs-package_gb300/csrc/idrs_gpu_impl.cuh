@@ -141,6 +141,8 @@ void IdrsGpu<T>::solve(const T* b, T* x, const SolveOpts& o) {
   init.n_omega = o.omega ? o.n_omega : 0;
   init.om = W(1.0);
   init.relres = 1.0;
+  init.xpend = 0;
+  init.xdone = 1;
   const int* ostop = o.inner ? o.outer_stop : nullptr;
   k_idrs_state_init<W><<<1, 1, 0, st>>>(d_st, init, ostop);
   IDRS_LAUNCH_CHECK();
@@ -192,6 +194,11 @@ void IdrsGpu<T>::solve(const T* b, T* x, const SolveOpts& o) {
       if (h_stop[(c - 1) & 1]) break;
     }
   }
+  // x updates of the steps of a cycle the solve stopped in (skipped when none
+  // is pending)
+  launch_fused<0, T>(n, BXFlush<T, W>{x, U, n, s, d_st}, NoTail(), rb, &d_st->xdone, st);
+  k_xflush_done<W><<<1, 1, 0, st>>>(d_st);
+  IDRS_LAUNCH_CHECK();
   if (!o.inner) {
     matvec(x, r, early, T(-1), T(1), b);  // true residual b - A x (idrs.inc:304)
     launch_fused<1, T>(n, BNorm<T>{r}, TIdrsFinal<W>{d_st}, rb, early, st);
@@ -228,7 +235,7 @@ void IdrsGpu<T>::enqueue_cycle(const T* b, T* x, const SolveOpts& o, int cycle, 
       matvec(Uk, Gk, stop);
       launch_fused_nd<T>(s, n, BPdot<T>{PT, n, Gk, s}, TIdrsMu<W>{d_st, k}, rb, stop, st);
     }
-    launch_fused<1, T>(n, BIdrUpd<T, W>{G, U, n, k, r, x, d_st}, TIdrsNorm<W>{d_st, k}, rb, stop, st);
+    launch_fused<1, T>(n, BIdrUpd<T, W>{G, U, n, k, r, d_st}, TIdrsNorm<W>{d_st, k}, rb, stop, st);
   }
   // omega step (idrs.inc:254-299)
   const T* vv = r;
@@ -246,7 +253,8 @@ void IdrsGpu<T>::enqueue_cycle(const T* b, T* x, const SolveOpts& o, int cycle, 
     matvec(vv, t, stop);
     launch_fused<3, T>(n, BOmDots<T>{t, r}, TIdrsOm<W>{d_st}, rb, stop, st);
   }
-  launch_fused_nd<T>(s + 1, n, BOmUpd<T, W>{r, t, x, vv, PT, n, s, &d_st->om}, TIdrsNormOm<W>{d_st}, rb, stop, st);
+  launch_fused_nd<T>(s + 1, n, BOmUpd<T, W>{r, t, x, vv, PT, n, s, &d_st->om, U, d_st}, TIdrsNormOm<W>{d_st}, rb,
+                     stop, st);
 }
 
 template <class T>
