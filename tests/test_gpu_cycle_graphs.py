@@ -3,7 +3,8 @@ the inner solves of a flexible QMRIDR(s), which share one graph per outer
 solve) against the same cycles launched one by one (IDRS_CYCLE_GRAPHS=0, in a
 child process): the graph runs the same kernels with the same arguments, so
 solutions, residual histories and iteration counts agree bit for bit, and the
-library's launch counter reports the same launches."""
+library's launch counter reports the same launches.  Direct launches with and
+without programmatic dependent launch (IDRS_PDL=0) agree bit for bit too."""
 import os
 import subprocess
 import sys
@@ -50,9 +51,9 @@ np.savez(sys.argv[2], *out)
 """
 
 
-def _run(tmp_path, graphs):
-    path = str(tmp_path / ("graphs" if graphs else "direct")) + ".npz"
-    env = dict(os.environ, IDRS_CYCLE_GRAPHS="1" if graphs else "0")
+def _run(tmp_path, graphs, pdl=True):
+    path = str(tmp_path / (("graphs" if graphs else "direct") + ("" if pdl else "_nopdl"))) + ".npz"
+    env = dict(os.environ, IDRS_CYCLE_GRAPHS="1" if graphs else "0", IDRS_PDL="1" if pdl else "0")
     subprocess.run([sys.executable, "-c", CHILD, ROOT, path], env=env, check=True, timeout=600)
     d = np.load(path)
     return [d[f"arr_{i}"] for i in range(len(d.files))]
@@ -67,3 +68,13 @@ def test_cycle_graphs_equal_direct_launches(gpu, tmp_path):
     assert gr[2][0] == gr[5][0] == 0  # standalone IDR(1), IDR(4) converged
     assert gr[7][0] == gr[9][0] == 0 and gr[7][2] > 0  # mixed PP_IDRS ran inner solves
     assert gr[12][0] > 0
+
+
+def test_programmatic_launch_equals_stream_order(gpu, tmp_path):
+    """Direct launches with programmatic dependent launch (the default) and
+    without it (IDRS_PDL=0): every kernel launched so waits for its
+    predecessor before it reads anything, so the results agree bit for bit."""
+    on, off = _run(tmp_path, False, True), _run(tmp_path, False, False)
+    assert len(on) == len(off) == 13
+    for a, b in zip(on, off):
+        np.testing.assert_array_equal(a, b)
