@@ -119,6 +119,21 @@ __device__ __forceinline__ void two_sum_add(float& s, float& c, float v) {
   c += err;
 }
 
+// two compensated accumulators advanced together: every step of two_sum_add
+// for both by one paired instruction (__fadd2_rn: each lane rounded as the
+// scalar addition; x - y is x + (-y) exactly)
+struct kfloat2 {
+  float2 s, c;
+};
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ void two_sum_add2(kfloat2& a, float2 v) {
+  const float2 t = __fadd2_rn(a.s, v);
+  const float2 bp = __fadd2_rn(t, neg2(a.s));
+  const float2 err = __fadd2_rn(__fadd2_rn(a.s, neg2(__fadd2_rn(t, neg2(bp)))), __fadd2_rn(v, neg2(bp)));
+  a.s = t;
+  a.c = __fadd2_rn(a.c, err);
+}
+
 template <class T> struct acc_of;
 template <> struct acc_of<double> { using type = double; };
 template <> struct acc_of<c128> { using type = c128; };

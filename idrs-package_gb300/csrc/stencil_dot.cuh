@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(32 * kF4Rows) k_stencil7_f4_dot(int nx, int ny
   kfloat acc[ND];
 #pragma unroll
   for (int d = 0; d < ND; ++d) acc_zero(acc[d]);
+  kfloat2 a01 = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // accumulators 0 and 1 (OM, ND 2)
   float4 xm = (in && z0 > 0) ? ld4(x + p - plane) : zero;
   float4 xc = in ? ld4(x + p) : zero;
   float4 xp = (in && z0 + 1 < nz) ? ld4(x + p + plane) : zero;
@@ -67,25 +68,27 @@ __global__ void __launch_bounds__(32 * kF4Rows) k_stencil7_f4_dot(int nx, int ny
     float right = __shfl_down_sync(0xffffffffu, xc.x, 1);
     if (lane == 0) left = (in && i0 > 0) ? __ldg(x + p - 1) : 0.f;
     if (lane == 31) right = (in && i0 + 4 < nx) ? __ldg(x + p + 4) : 0.f;
-
     if (in) {
       const float4 r = st7_apply(c, xm, xc, xp, xs, xn, left, right);
       *reinterpret_cast<float4*>(y + p) = r;
       // every product added to the compensated accumulator, as in the
-      // separate pass (the projection's accuracy steers the fp32 IDR(s))
+      // separate pass (the projection's accuracy steers the fp32 IDR(s));
+      // accumulators 0 and 1 advance together by paired instructions (the
+      // rounded product, then TwoSum)
       if constexpr (OM) {
-        acc_add(acc[0], q[0].x * r.x);
-        acc_add(acc[0], q[0].y * r.y);
-        acc_add(acc[0], q[0].z * r.z);
-        acc_add(acc[0], q[0].w * r.w);
-        acc_add(acc[1], r.x * r.x);
-        acc_add(acc[1], r.y * r.y);
-        acc_add(acc[1], r.z * r.z);
-        acc_add(acc[1], r.w * r.w);
+        two_sum_add2(a01, __fmul2_rn(make_float2(q[0].x, r.x), make_float2(r.x, r.x)));
+        two_sum_add2(a01, __fmul2_rn(make_float2(q[0].y, r.y), make_float2(r.y, r.y)));
+        two_sum_add2(a01, __fmul2_rn(make_float2(q[0].z, r.z), make_float2(r.z, r.z)));
+        two_sum_add2(a01, __fmul2_rn(make_float2(q[0].w, r.w), make_float2(r.w, r.w)));
         acc_add(acc[2], q[0].x * q[0].x);
         acc_add(acc[2], q[0].y * q[0].y);
         acc_add(acc[2], q[0].z * q[0].z);
         acc_add(acc[2], q[0].w * q[0].w);
+      } else if constexpr (ND == 2) {  // row 1 of q is zero when nd = 1; its sum is then unused
+        two_sum_add2(a01, __fmul2_rn(make_float2(q[0].x, q[1].x), make_float2(r.x, r.x)));
+        two_sum_add2(a01, __fmul2_rn(make_float2(q[0].y, q[1].y), make_float2(r.y, r.y)));
+        two_sum_add2(a01, __fmul2_rn(make_float2(q[0].z, q[1].z), make_float2(r.z, r.z)));
+        two_sum_add2(a01, __fmul2_rn(make_float2(q[0].w, q[1].w), make_float2(r.w, r.w)));
       } else {
 #pragma unroll
         for (int d = 0; d < ND; ++d)
@@ -100,6 +103,12 @@ __global__ void __launch_bounds__(32 * kF4Rows) k_stencil7_f4_dot(int nx, int ny
     xm = xc;
     xc = xp;
     xp = xpp;
+  }
+  if constexpr (OM || ND == 2) {
+    acc[0].s = a01.s.x;
+    acc[0].c = a01.c.x;
+    acc[1].s = a01.s.y;
+    acc[1].c = a01.c.y;
   }
   const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
   grid_reduce_tail_at<ND>(acc, rb, tail, lane + 32 * threadIdx.y, bid, gridDim.x * gridDim.y * gridDim.z);
