@@ -1560,7 +1560,9 @@ int idrs_time_matvec(idrs_matrix A, int prec, int warmup, int reps, double* ms_p
 
 int idrs_time_matvec_graph(idrs_matrix A, int prec, int warmup, int reps, double* ms_per_product) {
   return guard([&] {
-    REQUIRE(A && (prec == 64 || prec == 32) && reps >= 1 && warmup >= 0 && ms_per_product,
+    // warmup >= 1: the direct products before the capture make every lazily
+    // allocated work array of the operator exist outside the graph
+    REQUIRE(A && (prec == 64 || prec == 32) && reps >= 1 && warmup >= 1 && ms_per_product,
             "time_matvec_graph: bad arguments");
     long n = A->n();
     cudaStream_t st = A->stream;

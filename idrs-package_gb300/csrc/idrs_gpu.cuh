@@ -203,11 +203,14 @@ struct BGsUpd {
   }
 };
 
+// p /= rho as a multiplication by the reciprocal (one FP64 division per
+// thread instead of one per element: GB300's FP64 division is a sequence of
+// FP64 instructions; the row changes by at most 1 ulp)
 template <class T>
 __global__ void k_div_row(long n, T* p, const double* rho, bool conj_it) {
-  double d = *rho;
+  const auto inv = narrow<typename traits<T>::real>(1.0 / *rho);
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += gridDim.x * (long)blockDim.x) {
-    T v = p[i] / narrow<typename traits<T>::real>(d);
+    T v = p[i] * inv;
     p[i] = conj_it ? conj_(v) : v;
   }
 }

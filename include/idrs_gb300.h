@@ -232,7 +232,8 @@ int idrs_time_matvec(idrs_matrix A, int prec, int warmup, int reps, double *ms_p
 /* The same products as idrs_time_matvec, captured once as a CUDA graph and
  * replayed `reps` times between CUDA events (no counterpart in the
  * reference): the product as the IDR(s) cycles run it, whose captured cycles
- * are replayed graphs too. */
+ * are replayed graphs too.  warmup >= 1 (the products before the capture
+ * allocate the operator's lazily created work arrays). */
 int idrs_time_matvec_graph(idrs_matrix A, int prec, int warmup, int reps, double *ms_per_product);
 /* Device time of the sparse gradient kernel (idrs_rsparse_outer_grad) on A's
  * CRS matrix: reps launches back to back on A's stream between CUDA events,
