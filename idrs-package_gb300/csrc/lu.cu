@@ -154,6 +154,80 @@ __global__ void __launch_bounds__(kLUThreads) k_lu_factor(long n, int hb, bool b
   }
 }
 
+// Dense LU on all SMs (n >= kLUBlockedMin): blocks of kLUBlk pivots, every
+// entry given the same operations in the same order as in k_lu_factor, so
+// the factor is the same bit for bit.  For the block of pivots k0 ..
+// k0+nb-1: (1) the panel -- the block's columns below their pivots -- by one
+// CTA walking the pivots; (2) the block row -- the block's rows right of the
+// panel -- by forward substitution in pivot order, one thread per column;
+// (3) the trailing matrix, nb multiply-subtracts per entry in pivot order, in
+// 16 x 16 tiles of all SMs.  Every kernel returns at once after a zero pivot.
+constexpr int kLUBlk = 16;
+constexpr long kLUBlockedMin = 256;
+
+template <class V>
+__global__ void __launch_bounds__(kLUThreads) k_lu_panel(long n, long k0, int nb, V* S, int* bad) {
+  if (*(volatile int*)bad) return;
+  auto at = [&](long i, long j) -> V& { return S[i + n * j]; };
+  for (int q = 0; q < nb; ++q) {
+    const long k = k0 + q;
+    const V p = at(k, k);
+    if (is_zero(p)) {  // uniform over the block
+      if (threadIdx.x == 0) *bad = (int)(k + 1);
+      return;
+    }
+    for (long i = k + 1 + threadIdx.x; i < n; i += blockDim.x) {
+      V& l = at(i, k);
+      if (!is_zero(l)) l = lu_div(l, p);
+    }
+    __syncthreads();
+    const long rows = n - 1 - k, cols = k0 + nb - 1 - k;  // the panel's columns right of k
+    for (long t = threadIdx.x; t < rows * cols; t += blockDim.x) {
+      const long i = k + 1 + t % rows, j = k + 1 + t / rows;
+      const V l = at(i, k);
+      if (!is_zero(l)) at(i, j) = lu_msub(at(i, j), l, at(k, j));
+    }
+    __syncthreads();
+  }
+}
+
+template <class V>
+__global__ void k_lu_blockrow(long n, long k0, int nb, V* S, const int* bad) {
+  if (*(volatile const int*)bad) return;
+  auto at = [&](long i, long j) -> V& { return S[i + n * j]; };
+  for (long j = k0 + nb + blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += gridDim.x * (long)blockDim.x)
+    for (int q = 1; q < nb; ++q) {
+      V a = at(k0 + q, j);
+      for (int r = 0; r < q; ++r) {
+        const V l = at(k0 + q, k0 + r);
+        if (!is_zero(l)) a = lu_msub(a, l, at(k0 + r, j));
+      }
+      at(k0 + q, j) = a;
+    }
+}
+
+template <class V>
+__global__ void __launch_bounds__(256) k_lu_trail(long n, long k0, int nb, V* S, const int* bad) {
+  if (*(volatile const int*)bad) return;
+  __shared__ V sl[16][kLUBlk + 1];  // l(i, k0 + q) of the tile's rows
+  __shared__ V su[kLUBlk][16 + 1];  // u(k0 + q, j) of the tile's columns
+  const long base = k0 + nb;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const long i0 = base + blockIdx.x * 16L, j0 = base + blockIdx.y * 16L;
+  const V zero = narrow<V>(c128(0.0, 0.0));
+  if (ty < nb) sl[tx][ty] = (i0 + tx < n) ? S[(i0 + tx) + n * (k0 + ty)] : zero;  // row i0+tx, column k0+ty
+  if (tx < nb) su[tx][ty] = (j0 + ty < n) ? S[(k0 + tx) + n * (j0 + ty)] : zero;  // row k0+tx, column j0+ty
+  __syncthreads();
+  const long i = i0 + tx, j = j0 + ty;
+  if (i >= n || j >= n) return;
+  V a = S[i + n * j];
+  for (int q = 0; q < nb; ++q) {
+    const V l = sl[tx][q];
+    if (!is_zero(l)) a = lu_msub(a, l, su[q][ty]);
+  }
+  S[i + n * j] = a;
+}
+
 // W(i,k) = U(i,k) / U(k,k) and D(k) = 1 / U(k,k), one thread per column
 template <class V>
 __global__ void k_band_finish(long n, int hb, V* S) {
@@ -562,8 +636,24 @@ void build_typed(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, 
   int* bad = nullptr;
   IDRS_CUDA(cudaMalloc((void**)&bad, sizeof(int)));
   IDRS_CUDA(cudaMemset(bad, 0, sizeof(int)));
-  k_lu_factor<V><<<1, kLUThreads>>>(n, dense ? n : hb, !dense, S, bad);
-  IDRS_LAUNCH_CHECK();
+  if (dense && n >= kLUBlockedMin) {
+    for (long k0 = 0; k0 < n; k0 += kLUBlk) {
+      const int nb = (int)std::min<long>(kLUBlk, n - k0);
+      k_lu_panel<V><<<1, kLUThreads>>>(n, k0, nb, S, bad);
+      IDRS_LAUNCH_CHECK();
+      const long rest = n - k0 - nb;
+      if (rest > 0) {
+        k_lu_blockrow<V><<<stream_grid(rest), kThreads>>>(n, k0, nb, S, bad);
+        IDRS_LAUNCH_CHECK();
+        const dim3 g((unsigned)((rest + 15) / 16), (unsigned)((rest + 15) / 16));
+        k_lu_trail<V><<<g, dim3(16, 16)>>>(n, k0, nb, S, bad);
+        IDRS_LAUNCH_CHECK();
+      }
+    }
+  } else {
+    k_lu_factor<V><<<1, kLUThreads>>>(n, dense ? n : hb, !dense, S, bad);
+    IDRS_LAUNCH_CHECK();
+  }
   if (!dense) {
     k_band_finish<V><<<stream_grid(n), kThreads>>>(n, hb, S);
     IDRS_LAUNCH_CHECK();

@@ -75,3 +75,43 @@ def test_band_lu_of_a_dense_matrix_is_a_zero_pivot(gpu):
     K = gpu.dense_format(rmat=np.eye(3) * 2.0)
     with pytest.raises(gpu.IDRSError):
         gpu.real_precon(3, K)
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_blocked_dense_lu_matches_oracle(gpu, oracle, cplx):
+    """Dense LU from n = 256 on runs on all SMs in blocks of 16 pivots (panel,
+    block row, trailing tiles) with the same operations per entry in the same
+    order as the one-CTA factorisation and the oracle: the dense-LU
+    preconditioner agrees with the oracle's to rounding of the solve alone.
+    n = 600 is not a multiple of the block; the matrix is the RANDOM examples'
+    uniform matrix made diagonally dominant, so the solve is well posed."""
+    rng = np.random.default_rng(21 if cplx else 20)
+    n = 600
+    A = rng.uniform(size=(n, n)) + (1j * rng.uniform(size=(n, n)) if cplx else 0)
+    A = A + n * np.eye(n)
+    if cplx:
+        Kg, Ko = gpu.dense_format(cmat=A), oracle.dense_format(A)
+        Pg, Po = gpu.complex_precon(2, Kg), oracle.complex_precon(2, Ko)
+    else:
+        Kg, Ko = gpu.dense_format(rmat=A), oracle.dense_format(A)
+        Pg, Po = gpu.real_precon(2, Kg), oracle.real_precon(2, Ko)
+    Ag, Ao = gpu.Matrix(Kg, P=Pg, complex=cplx), oracle.Matrix(Ko, P=Po, cplx=cplx)
+    v = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0)
+    xg, xo = v / Ag, Ao.precon(v)
+    np.testing.assert_allclose(xg, xo, rtol=1e-13, atol=0)
+    berr = np.linalg.norm(A @ xg - v) / (np.linalg.norm(A, 2) * np.linalg.norm(xg))
+    assert berr <= 1e-13, berr
+
+
+def test_blocked_dense_lu_zero_pivot(gpu):
+    """A pivot that stays exactly zero (row and column 300 are zero left of
+    and above the diagonal, and the diagonal entry is zero) stops the blocked
+    factorisation with the reference's error."""
+    n = 600
+    A = np.eye(n) * 4.0 + np.triu(np.full((n, n), 0.01), 1)
+    A[300, :] = 0.0
+    A[:, 300] = 0.0
+    A[300, 301:] = 1.0
+    K = gpu.dense_format(rmat=A)
+    with pytest.raises(gpu.IDRSError):
+        gpu.real_precon(2, K)
