@@ -154,34 +154,41 @@ __global__ void __launch_bounds__(kLUThreads) k_lu_factor(long n, int hb, bool b
   }
 }
 
-// Dense LU on all SMs (n >= kLUBlockedMin): blocks of kLUBlk pivots, every
-// entry given the same operations in the same order as in k_lu_factor, so
-// the factor is the same bit for bit.  For the block of pivots k0 ..
-// k0+nb-1: (1) the panel -- the block's columns below their pivots -- by one
-// CTA walking the pivots; (2) the block row -- the block's rows right of the
-// panel -- by forward substitution in pivot order, one thread per column;
-// (3) the trailing matrix, nb multiply-subtracts per entry in pivot order, in
-// 16 x 16 tiles of all SMs.  Every kernel returns at once after a zero pivot.
+// LU on all SMs for large matrices (dense n >= kLUBlockedMin, band hb >=
+// kLUBlk as well): blocks of kLUBlk pivots, every entry given the same
+// operations in the same order as in k_lu_factor, so the factor is the same
+// bit for bit.  Pivot k updates the entries (i, j) with k < i, j <= min(k +
+// hb, n - 1) (hb = n dense).  For the block of pivots k0 .. k0+nb-1: (1) the
+// panel -- the block's columns below their pivots -- by one CTA walking the
+// pivots; (2) the block row -- the block's rows right of the panel -- by
+// forward substitution in pivot order, one thread per column; (3) the
+// trailing entries, up to nb multiply-subtracts each in pivot order, in 16 x
+// 16 tiles of all SMs.  Every kernel returns at once after a zero pivot.
 constexpr int kLUBlk = 16;
 constexpr long kLUBlockedMin = 256;
 
 template <class V>
-__global__ void __launch_bounds__(kLUThreads) k_lu_panel(long n, long k0, int nb, V* S, int* bad) {
+__global__ void __launch_bounds__(kLUThreads) k_lu_panel(long n, int hb, bool band, long last_k, long k0, int nb,
+                                                         V* S, int* bad) {
   if (*(volatile int*)bad) return;
-  auto at = [&](long i, long j) -> V& { return S[i + n * j]; };
+  const long n_pad = pad32(n);
+  auto at = [&](long i, long j) -> V& { return band ? S[band_idx(n_pad, hb, i, j)] : S[i + n * j]; };
   for (int q = 0; q < nb; ++q) {
     const long k = k0 + q;
+    if (k >= last_k) return;  // the band form never tests the last pivot
     const V p = at(k, k);
     if (is_zero(p)) {  // uniform over the block
       if (threadIdx.x == 0) *bad = (int)(k + 1);
       return;
     }
-    for (long i = k + 1 + threadIdx.x; i < n; i += blockDim.x) {
+    const long last = k + hb < n - 1 ? k + hb : n - 1;
+    for (long i = k + 1 + threadIdx.x; i <= last; i += blockDim.x) {
       V& l = at(i, k);
       if (!is_zero(l)) l = lu_div(l, p);
     }
     __syncthreads();
-    const long rows = n - 1 - k, cols = k0 + nb - 1 - k;  // the panel's columns right of k
+    const long jl = (k0 + nb - 1 < last) ? k0 + nb - 1 : last;  // the panel's columns right of k
+    const long rows = last - k, cols = jl - k;
     for (long t = threadIdx.x; t < rows * cols; t += blockDim.x) {
       const long i = k + 1 + t % rows, j = k + 1 + t / rows;
       const V l = at(i, k);
@@ -192,40 +199,55 @@ __global__ void __launch_bounds__(kLUThreads) k_lu_panel(long n, long k0, int nb
 }
 
 template <class V>
-__global__ void k_lu_blockrow(long n, long k0, int nb, V* S, const int* bad) {
+__global__ void k_lu_blockrow(long n, int hb, bool band, long last_k, long k0, int nb, V* S, const int* bad) {
   if (*(volatile const int*)bad) return;
-  auto at = [&](long i, long j) -> V& { return S[i + n * j]; };
-  for (long j = k0 + nb + blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += gridDim.x * (long)blockDim.x)
-    for (int q = 1; q < nb; ++q) {
+  const long n_pad = pad32(n);
+  auto at = [&](long i, long j) -> V& { return band ? S[band_idx(n_pad, hb, i, j)] : S[i + n * j]; };
+  const long jend = (k0 + nb - 1 + hb < n - 1) ? k0 + nb - 1 + hb : n - 1;  // the last column any pivot reaches
+  for (long j = k0 + nb + blockIdx.x * (long)blockDim.x + threadIdx.x; j <= jend; j += gridDim.x * (long)blockDim.x)
+    for (int q = 1; q < nb; ++q) {  // row k0+q: updated by the pivots k0+r, r < q, that reach (k0+q, j)
+      if (j - (k0 + q) > hb) continue;  // outside the band: never updated
       V a = at(k0 + q, j);
       for (int r = 0; r < q; ++r) {
-        const V l = at(k0 + q, k0 + r);
-        if (!is_zero(l)) a = lu_msub(a, l, at(k0 + r, j));
+        const long k = k0 + r;
+        if (k >= last_k || j - k > hb || q - r > hb) continue;
+        const V l = at(k0 + q, k);
+        if (!is_zero(l)) a = lu_msub(a, l, at(k, j));
       }
       at(k0 + q, j) = a;
     }
 }
 
 template <class V>
-__global__ void __launch_bounds__(256) k_lu_trail(long n, long k0, int nb, V* S, const int* bad) {
+__global__ void __launch_bounds__(256) k_lu_trail(long n, int hb, bool band, long last_k, long k0, int nb, V* S,
+                                                  const int* bad) {
   if (*(volatile const int*)bad) return;
-  __shared__ V sl[16][kLUBlk + 1];  // l(i, k0 + q) of the tile's rows
-  __shared__ V su[kLUBlk][16 + 1];  // u(k0 + q, j) of the tile's columns
+  __shared__ V sl[16][kLUBlk + 1];  // l(i, k0 + q) of the tile's rows (0 outside the band)
+  __shared__ V su[kLUBlk][16 + 1];  // u(k0 + q, j) of the tile's columns (0 outside the band)
+  const long n_pad = pad32(n);
+  auto at = [&](long i, long j) -> V& { return band ? S[band_idx(n_pad, hb, i, j)] : S[i + n * j]; };
   const long base = k0 + nb;
+  const long end = (k0 + nb - 1 + hb < n - 1) ? k0 + nb - 1 + hb : n - 1;  // rows / columns up to end
   const int tx = threadIdx.x, ty = threadIdx.y;
   const long i0 = base + blockIdx.x * 16L, j0 = base + blockIdx.y * 16L;
   const V zero = narrow<V>(c128(0.0, 0.0));
-  if (ty < nb) sl[tx][ty] = (i0 + tx < n) ? S[(i0 + tx) + n * (k0 + ty)] : zero;  // row i0+tx, column k0+ty
-  if (tx < nb) su[tx][ty] = (j0 + ty < n) ? S[(k0 + tx) + n * (j0 + ty)] : zero;  // row k0+tx, column j0+ty
+  if (ty < nb) {
+    const long i = i0 + tx, k = k0 + ty;
+    sl[tx][ty] = (i <= end && k < last_k && i - k <= hb) ? at(i, k) : zero;
+  }
+  if (tx < nb) {
+    const long j = j0 + ty, k = k0 + tx;
+    su[tx][ty] = (j <= end && k < last_k && j - k <= hb) ? at(k, j) : zero;
+  }
   __syncthreads();
   const long i = i0 + tx, j = j0 + ty;
-  if (i >= n || j >= n) return;
-  V a = S[i + n * j];
+  if (i > end || j > end || (band && (i - j > hb || j - i > hb))) return;
+  V a = at(i, j);
   for (int q = 0; q < nb; ++q) {
     const V l = sl[tx][q];
-    if (!is_zero(l)) a = lu_msub(a, l, su[q][ty]);
+    if (!is_zero(l) && j - (k0 + q) <= hb) a = lu_msub(a, l, su[q][ty]);
   }
-  S[i + n * j] = a;
+  at(i, j) = a;
 }
 
 // W(i,k) = U(i,k) / U(k,k) and D(k) = 1 / U(k,k), one thread per column
@@ -636,22 +658,25 @@ void build_typed(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, 
   int* bad = nullptr;
   IDRS_CUDA(cudaMalloc((void**)&bad, sizeof(int)));
   IDRS_CUDA(cudaMemset(bad, 0, sizeof(int)));
-  if (dense && n >= kLUBlockedMin) {
-    for (long k0 = 0; k0 < n; k0 += kLUBlk) {
-      const int nb = (int)std::min<long>(kLUBlk, n - k0);
-      k_lu_panel<V><<<1, kLUThreads>>>(n, k0, nb, S, bad);
+  const int hbf = dense ? (int)n : hb;
+  if (n >= kLUBlockedMin && (dense || hb >= kLUBlk)) {
+    const long last_k = dense ? n : n - 1;  // the band form never tests the last pivot
+    for (long k0 = 0; k0 < last_k; k0 += kLUBlk) {
+      const int nb = (int)std::min<long>(kLUBlk, last_k - k0);
+      k_lu_panel<V><<<1, kLUThreads>>>(n, hbf, !dense, last_k, k0, nb, S, bad);
       IDRS_LAUNCH_CHECK();
-      const long rest = n - k0 - nb;
+      const long end = std::min<long>(k0 + nb - 1 + hbf, n - 1);
+      const long rest = end - (k0 + nb) + 1;
       if (rest > 0) {
-        k_lu_blockrow<V><<<stream_grid(rest), kThreads>>>(n, k0, nb, S, bad);
+        k_lu_blockrow<V><<<stream_grid(rest), kThreads>>>(n, hbf, !dense, last_k, k0, nb, S, bad);
         IDRS_LAUNCH_CHECK();
         const dim3 g((unsigned)((rest + 15) / 16), (unsigned)((rest + 15) / 16));
-        k_lu_trail<V><<<g, dim3(16, 16)>>>(n, k0, nb, S, bad);
+        k_lu_trail<V><<<g, dim3(16, 16)>>>(n, hbf, !dense, last_k, k0, nb, S, bad);
         IDRS_LAUNCH_CHECK();
       }
     }
   } else {
-    k_lu_factor<V><<<1, kLUThreads>>>(n, dense ? n : hb, !dense, S, bad);
+    k_lu_factor<V><<<1, kLUThreads>>>(n, hbf, !dense, S, bad);
     IDRS_LAUNCH_CHECK();
   }
   if (!dense) {

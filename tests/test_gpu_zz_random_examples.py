@@ -115,3 +115,29 @@ def test_blocked_dense_lu_zero_pivot(gpu):
     K = gpu.dense_format(rmat=A)
     with pytest.raises(gpu.IDRSError):
         gpu.real_precon(2, K)
+
+
+@pytest.mark.parametrize("kind", ["band_real", "band_complex"])
+def test_blocked_band_lu_matches_oracle(gpu, oracle, kind):
+    """Band LU with n >= 256 and hb >= 16 runs in blocks of 16 pivots on all
+    SMs with the one-CTA kernel's operations per entry in its order; n = 1000
+    and hb = 40 (neither a multiple of the block) as the RANDOM band example
+    builds them plus 2 hb on the diagonal (moderate growth without
+    pivoting), compared with the oracle as the one-CTA band test is."""
+    rng = np.random.default_rng({"band_real": 31, "band_complex": 32}[kind])
+    n, hb = 1000, 40
+    A, R, cplx = _random_example(kind, n, hb, rng)
+    R[:, hb] += 2 * hb
+    A = A + 2 * hb * np.eye(n)
+    Kg = gpu.cds_format(n, n, hb, **({"cband": R} if cplx else {"rband": R}))
+    Ko = oracle.cds_format(n, n, hb, R)
+    if cplx:
+        Pg, Po = gpu.complex_precon(3, Kg), oracle.complex_precon(3, Ko)
+    else:
+        Pg, Po = gpu.real_precon(3, Kg), oracle.real_precon(3, Ko)
+    Ag, Ao = gpu.Matrix(Kg, P=Pg, complex=cplx), oracle.Matrix(Ko, P=Po, cplx=cplx)
+    v = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0)
+    xg, xo = v / Ag, Ao.precon(v)
+    np.testing.assert_allclose(xg, xo, rtol=1e-10, atol=1e-12 * np.abs(xo).max())
+    berr = np.linalg.norm(A @ xg - v) / (np.linalg.norm(A, 2) * np.linalg.norm(xg))
+    assert berr <= 1e-12, berr
