@@ -167,6 +167,55 @@ __global__ void __launch_bounds__(kLUThreads) k_lu_factor(long n, int hb, bool b
 constexpr int kLUBlk = 16;
 constexpr long kLUBlockedMin = 256;
 
+// the band panel in shared memory: rows k0 .. rl, the block's columns, as
+// P[c - k0][r - k0] (entries outside the band read as 0, never written);
+// the same pivot steps as k_lu_panel, then the in-band entries written back
+template <class V>
+__global__ void __launch_bounds__(kLUThreads) k_lu_panel_smem(long n, int hb, long last_k, long k0, int nb, V* S,
+                                                              int* bad) {
+  if (*(volatile int*)bad) return;
+  extern __shared__ __align__(16) unsigned char lu_sm[];
+  V* P = reinterpret_cast<V*>(lu_sm);
+  const long n_pad = pad32(n);
+  const long rl = (k0 + nb - 1 + hb < n - 1) ? k0 + nb - 1 + hb : n - 1;
+  const long ld = rl - k0 + 1;
+  const V zero = narrow<V>(c128(0.0, 0.0));
+  auto in_band = [&](long i, long j) { return i - j <= hb && j - i <= hb; };
+  for (long t = threadIdx.x; t < nb * ld; t += blockDim.x) {
+    const long c = k0 + t / ld, r = k0 + t % ld;
+    P[t] = in_band(r, c) ? S[band_idx(n_pad, hb, r, c)] : zero;
+  }
+  __syncthreads();
+  auto at = [&](long i, long j) -> V& { return P[(j - k0) * ld + (i - k0)]; };
+  for (int q = 0; q < nb; ++q) {
+    const long k = k0 + q;
+    if (k >= last_k) break;  // the band form never tests the last pivot
+    const V p = at(k, k);
+    if (is_zero(p)) {  // uniform over the block; the factor is discarded
+      if (threadIdx.x == 0) *bad = (int)(k + 1);
+      return;
+    }
+    const long last = k + hb < n - 1 ? k + hb : n - 1;
+    for (long i = k + 1 + threadIdx.x; i <= last; i += blockDim.x) {
+      V& l = at(i, k);
+      if (!is_zero(l)) l = lu_div(l, p);
+    }
+    __syncthreads();
+    const long jl = (k0 + nb - 1 < last) ? k0 + nb - 1 : last;
+    const long rows = last - k, cols = jl - k;
+    for (long t = threadIdx.x; t < rows * cols; t += blockDim.x) {
+      const long i = k + 1 + t % rows, j = k + 1 + t / rows;
+      const V l = at(i, k);
+      if (!is_zero(l)) at(i, j) = lu_msub(at(i, j), l, at(k, j));
+    }
+    __syncthreads();
+  }
+  for (long t = threadIdx.x; t < nb * ld; t += blockDim.x) {
+    const long c = k0 + t / ld, r = k0 + t % ld;
+    if (in_band(r, c)) S[band_idx(n_pad, hb, r, c)] = P[t];
+  }
+}
+
 template <class V>
 __global__ void __launch_bounds__(kLUThreads) k_lu_panel(long n, int hb, bool band, long last_k, long k0, int nb,
                                                          V* S, int* bad) {
@@ -198,24 +247,41 @@ __global__ void __launch_bounds__(kLUThreads) k_lu_panel(long n, int hb, bool ba
   }
 }
 
+// block row: the block's strictly lower 16 x 16 part of L in shared memory,
+// each thread's column of the block rows in registers (the loads of both are
+// independent), then the forward substitution in pivot order
 template <class V>
-__global__ void k_lu_blockrow(long n, int hb, bool band, long last_k, long k0, int nb, V* S, const int* bad) {
+__global__ void __launch_bounds__(256) k_lu_blockrow(long n, int hb, bool band, long last_k, long k0, int nb, V* S,
+                                                     const int* bad) {
   if (*(volatile const int*)bad) return;
   const long n_pad = pad32(n);
   auto at = [&](long i, long j) -> V& { return band ? S[band_idx(n_pad, hb, i, j)] : S[i + n * j]; };
+  __shared__ V sL[kLUBlk][kLUBlk];  // sL[q][r] = l(k0+q, k0+r), r < q (0 where the pivot does not reach)
+  const V zero = narrow<V>(c128(0.0, 0.0));
+  for (int t = threadIdx.x; t < kLUBlk * kLUBlk; t += blockDim.x) {
+    const int q = t / kLUBlk, r = t % kLUBlk;
+    sL[q][r] = (r < q && q < nb && k0 + r < last_k && q - r <= hb) ? at(k0 + q, k0 + r) : zero;
+  }
+  __syncthreads();
   const long jend = (k0 + nb - 1 + hb < n - 1) ? k0 + nb - 1 + hb : n - 1;  // the last column any pivot reaches
-  for (long j = k0 + nb + blockIdx.x * (long)blockDim.x + threadIdx.x; j <= jend; j += gridDim.x * (long)blockDim.x)
-    for (int q = 1; q < nb; ++q) {  // row k0+q: updated by the pivots k0+r, r < q, that reach (k0+q, j)
-      if (j - (k0 + q) > hb) continue;  // outside the band: never updated
-      V a = at(k0 + q, j);
+  for (long j = k0 + nb + blockIdx.x * (long)blockDim.x + threadIdx.x; j <= jend; j += gridDim.x * (long)blockDim.x) {
+    V c[kLUBlk];  // c[q] = S(k0+q, j), zero outside the band (never read there)
+#pragma unroll
+    for (int q = 0; q < kLUBlk; ++q) c[q] = (q < nb && j - (k0 + q) <= hb) ? at(k0 + q, j) : zero;
+#pragma unroll
+    for (int q = 1; q < kLUBlk; ++q) {
+      if (q >= nb || j - (k0 + q) > hb) continue;  // outside the band: never updated
+      V a = c[q];
+#pragma unroll
       for (int r = 0; r < q; ++r) {
-        const long k = k0 + r;
-        if (k >= last_k || j - k > hb || q - r > hb) continue;
-        const V l = at(k0 + q, k);
-        if (!is_zero(l)) a = lu_msub(a, l, at(k, j));
+        if (j - (k0 + r) > hb) continue;  // pivot k0+r does not reach column j
+        const V l = sL[q][r];
+        if (!is_zero(l)) a = lu_msub(a, l, c[r]);
       }
+      c[q] = a;
       at(k0 + q, j) = a;
     }
+  }
 }
 
 template <class V>
@@ -661,9 +727,25 @@ void build_typed(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, 
   const int hbf = dense ? (int)n : hb;
   if (n >= kLUBlockedMin && (dense || hb >= kLUBlk)) {
     const long last_k = dense ? n : n - 1;  // the band form never tests the last pivot
+    // band panels (kLUBlk x (kLUBlk + hb) entries) fit in shared memory
+    const size_t panel_bytes = sizeof(V) * (size_t)kLUBlk * (size_t)(kLUBlk + hbf);
+    bool smem_panel = !dense && panel_bytes <= kTrsvSmemBudget;
+    if (smem_panel && panel_bytes > 48 * 1024) {
+      if (cudaFuncSetAttribute(k_lu_panel_smem<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_bytes) !=
+          cudaSuccess) {
+        cudaGetLastError();
+        smem_panel = false;
+      }
+    }
     for (long k0 = 0; k0 < last_k; k0 += kLUBlk) {
       const int nb = (int)std::min<long>(kLUBlk, last_k - k0);
-      k_lu_panel<V><<<1, kLUThreads>>>(n, hbf, !dense, last_k, k0, nb, S, bad);
+      if (smem_panel) {
+        const long rl = std::min<long>(k0 + nb - 1 + hbf, n - 1);
+        k_lu_panel_smem<V><<<1, kLUThreads, sizeof(V) * (size_t)nb * (size_t)(rl - k0 + 1)>>>(n, hbf, last_k, k0, nb,
+                                                                                             S, bad);
+      } else {
+        k_lu_panel<V><<<1, kLUThreads>>>(n, hbf, !dense, last_k, k0, nb, S, bad);
+      }
       IDRS_LAUNCH_CHECK();
       const long end = std::min<long>(k0 + nb - 1 + hbf, n - 1);
       const long rest = end - (k0 + nb) + 1;
