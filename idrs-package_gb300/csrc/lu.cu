@@ -159,91 +159,85 @@ __global__ void __launch_bounds__(kLUThreads) k_lu_factor(long n, int hb, bool b
 // operations in the same order as in k_lu_factor, so the factor is the same
 // bit for bit.  Pivot k updates the entries (i, j) with k < i, j <= min(k +
 // hb, n - 1) (hb = n dense).  For the block of pivots k0 .. k0+nb-1: (1) the
-// panel -- the block's columns below their pivots -- by one CTA walking the
-// pivots; (2) the block row -- the block's rows right of the panel -- by
+// panel -- the block's columns below their pivots -- one thread per row, after
+// each CTA has factored the block's diagonal part; (2) the block row -- the block's rows right of the panel -- by
 // forward substitution in pivot order, one thread per column; (3) the
 // trailing entries, up to nb multiply-subtracts each in pivot order, in 16 x
 // 16 tiles of all SMs.  Every kernel returns at once after a zero pivot.
 constexpr int kLUBlk = 16;
 constexpr long kLUBlockedMin = 256;
 
-// the band panel in shared memory: rows k0 .. rl, the block's columns, as
-// P[c - k0][r - k0] (entries outside the band read as 0, never written);
-// the same pivot steps as k_lu_panel, then the in-band entries written back
-template <class V>
-__global__ void __launch_bounds__(kLUThreads) k_lu_panel_smem(long n, int hb, long last_k, long k0, int nb, V* S,
-                                                              int* bad) {
-  if (*(volatile int*)bad) return;
-  extern __shared__ __align__(16) unsigned char lu_sm[];
-  V* P = reinterpret_cast<V*>(lu_sm);
-  const long n_pad = pad32(n);
-  const long rl = (k0 + nb - 1 + hb < n - 1) ? k0 + nb - 1 + hb : n - 1;
-  const long ld = rl - k0 + 1;
-  const V zero = narrow<V>(c128(0.0, 0.0));
-  auto in_band = [&](long i, long j) { return i - j <= hb && j - i <= hb; };
-  for (long t = threadIdx.x; t < nb * ld; t += blockDim.x) {
-    const long c = k0 + t / ld, r = k0 + t % ld;
-    P[t] = in_band(r, c) ? S[band_idx(n_pad, hb, r, c)] : zero;
-  }
-  __syncthreads();
-  auto at = [&](long i, long j) -> V& { return P[(j - k0) * ld + (i - k0)]; };
-  for (int q = 0; q < nb; ++q) {
-    const long k = k0 + q;
-    if (k >= last_k) break;  // the band form never tests the last pivot
-    const V p = at(k, k);
-    if (is_zero(p)) {  // uniform over the block; the factor is discarded
-      if (threadIdx.x == 0) *bad = (int)(k + 1);
-      return;
-    }
-    const long last = k + hb < n - 1 ? k + hb : n - 1;
-    for (long i = k + 1 + threadIdx.x; i <= last; i += blockDim.x) {
-      V& l = at(i, k);
-      if (!is_zero(l)) l = lu_div(l, p);
-    }
-    __syncthreads();
-    const long jl = (k0 + nb - 1 < last) ? k0 + nb - 1 : last;
-    const long rows = last - k, cols = jl - k;
-    for (long t = threadIdx.x; t < rows * cols; t += blockDim.x) {
-      const long i = k + 1 + t % rows, j = k + 1 + t / rows;
-      const V l = at(i, k);
-      if (!is_zero(l)) at(i, j) = lu_msub(at(i, j), l, at(k, j));
-    }
-    __syncthreads();
-  }
-  for (long t = threadIdx.x; t < nb * ld; t += blockDim.x) {
-    const long c = k0 + t / ld, r = k0 + t % ld;
-    if (in_band(r, c)) S[band_idx(n_pad, hb, r, c)] = P[t];
-  }
-}
+// The panel on as many CTAs as its rows need (kLUPanelRows rows each).  Every
+// CTA factors the block's nb x nb diagonal part in shared memory (the steps of
+// k_lu_factor), then each thread takes one row below the block and applies
+// the block's pivots to the row's panel entries in pivot order: once the
+// pivot rows are final the rows are independent, and every entry gets the
+// same operations in the same order as in k_lu_factor.  The diagonal part is
+// written back by the CTA that read it last (ctl[1] counts the CTAs that hold
+// their copy; ctl[0] is the zero-pivot flag), so no CTA reads a factored entry.
+constexpr int kLUPanelRows = 64;
 
 template <class V>
-__global__ void __launch_bounds__(kLUThreads) k_lu_panel(long n, int hb, bool band, long last_k, long k0, int nb,
-                                                         V* S, int* bad) {
-  if (*(volatile int*)bad) return;
+__global__ void __launch_bounds__(kLUPanelRows) k_lu_panel(long n, int hb, bool band, long k0, int nb, V* S,
+                                                           int* ctl) {
+  if (*(volatile int*)ctl) return;
   const long n_pad = pad32(n);
   auto at = [&](long i, long j) -> V& { return band ? S[band_idx(n_pad, hb, i, j)] : S[i + n * j]; };
-  for (int q = 0; q < nb; ++q) {
-    const long k = k0 + q;
-    if (k >= last_k) return;  // the band form never tests the last pivot
-    const V p = at(k, k);
-    if (is_zero(p)) {  // uniform over the block
-      if (threadIdx.x == 0) *bad = (int)(k + 1);
+  __shared__ V D[kLUBlk][kLUBlk + 1];  // D[r][c] = S(k0 + r, k0 + c), in the band (hb >= kLUBlk)
+  __shared__ bool writer;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) D[t % nb][t / nb] = at(k0 + t % nb, k0 + t / nb);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    writer = atomicAdd(ctl + 1, 1) == (int)gridDim.x - 1;
+    if (writer) {
+      __threadfence();
+      ctl[1] = 0;
+    }
+  }
+  for (int q = 0; q < nb; ++q) {  // k0 + q < last_k: nb <= last_k - k0
+    __syncthreads();
+    const V p = D[q][q];
+    if (is_zero(p)) {  // the same in every CTA; the factor is discarded
+      if (blockIdx.x == 0 && threadIdx.x == 0) *ctl = (int)(k0 + q + 1);
       return;
     }
-    const long last = k + hb < n - 1 ? k + hb : n - 1;
-    for (long i = k + 1 + threadIdx.x; i <= last; i += blockDim.x) {
-      V& l = at(i, k);
-      if (!is_zero(l)) l = lu_div(l, p);
+    for (int i = q + 1 + threadIdx.x; i < nb; i += blockDim.x) {
+      const V l = D[i][q];
+      if (!is_zero(l)) D[i][q] = lu_div(l, p);
     }
     __syncthreads();
-    const long jl = (k0 + nb - 1 < last) ? k0 + nb - 1 : last;  // the panel's columns right of k
-    const long rows = last - k, cols = jl - k;
-    for (long t = threadIdx.x; t < rows * cols; t += blockDim.x) {
-      const long i = k + 1 + t % rows, j = k + 1 + t / rows;
-      const V l = at(i, k);
-      if (!is_zero(l)) at(i, j) = lu_msub(at(i, j), l, at(k, j));
+    const int m = nb - 1 - q;
+    for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+      const int i = q + 1 + t % m, j = q + 1 + t / m;
+      const V l = D[i][q];
+      if (!is_zero(l)) D[i][j] = lu_msub(D[i][j], l, D[q][j]);
     }
-    __syncthreads();
+  }
+  __syncthreads();
+  if (writer)
+    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) at(k0 + t % nb, k0 + t / nb) = D[t % nb][t / nb];
+  const V zero = narrow<V>(c128(0.0, 0.0));
+  const long rend = (k0 + nb - 1 + hb < n - 1) ? k0 + nb - 1 + hb : n - 1;  // the last row a pivot reaches
+  for (long i = k0 + nb + blockIdx.x * (long)blockDim.x + threadIdx.x; i <= rend; i += gridDim.x * (long)blockDim.x) {
+    V c[kLUBlk];  // c[q] = S(i, k0 + q), zero where pivot k0 + q does not reach row i
+#pragma unroll
+    for (int q = 0; q < kLUBlk; ++q) c[q] = (q < nb && i - (k0 + q) <= hb) ? at(i, k0 + q) : zero;
+#pragma unroll
+    for (int q = 0; q < kLUBlk; ++q) {
+      if (q >= nb || i - (k0 + q) > hb) continue;
+      V l = c[q];
+      if (!is_zero(l)) l = lu_div(l, D[q][q]);
+      c[q] = l;
+      if (!is_zero(l)) {
+#pragma unroll
+        for (int j = q + 1; j < kLUBlk; ++j)
+          if (j < nb) c[j] = lu_msub(c[j], l, D[q][j]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kLUBlk; ++q)
+      if (q < nb && i - (k0 + q) <= hb) at(i, k0 + q) = c[q];
   }
 }
 
@@ -722,31 +716,18 @@ void build_typed(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, 
     if (Md) cudaFree(Md);
   }
   int* bad = nullptr;
-  IDRS_CUDA(cudaMalloc((void**)&bad, sizeof(int)));
-  IDRS_CUDA(cudaMemset(bad, 0, sizeof(int)));
+  IDRS_CUDA(cudaMalloc((void**)&bad, 2 * sizeof(int)));  // the zero-pivot flag, the panel's CTA count
+  IDRS_CUDA(cudaMemset(bad, 0, 2 * sizeof(int)));
   const int hbf = dense ? (int)n : hb;
   if (n >= kLUBlockedMin && (dense || hb >= kLUBlk)) {
     const long last_k = dense ? n : n - 1;  // the band form never tests the last pivot
-    // band panels (kLUBlk x (kLUBlk + hb) entries) fit in shared memory
-    const size_t panel_bytes = sizeof(V) * (size_t)kLUBlk * (size_t)(kLUBlk + hbf);
-    bool smem_panel = !dense && panel_bytes <= kTrsvSmemBudget;
-    if (smem_panel && panel_bytes > 48 * 1024) {
-      if (cudaFuncSetAttribute(k_lu_panel_smem<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_bytes) !=
-          cudaSuccess) {
-        cudaGetLastError();
-        smem_panel = false;
-      }
-    }
     for (long k0 = 0; k0 < last_k; k0 += kLUBlk) {
       const int nb = (int)std::min<long>(kLUBlk, last_k - k0);
-      if (smem_panel) {
-        const long rl = std::min<long>(k0 + nb - 1 + hbf, n - 1);
-        k_lu_panel_smem<V><<<1, kLUThreads, sizeof(V) * (size_t)nb * (size_t)(rl - k0 + 1)>>>(n, hbf, last_k, k0, nb,
-                                                                                             S, bad);
-      } else {
-        k_lu_panel<V><<<1, kLUThreads>>>(n, hbf, !dense, last_k, k0, nb, S, bad);
+      {
+        const long below = std::min<long>(k0 + nb - 1 + hbf, n - 1) - (k0 + nb) + 1;  // rows under the block
+        const long g = std::max<long>(1, (below + kLUPanelRows - 1) / kLUPanelRows);
+        k_lu_panel<V><<<(unsigned)g, kLUPanelRows>>>(n, hbf, !dense, k0, nb, S, bad);
       }
-      IDRS_LAUNCH_CHECK();
       const long end = std::min<long>(k0 + nb - 1 + hbf, n - 1);
       const long rest = end - (k0 + nb) + 1;
       if (rest > 0) {
