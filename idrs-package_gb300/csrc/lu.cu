@@ -70,8 +70,15 @@ __device__ __forceinline__ c128 lu_div(c128 a, c128 b) {
 }
 
 template <class V> __device__ __forceinline__ bool is_zero(V v);
-template <> __device__ __forceinline__ bool is_zero<double>(double v) { return v == 0.0; }
-template <> __device__ __forceinline__ bool is_zero<c128>(c128 v) { return v.x == 0.0 && v.y == 0.0; }
+// +0 or -0, tested on the bits (the same answer as v == 0.0): an FP64 compare
+// would take a slot of GB300's FP64 pipe beside every multiply-subtract
+template <> __device__ __forceinline__ bool is_zero<double>(double v) {
+  return ((unsigned long long)__double_as_longlong(v) << 1) == 0ull;
+}
+template <> __device__ __forceinline__ bool is_zero<c128>(c128 v) {
+  return (((unsigned long long)__double_as_longlong(v.x) | (unsigned long long)__double_as_longlong(v.y)) << 1) ==
+         0ull;
+}
 
 // index of entry (i, j), |i - j| <= hb, in the band factor layout above
 __host__ __device__ __forceinline__ long band_idx(long n_pad, int hb, long i, long j) {
@@ -308,6 +315,55 @@ __global__ void __launch_bounds__(256) k_lu_trail(long n, int hb, bool band, lon
     if (!is_zero(l) && j - (k0 + q) <= hb) a = lu_msub(a, l, su[q][ty]);
   }
   at(i, j) = a;
+}
+
+// the dense trailing update in 64 x 64 tiles: each thread of 16 x 16 owns the
+// entries (i0 + tx + 16a, j0 + ty + 16b), a, b < 4, so a pivot costs 8 shared
+// loads for 16 multiply-subtracts (k_lu_trail: 2 per one); every entry gets
+// k_lu_trail's operations in the same order
+template <class V>
+__global__ void __launch_bounds__(256) k_lu_trail_dense4(long n, long k0, int nb, V* S, const int* bad) {
+  if (*(volatile const int*)bad) return;
+  __shared__ V sl[kLUBlk][64 + 1];  // sl[q][r] = l(i0 + r, k0 + q)
+  __shared__ V su[kLUBlk][64 + 1];  // su[q][c] = u(k0 + q, j0 + c)
+  const long base = k0 + nb, end = n - 1;
+  const int tx = threadIdx.x, ty = threadIdx.y, t = tx + 16 * ty;
+  const long i0 = base + blockIdx.x * 64L, j0 = base + blockIdx.y * 64L;
+  const V zero = narrow<V>(c128(0.0, 0.0));
+  for (int e = t; e < kLUBlk * 64; e += 256) {
+    const int r = e % 64, q = e / 64;  // column k0 + q of L, down the rows
+    sl[q][r] = (q < nb && i0 + r <= end) ? S[(i0 + r) + n * (k0 + q)] : zero;
+    const int qu = e % kLUBlk, c = e / kLUBlk;  // row k0 + qu of U, one column at a time
+    su[qu][c] = (qu < nb && j0 + c <= end) ? S[(k0 + qu) + n * (j0 + c)] : zero;
+  }
+  __syncthreads();
+  V acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const long i = i0 + tx + 16 * a, j = j0 + ty + 16 * b;
+      acc[a][b] = (i <= end && j <= end) ? S[i + n * j] : zero;
+    }
+  for (int q = 0; q < nb; ++q) {
+    V l[4], u[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) l[a] = sl[q][tx + 16 * a];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) u[b] = su[q][ty + 16 * b];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+      if (!is_zero(l[a]))
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = lu_msub(acc[a][b], l[a], u[b]);
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const long i = i0 + tx + 16 * a, j = j0 + ty + 16 * b;
+      if (i <= end && j <= end) S[i + n * j] = acc[a][b];
+    }
 }
 
 // W(i,k) = U(i,k) / U(k,k) and D(k) = 1 / U(k,k), one thread per column
@@ -733,8 +789,13 @@ void build_typed(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, 
       if (rest > 0) {
         k_lu_blockrow<V><<<stream_grid(rest), kThreads>>>(n, hbf, !dense, last_k, k0, nb, S, bad);
         IDRS_LAUNCH_CHECK();
-        const dim3 g((unsigned)((rest + 15) / 16), (unsigned)((rest + 15) / 16));
-        k_lu_trail<V><<<g, dim3(16, 16)>>>(n, hbf, !dense, last_k, k0, nb, S, bad);
+        const long g4 = (rest + 63) / 64;
+        if (dense && g4 * g4 >= 2L * num_sms()) {  // 64 x 64 tiles while they fill the SMs twice
+          k_lu_trail_dense4<V><<<dim3((unsigned)g4, (unsigned)g4), dim3(16, 16)>>>(n, k0, nb, S, bad);
+        } else {
+          const dim3 g((unsigned)((rest + 15) / 16), (unsigned)((rest + 15) / 16));
+          k_lu_trail<V><<<g, dim3(16, 16)>>>(n, hbf, !dense, last_k, k0, nb, S, bad);
+        }
         IDRS_LAUNCH_CHECK();
       }
     }

@@ -77,16 +77,18 @@ def test_band_lu_of_a_dense_matrix_is_a_zero_pivot(gpu):
         gpu.real_precon(3, K)
 
 
+@pytest.mark.parametrize("n", [600, 1208])
 @pytest.mark.parametrize("cplx", [False, True])
-def test_blocked_dense_lu_matches_oracle(gpu, oracle, cplx):
+def test_blocked_dense_lu_matches_oracle(gpu, oracle, cplx, n):
     """Dense LU from n = 256 on runs on all SMs in blocks of 16 pivots (panel,
     block row, trailing tiles) with the same operations per entry in the same
     order as the one-CTA factorisation and the oracle: the dense-LU
     preconditioner agrees with the oracle's to rounding of the solve alone.
-    n = 600 is not a multiple of the block; the matrix is the RANDOM examples'
-    uniform matrix made diagonally dominant, so the solve is well posed."""
-    rng = np.random.default_rng(21 if cplx else 20)
-    n = 600
+    Neither n is a multiple of the block; at n = 1208 the first blocks' trailing
+    updates run in 64 x 64 tiles (ragged at the edge), the later ones in 16 x
+    16.  The matrix is the RANDOM examples' uniform matrix made diagonally
+    dominant, so the solve is well posed."""
+    rng = np.random.default_rng((21 if cplx else 20) + n)
     A = rng.uniform(size=(n, n)) + (1j * rng.uniform(size=(n, n)) if cplx else 0)
     A = A + n * np.eye(n)
     if cplx:
