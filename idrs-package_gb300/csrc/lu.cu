@@ -684,46 +684,45 @@ void band_solve(const UserMatrix& P, const T* b, T* x, const int* skip, cudaStre
   IDRS_LAUNCH_CHECK();
 }
 
-// X's terms for the formats the scatter kernel does not read: a CDS matrix
-// into the band factor, a dense matrix into the dense factor, each built on
-// the host from X's values and uploaded into the ZEROED buffer dst (every
-// caller adds its terms with coefficient one into a fresh buffer).  Band
-// entries whose column lies outside the matrix are left out (the
-// elimination never reads them).  The reference has no band form of a dense
-// matrix and no dense form of a CDS one (real_band / real_dense leave the
-// result zero, user_module.f90:1163-1235, :1981-2066), so those
-// combinations add nothing here either.
+// dst = X's first cnt values (a dense X, column-major like the dense factor)
 template <class V>
-void host_form(const UserMatrix& X, V* dst, bool dense, int hb) {
+__global__ void k_form_dense(long cnt, const void* __restrict__ src, int vals, V* dst) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * (long)blockDim.x)
+    dst[k] = entry<V>(src, vals, k);
+}
+
+// a CDS X (diagonal d of row i at band[i + n (d + hx)]) into the band factor
+// layout, entries whose column lies outside the matrix left out
+template <class V>
+__global__ void k_form_cds(long n, long n_pad, int hx, int hb, const void* __restrict__ src, int vals, V* dst) {
+  const long cnt = n * (2L * hx + 1);
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < cnt; t += gridDim.x * (long)blockDim.x) {
+    const long i = t % n, j = i + (t / n - hx);
+    if (j >= 0 && j < n) dst[band_idx(n_pad, hb, i, j)] = entry<V>(src, vals, t);
+  }
+}
+
+// X's terms for the formats the scatter kernel does not read: a CDS matrix
+// into the band factor, a dense matrix into the dense factor, written on the
+// device into the ZEROED buffer dst (every caller adds its terms with
+// coefficient one into a fresh buffer; hb >= X's half band).  Band entries
+// whose column lies outside the matrix are left out (the elimination never
+// reads them).  The reference has no band form of a dense matrix and no dense
+// form of a CDS one (real_band / real_dense leave the result zero,
+// user_module.f90:1163-1235, :1981-2066), so those combinations add nothing
+// here either.
+template <class V>
+void device_form(const UserMatrix& X, V* dst, bool dense, int hb) {
   const long n = X.nrows;
-  auto fetch = [&](const void* src, long cnt) {  // X's values widened to complex
-    std::vector<c128> v((size_t)std::max(cnt, 1L));
-    if (X.vals == 2) {
-      IDRS_CUDA(cudaMemcpy(v.data(), src, sizeof(c128) * cnt, cudaMemcpyDeviceToHost));
-    } else {
-      std::vector<double> r((size_t)std::max(cnt, 1L));
-      IDRS_CUDA(cudaMemcpy(r.data(), src, sizeof(double) * cnt, cudaMemcpyDeviceToHost));
-      for (long k = 0; k < cnt; ++k) v[k] = c128(r[k], 0.0);
-    }
-    return v;
-  };
+  const int vals = X.vals == 2 ? 2 : 1;  // dense and CDS values are real or complex
   if (dense && X.format == FMT_DENSE) {
     const long cnt = n * std::min<long>(n, X.ncols);
-    const std::vector<c128> v = fetch(X.mat, cnt);
-    std::vector<V> h((size_t)std::max(cnt, 1L));
-    for (long k = 0; k < cnt; ++k) h[k] = narrow<V>(v[k]);
-    IDRS_CUDA(cudaMemcpy(dst, h.data(), sizeof(V) * cnt, cudaMemcpyHostToDevice));
+    k_form_dense<V><<<stream_grid(cnt), kThreads>>>(cnt, X.mat, vals, dst);
+    IDRS_LAUNCH_CHECK();
   } else if (!dense && X.format == FMT_CDS) {
-    const long n_pad = pad32(n), hx = X.half_band;
-    const std::vector<c128> v = fetch(X.band, n * (2 * hx + 1));
-    const long cnt = (2L * hb + 1) * n_pad;
-    std::vector<V> h((size_t)std::max(cnt, 1L), narrow<V>(c128(0.0, 0.0)));
-    for (long d = -hx; d <= hx; ++d)
-      for (long i = 0; i < n; ++i) {
-        const long j = i + d;
-        if (j >= 0 && j < n) h[band_idx(n_pad, hb, i, j)] = narrow<V>(v[i + n * (d + hx)]);
-      }
-    IDRS_CUDA(cudaMemcpy(dst, h.data(), sizeof(V) * cnt, cudaMemcpyHostToDevice));
+    const int hx = X.half_band;
+    k_form_cds<V><<<stream_grid(n * (2L * hx + 1)), kThreads>>>(n, pad32(n), hx, hb, X.band, vals, dst);
+    IDRS_LAUNCH_CHECK();
   }
 }
 
@@ -741,7 +740,7 @@ void build_typed(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, 
       k_scatter<V><<<stream_grid(n), kThreads>>>(n, X.row_ptr, X.col_ind, X.val, X.vals, coef, hbs, dst);
       IDRS_LAUNCH_CHECK();
     } else {
-      host_form<V>(X, dst, dense, hb);  // coef is one at every call
+      device_form<V>(X, dst, dense, hb);  // coef is one at every call
     }
   };
   const V one = narrow<V>(c128(1.0, 0.0));
