@@ -176,10 +176,12 @@ constexpr long kLUBlockedMin = 256;
 
 // The panel on as many CTAs as its rows need (kLUPanelRows rows each).  Every
 // CTA factors the block's nb x nb diagonal part in shared memory (the steps of
-// k_lu_factor), then each thread takes one row below the block and applies
-// the block's pivots to the row's panel entries in pivot order: once the
-// pivot rows are final the rows are independent, and every entry gets the
-// same operations in the same order as in k_lu_factor.  The diagonal part is
+// k_lu_factor) and each thread owns one row below the block: pivot q needs
+// only row q of the diagonal part, final after step q - 1, so the rows take
+// pivot q while the diagonal part divides its column q (GB300's FP64 pipe is
+// slow enough that the two chains would otherwise add up).  Once the pivot
+// rows are final the rows are independent, and every entry gets the same
+// operations in the same order as in k_lu_factor.  The diagonal part is
 // written back by the CTA that read it last (ctl[1] counts the CTAs that hold
 // their copy; ctl[0] is the zero-pivot flag), so no CTA reads a factored entry.
 constexpr int kLUPanelRows = 64;
@@ -193,6 +195,14 @@ __global__ void __launch_bounds__(kLUPanelRows) k_lu_panel(long n, int hb, bool 
   __shared__ V D[kLUBlk][kLUBlk + 1];  // D[r][c] = S(k0 + r, k0 + c), in the band (hb >= kLUBlk)
   __shared__ bool writer;
   for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) D[t % nb][t / nb] = at(k0 + t % nb, k0 + t / nb);
+  // this thread's row (the grid covers every row a pivot of the block reaches)
+  const long rend = (k0 + nb - 1 + hb < n - 1) ? k0 + nb - 1 + hb : n - 1;
+  const long i = k0 + nb + blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const bool row = i <= rend;
+  const V zero = narrow<V>(c128(0.0, 0.0));
+  V c[kLUBlk];  // c[q] = S(i, k0 + q), zero where pivot k0 + q does not reach row i
+#pragma unroll
+  for (int q = 0; q < kLUBlk; ++q) c[q] = (row && q < nb && i - (k0 + q) <= hb) ? at(i, k0 + q) : zero;
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -202,39 +212,18 @@ __global__ void __launch_bounds__(kLUPanelRows) k_lu_panel(long n, int hb, bool 
       ctl[1] = 0;
     }
   }
-  for (int q = 0; q < nb; ++q) {  // k0 + q < last_k: nb <= last_k - k0
+#pragma unroll
+  for (int q = 0; q < kLUBlk; ++q) {
+    if (q >= nb) break;  // k0 + q < last_k: nb <= last_k - k0
     __syncthreads();
     const V p = D[q][q];
     if (is_zero(p)) {  // the same in every CTA; the factor is discarded
       if (blockIdx.x == 0 && threadIdx.x == 0) *ctl = (int)(k0 + q + 1);
       return;
     }
-    for (int i = q + 1 + threadIdx.x; i < nb; i += blockDim.x) {
-      const V l = D[i][q];
-      if (!is_zero(l)) D[i][q] = lu_div(l, p);
-    }
-    __syncthreads();
-    const int m = nb - 1 - q;
-    for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
-      const int i = q + 1 + t % m, j = q + 1 + t / m;
-      const V l = D[i][q];
-      if (!is_zero(l)) D[i][j] = lu_msub(D[i][j], l, D[q][j]);
-    }
-  }
-  __syncthreads();
-  if (writer)
-    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) at(k0 + t % nb, k0 + t / nb) = D[t % nb][t / nb];
-  const V zero = narrow<V>(c128(0.0, 0.0));
-  const long rend = (k0 + nb - 1 + hb < n - 1) ? k0 + nb - 1 + hb : n - 1;  // the last row a pivot reaches
-  for (long i = k0 + nb + blockIdx.x * (long)blockDim.x + threadIdx.x; i <= rend; i += gridDim.x * (long)blockDim.x) {
-    V c[kLUBlk];  // c[q] = S(i, k0 + q), zero where pivot k0 + q does not reach row i
-#pragma unroll
-    for (int q = 0; q < kLUBlk; ++q) c[q] = (q < nb && i - (k0 + q) <= hb) ? at(i, k0 + q) : zero;
-#pragma unroll
-    for (int q = 0; q < kLUBlk; ++q) {
-      if (q >= nb || i - (k0 + q) > hb) continue;
+    if (row && i - (k0 + q) <= hb) {  // pivot k0 + q on this thread's row
       V l = c[q];
-      if (!is_zero(l)) l = lu_div(l, D[q][q]);
+      if (!is_zero(l)) l = lu_div(l, p);
       c[q] = l;
       if (!is_zero(l)) {
 #pragma unroll
@@ -242,6 +231,22 @@ __global__ void __launch_bounds__(kLUPanelRows) k_lu_panel(long n, int hb, bool 
           if (j < nb) c[j] = lu_msub(c[j], l, D[q][j]);
       }
     }
+    for (int r = q + 1 + threadIdx.x; r < nb; r += blockDim.x) {
+      const V l = D[r][q];
+      if (!is_zero(l)) D[r][q] = lu_div(l, p);
+    }
+    __syncthreads();
+    const int m = nb - 1 - q;
+    for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+      const int r = q + 1 + t % m, j = q + 1 + t / m;
+      const V l = D[r][q];
+      if (!is_zero(l)) D[r][j] = lu_msub(D[r][j], l, D[q][j]);
+    }
+  }
+  __syncthreads();
+  if (writer)
+    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) at(k0 + t % nb, k0 + t / nb) = D[t % nb][t / nb];
+  if (row) {
 #pragma unroll
     for (int q = 0; q < kLUBlk; ++q)
       if (q < nb && i - (k0 + q) <= hb) at(i, k0 + q) = c[q];
@@ -786,7 +791,9 @@ void build_typed(const UserMatrix& K, const UserMatrix* M, const UserMatrix* C, 
       const long end = std::min<long>(k0 + nb - 1 + hbf, n - 1);
       const long rest = end - (k0 + nb) + 1;
       if (rest > 0) {
-        k_lu_blockrow<V><<<stream_grid(rest), kThreads>>>(n, hbf, !dense, last_k, k0, nb, S, bad);
+        // one warp per CTA: each column is a chain of FP64 multiply-subtracts, so
+        // the columns go to as many SMs as they fill
+        k_lu_blockrow<V><<<(unsigned)((rest + 31) / 32), 32>>>(n, hbf, !dense, last_k, k0, nb, S, bad);
         IDRS_LAUNCH_CHECK();
         const long g4 = (rest + 63) / 64;
         if (dense && g4 * g4 >= 2L * num_sms()) {  // 64 x 64 tiles while they fill the SMs twice
