@@ -57,7 +57,7 @@ def parse():
     p.add_argument("--profile", choices=["solve", "chain32", "chain64", "spmv_pagerank", "grad128"], default=None,
                    help="profiling driver: one mixed solve, or the fp32/fp64 Chebyshev(8) chain alone")
     p.add_argument("--workload", choices=["cdr256", "pagerank", "multishift", "adjoint", "sequence",
-                                          "deflation", "shift_invert", "matrix_market"],
+                                          "deflation", "shift_invert", "matrix_market", "lu_random"],
                    default="cdr256",
                    help="cdr256: the headline line; the others measure the remaining configurations "
                         "(PageRank 4M, complex multishift 128^3, adjoint 128^3, an 8 right-hand-side "
@@ -1069,6 +1069,52 @@ def run_shift_invert(args):
                       "multishift": res}), flush=True)
 
 
+def run_lu_random(args):
+    """The shift-and-invert factorisations at the sizes of the reference's
+    RANDOM examples (E/RANDOM/dense_real.f90, dense_complex.f90,
+    band_real.f90, band_complex.f90): real_precon / complex_precon 2 (dense LU)
+    and 3 (band LU) built on the device from dense / CDS storage, wall time of
+    the whole build (one untimed build first), and the residual of one solve
+    with the factor.  The matrices are the examples' uniform ones made
+    diagonally dominant (n on the dense diagonal, 2 hb on the band's) so the
+    factor without pivoting is well conditioned."""
+    import __graft_entry__ as g
+    pkg = g.load_package()
+    pkg.load()
+    rng = np.random.default_rng(0)
+    out = {}
+    for n, hb, cplx in ((2048, 0, False), (4096, 0, False), (4096, 0, True), (65536, 256, False),
+                        (65536, 256, True)):
+        if hb:
+            R = rng.uniform(size=(n, 2 * hb + 1))
+            if cplx:
+                R = R + 1j * rng.uniform(size=(n, 2 * hb + 1))
+            for d in range(-hb, hb + 1):  # entries outside the matrix are zero, as the example builds them
+                if d < 0:
+                    R[:(-d), d + hb] = 0
+                elif d > 0:
+                    R[n - d:, d + hb] = 0
+            R[:, hb] += 2 * hb
+            K = pkg.cds_format(n, n, hb, **({"cband": R} if cplx else {"rband": R}))
+            which = 3
+        else:
+            A = rng.uniform(size=(n, n))
+            if cplx:
+                A = A + 1j * rng.uniform(size=(n, n))
+            A = A + n * np.eye(n)
+            K = pkg.dense_format(**({"cmat": A} if cplx else {"rmat": A}))
+            which = 2
+        build = pkg.complex_precon if cplx else pkg.real_precon
+        P, sec = _wall(lambda: build(which, K))
+        v = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0)
+        x = v / pkg.Matrix(K, P=P, complex=cplx)
+        res = float(np.linalg.norm(np.asarray(K * x) - v) / np.linalg.norm(v))
+        out[f"{'band' if hb else 'dense'}_{'complex' if cplx else 'real'}_n{n}" + (f"_hb{hb}" if hb else "")] = {
+            "build_seconds": round(sec, 4), "solve_relres": res}
+    print(json.dumps({"workload": "lu_random_examples", "factor": "no pivoting, blocks of 16 pivots",
+                      "results": out}), flush=True)
+
+
 def run_matrix_market(args):
     """Matrix Market ingestion (mm_module.f90:48-154): the 64^3 convection-
     diffusion CRS matrix (1.81M nonzeros) and a 12-column right-hand side
@@ -1118,7 +1164,7 @@ def main():
     if args.workload != "cdr256":
         {"pagerank": run_pagerank, "multishift": run_multishift, "adjoint": run_adjoint,
          "sequence": run_sequence, "deflation": run_deflation, "shift_invert": run_shift_invert,
-         "matrix_market": run_matrix_market}[args.workload](args)
+         "matrix_market": run_matrix_market, "lu_random": run_lu_random}[args.workload](args)
         return
     rank, world, dist = dist_init(args.gpus)
     if args.impl == "reference":
